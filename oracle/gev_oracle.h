@@ -1,0 +1,147 @@
+/*
+ * gev_oracle.h -- CPU restatement (FP64, single core) of gevolution 1.2's
+ * per-step particle-mesh path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This library is the checker for the CUDA path:
+ * only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.
+ * The product path never calls it and has no CPU fallback.
+ *
+ * Every function cites the reference file:line whose arithmetic it restates
+ * (paths are relative to the gevolution-1.2 source tree).  Parts of the path
+ * that live in the external library LATfield2 v1.1 (particle lists and their
+ * relink, CIC halo folds, FFT conventions) are restated from the call sites in
+ * gevolution.hpp / main.cpp / ic_basic.hpp; their conventions are fixed here:
+ *
+ *   - Real fields: flat periodic arrays, no halo, x fastest:
+ *       f[c*N^3 + x + N*(y + N*z)]
+ *   - Symmetric tensors: 6 components in the order 00, 01, 02, 11, 12, 22.
+ *   - Half spectra (r2c): interleaved complex, kx fastest, kx in [0, N/2]:
+ *       F[c*N*N*NH + kx + NH*(ky + N*kz)],  NH = N/2 + 1
+ *     coordinates kx, ky, kz play the roles of rKSite coord(0), (1), (2).
+ *   - FFT: unnormalised, FFTW sign convention (forward e^{-i...}); the c2r
+ *     never modifies its complex input.
+ *   - Particles: records {pos[3], vel[3], ID} (part_simple), pos in box units
+ *     [0,1), vel = q/m.  A particle belongs to cell floor(pos/dx) (clamped to
+ *     N-1).  Each cell's list is ordered by ascending ID; the store is the
+ *     concatenation of the lists in site order (x fastest).
+ *   - Deposits accumulate into a field with an upper halo and fold the halo
+ *     back in the order x, y, z (the *_comm folds).
+ *   - updateVel returns sqrt(max over particles of the callback's value).
+ *   - moveParticles wraps pos into [0,1) per axis (p>=1 -> p-1, p<0 -> p+1,
+ *     then once more p>=1 -> p-1) and relinks.
+ */
+#ifndef GEV_ORACLE_H
+#define GEV_ORACLE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  double pos[3];
+  double vel[3];
+  int64_t ID;
+} gevo_part;
+
+/* ---- FFT (project-written mixed-radix, double) ---- */
+void gevo_fft1d(int L, double *data, int sign); /* in place, sign -1 forward */
+void gevo_fft_r2c(int N, const double *in, double *out);
+void gevo_fft_c2r(int N, const double *in, double *out);
+
+/* ---- k-space operators (gevolution.hpp:211-535) ---- */
+void gevo_kspace_tables(int N, double *gridk2, double *kshift /* 2N */);
+void gevo_poisson(int N, const double *srcFT, double *potFT, double coeff, double modif);
+void gevo_project_scalar(int N, const double *SijFT, double *chiFT, int add);
+void gevo_evolve_vector(int N, const double *SijFT, double *BiFT, double a2dtau);
+void gevo_project_vector(int N, const double *SiFT, double *BiFT, double coeff, double modif);
+void gevo_project_tensor(int N, const double *SijFT, double *hijFT);
+
+/* ---- real-space sources (gevolution.hpp:56-192) ---- */
+void gevo_prepare_source_tensor(int N, const double *phi, const double *Tij, double *Sij, double coeff);
+void gevo_prepare_source_scalar(int N, const double *phi, const double *chi, const double *source,
+                                double bgmodel, double *result, double coeff, double coeff2,
+                                double coeff3);
+
+/* ---- particle store ---- */
+int gevo_cell_of(int N, double p);
+void gevo_wrap(double *p);
+/* sort by (cell, ID); fills cell_start[N^3+1] if non-NULL */
+void gevo_sort(int N, long np, gevo_part *p, long *cell_start);
+
+/* ---- deposits (gevolution.hpp:926-1297; LATfield2 scalarProjectionCIC_*) ---- */
+void gevo_deposit_T00(int N, long np, const gevo_part *p, const long *cell_start, double mass,
+                      double a, const double *phi, double coeff, double *T00);
+void gevo_deposit_T0i(int N, long np, const gevo_part *p, const long *cell_start, double mass,
+                      const double *phi, double coeff, double *T0i);
+void gevo_deposit_Tij(int N, long np, const gevo_part *p, const long *cell_start, double mass,
+                      double a, const double *phi, double coeff, double *Tij);
+void gevo_deposit_mass(int N, long np, const gevo_part *p, const long *cell_start, double mass,
+                       double *rho);
+
+/* ---- particle updates (gevolution.hpp:570-903) ----
+ * kind 0 = GR (update_q / update_pos), 1 = Newton (update_q_Newton / update_pos_Newton).
+ * fields: phi, chi, Bi (3 comps); nfield as in Particles::updateVel/moveParticles.
+ * params: {a, a^2 N}.  kick returns sqrt(max v^2/a^2). drift relinks (sorts). */
+double gevo_kick(int N, long np, gevo_part *p, int kind, double dtau, const double *phi,
+                 const double *chi, const double *Bi, int nfield, double a, double a2N);
+void gevo_drift(int N, long np, gevo_part *p, int kind, double dtau, const double *phi,
+                const double *chi, const double *Bi, int nfield, double a, double a2N,
+                long *cell_start);
+
+/* ---- background (background.hpp:137-177), no ncdm / fluid ---- */
+typedef struct {
+  double Omega_cdm, Omega_b, Omega_m, Omega_Lambda, Omega_rad;
+} gevo_cosmo;
+double gevo_hconf(double a, double fourpiG, const gevo_cosmo *c);
+void gevo_rk4bg(double *a, double fourpiG, const gevo_cosmo *c, double dtau);
+
+/* ---- full simulation state and one GR time step (main.cpp:372-879) ---- */
+typedef struct {
+  int N;
+  long np;
+  gevo_part *p;
+  long *cell_start; /* N^3 + 1 */
+  double mass;      /* particle mass in units of the critical density */
+  double *phi, *chi, *source, *Sij, *Bi; /* real fields */
+  double *scalarFT, *SijFT, *BiFT;        /* half spectra */
+  double a, tau, dtau, dtau_old, fourpiG, Cf, steplimit, z_relax, maxvel, T00hom, phik0;
+  gevo_cosmo cosmo;
+  int vector_elliptic;
+  int cycle;
+} gevo_sim;
+
+int gevo_sim_alloc(gevo_sim *s, int N, long np);
+void gevo_sim_free(gevo_sim *s);
+/* one cycle of the main loop body (GR): deposits, phi/chi/B solves, kick, drift,
+ * background, next dtau.  Returns 0. */
+int gevo_sim_step(gevo_sim *s);
+double gevo_next_dtau(const gevo_sim *s);
+
+/* ---- initial conditions (restating the mPk path of ic_basic.hpp) ----
+ * gaussian potential: unit-variance complex modes from a counter-based hash,
+ * scaled by sqrt(P(k)) of a BBKS spectrum; see gev_ic.c */
+typedef struct {
+  double h, Omega_cdm, Omega_b, n_s, sigma8, z_in, boxsize, Cf, steplimit;
+  uint64_t seed;
+  int ksphere;
+} gevo_icparams;
+/* BBKS linear P(k) [(Mpc/h)^3] at z_in for k [h/Mpc], sigma8-normalised */
+double gevo_ic_pk(const gevo_icparams *ic, double k);
+/* amplitude factor A*D(z_in)^2/D(0)^2 so that P = amp * k^n_s T(k)^2 */
+double gevo_ic_pk_amplitude(const gevo_icparams *ic);
+double gevo_bbks_T(double k, double Gamma);
+uint64_t gevo_hash64(uint64_t seed, uint64_t counter);
+void gevo_ic_potential_k(int N, const gevo_icparams *ic, double *potFT);
+int gevo_ic_generate(gevo_sim *s, const gevo_icparams *ic);
+
+/* ---- power spectrum (tools.hpp:53-212, extractPowerSpectrum) ---- */
+void gevo_power_spectrum(int N, const double *FT, int ncomp, int symmetric, int numbins,
+                         int deconvolve, double *kbin, double *power, double *kscatter,
+                         double *pscatter, int *occupation);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
