@@ -1,0 +1,319 @@
+// gev_capi.cu -- context, field and FFT entry points of the C-ABI
+// (include/gev_gb300.h).  The context owns the stream, the k-space and twiddle
+// tables, and the scratch buffers (c2r staging spectrum, deposit cubes,
+// reduction words); fields are plain device arrays in the layouts of
+// gev_internal.cuh.
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "gev_internal.cuh"
+
+int fft_init_kernels(int prec);
+
+namespace {
+
+// gridk2 / kshift exactly as gevolution.hpp:222-227 builds them
+template <typename T>
+void kspace_tables(int N, std::vector<T> &g, std::vector<T> &ks) {
+  g.resize(N);
+  ks.resize(2 * N);
+  for (int i = 0; i < N; i++) {
+    double gi = 2. * (double)N * sin(M_PI * (double)i / (double)N);
+    ks[2 * i] = (T)(gi * cos(M_PI * (double)i / (double)N));
+    ks[2 * i + 1] = (T)(gi * -sin(M_PI * (double)i / (double)N));
+    g[i] = (T)(gi * gi);
+  }
+}
+
+template <typename T>
+void twiddles(int L, std::vector<T> &tw) {
+  tw.resize(2 * (size_t)L);
+  for (int j = 0; j < L; j++) {
+    long double ang = 2.0L * 3.14159265358979323846264338327950288L * (long double)j / (long double)L;
+    tw[2 * j] = (T)cosl(ang);
+    tw[2 * j + 1] = (T)-sinl(ang);
+  }
+}
+
+template <typename T>
+int upload_tables(gev_ctx *ctx) {
+  std::vector<T> g, ks, twN, twH;
+  kspace_tables<T>(ctx->N, g, ks);
+  twiddles<T>(ctx->N, twN);
+  twiddles<T>(ctx->N / 2, twH);
+  const size_t sz = sizeof(T);
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&ctx->d_gridk2, g.size() * sz));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&ctx->d_kshift, ks.size() * sz));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&ctx->d_twN, twN.size() * sz));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&ctx->d_twH, twH.size() * sz));
+  GEV_CHECK_CUDA(ctx, cudaMemcpy(ctx->d_gridk2, g.data(), g.size() * sz, cudaMemcpyHostToDevice));
+  GEV_CHECK_CUDA(ctx, cudaMemcpy(ctx->d_kshift, ks.data(), ks.size() * sz, cudaMemcpyHostToDevice));
+  GEV_CHECK_CUDA(ctx, cudaMemcpy(ctx->d_twN, twN.data(), twN.size() * sz, cudaMemcpyHostToDevice));
+  GEV_CHECK_CUDA(ctx, cudaMemcpy(ctx->d_twH, twH.data(), twH.size() * sz, cudaMemcpyHostToDevice));
+  return GEV_OK;
+}
+
+size_t real_size(const gev_ctx *ctx) { return ctx->prec == GEV_PREC_FP64 ? 8 : 4; }
+
+template <typename T>
+__global__ void k_from_double(const double *__restrict__ in, T *out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (T)in[i];
+}
+template <typename T>
+__global__ void k_to_double(const T *__restrict__ in, double *out, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    out[i] = (double)in[i];
+}
+
+}  // namespace
+
+int ctx_ensure_cube(gev_ctx *ctx, size_t bytes) {
+  if (ctx->cube_bytes >= bytes) return GEV_OK;
+  if (ctx->d_cube) {
+    GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->d_cube);
+    ctx->bytes_in_use -= ctx->cube_bytes;
+    ctx->d_cube = nullptr;
+    ctx->cube_bytes = 0;
+  }
+  if (cudaMalloc(&ctx->d_cube, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return gev_fail(ctx, GEV_ENOMEM, "deposit scratch allocation failed");
+  }
+  ctx->cube_bytes = bytes;
+  ctx->bytes_in_use += bytes;
+  return GEV_OK;
+}
+
+int ctx_ensure_red(gev_ctx *ctx, size_t elems) {
+  if (ctx->red_elems >= elems) return GEV_OK;
+  if (ctx->d_red) {
+    GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    cudaFree(ctx->d_red);
+  }
+  ctx->d_red = nullptr;
+  ctx->red_elems = 0;
+  if (cudaMalloc(&ctx->d_red, elems * sizeof(double)) != cudaSuccess) {
+    cudaGetLastError();
+    return gev_fail(ctx, GEV_ENOMEM, "reduction scratch allocation failed");
+  }
+  ctx->red_elems = elems;
+  return GEV_OK;
+}
+
+extern "C" {
+
+const char *gev_strerror(int s) {
+  switch (s) {
+    case GEV_OK:
+      return "ok";
+    case GEV_EINVAL:
+      return "invalid argument";
+    case GEV_ENOMEM:
+      return "device out of memory";
+    case GEV_ECUDA:
+      return "CUDA error";
+    case GEV_ETIMEOUT:
+      return "device wait timed out";
+    case GEV_ENODEV:
+      return "no usable CUDA device";
+    default:
+      return "unknown status";
+  }
+}
+
+int gev_ctx_create(int device, int N, int precision, gev_ctx **out) {
+  if (!out) return GEV_EINVAL;
+  *out = nullptr;
+  if (N < 8 || N > 2048 || N % 2 != 0 || (precision != GEV_PREC_FP64 && precision != GEV_PREC_MIXED))
+    return GEV_EINVAL;
+  FftPlan pN, pH;
+  if (fft_build_plan(N, &pN) != GEV_OK || fft_build_plan(N / 2, &pH) != GEV_OK) return GEV_EINVAL;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= device || device < 0) {
+    cudaGetLastError();
+    return GEV_ENODEV;
+  }
+  if (cudaSetDevice(device) != cudaSuccess) return GEV_ENODEV;
+  gev_ctx *ctx = new gev_ctx();
+  ctx->device = device;
+  ctx->N = N;
+  ctx->prec = precision;
+  ctx->planN = pN;
+  ctx->planH = pH;
+  cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+  int rc = GEV_OK;
+  if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess) rc = GEV_ECUDA;
+  if (!rc) rc = precision == GEV_PREC_FP64 ? upload_tables<double>(ctx) : upload_tables<float>(ctx);
+  if (!rc) rc = fft_init_kernels(precision);
+  if (!rc) {
+    const size_t spec = (size_t)N * N * (N / 2 + 1) * 2 * real_size(ctx);
+    if (cudaMalloc(&ctx->d_fft_scratch, spec) != cudaSuccess)
+      rc = GEV_ENOMEM;
+    else {
+      ctx->fft_scratch_bytes = spec;
+      ctx->bytes_in_use += spec;
+    }
+  }
+  if (!rc) rc = ctx_ensure_red(ctx, 1024);
+  if (rc) {
+    cudaGetLastError();
+    gev_ctx_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return GEV_OK;
+}
+
+int gev_ctx_destroy(gev_ctx *ctx) {
+  if (!ctx) return GEV_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->d_gridk2);
+  cudaFree(ctx->d_kshift);
+  cudaFree(ctx->d_twN);
+  cudaFree(ctx->d_twH);
+  cudaFree(ctx->d_fft_scratch);
+  cudaFree(ctx->d_cube);
+  cudaFree(ctx->d_red);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return GEV_OK;
+}
+
+int gev_ctx_sync(gev_ctx *ctx) {
+  if (!ctx) return GEV_EINVAL;
+  GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GEV_OK;
+}
+
+int gev_ctx_stream(gev_ctx *ctx, void **s) {
+  if (!ctx || !s) return GEV_EINVAL;
+  *s = (void *)ctx->stream;
+  return GEV_OK;
+}
+
+int gev_ctx_info(gev_ctx *ctx, int *N, int *precision, size_t *bytes) {
+  if (!ctx) return GEV_EINVAL;
+  if (N) *N = ctx->N;
+  if (precision) *precision = ctx->prec;
+  if (bytes) *bytes = ctx->bytes_in_use;
+  return GEV_OK;
+}
+
+const char *gev_ctx_last_error(gev_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+int gev_ctx_launch_count(gev_ctx *ctx, long long *count) {
+  if (!ctx || !count) return GEV_EINVAL;
+  *count = ctx->launches;
+  return GEV_OK;
+}
+
+int gev_field_create(gev_ctx *ctx, int kind, int ncomp, gev_field **out) {
+  if (!ctx || !out || ncomp < 1 || ncomp > 16 || (kind != GEV_FIELD_REAL && kind != GEV_FIELD_SPECTRUM))
+    return gev_fail(ctx, GEV_EINVAL, "field_create: bad kind or component count");
+  const int N = ctx->N;
+  gev_field *f = new gev_field();
+  f->ctx = ctx;
+  f->kind = kind;
+  f->ncomp = ncomp;
+  f->comp_elems = kind == GEV_FIELD_REAL ? (size_t)N * N * N : (size_t)N * N * (N / 2 + 1);
+  f->elem_bytes = real_size(ctx) * (kind == GEV_FIELD_REAL ? 1 : 2);
+  const size_t bytes = f->comp_elems * f->elem_bytes * ncomp;
+  if (cudaMalloc(&f->d, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    delete f;
+    return gev_fail(ctx, GEV_ENOMEM, "field_create: device allocation failed");
+  }
+  ctx->bytes_in_use += bytes;
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(f->d, 0, bytes, ctx->stream));
+  *out = f;
+  return GEV_OK;
+}
+
+int gev_field_destroy(gev_field *f) {
+  if (!f) return GEV_OK;
+  if (f->ctx) {
+    cudaStreamSynchronize(f->ctx->stream);
+    f->ctx->bytes_in_use -= f->comp_elems * f->elem_bytes * f->ncomp;
+  }
+  cudaFree(f->d);
+  delete f;
+  return GEV_OK;
+}
+
+int gev_field_upload(gev_field *f, const double *host) {
+  if (!f || !host) return GEV_EINVAL;
+  gev_ctx *ctx = f->ctx;
+  const size_t nd = f->comp_elems * f->ncomp * (f->kind == GEV_FIELD_SPECTRUM ? 2 : 1);
+  if (ctx->prec == GEV_PREC_FP64) {
+    GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(f->d, host, nd * 8, cudaMemcpyHostToDevice, ctx->stream));
+  } else {
+    double *tmp = nullptr;
+    GEV_CHECK_CUDA(ctx, cudaMallocAsync(&tmp, nd * 8, ctx->stream));
+    GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(tmp, host, nd * 8, cudaMemcpyHostToDevice, ctx->stream));
+    k_from_double<float><<<grid_for(ctx, nd, 256, 16), 256, 0, ctx->stream>>>(tmp, (float *)f->d, nd);
+    GEV_LAUNCH_CHECK(ctx);
+    GEV_CHECK_CUDA(ctx, cudaFreeAsync(tmp, ctx->stream));
+  }
+  GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GEV_OK;
+}
+
+int gev_field_download(gev_field *f, double *host) {
+  if (!f || !host) return GEV_EINVAL;
+  gev_ctx *ctx = f->ctx;
+  const size_t nd = f->comp_elems * f->ncomp * (f->kind == GEV_FIELD_SPECTRUM ? 2 : 1);
+  if (ctx->prec == GEV_PREC_FP64) {
+    GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(host, f->d, nd * 8, cudaMemcpyDeviceToHost, ctx->stream));
+  } else {
+    double *tmp = nullptr;
+    GEV_CHECK_CUDA(ctx, cudaMallocAsync(&tmp, nd * 8, ctx->stream));
+    k_to_double<float><<<grid_for(ctx, nd, 256, 16), 256, 0, ctx->stream>>>((const float *)f->d, tmp, nd);
+    GEV_LAUNCH_CHECK(ctx);
+    GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(host, tmp, nd * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    GEV_CHECK_CUDA(ctx, cudaFreeAsync(tmp, ctx->stream));
+  }
+  GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GEV_OK;
+}
+
+int gev_field_zero(gev_field *f) {
+  if (!f) return GEV_EINVAL;
+  GEV_CHECK_CUDA(f->ctx, cudaMemsetAsync(f->d, 0, f->comp_elems * f->elem_bytes * f->ncomp, f->ctx->stream));
+  return GEV_OK;
+}
+
+int gev_field_device_ptr(gev_field *f, void **ptr, size_t *bytes) {
+  if (!f) return GEV_EINVAL;
+  if (ptr) *ptr = f->d;
+  if (bytes) *bytes = f->comp_elems * f->elem_bytes * f->ncomp;
+  return GEV_OK;
+}
+
+int gev_fft_r2c(gev_ctx *ctx, const gev_field *real, gev_field *spec) {
+  if (!ctx || !real || !spec || real->ctx != ctx || spec->ctx != ctx || real->kind != GEV_FIELD_REAL ||
+      spec->kind != GEV_FIELD_SPECTRUM || real->ncomp != spec->ncomp)
+    return gev_fail(ctx, GEV_EINVAL, "fft_r2c: real field and spectrum with equal component counts");
+  for (int c = 0; c < real->ncomp; ++c) {
+    int rc = fft_r2c_comp(ctx, (const char *)real->d + c * real->comp_elems * real->elem_bytes,
+                          (char *)spec->d + c * spec->comp_elems * spec->elem_bytes);
+    if (rc) return rc;
+  }
+  return GEV_OK;
+}
+
+int gev_fft_c2r(gev_ctx *ctx, const gev_field *spec, gev_field *real) {
+  if (!ctx || !real || !spec || real->ctx != ctx || spec->ctx != ctx || real->kind != GEV_FIELD_REAL ||
+      spec->kind != GEV_FIELD_SPECTRUM || real->ncomp != spec->ncomp)
+    return gev_fail(ctx, GEV_EINVAL, "fft_c2r: spectrum and real field with equal component counts");
+  for (int c = 0; c < real->ncomp; ++c) {
+    int rc = fft_c2r_comp(ctx, (const char *)spec->d + c * spec->comp_elems * spec->elem_bytes,
+                          (char *)real->d + c * real->comp_elems * real->elem_bytes, ctx->d_fft_scratch);
+    if (rc) return rc;
+  }
+  return GEV_OK;
+}
+
+}  // extern "C"

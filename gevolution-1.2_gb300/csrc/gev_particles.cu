@@ -1,0 +1,667 @@
+// gev_particles.cu -- the device particle store and the particle updates.
+//
+// Replaces LATfield2's Particles (per-cell std::lists, updateVel /
+// moveParticles with callbacks; main.cpp:743-806) by a structure-of-arrays
+// store kept in (cell, ID) order:
+//   relink = periodic counting sort: atomic histogram of cell keys, exclusive
+//   scan into cell starts, scatter, then each cell's run is ordered by ID (so
+//   the order -- and every sum over it -- is independent of atomic timing),
+//   then one gather of the payload.
+// update_q / update_pos (gevolution.hpp:570-903) run one thread per particle
+// in that order, so neighbouring threads gather neighbouring field cells.
+#include <cmath>
+#include <cstring>
+
+#include "gev_internal.cuh"
+
+namespace {
+
+constexpr int SMALL_CELL = 32;  // runs up to this length are ordered by one thread
+
+// ------------------------------------------------------------ keys ------
+__device__ __forceinline__ int cell1(double p, double Nd, int N) {
+  int c = (int)(p * Nd);
+  return c >= N ? N - 1 : (c < 0 ? 0 : c);
+}
+__device__ __forceinline__ uint32_t cell_key(double x, double y, double z, int N) {
+  const double Nd = (double)N;
+  return (uint32_t)cell1(x, Nd, N) + (uint32_t)N * ((uint32_t)cell1(y, Nd, N) + (uint32_t)N * (uint32_t)cell1(z, Nd, N));
+}
+// periodic wrap into [0,1), as moveParticles does for the box {1,1,1}
+__device__ __forceinline__ double wrap01(double p) {
+  if (p >= 1.0)
+    p -= 1.0;
+  else if (p < 0.0) {
+    p += 1.0;
+    if (p >= 1.0) p -= 1.0;
+  }
+  return p;
+}
+
+// ------------------------------------------------------------ upload ----
+template <typename V>
+__global__ void k_unpack(const gev_part *__restrict__ in, long n, PclsArrays P, int N) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const gev_part q = in[i];
+    P.px[i] = q.pos[0];
+    P.py[i] = q.pos[1];
+    P.pz[i] = q.pos[2];
+    ((V *)P.vx)[i] = (V)q.vel[0];
+    ((V *)P.vy)[i] = (V)q.vel[1];
+    ((V *)P.vz)[i] = (V)q.vel[2];
+    P.id[i] = q.ID;
+    P.cell[i] = cell_key(q.pos[0], q.pos[1], q.pos[2], N);
+  }
+}
+template <typename V>
+__global__ void k_pack(gev_part *__restrict__ out, long n, PclsArrays P) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    gev_part q;
+    q.pos[0] = P.px[i];
+    q.pos[1] = P.py[i];
+    q.pos[2] = P.pz[i];
+    q.vel[0] = (double)((const V *)P.vx)[i];
+    q.vel[1] = (double)((const V *)P.vy)[i];
+    q.vel[2] = (double)((const V *)P.vz)[i];
+    q.ID = P.id[i];
+    out[i] = q;
+  }
+}
+
+// ------------------------------------------------------------ sort ------
+__global__ void k_count(const uint32_t *__restrict__ cell, long n, uint32_t *count, uint32_t *rank) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    rank[i] = atomicAdd(&count[cell[i]], 1u);
+}
+
+constexpr int SCAN_T = 256, SCAN_PER = 16, SCAN_TILE = SCAN_T * SCAN_PER;
+
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *sh, uint32_t &total) {
+  // warp-shuffle scan then a scan of the warp totals
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  uint32_t x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    uint32_t t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0u;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      uint32_t y = __shfl_up_sync(0xffffffffu, t, o);
+      if (lane >= o) t += y;
+    }
+    sh[lane + 32] = t;
+  }
+  __syncthreads();
+  total = sh[32 + (blockDim.x >> 5) - 1];
+  const uint32_t before = w > 0 ? sh[32 + w - 1] : 0u;
+  __syncthreads();
+  return before + x - v;
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_reduce(const uint32_t *__restrict__ in, long n, uint32_t *bsum) {
+  __shared__ uint32_t sh[64];
+  const long base = (long)blockIdx.x * SCAN_TILE;
+  uint32_t s = 0;
+  for (int k = 0; k < SCAN_PER; ++k) {
+    const long i = base + (long)k * SCAN_T + threadIdx.x;
+    if (i < n) s += in[i];
+  }
+  uint32_t total;
+  block_exclusive_scan(s, sh, total);
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+// one block: exclusive scan of nb block sums in place
+__global__ void __launch_bounds__(1024) k_scan_blocks(uint32_t *bsum, long nb) {
+  __shared__ uint32_t sh[64];
+  const long per = (nb + blockDim.x - 1) / blockDim.x;
+  const long b0 = threadIdx.x * per;
+  uint32_t s = 0;
+  for (long i = b0; i < b0 + per && i < nb; ++i) s += bsum[i];
+  uint32_t total;
+  uint32_t off = block_exclusive_scan(s, sh, total);
+  for (long i = b0; i < b0 + per && i < nb; ++i) {
+    const uint32_t v = bsum[i];
+    bsum[i] = off;
+    off += v;
+  }
+}
+
+__global__ void __launch_bounds__(SCAN_T) k_scan_down(const uint32_t *__restrict__ in, long n,
+                                                      const uint32_t *__restrict__ bsum, uint32_t *out,
+                                                      uint32_t total_n) {
+  __shared__ uint32_t tile[SCAN_TILE];
+  __shared__ uint32_t sh[64];
+  const long base = (long)blockIdx.x * SCAN_TILE;
+  for (int k = 0; k < SCAN_PER; ++k) {
+    const long i = base + (long)k * SCAN_T + threadIdx.x;
+    tile[k * SCAN_T + threadIdx.x] = i < n ? in[i] : 0u;
+  }
+  __syncthreads();
+  uint32_t loc[SCAN_PER], s = 0;
+#pragma unroll
+  for (int k = 0; k < SCAN_PER; ++k) {
+    loc[k] = tile[threadIdx.x * SCAN_PER + k];
+    s += loc[k];
+  }
+  uint32_t total;
+  uint32_t off = block_exclusive_scan(s, sh, total) + bsum[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < SCAN_PER; ++k) {
+    tile[threadIdx.x * SCAN_PER + k] = off;
+    off += loc[k];
+  }
+  __syncthreads();
+  for (int k = 0; k < SCAN_PER; ++k) {
+    const long i = base + (long)k * SCAN_T + threadIdx.x;
+    if (i < n) out[i] = tile[k * SCAN_T + threadIdx.x];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = total_n;
+}
+
+__global__ void k_scatter(const uint32_t *__restrict__ cell, const uint32_t *__restrict__ rank, long n,
+                          const uint32_t *__restrict__ start, uint32_t *perm) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    perm[start[cell[i]] + rank[i]] = (uint32_t)i;
+}
+
+// order each cell's run by ID; long runs are queued for k_canon_big
+__global__ void k_canon(const uint32_t *__restrict__ start, long ncell, const int64_t *__restrict__ id,
+                        uint32_t *perm, uint32_t *big) {
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < ncell; c += (long)gridDim.x * blockDim.x) {
+    const uint32_t s = start[c], e = start[c + 1];
+    const uint32_t n = e - s;
+    if (n <= 1) continue;
+    if (n > SMALL_CELL) {
+      const uint32_t slot = atomicAdd(&big[0], 1u);
+      big[1 + slot] = (uint32_t)c;
+      continue;
+    }
+    int64_t key[SMALL_CELL];
+    uint32_t val[SMALL_CELL];
+    for (uint32_t j = 0; j < n; ++j) {
+      val[j] = perm[s + j];
+      key[j] = id[val[j]];
+    }
+    for (uint32_t j = 1; j < n; ++j) {
+      const int64_t k = key[j];
+      const uint32_t v = val[j];
+      int m = (int)j - 1;
+      while (m >= 0 && key[m] > k) {
+        key[m + 1] = key[m];
+        val[m + 1] = val[m];
+        --m;
+      }
+      key[m + 1] = k;
+      val[m + 1] = v;
+    }
+    for (uint32_t j = 0; j < n; ++j) perm[s + j] = val[j];
+  }
+}
+
+// one block per long run: rank by ID (IDs are unique), then copy back
+__global__ void k_canon_big(const uint32_t *__restrict__ start, const int64_t *__restrict__ id, uint32_t *perm,
+                            uint32_t *tmp, const uint32_t *__restrict__ big) {
+  const uint32_t nbig = big[0];
+  for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
+    const uint32_t c = big[1 + b];
+    const uint32_t s = start[c], e = start[c + 1];
+    for (uint32_t i = s + threadIdx.x; i < e; i += blockDim.x) {
+      const int64_t k = id[perm[i]];
+      uint32_t r = 0;
+      for (uint32_t j = s; j < e; ++j) r += id[perm[j]] < k ? 1u : 0u;
+      tmp[s + r] = perm[i];
+    }
+    __syncthreads();
+    for (uint32_t i = s + threadIdx.x; i < e; i += blockDim.x) perm[i] = tmp[i];
+    __syncthreads();
+  }
+}
+
+template <typename V>
+__global__ void k_gather(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ perm, long n) {
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
+    const uint32_t i = perm[j];
+    dst.px[j] = src.px[i];
+    dst.py[j] = src.py[i];
+    dst.pz[j] = src.pz[i];
+    ((V *)dst.vx)[j] = ((const V *)src.vx)[i];
+    ((V *)dst.vy)[j] = ((const V *)src.vy)[i];
+    ((V *)dst.vz)[j] = ((const V *)src.vz)[i];
+    dst.id[j] = src.id[i];
+    dst.cell[j] = src.cell[i];
+  }
+}
+
+// ------------------------------------------------------- particle updates --
+struct Params {
+  double dtau, a, a2N, inv_a2, inv_a2N;
+  int nfield, N;
+};
+
+template <typename T>
+__device__ __forceinline__ T F(const T *__restrict__ f, int x, int y, int z, int N) {
+  return __ldg(&f[sidx(wrapi(x, N), wrapi(y, N), wrapi(z, N), N)]);
+}
+
+// update_q, gevolution.hpp:570-678 (GRADIENT_ORDER 1).  The field values at the
+// particle's cell corners are gathered once; ref_dist = pos*N - cell.
+template <typename T, typename V, int KIND>
+__global__ void __launch_bounds__(256) k_update_q(PclsArrays P, long n, const T *__restrict__ phi,
+                                                  const T *__restrict__ chi, const T *__restrict__ Bi, Params pr,
+                                                  unsigned long long *maxbits) {
+  const int N = pr.N;
+  const size_t NV = (size_t)N * N * N;
+  double vmax = 0.;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t c = P.cell[i];
+    const int cx = (int)(c % N), cy = (int)((c / N) % N), cz = (int)(c / ((uint32_t)N * N));
+    const T r0 = (T)(P.px[i] * (double)N - cx), r1 = (T)(P.py[i] * (double)N - cy), r2 = (T)(P.pz[i] * (double)N - cz);
+    T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
+    const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
+    T g0, g1, g2;
+    {
+      const T f000 = F(phi, cx, cy, cz, N), f100 = F(phi, cx + 1, cy, cz, N), f010 = F(phi, cx, cy + 1, cz, N),
+              f110 = F(phi, cx + 1, cy + 1, cz, N), f001 = F(phi, cx, cy, cz + 1, N),
+              f101 = F(phi, cx + 1, cy, cz + 1, N), f011 = F(phi, cx, cy + 1, cz + 1, N),
+              f111 = F(phi, cx + 1, cy + 1, cz + 1, N);
+      g0 = s1 * s2 * (f100 - f000) + r1 * s2 * (f110 - f010) + s1 * r2 * (f101 - f001) + r1 * r2 * (f111 - f011);
+      g1 = s0 * s2 * (f010 - f000) + r0 * s2 * (f110 - f100) + s0 * r2 * (f011 - f001) + r0 * r2 * (f111 - f101);
+      g2 = s0 * s1 * (f001 - f000) + r0 * s1 * (f101 - f100) + s0 * r1 * (f011 - f010) + r0 * r1 * (f111 - f110);
+    }
+    const T a = (T)pr.a;
+    T e2 = (T)0, e = (T)0, inv_e = (T)0;
+    if (KIND == GEV_GR) {
+      const T v2 = q0 * q0 + q1 * q1 + q2 * q2;
+      e2 = v2 + a * a;
+      const T fac = (v2 + e2) / e2;
+      g0 *= fac;
+      g1 *= fac;
+      g2 *= fac;
+    }
+    if (pr.nfield >= 2 && chi != nullptr) {
+      const T f000 = F(chi, cx, cy, cz, N), f100 = F(chi, cx + 1, cy, cz, N), f010 = F(chi, cx, cy + 1, cz, N),
+              f110 = F(chi, cx + 1, cy + 1, cz, N), f001 = F(chi, cx, cy, cz + 1, N),
+              f101 = F(chi, cx + 1, cy, cz + 1, N), f011 = F(chi, cx, cy + 1, cz + 1, N),
+              f111 = F(chi, cx + 1, cy + 1, cz + 1, N);
+      g0 -= s1 * s2 * (f100 - f000) + r1 * s2 * (f110 - f010) + s1 * r2 * (f101 - f001) + r1 * r2 * (f111 - f011);
+      g1 -= s0 * s2 * (f010 - f000) + r0 * s2 * (f110 - f100) + s0 * r2 * (f011 - f001) + r0 * r2 * (f111 - f101);
+      g2 -= s0 * s1 * (f001 - f000) + r0 * s1 * (f101 - f100) + s0 * r1 * (f011 - f010) + r0 * r1 * (f111 - f110);
+    }
+    if (KIND == GEV_GR) {
+      e = sqrt(e2);
+      inv_e = (T)1 / e;
+      if (pr.nfield >= 3 && Bi != nullptr) {
+        const T *B0 = Bi, *B1 = Bi + NV, *B2 = Bi + 2 * NV;
+        const T t0 = (T)2 * r0, t1 = (T)2 * r1, t2 = (T)2 * r2;
+        T p0, p1, p2;
+        p0 = (s2 * (F(B1, cx + 1, cy, cz, N) - F(B1, cx, cy, cz, N)) +
+              r2 * (F(B1, cx + 1, cy, cz + 1, N) - F(B1, cx, cy, cz + 1, N))) * q1;
+        p0 += (s1 * (F(B2, cx + 1, cy, cz, N) - F(B2, cx, cy, cz, N)) +
+               r1 * (F(B2, cx + 1, cy + 1, cz, N) - F(B2, cx, cy + 1, cz, N))) * q2;
+        p0 += (s1 * s2 * ((r0 - (T)1) * F(B0, cx - 1, cy, cz, N) + ((T)1 - t0) * F(B0, cx, cy, cz, N) + r0 * F(B0, cx + 1, cy, cz, N)) +
+               r1 * s2 * ((r0 - (T)1) * F(B0, cx - 1, cy + 1, cz, N) + ((T)1 - t0) * F(B0, cx, cy + 1, cz, N) + r0 * F(B0, cx + 1, cy + 1, cz, N)) +
+               s1 * r2 * ((r0 - (T)1) * F(B0, cx - 1, cy, cz + 1, N) + ((T)1 - t0) * F(B0, cx, cy, cz + 1, N) + r0 * F(B0, cx + 1, cy, cz + 1, N)) +
+               r1 * r2 * ((r0 - (T)1) * F(B0, cx - 1, cy + 1, cz + 1, N) + ((T)1 - t0) * F(B0, cx, cy + 1, cz + 1, N) + r0 * F(B0, cx + 1, cy + 1, cz + 1, N))) * q0;
+        p1 = (s0 * (F(B2, cx, cy + 1, cz, N) - F(B2, cx, cy, cz, N)) +
+              r0 * (F(B2, cx + 1, cy + 1, cz, N) - F(B2, cx + 1, cy, cz, N))) * q2;
+        p1 += (s2 * (F(B0, cx, cy + 1, cz, N) - F(B0, cx, cy, cz, N)) +
+               r2 * (F(B0, cx, cy + 1, cz + 1, N) - F(B0, cx, cy, cz + 1, N))) * q0;
+        p1 += (s0 * s2 * ((r1 - (T)1) * F(B1, cx, cy - 1, cz, N) + ((T)1 - t1) * F(B1, cx, cy, cz, N) + r1 * F(B1, cx, cy + 1, cz, N)) +
+               r0 * s2 * ((r1 - (T)1) * F(B1, cx + 1, cy - 1, cz, N) + ((T)1 - t1) * F(B1, cx + 1, cy, cz, N) + r1 * F(B1, cx + 1, cy + 1, cz, N)) +
+               s0 * r2 * ((r1 - (T)1) * F(B1, cx, cy - 1, cz + 1, N) + ((T)1 - t1) * F(B1, cx, cy, cz + 1, N) + r1 * F(B1, cx, cy + 1, cz + 1, N)) +
+               r0 * r2 * ((r1 - (T)1) * F(B1, cx + 1, cy - 1, cz + 1, N) + ((T)1 - t1) * F(B1, cx + 1, cy, cz + 1, N) + r1 * F(B1, cx + 1, cy + 1, cz + 1, N))) * q1;
+        p2 = (s1 * (F(B0, cx, cy, cz + 1, N) - F(B0, cx, cy, cz, N)) +
+              r1 * (F(B0, cx, cy + 1, cz + 1, N) - F(B0, cx, cy + 1, cz, N))) * q0;
+        p2 += (s0 * (F(B1, cx, cy, cz + 1, N) - F(B1, cx, cy, cz, N)) +
+               r0 * (F(B1, cx + 1, cy, cz + 1, N) - F(B1, cx + 1, cy, cz, N))) * q1;
+        p2 += (s0 * s1 * ((r2 - (T)1) * F(B2, cx, cy, cz - 1, N) + ((T)1 - t2) * F(B2, cx, cy, cz, N) + r2 * F(B2, cx, cy, cz + 1, N)) +
+               r0 * s1 * ((r2 - (T)1) * F(B2, cx + 1, cy, cz - 1, N) + ((T)1 - t2) * F(B2, cx + 1, cy, cz, N) + r2 * F(B2, cx + 1, cy, cz + 1, N)) +
+               s0 * r1 * ((r2 - (T)1) * F(B2, cx, cy + 1, cz - 1, N) + ((T)1 - t2) * F(B2, cx, cy + 1, cz, N) + r2 * F(B2, cx, cy + 1, cz + 1, N)) +
+               r0 * r1 * ((r2 - (T)1) * F(B2, cx + 1, cy + 1, cz - 1, N) + ((T)1 - t2) * F(B2, cx + 1, cy + 1, cz, N) + r2 * F(B2, cx + 1, cy + 1, cz + 1, N))) * q2;
+        const T k = (T)pr.inv_a2N * inv_e;
+        g0 += p0 * k;
+        g1 += p1 * k;
+        g2 += p2 * k;
+      }
+    }
+    // vel -= dtau * e * grad / dx   (GR);  vel -= dtau * a * grad / dx   (Newton)
+    const T m = (T)pr.dtau * (KIND == GEV_GR ? e : a) * (T)N;
+    q0 -= m * g0;
+    q1 -= m * g1;
+    q2 -= m * g2;
+    ((V *)P.vx)[i] = (V)q0;
+    ((V *)P.vy)[i] = (V)q1;
+    ((V *)P.vz)[i] = (V)q2;
+    const double v2 = ((double)q0 * q0 + (double)q1 * q1 + (double)q2 * q2) * pr.inv_a2;
+    vmax = v2 > vmax ? v2 : vmax;
+  }
+  // max over the block, then one atomic on the bit pattern (non-negative doubles order as integers)
+  for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+  __shared__ double sh[8];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = vmax;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double m = 0.;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) m = fmax(m, sh[w]);
+    atomicMax(maxbits, (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+// update_pos, gevolution.hpp:810-871, and update_pos_Newton, 900-903; then the
+// periodic wrap and the new cell key for the relink
+template <typename T, typename V, int KIND>
+__global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const T *__restrict__ phi,
+                                                    const T *__restrict__ chi, const T *__restrict__ Bi, Params pr) {
+  const int N = pr.N;
+  const size_t NV = (size_t)N * N * N;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    double x = P.px[i], y = P.py[i], z = P.pz[i];
+    const T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
+    if (KIND == GEV_NEWTON) {
+      const double f = pr.dtau / pr.a;
+      x += (double)q0 * f;
+      y += (double)q1 * f;
+      z += (double)q2 * f;
+    } else {
+      const uint32_t c = P.cell[i];
+      const int cx = (int)(c % N), cy = (int)((c / N) % N), cz = (int)(c / ((uint32_t)N * N));
+      const T r0 = (T)(x * (double)N - cx), r1 = (T)(y * (double)N - cy), r2 = (T)(z * (double)N - cz);
+      const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
+      const T a = (T)pr.a;
+      const T v2 = q0 * q0 + q1 * q1 + q2 * q2;
+      const T e2 = v2 + a * a;
+      T ph = (T)0, ch = (T)0;
+      const T w000 = s0 * s1 * s2, w100 = r0 * s1 * s2, w010 = s0 * r1 * s2, w110 = r0 * r1 * s2;
+      const T w001 = s0 * s1 * r2, w101 = r0 * s1 * r2, w011 = s0 * r1 * r2, w111 = r0 * r1 * r2;
+      if (pr.nfield >= 1)
+        ph = F(phi, cx, cy, cz, N) * w000 + F(phi, cx + 1, cy, cz, N) * w100 + F(phi, cx, cy + 1, cz, N) * w010 +
+             F(phi, cx + 1, cy + 1, cz, N) * w110 + F(phi, cx, cy, cz + 1, N) * w001 +
+             F(phi, cx + 1, cy, cz + 1, N) * w101 + F(phi, cx, cy + 1, cz + 1, N) * w011 +
+             F(phi, cx + 1, cy + 1, cz + 1, N) * w111;
+      if (pr.nfield >= 2)
+        ch = F(chi, cx, cy, cz, N) * w000 + F(chi, cx + 1, cy, cz, N) * w100 + F(chi, cx, cy + 1, cz, N) * w010 +
+             F(chi, cx + 1, cy + 1, cz, N) * w110 + F(chi, cx, cy, cz + 1, N) * w001 +
+             F(chi, cx + 1, cy, cz + 1, N) * w101 + F(chi, cx, cy + 1, cz + 1, N) * w011 +
+             F(chi, cx + 1, cy + 1, cz + 1, N) * w111;
+      const T inv_e2 = (T)1 / e2;
+      const T fac = ((T)1 + ((T)3 - v2 * inv_e2) * ph - ch) * sqrt(inv_e2);
+      T v0 = q0 * fac, v1 = q1 * fac, vv2 = q2 * fac;
+      if (pr.nfield >= 3) {
+        const T *B0 = Bi, *B1 = Bi + NV, *B2 = Bi + 2 * NV;
+        T b0 = F(B0, cx, cy, cz, N) * s1 * s2 + F(B0, cx, cy + 1, cz, N) * r1 * s2 + F(B0, cx, cy, cz + 1, N) * s1 * r2 +
+               F(B0, cx, cy + 1, cz + 1, N) * r1 * r2;
+        T b1 = F(B1, cx, cy, cz, N) * s0 * s2 + F(B1, cx + 1, cy, cz, N) * r0 * s2 + F(B1, cx, cy, cz + 1, N) * s0 * r2 +
+               F(B1, cx + 1, cy, cz + 1, N) * r0 * r2;
+        T b2 = F(B2, cx, cy, cz, N) * s0 * s1 + F(B2, cx + 1, cy, cz, N) * r0 * s1 + F(B2, cx, cy + 1, cz, N) * s0 * r1 +
+               F(B2, cx + 1, cy + 1, cz, N) * r0 * r1;
+        const T ib = (T)pr.inv_a2N;
+        v0 += b0 * ib;
+        v1 += b1 * ib;
+        vv2 += b2 * ib;
+      }
+      x += pr.dtau * (double)v0;
+      y += pr.dtau * (double)v1;
+      z += pr.dtau * (double)vv2;
+    }
+    x = wrap01(x);
+    y = wrap01(y);
+    z = wrap01(z);
+    P.px[i] = x;
+    P.py[i] = y;
+    P.pz[i] = z;
+    P.cell[i] = cell_key(x, y, z, N);
+  }
+}
+
+template <typename V>
+size_t vbytes() {
+  return sizeof(V);
+}
+
+int alloc_arrays(gev_ctx *ctx, PclsArrays &A, long cap, size_t vsz) {
+  const size_t n = (size_t)cap;
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.px, n * 8));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.py, n * 8));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.pz, n * 8));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.vx, n * vsz));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.vy, n * vsz));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.vz, n * vsz));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.id, n * 8));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.cell, n * 4));
+  ctx->bytes_in_use += n * (8 * 4 + 4 + 3 * vsz);
+  return GEV_OK;
+}
+void free_arrays(PclsArrays &A) {
+  cudaFree(A.px);
+  cudaFree(A.py);
+  cudaFree(A.pz);
+  cudaFree(A.vx);
+  cudaFree(A.vy);
+  cudaFree(A.vz);
+  cudaFree(A.id);
+  cudaFree(A.cell);
+  A = PclsArrays();
+}
+
+int scan_cells(gev_ctx *ctx, gev_pcls *p) {
+  const long C = (long)ctx->N * ctx->N * ctx->N;
+  const long nb = (C + SCAN_TILE - 1) / SCAN_TILE;
+  k_scan_reduce<<<(unsigned)nb, SCAN_T, 0, ctx->stream>>>(p->count, C, p->scan_tmp);
+  GEV_LAUNCH_CHECK(ctx);
+  k_scan_blocks<<<1, 1024, 0, ctx->stream>>>(p->scan_tmp, nb);
+  GEV_LAUNCH_CHECK(ctx);
+  k_scan_down<<<(unsigned)nb, SCAN_T, 0, ctx->stream>>>(p->count, C, p->scan_tmp, p->start, (uint32_t)p->n);
+  GEV_LAUNCH_CHECK(ctx);
+  return GEV_OK;
+}
+
+template <typename T, typename V>
+int launch_update_q(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
+                    const gev_field *Bi, int nfield, double a, double a2N, unsigned long long *mb) {
+  Params pr{dtau, a, a2N, 1.0 / (a * a), 1.0 / a2N, nfield, ctx->N};
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(mb, 0, sizeof(unsigned long long), ctx->stream));
+  const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
+  const T *fphi = (const T *)phi->d, *fchi = chi ? (const T *)chi->d : nullptr, *fB = Bi ? (const T *)Bi->d : nullptr;
+  if (kind == GEV_GR)
+    k_update_q<T, V, GEV_GR><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, fphi, fchi, fB, pr, mb);
+  else
+    k_update_q<T, V, GEV_NEWTON><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, fphi, fchi, fB, pr, mb);
+  GEV_LAUNCH_CHECK(ctx);
+  return GEV_OK;
+}
+
+template <typename T, typename V>
+int update_pos_t(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
+                 const gev_field *Bi, int nfield, double a, double a2N) {
+  Params pr{dtau, a, a2N, 1.0 / (a * a), 1.0 / a2N, nfield, ctx->N};
+  const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
+  const T *fphi = phi ? (const T *)phi->d : nullptr, *fchi = chi ? (const T *)chi->d : nullptr,
+          *fB = Bi ? (const T *)Bi->d : nullptr;
+  if (kind == GEV_GR)
+    k_update_pos<T, V, GEV_GR><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, fphi, fchi, fB, pr);
+  else
+    k_update_pos<T, V, GEV_NEWTON><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, fphi, fchi, fB, pr);
+  GEV_LAUNCH_CHECK(ctx);
+  return pcls_relink(ctx, p);
+}
+
+bool field_ok(gev_ctx *ctx, const gev_field *f, int ncomp) {
+  return f && f->ctx == ctx && f->kind == GEV_FIELD_REAL && f->ncomp == ncomp;
+}
+
+}  // namespace
+
+int pcls_kick_async(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
+                    const gev_field *Bi, int nfield, double a, double a2N, unsigned long long *maxbits_dev) {
+  if (nfield < 2) chi = nullptr;
+  if (nfield < 3) Bi = nullptr;
+  return ctx->prec == GEV_PREC_FP64
+             ? launch_update_q<double, double>(ctx, p, kind, dtau, phi, chi, Bi, nfield, a, a2N, maxbits_dev)
+             : launch_update_q<float, float>(ctx, p, kind, dtau, phi, chi, Bi, nfield, a, a2N, maxbits_dev);
+}
+
+int pcls_relink(gev_ctx *ctx, gev_pcls *p) {
+  const long C = (long)ctx->N * ctx->N * ctx->N;
+  if (p->n == 0) {
+    GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->start, 0, (C + 1) * sizeof(uint32_t), ctx->stream));
+    return GEV_OK;
+  }
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->count, 0, C * sizeof(uint32_t), ctx->stream));
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->big, 0, sizeof(uint32_t), ctx->stream));
+  const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
+  k_count<<<pb, 256, 0, ctx->stream>>>(p->cur.cell, p->n, p->count, p->rank);
+  GEV_LAUNCH_CHECK(ctx);
+  int rc = scan_cells(ctx, p);
+  if (rc) return rc;
+  k_scatter<<<pb, 256, 0, ctx->stream>>>(p->cur.cell, p->rank, p->n, p->start, p->perm);
+  GEV_LAUNCH_CHECK(ctx);
+  k_canon<<<grid_for(ctx, (size_t)C, 256, 16), 256, 0, ctx->stream>>>(p->start, C, p->cur.id, p->perm, p->big);
+  GEV_LAUNCH_CHECK(ctx);
+  k_canon_big<<<ctx->sms * 2, 256, 0, ctx->stream>>>(p->start, p->cur.id, p->perm, p->rank, p->big);
+  GEV_LAUNCH_CHECK(ctx);
+  if (ctx->prec == GEV_PREC_FP64)
+    k_gather<double><<<pb, 256, 0, ctx->stream>>>(p->cur, p->alt, p->perm, p->n);
+  else
+    k_gather<float><<<pb, 256, 0, ctx->stream>>>(p->cur, p->alt, p->perm, p->n);
+  GEV_LAUNCH_CHECK(ctx);
+  std::swap(p->cur, p->alt);
+  return GEV_OK;
+}
+
+extern "C" {
+
+int gev_pcls_create(gev_ctx *ctx, long capacity, double mass, gev_pcls **out) {
+  if (!ctx || !out || capacity < 0 || capacity > 0xFFFFFFFFL) return gev_fail(ctx, GEV_EINVAL, "pcls_create: bad capacity");
+  gev_pcls *p = new gev_pcls();
+  p->ctx = ctx;
+  p->cap = capacity;
+  p->mass = mass;
+  const size_t vsz = ctx->prec == GEV_PREC_FP64 ? 8 : 4;
+  const long C = (long)ctx->N * ctx->N * ctx->N;
+  const long cap = capacity > 0 ? capacity : 1;
+  int rc = alloc_arrays(ctx, p->cur, cap, vsz);
+  if (!rc) rc = alloc_arrays(ctx, p->alt, cap, vsz);
+  if (!rc) {
+    p->scan_tmp_elems = (size_t)((C + SCAN_TILE - 1) / SCAN_TILE) + 1;
+    if (cudaMalloc(&p->count, C * 4) != cudaSuccess || cudaMalloc(&p->start, (C + 1) * 4) != cudaSuccess ||
+        cudaMalloc(&p->rank, cap * 4) != cudaSuccess || cudaMalloc(&p->perm, cap * 4) != cudaSuccess ||
+        cudaMalloc(&p->big, (C + 1) * 4) != cudaSuccess ||
+        cudaMalloc(&p->scan_tmp, p->scan_tmp_elems * 4) != cudaSuccess)
+      rc = gev_fail(ctx, GEV_ENOMEM, "pcls_create: device allocation failed");
+    else
+      ctx->bytes_in_use += (size_t)C * 12 + (size_t)cap * 8 + p->scan_tmp_elems * 4;
+  }
+  if (rc) {
+    gev_pcls_destroy(p);
+    cudaGetLastError();
+    return rc == GEV_ECUDA ? GEV_ENOMEM : rc;
+  }
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->start, 0, (C + 1) * 4, ctx->stream));
+  *out = p;
+  return GEV_OK;
+}
+
+int gev_pcls_destroy(gev_pcls *p) {
+  if (!p) return GEV_OK;
+  free_arrays(p->cur);
+  free_arrays(p->alt);
+  cudaFree(p->count);
+  cudaFree(p->start);
+  cudaFree(p->rank);
+  cudaFree(p->perm);
+  cudaFree(p->big);
+  cudaFree(p->scan_tmp);
+  delete p;
+  return GEV_OK;
+}
+
+int gev_pcls_upload(gev_pcls *p, const gev_part *host, long n) {
+  if (!p || (n > 0 && !host) || n < 0 || n > p->cap) return gev_fail(p ? p->ctx : nullptr, GEV_EINVAL, "pcls_upload: n exceeds capacity");
+  gev_ctx *ctx = p->ctx;
+  p->n = n;
+  if (n > 0) {
+    gev_part *d = nullptr;
+    GEV_CHECK_CUDA(ctx, cudaMallocAsync(&d, n * sizeof(gev_part), ctx->stream));
+    GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(d, host, n * sizeof(gev_part), cudaMemcpyHostToDevice, ctx->stream));
+    const int b = grid_for(ctx, (size_t)n, 256, 16);
+    if (ctx->prec == GEV_PREC_FP64)
+      k_unpack<double><<<b, 256, 0, ctx->stream>>>(d, n, p->cur, ctx->N);
+    else
+      k_unpack<float><<<b, 256, 0, ctx->stream>>>(d, n, p->cur, ctx->N);
+    GEV_LAUNCH_CHECK(ctx);
+    GEV_CHECK_CUDA(ctx, cudaFreeAsync(d, ctx->stream));
+  }
+  return pcls_relink(ctx, p);
+}
+
+int gev_pcls_download(gev_pcls *p, gev_part *host, long *n) {
+  if (!p || (!host && p->n > 0)) return gev_fail(p ? p->ctx : nullptr, GEV_EINVAL, "pcls_download: null buffer");
+  gev_ctx *ctx = p->ctx;
+  if (n) *n = p->n;
+  if (p->n > 0) {
+    gev_part *d = nullptr;
+    GEV_CHECK_CUDA(ctx, cudaMallocAsync(&d, p->n * sizeof(gev_part), ctx->stream));
+    const int b = grid_for(ctx, (size_t)p->n, 256, 16);
+    if (ctx->prec == GEV_PREC_FP64)
+      k_pack<double><<<b, 256, 0, ctx->stream>>>(d, p->n, p->cur);
+    else
+      k_pack<float><<<b, 256, 0, ctx->stream>>>(d, p->n, p->cur);
+    GEV_LAUNCH_CHECK(ctx);
+    GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(host, d, p->n * sizeof(gev_part), cudaMemcpyDeviceToHost, ctx->stream));
+    GEV_CHECK_CUDA(ctx, cudaFreeAsync(d, ctx->stream));
+  }
+  GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  return GEV_OK;
+}
+
+int gev_pcls_count(gev_pcls *p, long *n) {
+  if (!p || !n) return GEV_EINVAL;
+  *n = p->n;
+  return GEV_OK;
+}
+
+int gev_update_q(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
+                 const gev_field *Bi, int nfield, double a, double a2N, double *maxvel) {
+  if (!ctx || !p || p->ctx != ctx || (kind != GEV_GR && kind != GEV_NEWTON) || nfield < 1 || !field_ok(ctx, phi, 1) ||
+      (nfield >= 2 && !field_ok(ctx, chi, 1)) || (kind == GEV_GR && nfield >= 3 && !field_ok(ctx, Bi, 3)) || a <= 0.)
+    return gev_fail(ctx, GEV_EINVAL, "update_q: needs phi (and chi for nfield>=2, Bi for nfield>=3) and a > 0");
+  if (nfield < 2) chi = nullptr;
+  if (nfield < 3) Bi = nullptr;
+  int rc = ctx_ensure_red(ctx, 2);
+  if (rc) return rc;
+  unsigned long long *mb = (unsigned long long *)ctx->d_red;
+  rc = pcls_kick_async(ctx, p, kind, dtau, phi, chi, Bi, nfield, a, a2N, mb);
+  if (rc) return rc;
+  if (maxvel) {
+    unsigned long long bits = 0;
+    GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(&bits, mb, sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream));
+    GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double m;
+    memcpy(&m, &bits, sizeof(m));
+    *maxvel = sqrt(m);
+  }
+  return GEV_OK;
+}
+
+int gev_update_pos(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
+                   const gev_field *Bi, int nfield, double a, double a2N) {
+  if (!ctx || !p || p->ctx != ctx || (kind != GEV_GR && kind != GEV_NEWTON) || a <= 0. || nfield < 0 ||
+      (kind == GEV_GR && ((nfield >= 1 && !field_ok(ctx, phi, 1)) || (nfield >= 2 && !field_ok(ctx, chi, 1)) ||
+                          (nfield >= 3 && !field_ok(ctx, Bi, 3)))))
+    return gev_fail(ctx, GEV_EINVAL, "update_pos: needs phi/chi/Bi for nfield >= 1/2/3 and a > 0");
+  if (kind == GEV_NEWTON) nfield = 0;
+  if (nfield < 1) phi = nullptr;
+  if (nfield < 2) chi = nullptr;
+  if (nfield < 3) Bi = nullptr;
+  return ctx->prec == GEV_PREC_FP64
+             ? update_pos_t<double, double>(ctx, p, kind, dtau, phi, chi, Bi, nfield, a, a2N)
+             : update_pos_t<float, float>(ctx, p, kind, dtau, phi, chi, Bi, nfield, a, a2N);
+}
+
+}  // extern "C"

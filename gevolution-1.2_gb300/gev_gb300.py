@@ -1,0 +1,444 @@
+"""Python front end of libgev_gb300.so over its C-ABI (include/gev_gb300.h).
+
+This is the binding the tests and bench.py use; it mirrors the reference's
+objects -- Field<Real>, Field<Cplx>, Particles -- as device-resident handles
+and calls the GPU kernels through ctypes.  There is no CPU fallback: if the
+library or a GPU is missing every call raises GevError.
+
+Host arrays use the oracle's layouts: real fields (ncomp, N, N, N) float64
+indexed [c, z, y, x]; spectra (ncomp, N, N, N//2+1) complex128 indexed
+[c, kz, ky, kx]; particles are records of PART.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgev_gb300.so")
+PART = np.dtype([("pos", "<f8", (3,)), ("vel", "<f8", (3,)), ("ID", "<i8")])
+
+OK, EINVAL, ENOMEM, ECUDA, ETIMEOUT, ENODEV = 0, -1, -2, -3, -4, -5
+PREC_FP64, PREC_MIXED = 0, 1
+FIELD_REAL, FIELD_SPECTRUM = 0, 1
+GR, NEWTON = 0, 1
+
+_vp = ctypes.c_void_p
+_d = ctypes.c_double
+_i = ctypes.c_int
+_l = ctypes.c_long
+
+
+class GevError(RuntimeError):
+    pass
+
+
+_lib = None
+
+_SIGS = {
+    "gev_ctx_create": [_i, _i, _i, ctypes.POINTER(_vp)],
+    "gev_ctx_destroy": [_vp],
+    "gev_ctx_sync": [_vp],
+    "gev_ctx_stream": [_vp, ctypes.POINTER(_vp)],
+    "gev_ctx_info": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_size_t)],
+    "gev_ctx_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "gev_field_create": [_vp, _i, _i, ctypes.POINTER(_vp)],
+    "gev_field_destroy": [_vp],
+    "gev_field_upload": [_vp, _vp],
+    "gev_field_download": [_vp, _vp],
+    "gev_field_zero": [_vp],
+    "gev_field_device_ptr": [_vp, ctypes.POINTER(_vp), ctypes.POINTER(ctypes.c_size_t)],
+    "gev_pcls_create": [_vp, _l, _d, ctypes.POINTER(_vp)],
+    "gev_pcls_destroy": [_vp],
+    "gev_pcls_upload": [_vp, _vp, _l],
+    "gev_pcls_download": [_vp, _vp, ctypes.POINTER(_l)],
+    "gev_pcls_count": [_vp, ctypes.POINTER(_l)],
+    "gev_projection_T00": [_vp, _vp, _vp, _d, _vp, _d],
+    "gev_projection_T0i": [_vp, _vp, _vp, _vp, _d],
+    "gev_projection_Tij": [_vp, _vp, _vp, _d, _vp, _d],
+    "gev_projection_mass": [_vp, _vp, _vp],
+    "gev_prepare_source_tensor": [_vp, _vp, _vp, _vp, _d],
+    "gev_prepare_source_scalar": [_vp, _vp, _vp, _vp, _d, _vp, _d, _d, _d],
+    "gev_fft_r2c": [_vp, _vp, _vp],
+    "gev_fft_c2r": [_vp, _vp, _vp],
+    "gev_solve_poisson": [_vp, _vp, _vp, _d, _d],
+    "gev_project_scalar": [_vp, _vp, _vp, _i],
+    "gev_evolve_vector": [_vp, _vp, _vp, _d],
+    "gev_project_vector": [_vp, _vp, _vp, _d, _d],
+    "gev_project_tensor": [_vp, _vp, _vp],
+    "gev_update_q": [_vp, _vp, _i, _d, _vp, _vp, _vp, _i, _d, _d, ctypes.POINTER(_d)],
+    "gev_update_pos": [_vp, _vp, _i, _d, _vp, _vp, _vp, _i, _d, _d],
+    "gev_field_sum": [_vp, _vp, _i, ctypes.POINTER(_d)],
+}
+
+
+def lib():
+    """Loads libgev_gb300.so (building it first if the sources are newer)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise GevError("libgev_gb300.so is not built: run __graft_entry__.build() or "
+                           "python gevolution-1.2_gb300/build.py")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L.gev_strerror.restype = ctypes.c_char_p
+        L.gev_strerror.argtypes = [_i]
+        L.gev_ctx_last_error.restype = ctypes.c_char_p
+        L.gev_ctx_last_error.argtypes = [_vp]
+        _lib = L
+    return _lib
+
+
+def _check(rc, ctx=None, what=""):
+    if rc != OK:
+        msg = lib().gev_strerror(rc).decode()
+        if ctx is not None and ctx.handle:
+            detail = lib().gev_ctx_last_error(ctx.handle)
+            if detail:
+                msg += ": " + detail.decode()
+        raise GevError("%s failed (%d): %s" % (what, rc, msg))
+
+
+def _h(obj):
+    return None if obj is None else obj.handle
+
+
+class Context:
+    """One grid of N^3 cells on one GPU (the Lattice / latFT pair of main.cpp:213-215)."""
+
+    def __init__(self, N, precision=PREC_FP64, device=0):
+        self.handle = None
+        h = _vp()
+        _check(lib().gev_ctx_create(device, N, precision, ctypes.byref(h)), None, "gev_ctx_create(N=%d)" % N)
+        self.handle = h.value
+        self.N = N
+        self.precision = precision
+
+    def close(self):
+        if self.handle:
+            lib().gev_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        _check(lib().gev_ctx_sync(self.handle), self, "gev_ctx_sync")
+
+    def stream(self):
+        s = _vp()
+        _check(lib().gev_ctx_stream(self.handle, ctypes.byref(s)), self, "gev_ctx_stream")
+        return s.value
+
+    def launches(self):
+        n = ctypes.c_longlong()
+        _check(lib().gev_ctx_launch_count(self.handle, ctypes.byref(n)), self, "gev_ctx_launch_count")
+        return n.value
+
+    def bytes_in_use(self):
+        b = ctypes.c_size_t()
+        _check(lib().gev_ctx_info(self.handle, None, None, ctypes.byref(b)), self, "gev_ctx_info")
+        return b.value
+
+    # factories
+    def real(self, ncomp=1):
+        return Field(self, FIELD_REAL, ncomp)
+
+    def spectrum(self, ncomp=1):
+        return Field(self, FIELD_SPECTRUM, ncomp)
+
+    def particles(self, capacity, mass):
+        return Particles(self, capacity, mass)
+
+
+class Field:
+    def __init__(self, ctx, kind, ncomp):
+        self.ctx = ctx
+        self.kind = kind
+        self.ncomp = ncomp
+        self.handle = None
+        h = _vp()
+        _check(lib().gev_field_create(ctx.handle, kind, ncomp, ctypes.byref(h)), ctx, "gev_field_create")
+        self.handle = h.value
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().gev_field_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+    @property
+    def shape(self):
+        N = self.ctx.N
+        return (self.ncomp, N, N, N) if self.kind == FIELD_REAL else (self.ncomp, N, N, N // 2 + 1)
+
+    def upload(self, arr):
+        dt = np.float64 if self.kind == FIELD_REAL else np.complex128
+        a = np.ascontiguousarray(np.asarray(arr, dtype=dt).reshape(self.shape))
+        _check(lib().gev_field_upload(self.handle, a.ctypes.data), self.ctx, "gev_field_upload")
+        return self
+
+    def download(self):
+        dt = np.float64 if self.kind == FIELD_REAL else np.complex128
+        out = np.empty(self.shape, dt)
+        _check(lib().gev_field_download(self.handle, out.ctypes.data), self.ctx, "gev_field_download")
+        return out
+
+    def zero(self):
+        _check(lib().gev_field_zero(self.handle), self.ctx, "gev_field_zero")
+        return self
+
+    def device_ptr(self):
+        p = _vp()
+        n = ctypes.c_size_t()
+        _check(lib().gev_field_device_ptr(self.handle, ctypes.byref(p), ctypes.byref(n)), self.ctx,
+               "gev_field_device_ptr")
+        return p.value, n.value
+
+    def sum(self, comp=0):
+        out = _d()
+        _check(lib().gev_field_sum(self.ctx.handle, self.handle, comp, ctypes.byref(out)), self.ctx, "gev_field_sum")
+        return out.value
+
+
+class Particles:
+    def __init__(self, ctx, capacity, mass):
+        self.ctx = ctx
+        self.handle = None
+        h = _vp()
+        _check(lib().gev_pcls_create(ctx.handle, capacity, mass, ctypes.byref(h)), ctx, "gev_pcls_create")
+        self.handle = h.value
+        self.mass = mass
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().gev_pcls_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+    def upload(self, parts):
+        p = np.ascontiguousarray(parts, dtype=PART)
+        _check(lib().gev_pcls_upload(self.handle, p.ctypes.data if len(p) else None, len(p)), self.ctx,
+               "gev_pcls_upload")
+        return self
+
+    def count(self):
+        n = _l()
+        _check(lib().gev_pcls_count(self.handle, ctypes.byref(n)), self.ctx, "gev_pcls_count")
+        return n.value
+
+    def download(self):
+        out = np.empty(self.count(), PART)
+        n = _l()
+        _check(lib().gev_pcls_download(self.handle, out.ctypes.data if len(out) else None, ctypes.byref(n)),
+               self.ctx, "gev_pcls_download")
+        return out
+
+
+# ------------------------------------------------- reference-named operations --
+def projection_T00(pcls, T00, a=1.0, phi=None, coeff=1.0):
+    _check(lib().gev_projection_T00(pcls.ctx.handle, pcls.handle, T00.handle, a, _h(phi), coeff), pcls.ctx,
+           "gev_projection_T00")
+
+
+def projection_T0i(pcls, T0i, phi=None, coeff=1.0):
+    _check(lib().gev_projection_T0i(pcls.ctx.handle, pcls.handle, T0i.handle, _h(phi), coeff), pcls.ctx,
+           "gev_projection_T0i")
+
+
+def projection_Tij(pcls, Tij, a=1.0, phi=None, coeff=1.0):
+    _check(lib().gev_projection_Tij(pcls.ctx.handle, pcls.handle, Tij.handle, a, _h(phi), coeff), pcls.ctx,
+           "gev_projection_Tij")
+
+
+def projection_mass(pcls, rho):
+    _check(lib().gev_projection_mass(pcls.ctx.handle, pcls.handle, rho.handle), pcls.ctx, "gev_projection_mass")
+
+
+def prepare_source_tensor(phi, Tij, Sij, coeff):
+    _check(lib().gev_prepare_source_tensor(phi.ctx.handle, phi.handle, Tij.handle, Sij.handle, coeff), phi.ctx,
+           "gev_prepare_source_tensor")
+
+
+def prepare_source_scalar(phi, chi, source, bgmodel, result, coeff, coeff2, coeff3):
+    _check(lib().gev_prepare_source_scalar(phi.ctx.handle, phi.handle, chi.handle, source.handle, bgmodel,
+                                           result.handle, coeff, coeff2, coeff3), phi.ctx, "gev_prepare_source_scalar")
+
+
+def fft_r2c(real, spec):
+    _check(lib().gev_fft_r2c(real.ctx.handle, real.handle, spec.handle), real.ctx, "gev_fft_r2c")
+
+
+def fft_c2r(spec, real):
+    _check(lib().gev_fft_c2r(spec.ctx.handle, spec.handle, real.handle), spec.ctx, "gev_fft_c2r")
+
+
+def solve_poisson(srcFT, potFT, coeff, modif=0.0):
+    _check(lib().gev_solve_poisson(srcFT.ctx.handle, srcFT.handle, potFT.handle, coeff, modif), srcFT.ctx,
+           "gev_solve_poisson")
+
+
+def project_scalar(SijFT, chiFT, add=0):
+    _check(lib().gev_project_scalar(SijFT.ctx.handle, SijFT.handle, chiFT.handle, add), SijFT.ctx,
+           "gev_project_scalar")
+
+
+def evolve_vector(SijFT, BiFT, a2dtau):
+    _check(lib().gev_evolve_vector(SijFT.ctx.handle, SijFT.handle, BiFT.handle, a2dtau), SijFT.ctx,
+           "gev_evolve_vector")
+
+
+def project_vector(SiFT, BiFT, coeff=1.0, modif=0.0):
+    _check(lib().gev_project_vector(SiFT.ctx.handle, SiFT.handle, BiFT.handle, coeff, modif), SiFT.ctx,
+           "gev_project_vector")
+
+
+def project_tensor(SijFT, hijFT):
+    _check(lib().gev_project_tensor(SijFT.ctx.handle, SijFT.handle, hijFT.handle), SijFT.ctx, "gev_project_tensor")
+
+
+def update_q(pcls, kind, dtau, phi, chi, Bi, nfield, a, a2N):
+    out = _d()
+    _check(lib().gev_update_q(pcls.ctx.handle, pcls.handle, kind, dtau, _h(phi), _h(chi), _h(Bi), nfield, a, a2N,
+                              ctypes.byref(out)), pcls.ctx, "gev_update_q")
+    return out.value
+
+
+def update_pos(pcls, kind, dtau, phi, chi, Bi, nfield, a, a2N):
+    _check(lib().gev_update_pos(pcls.ctx.handle, pcls.handle, kind, dtau, _h(phi), _h(chi), _h(Bi), nfield, a, a2N),
+           pcls.ctx, "gev_update_pos")
+
+
+# ------------------------------------------------------------- simulation --
+class Cosmology(ctypes.Structure):
+    _fields_ = [(n, _d) for n in ("Omega_cdm", "Omega_b", "Omega_m", "Omega_Lambda", "Omega_rad")]
+
+
+class SimState(ctypes.Structure):
+    _fields_ = [(n, _d) for n in ("a", "tau", "dtau", "dtau_old", "fourpiG", "Cf", "steplimit", "z_relax", "maxvel",
+                                  "T00hom", "phik0", "mass")] + [
+        ("cosmo", Cosmology), ("vector_elliptic", _i), ("cycle", _i)]
+
+
+_SIM_SIGS = {
+    "gev_sim_create": [_vp, _l, ctypes.POINTER(_vp)],
+    "gev_sim_destroy": [_vp],
+    "gev_sim_set_state": [_vp, ctypes.POINTER(SimState)],
+    "gev_sim_get_state": [_vp, ctypes.POINTER(SimState)],
+    "gev_sim_field": [_vp, _i, ctypes.POINTER(_vp)],
+    "gev_sim_particles": [_vp, ctypes.POINTER(_vp)],
+    "gev_sim_step": [_vp],
+}
+
+SIM_FIELDS = {"phi": (0, FIELD_REAL, 1), "chi": (1, FIELD_REAL, 1), "source": (2, FIELD_REAL, 1),
+              "Sij": (3, FIELD_REAL, 6), "Bi": (4, FIELD_REAL, 3), "scalarFT": (5, FIELD_SPECTRUM, 1),
+              "SijFT": (6, FIELD_SPECTRUM, 6), "BiFT": (7, FIELD_SPECTRUM, 3)}
+
+
+def _sim_lib():
+    L = lib()
+    if not getattr(L, "_sim_ready", False):
+        for name, args in _SIM_SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L._sim_ready = True
+    return L
+
+
+class _View:
+    """Non-owning handle onto an object that a Sim owns."""
+
+    def __del__(self):
+        pass
+
+
+class Sim:
+    """Device state of one simulation and the main-loop cycle (include/gev_sim.h)."""
+
+    def __init__(self, ctx, npart):
+        self.ctx = ctx
+        self.handle = None
+        h = _vp()
+        _check(_sim_lib().gev_sim_create(ctx.handle, npart, ctypes.byref(h)), ctx, "gev_sim_create")
+        self.handle = h.value
+        self._views = {}
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _sim_lib().gev_sim_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+    def field(self, name):
+        if name not in self._views:
+            which, kind, ncomp = SIM_FIELDS[name]
+            h = _vp()
+            _check(_sim_lib().gev_sim_field(self.handle, which, ctypes.byref(h)), self.ctx, "gev_sim_field")
+            f = Field.__new__(Field)
+            f.ctx, f.kind, f.ncomp, f.handle = self.ctx, kind, ncomp, None
+            f._borrowed = h.value
+            self._views[name] = f
+        f = self._views[name]
+        return _Borrowed(f)
+
+    def particles(self):
+        h = _vp()
+        _check(_sim_lib().gev_sim_particles(self.handle, ctypes.byref(h)), self.ctx, "gev_sim_particles")
+        p = _BorrowedParticles(self.ctx, h.value)
+        return p
+
+    def set_state(self, **kw):
+        st = self.get_state_struct()
+        for k, v in kw.items():
+            if k == "cosmo":
+                for ck, cv in v.items():
+                    setattr(st.cosmo, ck, cv)
+            else:
+                setattr(st, k, v)
+        _check(_sim_lib().gev_sim_set_state(self.handle, ctypes.byref(st)), self.ctx, "gev_sim_set_state")
+
+    def get_state_struct(self):
+        st = SimState()
+        _check(_sim_lib().gev_sim_get_state(self.handle, ctypes.byref(st)), self.ctx, "gev_sim_get_state")
+        return st
+
+    def state(self):
+        st = self.get_state_struct()
+        d = {k: getattr(st, k) for k, _ in SimState._fields_ if k != "cosmo"}
+        d["cosmo"] = {k: getattr(st.cosmo, k) for k, _ in Cosmology._fields_}
+        return d
+
+    def step(self):
+        _check(_sim_lib().gev_sim_step(self.handle), self.ctx, "gev_sim_step")
+
+
+class _Borrowed(Field):
+    def __init__(self, f):
+        self.ctx, self.kind, self.ncomp = f.ctx, f.kind, f.ncomp
+        self.handle = f._borrowed
+
+    def __del__(self):
+        pass
+
+
+class _BorrowedParticles(Particles):
+    def __init__(self, ctx, handle):
+        self.ctx = ctx
+        self.handle = handle
+        self.mass = None
+
+    def __del__(self):
+        pass

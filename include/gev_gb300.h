@@ -1,0 +1,142 @@
+/*
+ * gev_gb300.h -- C-ABI of the GB300 implementation of gevolution 1.2's
+ * per-step particle-mesh hot path.
+ *
+ * One context owns one simulation grid (N^3 cells) on one GPU and one CUDA
+ * stream.  Fields, spectra and particle stores are device-resident objects of
+ * a context; every entry point enqueues work on the context's stream and
+ * returns a status code (GEV_OK = 0).  Host buffers passed in or out are plain
+ * arrays in the layouts below.  Nothing here falls back to the CPU: a missing
+ * GPU or extension is an error.
+ *
+ * Host layouts (shared with the CPU oracle):
+ *   real field   double[ncomp][N][N][N]            index c*N^3 + x + N*(y + N*z)
+ *   spectrum     double[ncomp][N][N][N/2+1][2]     interleaved complex, kx fastest
+ *   symmetric tensors store the components 00, 01, 02, 11, 12, 22
+ *   particles    gev_part records {pos[3], vel[3], ID} (gevolution's part_simple)
+ *
+ * Each function names the gevolution-1.2 interface it replaces (file:line).
+ */
+#ifndef GEV_GB300_H
+#define GEV_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---- */
+#define GEV_OK 0
+#define GEV_EINVAL -1   /* bad argument (sizes, kinds, null handles) */
+#define GEV_ENOMEM -2   /* device allocation failed */
+#define GEV_ECUDA -3    /* CUDA runtime / launch error */
+#define GEV_ETIMEOUT -4 /* a bounded device wait gave up */
+#define GEV_ENODEV -5   /* no usable GPU */
+
+/* ---- precision forms ---- */
+#define GEV_PREC_FP64 0  /* fields, spectra, FFTs, deposits and particles in FP64 */
+#define GEV_PREC_MIXED 1 /* FP32 fields/FFTs/momenta, FP64 positions, int64 fixed-point deposits */
+
+/* ---- object kinds ---- */
+#define GEV_FIELD_REAL 0
+#define GEV_FIELD_SPECTRUM 1
+
+/* ---- particle update kinds (the callbacks passed to updateVel / moveParticles) ---- */
+#define GEV_GR 0     /* update_q / update_pos            gevolution.hpp:570, 810 */
+#define GEV_NEWTON 1 /* update_q_Newton / update_pos_Newton gevolution.hpp:709, 900 */
+
+typedef struct {
+  double pos[3];
+  double vel[3];
+  int64_t ID;
+} gev_part;
+
+typedef struct gev_ctx gev_ctx;
+typedef struct gev_field gev_field;
+typedef struct gev_pcls gev_pcls;
+
+/* ---- context (replaces Lattice/latFT set-up, main.cpp:213-215) ---- */
+int gev_ctx_create(int device, int N, int precision, gev_ctx **out);
+int gev_ctx_destroy(gev_ctx *ctx);
+int gev_ctx_sync(gev_ctx *ctx);
+int gev_ctx_stream(gev_ctx *ctx, void **cuda_stream); /* the cudaStream_t the context enqueues on */
+int gev_ctx_info(gev_ctx *ctx, int *N, int *precision, size_t *device_bytes_in_use);
+const char *gev_ctx_last_error(gev_ctx *ctx);
+const char *gev_strerror(int status);
+/* count of kernels this library launched on the context since creation */
+int gev_ctx_launch_count(gev_ctx *ctx, long long *count);
+
+/* ---- fields (Field<Real> / Field<Cplx>::initialize, main.cpp:226-237) ---- */
+int gev_field_create(gev_ctx *ctx, int kind, int ncomp, gev_field **out);
+int gev_field_destroy(gev_field *f);
+int gev_field_upload(gev_field *f, const double *host);
+int gev_field_download(gev_field *f, double *host);
+/* projection_init (LATfield2, main.cpp:378/416/426/438): zero all components */
+int gev_field_zero(gev_field *f);
+int gev_field_device_ptr(gev_field *f, void **ptr, size_t *bytes);
+
+/* ---- particles (Particles<part_simple,...>::initialize / addParticle_global,
+ *      ic_basic.hpp:1990, 1429) ---- */
+int gev_pcls_create(gev_ctx *ctx, long capacity, double mass, gev_pcls **out);
+int gev_pcls_destroy(gev_pcls *p);
+/* copies n records in, wraps nothing, links them to their cells (counting sort) */
+int gev_pcls_upload(gev_pcls *p, const gev_part *host, long n);
+/* copies the records out in (cell, ID) order */
+int gev_pcls_download(gev_pcls *p, gev_part *host, long *n);
+int gev_pcls_count(gev_pcls *p, long *n);
+
+/* ---- stress-energy deposits; each accumulates into its target like the reference
+ *      and includes the periodic halo fold of the matching *_comm ---- */
+/* projection_T00_project + projection_T00_comm, gevolution.hpp:926-1024 */
+int gev_projection_T00(gev_ctx *ctx, gev_pcls *p, gev_field *T00, double a, const gev_field *phi, double coeff);
+/* projection_T0i_project + projection_T0i_comm, gevolution.hpp:1045-1149 */
+int gev_projection_T0i(gev_ctx *ctx, gev_pcls *p, gev_field *T0i, const gev_field *phi, double coeff);
+/* projection_Tij_project + projection_Tij_comm, gevolution.hpp:1172-1301 */
+int gev_projection_Tij(gev_ctx *ctx, gev_pcls *p, gev_field *Tij, double a, const gev_field *phi, double coeff);
+/* scalarProjectionCIC_project + _comm (LATfield2; main.cpp:402, ic_basic.hpp:2180) */
+int gev_projection_mass(gev_ctx *ctx, gev_pcls *p, gev_field *rho);
+
+/* ---- real-space sources ---- */
+/* prepareFTsource (tensor), gevolution.hpp:56-147; Sij may equal Tij */
+int gev_prepare_source_tensor(gev_ctx *ctx, const gev_field *phi, const gev_field *Tij, gev_field *Sij, double coeff);
+/* prepareFTsource (scalar), gevolution.hpp:169-192; result may equal source */
+int gev_prepare_source_scalar(gev_ctx *ctx, const gev_field *phi, const gev_field *chi, const gev_field *source,
+                              double bgmodel, gev_field *result, double coeff, double coeff2, double coeff3);
+
+/* ---- FFT (PlanFFT<Cplx>::execute, main.cpp:477-596); all components ---- */
+int gev_fft_r2c(gev_ctx *ctx, const gev_field *real, gev_field *spectrum);
+/* backward transform; never modifies its input spectrum */
+int gev_fft_c2r(gev_ctx *ctx, const gev_field *spectrum, gev_field *real);
+
+/* ---- k-space operators ---- */
+int gev_solve_poisson(gev_ctx *ctx, const gev_field *srcFT, gev_field *potFT, double coeff,
+                      double modif); /* solveModifiedPoissonFT, gevolution.hpp:501 */
+int gev_project_scalar(gev_ctx *ctx, const gev_field *SijFT, gev_field *chiFT,
+                       int add); /* projectFTscalar, gevolution.hpp:211 */
+int gev_evolve_vector(gev_ctx *ctx, const gev_field *SijFT, gev_field *BiFT,
+                      double a2dtau); /* evolveFTvector, gevolution.hpp:284 */
+int gev_project_vector(gev_ctx *ctx, const gev_field *SiFT, gev_field *BiFT, double coeff,
+                       double modif); /* projectFTvector, gevolution.hpp:350 */
+int gev_project_tensor(gev_ctx *ctx, const gev_field *SijFT,
+                       gev_field *hijFT); /* projectFTtensor, gevolution.hpp:411 */
+
+/* ---- particle updates ---- */
+/* Particles::updateVel(update_q | update_q_Newton, dtau, {phi, chi, Bi}, nfield, {a, a2N});
+ * main.cpp:775; *maxvel receives the reduction (sqrt of the maximum q^2/a^2) */
+int gev_update_q(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
+                 const gev_field *Bi, int nfield, double a, double a2N, double *maxvel);
+/* Particles::moveParticles(update_pos | update_pos_Newton, ...); main.cpp:798; the
+ * relink to the new cells is the on-device counting sort */
+int gev_update_pos(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
+                   const gev_field *Bi, int nfield, double a, double a2N);
+
+/* ---- reductions ---- */
+/* sum of one component over all cells (T00hom, main.cpp:459-463); deterministic order */
+int gev_field_sum(gev_ctx *ctx, const gev_field *f, int comp, double *out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

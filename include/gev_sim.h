@@ -1,0 +1,57 @@
+/*
+ * gev_sim.h -- the device-resident simulation state and one cycle of
+ * gevolution's main loop (main.cpp:372-879) for CDM in GR mode, on top of the
+ * hot-path C-ABI in gev_gb300.h.
+ *
+ * The state mirrors the locals of main() that the loop body reads and writes:
+ * the particles (pcls_cdm), the fields phi, chi, source, Sij, Bi and the
+ * spectra scalarFT, SijFT, BiFT (main.cpp:217-246), and the scalars a, tau,
+ * dtau, dtau_old, fourpiG and the cosmology.  gev_sim_step enqueues one cycle
+ * without waiting for the GPU; gev_sim_get_state waits and also returns the
+ * diagnostics the reference prints (T00hom, phi(k=0), max |v|).
+ */
+#ifndef GEV_SIM_H
+#define GEV_SIM_H
+
+#include "gev_gb300.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  double Omega_cdm, Omega_b, Omega_m, Omega_Lambda, Omega_rad;
+} gev_cosmology;
+
+typedef struct {
+  double a, tau, dtau, dtau_old, fourpiG, Cf, steplimit, z_relax, maxvel, T00hom, phik0, mass;
+  gev_cosmology cosmo;
+  int vector_elliptic; /* 0: parabolic (default, parser.hpp:1136), 1: elliptic */
+  int cycle;
+} gev_sim_state;
+
+/* gev_sim_field indices */
+#define GEV_SIM_PHI 0
+#define GEV_SIM_CHI 1
+#define GEV_SIM_SOURCE 2
+#define GEV_SIM_SIJ 3
+#define GEV_SIM_BI 4
+#define GEV_SIM_SCALARFT 5
+#define GEV_SIM_SIJFT 6
+#define GEV_SIM_BIFT 7
+
+typedef struct gev_sim gev_sim;
+
+int gev_sim_create(gev_ctx *ctx, long np, gev_sim **out);
+int gev_sim_destroy(gev_sim *s);
+int gev_sim_set_state(gev_sim *s, const gev_sim_state *st);
+int gev_sim_get_state(gev_sim *s, gev_sim_state *st);
+int gev_sim_field(gev_sim *s, int which, gev_field **out);
+int gev_sim_particles(gev_sim *s, gev_pcls **out);
+/* one cycle: deposits, phi / chi / B solves, kick, drift, background, next dtau */
+int gev_sim_step(gev_sim *s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,106 @@
+"""Generates the golden vectors in tests/golden/ from gevolution 1.2's own
+gevolution.hpp / background.hpp compiled against the single-rank LATfield2 shim
+(oracle/_ref/libgevref.so, built by `make -C oracle ref` where the reference
+sources are present).
+
+    python tests/golden/make_golden.py
+
+Every hot-path function is run on seeded random inputs at N = 8 and N = 12
+(a radix-3 size), and a full initial condition plus three cycles of the main
+loop are run at N = 8.  Inputs and the reference's outputs are stored in
+golden_N{8,12}.npz and golden_run_N8.npz; tests/test_oracle_golden.py checks
+the CPU restatement against them and the GPU tests check the CUDA path.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import gevoracle as G  # noqa: E402
+
+
+def particles(rng, N, n):
+    p = np.zeros(n, G.PART)
+    p["pos"] = rng.random((n, 3))
+    # edge cases: on a vertex, on cell faces, just below 1, exactly 0
+    k = min(n, 6)
+    p["pos"][:k] = np.array([[0.0, 0.0, 0.0], [1.0 / N, 2.0 / N, 0.5], [np.nextafter(1.0, 0.0)] * 3,
+                             [0.5, np.nextafter(1.0, 0.0), 0.0], [3.0 / N, 3.0 / N, 3.0 / N], [0.25, 0.75, 1.0 / N]])[:k]
+    p["vel"] = rng.standard_normal((n, 3)) * 2e-3
+    p["ID"] = rng.permutation(n * 3)[:n]
+    return p
+
+
+def one(N, seed):
+    R = G.ref()
+    rng = np.random.default_rng(seed)
+    d = {}
+    phi = rng.standard_normal((1, N, N, N)) * 1e-5
+    chi = rng.standard_normal((1, N, N, N)) * 1e-5
+    src = 0.3 + rng.standard_normal((1, N, N, N)) * 0.1
+    T = rng.standard_normal((6, N, N, N)) * 1e-3
+    Bi = rng.standard_normal((3, N, N, N)) * 1e-8
+    d.update(phi=phi, chi=chi, src=src, T=T, Bi=Bi)
+    d["out_pst"] = G.prepare_source_tensor(phi, T, 0.37, impl=R)
+    d["out_pss"] = G.prepare_source_scalar(phi, chi, src, 0.32, 1.3e-3, 2.1e-4, 3.7e-5, impl=R)
+    S = G.fft_r2c(T)
+    B = G.fft_r2c(rng.standard_normal((3, N, N, N)))
+    s1 = G.fft_r2c(src)
+    d.update(S=S, B=B, s1=s1)
+    d["out_poisson"] = G.poisson(s1, 3.0, 0.0, impl=R)
+    d["out_poisson_modif"] = G.poisson(s1, 3.0, 0.7, impl=R)
+    d["out_pscalar"] = G.project_scalar(S, None, 0, impl=R)
+    d["out_pscalar_add"] = G.project_scalar(S, s1, 1, impl=R)
+    d["out_evolve"] = G.evolve_vector(S, B, 0.013, impl=R)
+    d["out_pvector"] = G.project_vector(B, 0.3, 0.1, impl=R)
+    d["out_ptensor"] = G.project_tensor(S, impl=R)
+    n = N ** 3
+    p = particles(rng, N, n)
+    d["parts"] = p
+    for w, a in (("T00", 0.02), ("T0i", 0.02), ("Tij", 0.02)):
+        d["out_dep_" + w] = G.deposit(w, N, p, 1e-3, a, phi, 1.0, impl=R)
+    d["out_dep_T00_nophi"] = G.deposit("T00", N, p, 1e-3, 0.02, None, 1.0, impl=R)
+    a, a2N = 0.02, 0.02 ** 2 * N
+    for kind in (0, 1):
+        for nf in (1, 2, 3):
+            pk, vk = G.kick(N, p, kind, 0.011, phi, chi, Bi, nf, a, a2N, impl=R)
+            d["out_kick_%d_%d" % (kind, nf)] = pk
+            d["out_kick_max_%d_%d" % (kind, nf)] = np.array(vk)
+        for nf in (0, 1, 2, 3):
+            d["out_drift_%d_%d" % (kind, nf)] = G.drift(N, p, kind, 0.37, phi, chi, Bi, nf, a, a2N, impl=R)
+    cm = dict(Omega_cdm=0.27, Omega_b=0.05, Omega_m=0.32, Omega_Lambda=0.68, Omega_rad=0.0)
+    av = np.geomspace(0.005, 1.0, 9)
+    d["bg_a"] = av
+    d["out_hconf"] = np.array([G.hconf(x, 0.0123, cm, impl=R) for x in av])
+    d["out_rk4"] = np.array([G.rk4bg(x, 0.0123, cm, 0.5, impl=R) for x in av])
+    np.savez_compressed(os.path.join(HERE, "golden_N%d.npz" % N), **d)
+
+
+def run(N=8, steps=3):
+    R = G.ref()
+    s = G.Sim(N).ic(**G.default_icparams(N, 40.0, seed=11))
+    d = {"ic_parts": s.particles.copy(), "ic_phi": s.field("phi").copy(), "ic_chi": s.field("chi").copy(),
+         "ic_Bi": s.field("Bi").copy(), "ic_BiFT": s.spectrum("BiFT").copy(),
+         "ic_scalars": np.array([s.s.a, s.s.tau, s.s.dtau, s.s.dtau_old, s.s.fourpiG, s.s.mass, s.s.maxvel])}
+    for k in range(steps):
+        s.step(impl=R)
+        d["step%d_parts" % k] = s.particles.copy()
+        d["step%d_phi" % k] = s.field("phi").copy()
+        d["step%d_chi" % k] = s.field("chi").copy()
+        d["step%d_Bi" % k] = s.field("Bi").copy()
+        d["step%d_scalars" % k] = np.array([s.s.a, s.s.tau, s.s.dtau, s.s.dtau_old, s.s.maxvel, s.s.T00hom])
+    np.savez_compressed(os.path.join(HERE, "golden_run_N%d.npz" % N), **d)
+
+
+if __name__ == "__main__":
+    if G.ref() is None:
+        sys.exit("the reference sources are not available here; golden vectors cannot be regenerated")
+    one(8, 101)
+    one(12, 102)
+    run(8, 3)
+    for f in sorted(os.listdir(HERE)):
+        if f.endswith(".npz"):
+            print(f, os.path.getsize(os.path.join(HERE, f)))
