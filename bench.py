@@ -1,0 +1,333 @@
+"""Benchmark of the per-step particle-mesh hot path on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--grid 512] [--prec mixed|fp64]
+
+Workload (default): the precision form at 512^3 grid and 512^3 particles in a
+1 Gpc/h box (FP32 fields and FFTs, FP64 positions, int64 fixed-point
+deposits), seeded BBKS Zel'dovich initial conditions at z = 100 generated on
+the device, GR mode with phi, chi, B_i and T_ij active (parabolic vector
+method).  A step is one cycle of gevolution's main loop (main.cpp:372-879):
+the three deposits, the phi / chi / B solves with 12 FFTs, the kick, the drift
+with the relink, and the background update.  Metric: particle-steps/s.
+
+value    device-timed throughput with the state resident in HBM (CUDA events on
+         the library's stream, K cycles between two synchronised barriers);
+e2e      the same cycles through the C-ABI with the particle state copied in
+         from pinned host memory and back out every step;
+roofline the dominant kernel's algorithmic bytes per launch over its event-
+         timed duration, against the measured HBM copy bandwidth;
+cpu_baseline  the CPU restatement of the same path (oracle/) timed on this
+         host on a bounded sample (rank 0, N = 1 only).
+
+--impl reference runs the CPU implementation of the path (the oracle's port of
+the reference; the reference itself needs LATfield2, FFTW, MPI and HDF5, which
+the GPU hosts do not have) on all host cores, one independent simulation per
+core, and prints the same metric.  With --gpus N > 1 each rank runs its own
+simulation (replicas, no data exchange); the value is the sum over ranks of
+particles x steps divided by the slowest rank's time.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "gevolution-1.2_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+FALLBACK_HBM_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--grid", type=int, default=512)
+    ap.add_argument("--prec", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+# ------------------------------------------------------------ clocks --------
+class ClockSampler:
+    """nvidia-smi sampled every 200 ms during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        sm.sort()
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def hbm_peak():
+    try:
+        with open(PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return FALLBACK_HBM_GBS, "fallback"
+
+
+# ------------------------------------------------- algorithmic bytes --------
+def cycle_bytes(N, prec):
+    """Compulsory HBM bytes of one cycle: every persistent or intermediate array
+    read or written once per use, FFTs at three passes (one read and one write of
+    the array per pass).  Particles: deposit reads pos+vel, kick/drift read pos+vel
+    and write them back."""
+    r = 8 if prec == "fp64" else 4
+    V = N ** 3
+    K = N * N * (N // 2 + 1) * 2 * r  # bytes of one half spectrum component
+    pcl_state = 3 * 8 + 3 * r
+    particles = V * (pcl_state + 2 * pcl_state)
+    fields = 0
+    fields += V * r * (1 + 6)          # T00 and Tij written by the deposits
+    fields += V * r * 1                # phi read by the deposits
+    fields += V * r * 3 + V * r        # prepareFTsource (scalar): phi, chi, source in, source out
+    fields += 12 * 3 * 2 * K           # 12 FFTs x 3 passes x (read + write) of one component
+    fields += K * 2                    # Poisson in place
+    fields += V * r * 7 + V * r * 6    # prepareFTsource (tensor): phi + Sij in, Sij out
+    fields += 6 * K + K                # projectFTscalar
+    fields += 6 * K + 2 * 3 * K        # evolveFTvector (Sij in, B in/out)
+    fields += V * r * (1 + 1 + 3)      # kick/drift gather phi, chi, Bi
+    return particles + fields
+
+
+def run_ours(args, rank, world, local):
+    import torch
+    import gev_gb300 as gpu
+
+    torch.cuda.set_device(local)
+    N = args.grid
+    prec = gpu.PREC_FP64 if args.prec == "fp64" else gpu.PREC_MIXED
+    box = 1000.0 * N / 512
+    ctx = gpu.Context(N, prec, device=local)
+    sim = gpu.Sim(ctx, N ** 3)
+    sim.ic_generate(**gpu.ic_params(box, seed=args.seed + 1000 * rank))
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    for _ in range(args.warmup):
+        sim.step()
+    ctx.sync()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local)
+    clocks.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    l0 = ctx.launches()
+    e0.record(stream)
+    for _ in range(args.steps):
+        sim.step()
+    e1.record(stream)
+    e1.synchronize()
+    launches = ctx.launches() - l0
+    ms = e0.elapsed_time(e1)
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = N ** 3 * args.steps * world / (ms_max / 1e3)
+    st = sim.state()
+
+    # dominant-kernel roofline: the deposit of T_ij (see the design doc for the per-kernel bytes)
+    roof = dominant_kernel_roofline(gpu, ctx, sim, stream, N, args.prec)
+
+    # e2e: particle state from pinned host memory in, cycle, particle state out
+    e2e = None
+    if not args.no_e2e:
+        e2e = run_e2e(gpu, ctx, sim, stream, N, args.steps, torch)
+    return dict(value=value, ms=ms_max / args.steps, launches=launches, clocks=clk, state=st, roofline=roof,
+                e2e=e2e, box=box)
+
+
+def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
+    import torch
+    r = 8 if prec == "fp64" else 4
+    pcls = sim.particles()
+    Sij = sim.field("Sij")
+    phi = sim.field("phi")
+    st = sim.state()
+    reps = 3
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    gpu.projection_Tij(pcls, Sij, st["a"], phi, 1.0)
+    ctx.sync()
+    e0.record(stream)
+    for _ in range(reps):
+        gpu.projection_Tij(pcls, Sij, st["a"], phi, 1.0)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    V = N ** 3
+    # algorithmic bytes: particle pos+vel read once, phi read once, 6 components read-modify-written
+    alg = V * (3 * 8 + 3 * r) + V * r + 6 * V * r * 2
+    peak, kind = hbm_peak()
+    achieved = alg / (ms / 1e3) / 1e9
+    return {"kernel": "projection_Tij (deposit of T_ij, both passes)", "bound": "hbm", "achieved": achieved,
+            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None, "peak_kind": kind,
+            "ms_per_launch": ms, "alg_bytes": alg}
+
+
+def run_e2e(gpu, ctx, sim, stream, N, steps, torch):
+    import numpy as np
+    pcls = sim.particles()
+    n = N ** 3
+    host = torch.empty(n * 56, dtype=torch.uint8, pin_memory=True)
+    arr = host.numpy().view(gpu.PART)
+    back = torch.empty(n * 56, dtype=torch.uint8, pin_memory=True)
+    barr = back.numpy().view(gpu.PART)
+    arr[:] = pcls.download()
+    ctx.sync()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        pcls.upload(arr)
+        sim.step()
+        barr[:] = pcls.download()  # download synchronises the stream
+    dt = time.perf_counter() - t0
+    return {"value": n * steps / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 56,
+            "d2h_bytes_per_step": n * 56}
+
+
+# ---------------------------------------------------------- CPU side --------
+def _cpu_worker(args):
+    N, steps, seed = args
+    import gevoracle as G
+    s = G.Sim(N).ic(**G.default_icparams(N, 1000.0 * N / 512, seed=seed))
+    s.step()  # the first cycle skips the phi solve (dtau_old = 0)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        s.step()
+    return N ** 3 * steps, time.perf_counter() - t0
+
+
+def cpu_sample(N, steps, workers):
+    """particle-steps/s of the oracle on `workers` independent simulations."""
+    import multiprocessing as mp
+    import gevoracle
+    gevoracle.build()
+    if workers == 1:
+        n, t = _cpu_worker((N, steps, 1))
+        return n / t
+    ctx = mp.get_context("spawn")
+    with ctx.Pool(workers) as pool:
+        res = pool.map(_cpu_worker, [(N, steps, 1 + i) for i in range(workers)])
+    return sum(r[0] for r in res) / max(r[1] for r in res)
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch
+        torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
+    N = args.grid
+    metric = "particle-steps/s %d^3 %s" % (N, args.prec)
+    config = {"workload": "gevolution GR PM cycle, %d^3 grid, %d^3 CDM particles, box %g Mpc/h, %s form, "
+                          "BBKS Zel'dovich IC at z=100 (sigma8 0.81, h 0.67, Omega_cdm 0.27 + Omega_b 0.05), "
+                          "parabolic B, 12 FFTs per cycle" % (N, N, 1000.0 * N / 512, args.prec),
+              "grid": N, "particles": N ** 3, "precision": args.prec,
+              "l2": "inputs larger than L2 (fields >= %d MB each)" % (N ** 3 * (8 if args.prec == "fp64" else 4) // 2 ** 20)}
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        workers = os.cpu_count() or 1
+        sampleN = 64
+        t0 = time.perf_counter()
+        cpu_sample(sampleN, 1, workers)  # warm-up (builds, spawns)
+        vals = []
+        for _ in range(args.steps):
+            vals.append(cpu_sample(sampleN, 1, workers))
+        v = sorted(vals)[len(vals) // 2]
+        line = {"impl": "reference", "metric": metric, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": config,
+                "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": workers, "kind": "port",
+                                 "sample": "one cycle per worker of an independent %d^3 simulation (same IC recipe "
+                                           "and box per particle), %d workers; the FFT is the oracle's, not FFTW"
+                                           % (sampleN, workers)},
+                "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+                "wall_s": time.perf_counter() - t0}
+        print(json.dumps(line))
+        return
+    res = run_ours(args, rank, world, local)
+    if rank != 0:
+        return
+    cpu = None
+    if not args.no_cpu_baseline:
+        sampleN = 64
+        v = cpu_sample(sampleN, 3, 1)
+        cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "port",
+               "sample": "3 cycles of one %d^3 simulation with the same IC recipe (CPU restatement, FP64, single "
+                         "thread); the FFT is the oracle's, not FFTW" % sampleN}
+    line = {"metric": metric, "value": res["value"], "unit": "particle-steps/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.prec == "fp64" else "f32+f64pos+i64dep",
+            "data": "synthetic (device-generated BBKS Zel'dovich IC)", "config": config,
+            "roofline": res["roofline"], "cpu_baseline": cpu, "e2e": res["e2e"], "gpu_launches": res["launches"],
+            "clocks": res["clocks"], "bytes_per_cycle_alg": cycle_bytes(N, args.prec),
+            "final_a": res["state"]["a"]}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

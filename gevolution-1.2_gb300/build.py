@@ -19,6 +19,7 @@ ROOT = os.path.dirname(HERE)
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgev_gb300.so")
+CUDA_LIB = os.path.join(os.path.dirname(os.path.dirname(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")), "lib64")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
@@ -61,7 +62,7 @@ def build(force=False, verbose=False, extra=()):
                 if verbose and warn:
                     print(warn)
     if jobs or not os.path.exists(LIB):
-        cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs
+        cmd = [nvcc()] + ARCH + ["-shared", "-cudart", "shared", "-Xlinker", "-rpath", "-Xlinker", CUDA_LIB, "-o", LIB] + objs
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n%s%s" % (r.stdout, r.stderr))

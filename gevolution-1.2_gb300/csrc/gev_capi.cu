@@ -10,6 +10,7 @@
 #include "gev_internal.cuh"
 
 int fft_init_kernels(int prec);
+void fft_perm(const FftPlan &pl, std::vector<unsigned short> &perm);
 
 namespace {
 
@@ -51,6 +52,13 @@ int upload_tables(gev_ctx *ctx) {
   GEV_CHECK_CUDA(ctx, cudaMemcpy(ctx->d_kshift, ks.data(), ks.size() * sz, cudaMemcpyHostToDevice));
   GEV_CHECK_CUDA(ctx, cudaMemcpy(ctx->d_twN, twN.data(), twN.size() * sz, cudaMemcpyHostToDevice));
   GEV_CHECK_CUDA(ctx, cudaMemcpy(ctx->d_twH, twH.data(), twH.size() * sz, cudaMemcpyHostToDevice));
+  std::vector<unsigned short> pN, pH;
+  fft_perm(ctx->planN, pN);
+  fft_perm(ctx->planH, pH);
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&ctx->d_permN, pN.size() * 2));
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&ctx->d_permH, pH.size() * 2));
+  GEV_CHECK_CUDA(ctx, cudaMemcpy(ctx->d_permN, pN.data(), pN.size() * 2, cudaMemcpyHostToDevice));
+  GEV_CHECK_CUDA(ctx, cudaMemcpy(ctx->d_permH, pH.data(), pH.size() * 2, cudaMemcpyHostToDevice));
   return GEV_OK;
 }
 
@@ -101,6 +109,24 @@ int ctx_ensure_red(gev_ctx *ctx, size_t elems) {
   }
   ctx->red_elems = elems;
   return GEV_OK;
+}
+
+void ctx_retain(gev_ctx *ctx) { ctx->refs++; }
+
+void ctx_release(gev_ctx *ctx) {
+  if (--ctx->refs > 0) return;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  cudaFree(ctx->d_gridk2);
+  cudaFree(ctx->d_kshift);
+  cudaFree(ctx->d_twN);
+  cudaFree(ctx->d_twH);
+  cudaFree(ctx->d_permN);
+  cudaFree(ctx->d_permH);
+  cudaFree(ctx->d_fft_scratch);
+  cudaFree(ctx->d_cube);
+  cudaFree(ctx->d_red);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
 }
 
 extern "C" {
@@ -169,16 +195,10 @@ int gev_ctx_create(int device, int N, int precision, gev_ctx **out) {
 
 int gev_ctx_destroy(gev_ctx *ctx) {
   if (!ctx) return GEV_OK;
-  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-  cudaFree(ctx->d_gridk2);
-  cudaFree(ctx->d_kshift);
-  cudaFree(ctx->d_twN);
-  cudaFree(ctx->d_twH);
-  cudaFree(ctx->d_fft_scratch);
-  cudaFree(ctx->d_cube);
-  cudaFree(ctx->d_red);
-  if (ctx->stream) cudaStreamDestroy(ctx->stream);
-  delete ctx;
+  if (!ctx->closed) {
+    ctx->closed = true;
+    ctx_release(ctx);
+  }
   return GEV_OK;
 }
 
@@ -216,6 +236,7 @@ int gev_field_create(gev_ctx *ctx, int kind, int ncomp, gev_field **out) {
   const int N = ctx->N;
   gev_field *f = new gev_field();
   f->ctx = ctx;
+  ctx_retain(ctx);
   f->kind = kind;
   f->ncomp = ncomp;
   f->comp_elems = kind == GEV_FIELD_REAL ? (size_t)N * N * N : (size_t)N * N * (N / 2 + 1);
@@ -224,6 +245,7 @@ int gev_field_create(gev_ctx *ctx, int kind, int ncomp, gev_field **out) {
   if (cudaMalloc(&f->d, bytes) != cudaSuccess) {
     cudaGetLastError();
     delete f;
+    ctx_release(ctx);
     return gev_fail(ctx, GEV_ENOMEM, "field_create: device allocation failed");
   }
   ctx->bytes_in_use += bytes;
@@ -234,12 +256,14 @@ int gev_field_create(gev_ctx *ctx, int kind, int ncomp, gev_field **out) {
 
 int gev_field_destroy(gev_field *f) {
   if (!f) return GEV_OK;
-  if (f->ctx) {
-    cudaStreamSynchronize(f->ctx->stream);
-    f->ctx->bytes_in_use -= f->comp_elems * f->elem_bytes * f->ncomp;
+  gev_ctx *ctx = f->ctx;
+  if (ctx) {
+    cudaStreamSynchronize(ctx->stream);
+    ctx->bytes_in_use -= f->comp_elems * f->elem_bytes * f->ncomp;
   }
   cudaFree(f->d);
   delete f;
+  if (ctx) ctx_release(ctx);
   return GEV_OK;
 }
 

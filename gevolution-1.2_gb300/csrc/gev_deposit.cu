@@ -12,10 +12,12 @@
 //           cells that touch it, with periodic wrap (the halo fold), in a fixed
 //           order, and add them to the field.
 // Every sum therefore has a fixed order: results are bit-reproducible run to
-// run.  In the mixed-precision form each particle contribution is converted to
-// a 64-bit fixed-point integer and the cube sums are integer adds (exact and
-// order-independent); pass 2 converts the integer total once.
+// run.  This is the FP64 form; the mixed form uses the fixed-point column
+// sweep of gev_deposit_fx.cu.
 #include "gev_internal.cuh"
+
+int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass, double a, const gev_field *phi,
+               double bound);
 
 namespace {
 
@@ -26,12 +28,6 @@ struct DepParams {
   int N;
   double mass, a;
   double fx_scale;  // fixed-point scale (mixed form)
-};
-
-// fixed-point accumulator of the mixed form
-struct FixAcc {
-  long long v;
-  __device__ __forceinline__ void add(float x, double s) { v += __double2ll_rn((double)x * s); }
 };
 
 template <typename T>
@@ -144,102 +140,6 @@ __global__ void __launch_bounds__(256) k_cube_fp64(PclsArrays P, const uint32_t 
   }
 }
 
-// pass 1, mixed form: FP32 arithmetic per particle, int64 fixed-point sums
-template <int KIND>
-__global__ void __launch_bounds__(256) k_cube_mixed(PclsArrays P, const uint32_t *__restrict__ start,
-                                                    const float *__restrict__ phi, DepParams dp, long long *cube) {
-  const int N = dp.N;
-  const size_t C = (size_t)N * N * N;
-  const double Nd = (double)N, dx = 1.0 / Nd;
-  const double S = dp.fx_scale;
-  for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < C; c += (size_t)gridDim.x * blockDim.x) {
-    const int cx = (int)(c % N), cy = (int)((c / N) % N), cz = (int)(c / ((size_t)N * N));
-    const uint32_t s = start[c], e = start[c + 1];
-    float l[8];
-    if (phi != nullptr && KIND != DEP_MASS && e > s) {
-      l[0] = ldf(phi, cx, cy, cz, N);
-      l[1] = ldf(phi, cx, cy, cz + 1, N);
-      l[2] = ldf(phi, cx, cy + 1, cz, N);
-      l[3] = ldf(phi, cx, cy + 1, cz + 1, N);
-      l[4] = ldf(phi, cx + 1, cy, cz, N);
-      l[5] = ldf(phi, cx + 1, cy, cz + 1, N);
-      l[6] = ldf(phi, cx + 1, cy + 1, cz, N);
-      l[7] = ldf(phi, cx + 1, cy + 1, cz + 1, N);
-    } else {
-#pragma unroll
-      for (int k = 0; k < 8; ++k) l[k] = 0.f;
-    }
-    const double rx = cx * dx, ry = cy * dx, rz = cz * dx;
-    constexpr int NV = NVAL[KIND];
-    FixAcc acc[NV];
-#pragma unroll
-    for (int k = 0; k < NV; ++k) acc[k].v = 0;
-    const float a = (float)dp.a;
-    const float m = (float)dp.mass;
-    for (uint32_t j = s; j < e; ++j) {
-      const float u0 = (float)((P.px[j] - rx) * Nd), u1 = (float)((P.py[j] - ry) * Nd), u2 = (float)((P.pz[j] - rz) * Nd);
-      const float d0 = 1.f - u0, d1 = 1.f - u1, d2 = 1.f - u2;
-      const float w8[8] = {d0 * d1 * d2, d0 * d1 * u2, d0 * u1 * d2, d0 * u1 * u2,
-                           u0 * d1 * d2, u0 * d1 * u2, u0 * u1 * d2, u0 * u1 * u2};
-      if (KIND == DEP_MASS) {
-#pragma unroll
-        for (int k = 0; k < 8; ++k) acc[k].add(m * w8[k], S);
-      } else if (KIND == DEP_T00) {
-        float ee = a, ff = 0.f;
-        if (phi != nullptr) {
-          const float q0 = ((const float *)P.vx)[j], q1 = ((const float *)P.vy)[j], q2 = ((const float *)P.vz)[j];
-          const float f = q0 * q0 + q1 * q1 + q2 * q2;
-          ee = sqrtf(f + a * a);
-          ff = 3.f * ee + f / ee;
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) acc[k].add(m * w8[k] * (ee + ff * l[k]), S);
-      } else if (KIND == DEP_T0I) {
-        const float q0 = ((const float *)P.vx)[j], q1 = ((const float *)P.vy)[j], q2 = ((const float *)P.vz)[j];
-        float w = m * q0;
-        acc[0].add(w * d1 * d2 * (1.f + l[0] + l[4]), S);
-        acc[1].add(w * u1 * d2 * (1.f + l[2] + l[6]), S);
-        acc[2].add(w * d1 * u2 * (1.f + l[1] + l[5]), S);
-        acc[3].add(w * u1 * u2 * (1.f + l[3] + l[7]), S);
-        w = m * q1;
-        acc[4].add(w * d0 * d2 * (1.f + l[0] + l[2]), S);
-        acc[5].add(w * u0 * d2 * (1.f + l[4] + l[6]), S);
-        acc[6].add(w * d0 * u2 * (1.f + l[1] + l[3]), S);
-        acc[7].add(w * u0 * u2 * (1.f + l[5] + l[7]), S);
-        w = m * q2;
-        acc[8].add(w * d0 * d1 * (1.f + l[0] + l[1]), S);
-        acc[9].add(w * u0 * d1 * (1.f + l[4] + l[5]), S);
-        acc[10].add(w * d0 * u1 * (1.f + l[2] + l[3]), S);
-        acc[11].add(w * u0 * u1 * (1.f + l[6] + l[7]), S);
-      } else {
-        const float q[3] = {((const float *)P.vx)[j], ((const float *)P.vy)[j], ((const float *)P.vz)[j]};
-        float f = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-        const float ee = sqrtf(f + a * a);
-        const float inv_e = 1.f / ee;
-        f = 4.f + a * a / (f + a * a);
-#pragma unroll
-        for (int i = 0; i < 3; ++i) {
-          const float w = m * q[i] * q[i] * inv_e;
-#pragma unroll
-          for (int k = 0; k < 8; ++k) acc[8 * i + k].add(w * w8[k] * (1.f + f * l[k]), S);
-        }
-        const float qf = 0.25f * f;
-        float w = m * q[0] * q[1] * inv_e;
-        acc[24].add(w * d2 * (1.f + qf * (l[0] + l[2] + l[4] + l[6])), S);
-        acc[25].add(w * u2 * (1.f + qf * (l[1] + l[3] + l[5] + l[7])), S);
-        w = m * q[0] * q[2] * inv_e;
-        acc[26].add(w * d1 * (1.f + qf * (l[0] + l[1] + l[4] + l[5])), S);
-        acc[27].add(w * u1 * (1.f + qf * (l[2] + l[3] + l[6] + l[7])), S);
-        w = m * q[1] * q[2] * inv_e;
-        acc[28].add(w * d0 * (1.f + qf * (l[0] + l[1] + l[2] + l[3])), S);
-        acc[29].add(w * u0 * (1.f + qf * (l[4] + l[5] + l[6] + l[7])), S);
-      }
-    }
-#pragma unroll
-    for (int k = 0; k < NV; ++k) cube[k * C + c] = acc[k].v;
-  }
-}
-
 // pass 2: gather the cube entries touching each field cell, fixed order
 template <typename A>
 __device__ __forceinline__ A cv(const A *__restrict__ cube, int k, size_t C, int x, int y, int z, int N) {
@@ -313,28 +213,22 @@ int run_deposit(gev_ctx *ctx, gev_pcls *p, gev_field *out, double a, const gev_f
   mass *= p->mass;
   if (KIND == DEP_T00 || KIND == DEP_TIJ) mass /= a;
   if (KIND == DEP_MASS) mass = p->mass / (dx * dx * dx);
-  const size_t bytes = (size_t)NVAL[KIND] * C * 8;
-  int rc = ctx_ensure_cube(ctx, bytes);
-  if (rc) return rc;
   DepParams dp{N, mass, a, 0.};
   const int blocks = grid_for(ctx, C, 256, 16);
   if (ctx->prec == GEV_PREC_FP64) {
+    int rc = ctx_ensure_cube(ctx, (size_t)NVAL[KIND] * C * 8);
+    if (rc) return rc;
     k_cube_fp64<KIND><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->start, phi ? (const double *)phi->d : nullptr, dp,
                                                        (double *)ctx->d_cube);
     GEV_LAUNCH_CHECK(ctx);
     k_gather<KIND, double, double><<<blocks, 256, 0, ctx->stream>>>((const double *)ctx->d_cube, (double *)out->d, N, 1.);
     GEV_LAUNCH_CHECK(ctx);
   } else {
-    // scale so that all particles in one cell, each at the bound, cannot overflow 2^62
-    double vmax = 0.05;  // |q| bound used for the scale; momenta q = a v stay far below this for CDM
+    // fixed-point scale: all particles at the contribution bound in one cell stay below 2^62
+    const double vmax = 0.05;  // |q| bound for the scale; CDM momenta q = a v stay far below it
     const double bound = contribution_bound(KIND, mass, a, vmax) * (double)(p->n > 0 ? p->n : 1) * 8.;
-    dp.fx_scale = ldexp(1.0, 62) / bound;
-    k_cube_mixed<KIND><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->start, phi ? (const float *)phi->d : nullptr, dp,
-                                                        (long long *)ctx->d_cube);
-    GEV_LAUNCH_CHECK(ctx);
-    k_gather<KIND, long long, float><<<blocks, 256, 0, ctx->stream>>>((const long long *)ctx->d_cube, (float *)out->d, N,
-                                                                     1.0 / dp.fx_scale);
-    GEV_LAUNCH_CHECK(ctx);
+    int rc = deposit_fx(ctx, p, out, KIND, mass, a, phi, bound);
+    if (rc) return rc;
   }
   return GEV_OK;
 }

@@ -1,0 +1,309 @@
+// gev_deposit_fx.cu -- the mixed-precision deposit: per-particle FP32
+// contributions accumulated as 64-bit fixed-point integers.
+//
+// Same physics as projection_T00/T0i/Tij_project (gevolution.hpp:926-1297) and
+// scalarProjectionCIC_project.  Layout of the work:
+//   * a block owns a column tile of TX x TY cells and a chunk of TZ cell
+//     layers, and sweeps the chunk in z;
+//   * for each source layer z it walks the particles of the layer's TY rows
+//     (contiguous runs of the (cell, ID)-ordered store, one thread per
+//     particle) and adds each corner contribution, converted exactly to an
+//     int64 with a power-of-two scale, into two shared-memory layers (field
+//     z and z + 1) with 64-bit shared atomics -- integer adds, so the result
+//     does not depend on their order;
+//   * when layer z is complete it is flushed: cells that only this block can
+//     touch are added straight into the FP32 field; cells on a tile face
+//     (shared with a neighbouring block, including the periodic wrap) go into
+//     a compact int64 face buffer with global atomics, which a fix-up pass
+//     then adds to the field and clears.
+// HBM traffic is one read of the particles, one read-modify-write of the
+// target components, and the small face buffer -- no per-cell scratch.
+#include <cmath>
+
+#include "gev_internal.cuh"
+
+namespace {
+
+enum { FX_T00 = 0, FX_T0I = 1, FX_TIJ = 2, FX_MASS = 3 };
+constexpr int FX_NC[4] = {1, 3, 6, 1};
+constexpr int TX = 32, TY = 16, TZ = 32, FX_THREADS = 256;
+
+struct FxParams {
+  int N;
+  float mass, a;
+  float scale;  // 2^k
+  double inv_scale;
+  long nPX, nPY, nPZ;  // face planes per direction
+};
+
+__device__ __forceinline__ long face_index(int x, int y, int z, const FxParams &p) {
+  const long NN = (long)p.N * p.N;
+  if (x % TX == 0) return (long)(x / TX) * NN + (long)z * p.N + y;
+  if (y % TY == 0) return p.nPX * NN + (long)(y / TY) * NN + (long)z * p.N + x;
+  return (p.nPX + p.nPY) * NN + (long)(z / TZ) * NN + (long)y * p.N + x;
+}
+
+// v * 2^k rounded to the nearest integer (ties away from zero), with integer
+// instructions only: on GB300 the float -> int64 conversion instruction issues
+// on the FP64 pipe, which is 1/64 of the FP32 rate.  The scale is a power of
+// two, so v * s is exact and its value is mantissa * 2^(exponent - 150).
+__device__ __forceinline__ long long fixed_of(float y) {
+  const unsigned b = __float_as_uint(y);
+  const int sh = min((int)((b >> 23) & 0xffu) - 150, 39);  // the clamp only matters for inf / NaN
+  const long long m = (long long)((b & 0x7fffffu) | 0x800000u);
+  long long q;
+  if (sh >= 0)
+    q = m << sh;  // |y| < 2^62 keeps sh <= 38
+  else if (sh >= -24)
+    q = (m + (1ll << (-sh - 1))) >> (-sh);
+  else
+    q = 0;  // |y| < 0.5 (this also covers y = 0 and denormals)
+  return (b >> 31) ? -q : q;
+}
+
+__device__ __forceinline__ void sadd(unsigned long long *a, float v, float s) {
+  const long long q = fixed_of(v * s);
+  if (q != 0) atomicAdd(a, (unsigned long long)q);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint32_t *__restrict__ start,
+                                                       const float *__restrict__ phi, float *out,
+                                                       unsigned long long *face, FxParams p) {
+  constexpr int NC = FX_NC[KIND];
+  constexpr int SX = TX + 1, SY = TY + 1, SL = SX * SY;  // one shared layer per component
+  extern __shared__ __align__(16) unsigned long long lay[];  // [2][NC][SY][SX]
+  __shared__ uint32_t rowoff[TY + 1], rowbase[TY];
+  const int N = p.N;
+  const long C = (long)N * N * N;
+  const long NN = (long)N * N;
+  const int ntx = (N + TX - 1) / TX, nty = (N + TY - 1) / TY;
+  const int bx = blockIdx.x % ntx, by = (blockIdx.x / ntx) % nty, bz = blockIdx.x / (ntx * nty);
+  const int x0 = bx * TX, y0 = by * TY, z0 = bz * TZ;
+  const int nx = min(TX, N - x0), ny = min(TY, N - y0), nz = min(TZ, N - z0);
+  for (int i = threadIdx.x; i < 2 * NC * SL; i += blockDim.x) lay[i] = 0ull;
+  int cur = 0;  // layer holding field z = zs; 1 - cur holds z = zs + 1
+  for (int zs = z0; zs < z0 + nz; ++zs) {
+    if (threadIdx.x == 0) {
+      uint32_t acc = 0;
+      for (int yy = 0; yy < ny; ++yy) {
+        const long c0 = x0 + (long)N * (y0 + yy) + NN * zs;
+        const uint32_t s = start[c0], e = start[c0 + nx];
+        rowbase[yy] = s;
+        rowoff[yy] = acc;
+        acc += e - s;
+      }
+      rowoff[ny] = acc;
+    }
+    __syncthreads();
+    const uint32_t total = rowoff[ny];
+    unsigned long long *A = lay + cur * NC * SL, *B = lay + (1 - cur) * NC * SL;
+    for (uint32_t t = threadIdx.x; t < total; t += blockDim.x) {
+      int yy = 0;
+      while (rowoff[yy + 1] <= t) ++yy;
+      const uint32_t j = rowbase[yy] + (t - rowoff[yy]);
+      const uint32_t cell = P.cell[j];
+      const int cx = (int)(cell % N), cy = (int)((cell / N) % N);
+      const int lx = cx - x0, ly = cy - y0;
+      const float u0 = P.rx[j], u1 = P.ry[j], u2 = P.rz[j];
+      const float d0 = 1.f - u0, d1 = 1.f - u1, d2 = 1.f - u2;
+      const float w[8] = {d0 * d1 * d2, d0 * d1 * u2, d0 * u1 * d2, d0 * u1 * u2,
+                          u0 * d1 * d2, u0 * d1 * u2, u0 * u1 * d2, u0 * u1 * u2};
+      float l[8];
+      if (KIND != FX_MASS && phi != nullptr) {
+        const int xp = cx + 1 == N ? 0 : cx + 1, yp = cy + 1 == N ? 0 : cy + 1, zp = zs + 1 == N ? 0 : zs + 1;
+        l[0] = __ldg(&phi[sidx(cx, cy, zs, N)]);
+        l[1] = __ldg(&phi[sidx(cx, cy, zp, N)]);
+        l[2] = __ldg(&phi[sidx(cx, yp, zs, N)]);
+        l[3] = __ldg(&phi[sidx(cx, yp, zp, N)]);
+        l[4] = __ldg(&phi[sidx(xp, cy, zs, N)]);
+        l[5] = __ldg(&phi[sidx(xp, cy, zp, N)]);
+        l[6] = __ldg(&phi[sidx(xp, yp, zs, N)]);
+        l[7] = __ldg(&phi[sidx(xp, yp, zp, N)]);
+      } else {
+#pragma unroll
+        for (int k = 0; k < 8; ++k) l[k] = 0.f;
+      }
+      // corner k = 4 dx + 2 dy + dz goes to layer dz at (ly + dy, lx + dx)
+      const int o00 = ly * SX + lx, o01 = (ly + 1) * SX + lx, o10 = ly * SX + lx + 1, o11 = (ly + 1) * SX + lx + 1;
+      const int off[8] = {o00, o00, o01, o01, o10, o10, o11, o11};
+      const float s = p.scale, m = p.mass, a = p.a;
+      if (KIND == FX_MASS || KIND == FX_T00) {
+        float ee = a, ff = 0.f;
+        if (KIND == FX_T00 && phi != nullptr) {
+          const float q0 = ((const float *)P.vx)[j], q1 = ((const float *)P.vy)[j], q2 = ((const float *)P.vz)[j];
+          const float f = q0 * q0 + q1 * q1 + q2 * q2;
+          ee = sqrtf(f + a * a);
+          ff = 3.f * ee + f / ee;
+        }
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const float v = KIND == FX_MASS ? m * w[k] : m * w[k] * (ee + ff * l[k]);
+          sadd(((k & 1) ? B : A) + off[k], v, s);
+        }
+      } else if (KIND == FX_T0I) {
+        const float q0 = ((const float *)P.vx)[j], q1 = ((const float *)P.vy)[j], q2 = ((const float *)P.vz)[j];
+        // x component: CIC in y, z; NGP in x (gevolution.hpp:1107-1144)
+        float wq = m * q0;
+        sadd(A + o00, wq * d1 * d2 * (1.f + l[0] + l[4]), s);
+        sadd(A + o01, wq * u1 * d2 * (1.f + l[2] + l[6]), s);
+        sadd(B + o00, wq * d1 * u2 * (1.f + l[1] + l[5]), s);
+        sadd(B + o01, wq * u1 * u2 * (1.f + l[3] + l[7]), s);
+        wq = m * q1;
+        sadd(A + SL + o00, wq * d0 * d2 * (1.f + l[0] + l[2]), s);
+        sadd(A + SL + o10, wq * u0 * d2 * (1.f + l[4] + l[6]), s);
+        sadd(B + SL + o00, wq * d0 * u2 * (1.f + l[1] + l[3]), s);
+        sadd(B + SL + o10, wq * u0 * u2 * (1.f + l[5] + l[7]), s);
+        wq = m * q2;
+        sadd(A + 2 * SL + o00, wq * d0 * d1 * (1.f + l[0] + l[1]), s);
+        sadd(A + 2 * SL + o10, wq * u0 * d1 * (1.f + l[4] + l[5]), s);
+        sadd(A + 2 * SL + o01, wq * d0 * u1 * (1.f + l[2] + l[3]), s);
+        sadd(A + 2 * SL + o11, wq * u0 * u1 * (1.f + l[6] + l[7]), s);
+      } else {  // FX_TIJ, components 00 01 02 11 12 22
+        const float q[3] = {((const float *)P.vx)[j], ((const float *)P.vy)[j], ((const float *)P.vz)[j]};
+        float f = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+        const float ee = sqrtf(f + a * a), inv_e = 1.f / ee;
+        f = 4.f + a * a / (f + a * a);
+        const int dslot[3] = {0, 3, 5};
+#pragma unroll
+        for (int i = 0; i < 3; ++i) {
+          const float wi = m * q[i] * q[i] * inv_e;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) sadd(((k & 1) ? B : A) + dslot[i] * SL + off[k], wi * w[k] * (1.f + f * l[k]), s);
+        }
+        const float qf = 0.25f * f;
+        float wq = m * q[0] * q[1] * inv_e;  // 01 on plaquettes: CIC in z only
+        sadd(A + 1 * SL + o00, wq * d2 * (1.f + qf * (l[0] + l[2] + l[4] + l[6])), s);
+        sadd(B + 1 * SL + o00, wq * u2 * (1.f + qf * (l[1] + l[3] + l[5] + l[7])), s);
+        wq = m * q[0] * q[2] * inv_e;  // 02: CIC in y only
+        sadd(A + 2 * SL + o00, wq * d1 * (1.f + qf * (l[0] + l[1] + l[4] + l[5])), s);
+        sadd(A + 2 * SL + o01, wq * u1 * (1.f + qf * (l[2] + l[3] + l[6] + l[7])), s);
+        wq = m * q[1] * q[2] * inv_e;  // 12: CIC in x only
+        sadd(A + 4 * SL + o00, wq * d0 * (1.f + qf * (l[0] + l[1] + l[2] + l[3])), s);
+        sadd(A + 4 * SL + o10, wq * u0 * (1.f + qf * (l[4] + l[5] + l[6] + l[7])), s);
+      }
+    }
+    __syncthreads();
+    // flush field layer zs (complete now) and clear it
+    for (int i = threadIdx.x; i < NC * SL; i += blockDim.x) {
+      const int comp = i / SL, r = i - comp * SL, ly = r / SX, lx = r - ly * SX;
+      if (lx > nx || ly > ny) continue;
+      const unsigned long long v = A[i];
+      if (v == 0ull) continue;
+      A[i] = 0ull;
+      int x = x0 + lx, y = y0 + ly;
+      if (x == N) x = 0;
+      if (y == N) y = 0;
+      const bool onface = lx == 0 || lx == nx || ly == 0 || ly == ny || zs == z0;
+      const int oc = KIND == FX_TIJ ? comp : comp;  // output component index equals the slot
+      if (onface)
+        atomicAdd(&face[(long)oc * (p.nPX + p.nPY + p.nPZ) * NN + face_index(x, y, zs, p)], v);
+      else
+        out[(long)oc * C + sidx(x, y, zs, N)] += (float)((double)(long long)v * p.inv_scale);
+    }
+    __syncthreads();
+    cur = 1 - cur;
+  }
+  // the layer above the chunk belongs to the next chunk's lower face
+  {
+    unsigned long long *A = lay + cur * NC * SL;
+    int zf = z0 + nz;
+    if (zf == N) zf = 0;
+    for (int i = threadIdx.x; i < NC * SL; i += blockDim.x) {
+      const int comp = i / SL, r = i - comp * SL, ly = r / SX, lx = r - ly * SX;
+      if (lx > nx || ly > ny) continue;
+      const unsigned long long v = A[i];
+      if (v == 0ull) continue;
+      int x = x0 + lx, y = y0 + ly;
+      if (x == N) x = 0;
+      if (y == N) y = 0;
+      atomicAdd(&face[(long)comp * (p.nPX + p.nPY + p.nPZ) * NN + face_index(x, y, zf, p)], v);
+    }
+  }
+}
+
+// add the face accumulators into the field and clear them
+__global__ void k_face_fix(unsigned long long *face, float *out, int ncomp, FxParams p) {
+  const int N = p.N;
+  const long NN = (long)N * N, C = NN * N;
+  const long per = (p.nPX + p.nPY + p.nPZ) * NN;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < per * ncomp; i += (long)gridDim.x * blockDim.x) {
+    const unsigned long long v = face[i];
+    if (v == 0ull) continue;
+    face[i] = 0ull;
+    const long comp = i / per, r = i - comp * per;
+    int x, y, z;
+    if (r < p.nPX * NN) {
+      const long pl = r / NN, q = r - pl * NN;
+      x = (int)pl * TX;
+      z = (int)(q / N);
+      y = (int)(q - (long)z * N);
+    } else if (r < (p.nPX + p.nPY) * NN) {
+      const long rr = r - p.nPX * NN, pl = rr / NN, q = rr - pl * NN;
+      y = (int)pl * TY;
+      z = (int)(q / N);
+      x = (int)(q - (long)z * N);
+    } else {
+      const long rr = r - (p.nPX + p.nPY) * NN, pl = rr / NN, q = rr - pl * NN;
+      z = (int)pl * TZ;
+      y = (int)(q / N);
+      x = (int)(q - (long)y * N);
+    }
+    out[comp * C + sidx(x, y, z, N)] += (float)((double)(long long)v * p.inv_scale);
+  }
+}
+
+}  // namespace
+
+// the fixed-point deposit of the mixed form; kind: 0 T00, 1 T0i, 2 Tij, 3 mass
+int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass, double a, const gev_field *phi,
+               double bound) {
+  const int N = ctx->N;
+  const int NC = FX_NC[kind];
+  FxParams fp;
+  fp.N = N;
+  fp.mass = (float)mass;
+  fp.a = (float)a;
+  int e2 = 0;
+  frexp(bound, &e2);  // bound < 2^e2
+  const int k = 62 - e2;
+  fp.scale = ldexpf(1.f, k);
+  fp.inv_scale = ldexp(1.0, -k);
+  fp.nPX = (N + TX - 1) / TX;
+  fp.nPY = (N + TY - 1) / TY;
+  fp.nPZ = (N + TZ - 1) / TZ;
+  const size_t face_elems = (size_t)(fp.nPX + fp.nPY + fp.nPZ) * N * N * NC;
+  // the face buffer lives behind the deposit scratch pointer, kept zeroed between uses
+  if (ctx->cube_bytes < face_elems * 8) {
+    int rc = ctx_ensure_cube(ctx, face_elems * 8);
+    if (rc) return rc;
+    GEV_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_cube, 0, ctx->cube_bytes, ctx->stream));
+  }
+  const int ntx = (N + TX - 1) / TX, nty = (N + TY - 1) / TY, ntz = (N + TZ - 1) / TZ;
+  const size_t smem = 2 * (size_t)NC * (TX + 1) * (TY + 1) * 8;
+  unsigned long long *face = (unsigned long long *)ctx->d_cube;
+  const float *fphi = phi ? (const float *)phi->d : nullptr;
+  float *fo = (float *)out->d;
+  const unsigned blocks = (unsigned)(ntx * nty * ntz);
+  switch (kind) {
+    case FX_T00:
+      cudaFuncSetAttribute(k_dep_fx<FX_T00>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_dep_fx<FX_T00><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, fphi, fo, face, fp);
+      break;
+    case FX_T0I:
+      cudaFuncSetAttribute(k_dep_fx<FX_T0I>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_dep_fx<FX_T0I><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, fphi, fo, face, fp);
+      break;
+    case FX_TIJ:
+      cudaFuncSetAttribute(k_dep_fx<FX_TIJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_dep_fx<FX_TIJ><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, fphi, fo, face, fp);
+      break;
+    default:
+      cudaFuncSetAttribute(k_dep_fx<FX_MASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      k_dep_fx<FX_MASS><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, nullptr, fo, face, fp);
+  }
+  GEV_LAUNCH_CHECK(ctx);
+  k_face_fix<<<grid_for(ctx, face_elems, 256, 16), 256, 0, ctx->stream>>>(face, fo, NC, fp);
+  GEV_LAUNCH_CHECK(ctx);
+  return GEV_OK;
+}

@@ -20,6 +20,7 @@
 #include <vector>
 
 #include "../../include/gev_gb300.h"
+#include "../../include/gev_sim.h"
 
 #define GEV_MAX_RADICES 12
 
@@ -39,6 +40,8 @@ struct gev_ctx {
   void *d_gridk2 = nullptr, *d_kshift = nullptr;
   // twiddles e^{-2 pi i t / L} for L = N and L = N/2
   void *d_twN = nullptr, *d_twH = nullptr;
+  // output slot of each frequency after the in-place FFT stages (L = N, N/2)
+  void *d_permN = nullptr, *d_permH = nullptr;
   FftPlan planN{}, planH{};
   // scratch: one spectrum component for the input-preserving c2r, deposit cubes,
   // reductions
@@ -51,7 +54,15 @@ struct gev_ctx {
   long long launches = 0;
   size_t bytes_in_use = 0;
   std::string err;
+  // lifetime: the handle returned by gev_ctx_create holds one reference and
+  // every field / particle store / simulation holds one more, so the context's
+  // stream and buffers outlive all of them whatever order they are destroyed in
+  int refs = 1;
+  bool closed = false;
 };
+
+void ctx_retain(gev_ctx *ctx);
+void ctx_release(gev_ctx *ctx);
 
 struct gev_field {
   gev_ctx *ctx = nullptr;
@@ -67,6 +78,11 @@ struct PclsArrays {
   void *vx = nullptr, *vy = nullptr, *vz = nullptr;  // real type of the form
   int64_t *id = nullptr;
   uint32_t *cell = nullptr;
+  // mixed form only: the position inside the linked cell, pos * N - cell, as
+  // FP32.  The FP64 position stays the master state; the drift re-derives the
+  // offset from it, and the kick and the deposits read only the offset, so they
+  // issue no FP64 instructions (GB300 runs FP64 at 1/64 of the FP32 rate).
+  float *rx = nullptr, *ry = nullptr, *rz = nullptr;
 };
 
 struct gev_pcls {
@@ -81,6 +97,17 @@ struct gev_pcls {
   uint32_t *big = nullptr;    // list of cells needing the block-wide ID sort (+1 counter)
   uint32_t *scan_tmp = nullptr;
   size_t scan_tmp_elems = 0;
+};
+
+// one simulation (include/gev_sim.h)
+struct gev_sim {
+  gev_ctx *ctx = nullptr;
+  gev_pcls *pcls = nullptr;
+  gev_field *phi = nullptr, *chi = nullptr, *source = nullptr, *Sij = nullptr, *Bi = nullptr;
+  gev_field *scalarFT = nullptr, *SijFT = nullptr, *BiFT = nullptr;
+  gev_sim_state st{};
+  double *host_words = nullptr;  // pinned: [0] T00 sum, [1] max bits, [2] phi(k=0).re
+  double *dev_words = nullptr;
 };
 
 // ----------------------------------------------------------------- errors --
@@ -142,6 +169,61 @@ __device__ __forceinline__ C cscale(decltype(C::x) d, C a) { return cmk<C>(d * a
 __device__ __forceinline__ int wrapi(int i, int N) { return i < 0 ? i + N : (i >= N ? i - N : i); }
 __device__ __forceinline__ size_t sidx(int x, int y, int z, int N) {
   return (size_t)x + (size_t)N * ((size_t)y + (size_t)N * (size_t)z);
+}
+
+// lg of N when N is a power of two, else -1
+__host__ __device__ inline int lg_pow2(int N) {
+  int l = 0;
+  while ((1 << l) < N) ++l;
+  return (1 << l) == N ? l : -1;
+}
+
+// cell = floor(x N) (clamped to N-1) and r = x N - cell as FP32, for x in [0, 1).
+// With N = 2^lg the split reads the double's bits (x N is an exact exponent
+// shift), so it issues no FP64 instruction; r keeps the leading 24 bits of the
+// fraction.  Other N use FP64 arithmetic.
+__device__ __forceinline__ void pos_split(double x, int N, int lg, int &c, float &r) {
+  if (lg >= 0) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const int e = (int)((b >> 52) & 0x7ff);
+    const int sh = 1075 - e - lg;  // x N = m * 2^-sh, m the 53-bit significand; x < 1 gives sh >= 53 - lg
+    if (e == 0 || sh >= 88) {       // zero, denormal, or x N < 2^-35
+      c = 0;
+      r = 0.f;
+      return;
+    }
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
+    if (sh >= 64) {
+      c = 0;
+      r = (float)(unsigned)(m >> (sh - 24)) * 5.9604644775390625e-8f;
+    } else {
+      c = (int)(m >> sh);
+      const unsigned long long frac = m & ((1ull << sh) - 1ull);
+      r = (float)(unsigned)(frac >> (sh - 24)) * 5.9604644775390625e-8f;
+    }
+    if (c >= N) {
+      c = N - 1;
+      r = 1.f;
+    }
+  } else {
+    const double xn = x * (double)N;
+    c = (int)xn;
+    if (c >= N) c = N - 1;
+    if (c < 0) c = 0;
+    r = (float)(xn - (double)c);
+  }
+}
+
+// periodic wrap into [0, 1) deciding on the bit pattern (integer compares)
+__device__ __forceinline__ double wrap01_bits(double x) {
+  const long long b = __double_as_longlong(x);
+  if (b < 0) {  // negative (or -0)
+    x += 1.0;
+    if (__double_as_longlong(x) >= 0x3FF0000000000000ll) x -= 1.0;
+  } else if (b >= 0x3FF0000000000000ll) {  // >= 1
+    x -= 1.0;
+  }
+  return x;
 }
 
 inline int grid_for(const gev_ctx *ctx, size_t work, int threads, int per_sm = 8) {

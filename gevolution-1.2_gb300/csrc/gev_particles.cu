@@ -51,6 +51,14 @@ __global__ void k_unpack(const gev_part *__restrict__ in, long n, PclsArrays P, 
     ((V *)P.vz)[i] = (V)q.vel[2];
     P.id[i] = q.ID;
     P.cell[i] = cell_key(q.pos[0], q.pos[1], q.pos[2], N);
+    if (sizeof(V) == 4) {
+      const int lg = lg_pow2(N);
+      int cx, cy, cz;
+      pos_split(q.pos[0], N, lg, cx, P.rx[i]);
+      pos_split(q.pos[1], N, lg, cy, P.ry[i]);
+      pos_split(q.pos[2], N, lg, cz, P.rz[i]);
+      P.cell[i] = (uint32_t)cx + (uint32_t)N * ((uint32_t)cy + (uint32_t)N * (uint32_t)cz);
+    }
   }
 }
 template <typename V>
@@ -235,13 +243,18 @@ __global__ void k_gather(PclsArrays src, PclsArrays dst, const uint32_t *__restr
     ((V *)dst.vz)[j] = ((const V *)src.vz)[i];
     dst.id[j] = src.id[i];
     dst.cell[j] = src.cell[i];
+    if (sizeof(V) == 4) {
+      dst.rx[j] = src.rx[i];
+      dst.ry[j] = src.ry[i];
+      dst.rz[j] = src.rz[i];
+    }
   }
 }
 
 // ------------------------------------------------------- particle updates --
 struct Params {
   double dtau, a, a2N, inv_a2, inv_a2N;
-  int nfield, N;
+  int nfield, N, lg;
 };
 
 template <typename T>
@@ -257,11 +270,20 @@ __global__ void __launch_bounds__(256) k_update_q(PclsArrays P, long n, const T 
                                                   unsigned long long *maxbits) {
   const int N = pr.N;
   const size_t NV = (size_t)N * N * N;
-  double vmax = 0.;
+  T vmax = (T)0;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     const uint32_t c = P.cell[i];
     const int cx = (int)(c % N), cy = (int)((c / N) % N), cz = (int)(c / ((uint32_t)N * N));
-    const T r0 = (T)(P.px[i] * (double)N - cx), r1 = (T)(P.py[i] * (double)N - cy), r2 = (T)(P.pz[i] * (double)N - cz);
+    T r0, r1, r2;
+    if constexpr (sizeof(T) == 4) {
+      r0 = P.rx[i];
+      r1 = P.ry[i];
+      r2 = P.rz[i];
+    } else {
+      r0 = (T)(P.px[i] * (double)N - cx);
+      r1 = (T)(P.py[i] * (double)N - cy);
+      r2 = (T)(P.pz[i] * (double)N - cz);
+    }
     T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
     const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
     T g0, g1, g2;
@@ -338,13 +360,16 @@ __global__ void __launch_bounds__(256) k_update_q(PclsArrays P, long n, const T 
     ((V *)P.vx)[i] = (V)q0;
     ((V *)P.vy)[i] = (V)q1;
     ((V *)P.vz)[i] = (V)q2;
-    const double v2 = ((double)q0 * q0 + (double)q1 * q1 + (double)q2 * q2) * pr.inv_a2;
+    const T v2 = (q0 * q0 + q1 * q1 + q2 * q2) * (T)pr.inv_a2;
     vmax = v2 > vmax ? v2 : vmax;
   }
   // max over the block, then one atomic on the bit pattern (non-negative doubles order as integers)
-  for (int o = 16; o > 0; o >>= 1) vmax = fmax(vmax, __shfl_xor_sync(0xffffffffu, vmax, o));
+  for (int o = 16; o > 0; o >>= 1) {
+    const T other = __shfl_xor_sync(0xffffffffu, vmax, o);
+    vmax = other > vmax ? other : vmax;
+  }
   __shared__ double sh[8];
-  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = vmax;
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = (double)vmax;
   __syncthreads();
   if (threadIdx.x == 0) {
     double m = 0.;
@@ -371,7 +396,16 @@ __global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const 
     } else {
       const uint32_t c = P.cell[i];
       const int cx = (int)(c % N), cy = (int)((c / N) % N), cz = (int)(c / ((uint32_t)N * N));
-      const T r0 = (T)(x * (double)N - cx), r1 = (T)(y * (double)N - cy), r2 = (T)(z * (double)N - cz);
+      T r0, r1, r2;
+      if constexpr (sizeof(T) == 4) {
+        r0 = P.rx[i];
+        r1 = P.ry[i];
+        r2 = P.rz[i];
+      } else {
+        r0 = (T)(x * (double)N - cx);
+        r1 = (T)(y * (double)N - cy);
+        r2 = (T)(z * (double)N - cz);
+      }
       const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
       const T a = (T)pr.a;
       const T v2 = q0 * q0 + q1 * q1 + q2 * q2;
@@ -405,17 +439,39 @@ __global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const 
         v1 += b1 * ib;
         vv2 += b2 * ib;
       }
-      x += pr.dtau * (double)v0;
-      y += pr.dtau * (double)v1;
-      z += pr.dtau * (double)vv2;
+      if constexpr (sizeof(T) == 4) {
+        const float dt = (float)pr.dtau;
+        x += (double)(dt * v0);
+        y += (double)(dt * v1);
+        z += (double)(dt * vv2);
+      } else {
+        x += pr.dtau * (double)v0;
+        y += pr.dtau * (double)v1;
+        z += pr.dtau * (double)vv2;
+      }
     }
-    x = wrap01(x);
-    y = wrap01(y);
-    z = wrap01(z);
+    if constexpr (sizeof(T) == 4) {
+      x = wrap01_bits(x);
+      y = wrap01_bits(y);
+      z = wrap01_bits(z);
+      int cx, cy, cz;
+      float r0, r1, r2;
+      pos_split(x, N, pr.lg, cx, r0);
+      pos_split(y, N, pr.lg, cy, r1);
+      pos_split(z, N, pr.lg, cz, r2);
+      P.rx[i] = r0;
+      P.ry[i] = r1;
+      P.rz[i] = r2;
+      P.cell[i] = (uint32_t)cx + (uint32_t)N * ((uint32_t)cy + (uint32_t)N * (uint32_t)cz);
+    } else {
+      x = wrap01(x);
+      y = wrap01(y);
+      z = wrap01(z);
+      P.cell[i] = cell_key(x, y, z, N);
+    }
     P.px[i] = x;
     P.py[i] = y;
     P.pz[i] = z;
-    P.cell[i] = cell_key(x, y, z, N);
   }
 }
 
@@ -435,6 +491,12 @@ int alloc_arrays(gev_ctx *ctx, PclsArrays &A, long cap, size_t vsz) {
   GEV_CHECK_CUDA(ctx, cudaMalloc(&A.id, n * 8));
   GEV_CHECK_CUDA(ctx, cudaMalloc(&A.cell, n * 4));
   ctx->bytes_in_use += n * (8 * 4 + 4 + 3 * vsz);
+  if (vsz == 4) {  // mixed form: FP32 in-cell offsets
+    GEV_CHECK_CUDA(ctx, cudaMalloc(&A.rx, n * 4));
+    GEV_CHECK_CUDA(ctx, cudaMalloc(&A.ry, n * 4));
+    GEV_CHECK_CUDA(ctx, cudaMalloc(&A.rz, n * 4));
+    ctx->bytes_in_use += n * 12;
+  }
   return GEV_OK;
 }
 void free_arrays(PclsArrays &A) {
@@ -446,6 +508,9 @@ void free_arrays(PclsArrays &A) {
   cudaFree(A.vz);
   cudaFree(A.id);
   cudaFree(A.cell);
+  cudaFree(A.rx);
+  cudaFree(A.ry);
+  cudaFree(A.rz);
   A = PclsArrays();
 }
 
@@ -464,7 +529,7 @@ int scan_cells(gev_ctx *ctx, gev_pcls *p) {
 template <typename T, typename V>
 int launch_update_q(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
                     const gev_field *Bi, int nfield, double a, double a2N, unsigned long long *mb) {
-  Params pr{dtau, a, a2N, 1.0 / (a * a), 1.0 / a2N, nfield, ctx->N};
+  Params pr{dtau, a, a2N, 1.0 / (a * a), 1.0 / a2N, nfield, ctx->N, lg_pow2(ctx->N)};
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(mb, 0, sizeof(unsigned long long), ctx->stream));
   const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
   const T *fphi = (const T *)phi->d, *fchi = chi ? (const T *)chi->d : nullptr, *fB = Bi ? (const T *)Bi->d : nullptr;
@@ -479,7 +544,7 @@ int launch_update_q(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_
 template <typename T, typename V>
 int update_pos_t(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
                  const gev_field *Bi, int nfield, double a, double a2N) {
-  Params pr{dtau, a, a2N, 1.0 / (a * a), 1.0 / a2N, nfield, ctx->N};
+  Params pr{dtau, a, a2N, 1.0 / (a * a), 1.0 / a2N, nfield, ctx->N, lg_pow2(ctx->N)};
   const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
   const T *fphi = phi ? (const T *)phi->d : nullptr, *fchi = chi ? (const T *)chi->d : nullptr,
           *fB = Bi ? (const T *)Bi->d : nullptr;
@@ -540,6 +605,7 @@ int gev_pcls_create(gev_ctx *ctx, long capacity, double mass, gev_pcls **out) {
   if (!ctx || !out || capacity < 0 || capacity > 0xFFFFFFFFL) return gev_fail(ctx, GEV_EINVAL, "pcls_create: bad capacity");
   gev_pcls *p = new gev_pcls();
   p->ctx = ctx;
+  ctx_retain(ctx);
   p->cap = capacity;
   p->mass = mass;
   const size_t vsz = ctx->prec == GEV_PREC_FP64 ? 8 : 4;
@@ -577,7 +643,9 @@ int gev_pcls_destroy(gev_pcls *p) {
   cudaFree(p->perm);
   cudaFree(p->big);
   cudaFree(p->scan_tmp);
+  gev_ctx *ctx = p->ctx;
   delete p;
+  if (ctx) ctx_release(ctx);
   return GEV_OK;
 }
 

@@ -11,17 +11,6 @@
 #include <cstring>
 
 #include "gev_internal.cuh"
-#include "../../include/gev_sim.h"
-
-struct gev_sim {
-  gev_ctx *ctx = nullptr;
-  gev_pcls *pcls = nullptr;
-  gev_field *phi = nullptr, *chi = nullptr, *source = nullptr, *Sij = nullptr, *Bi = nullptr;
-  gev_field *scalarFT = nullptr, *SijFT = nullptr, *BiFT = nullptr;
-  gev_sim_state st{};
-  double *host_words = nullptr;  // pinned: [0] T00 sum, [1] max bits, [2] phi(k=0).re
-  double *dev_words = nullptr;
-};
 
 namespace {
 
@@ -97,6 +86,7 @@ int gev_sim_create(gev_ctx *ctx, long np, gev_sim **out) {
   if (!ctx || !out || np < 0) return gev_fail(ctx, GEV_EINVAL, "sim_create");
   gev_sim *s = new gev_sim();
   s->ctx = ctx;
+  ctx_retain(ctx);
   int rc = gev_pcls_create(ctx, np, 0., &s->pcls);
   if (!rc) rc = gev_field_create(ctx, GEV_FIELD_REAL, 1, &s->phi);
   if (!rc) rc = gev_field_create(ctx, GEV_FIELD_REAL, 1, &s->chi);
@@ -133,7 +123,9 @@ int gev_sim_destroy(gev_sim *s) {
   gev_field_destroy(s->BiFT);
   if (s->host_words) cudaFreeHost(s->host_words);
   cudaFree(s->dev_words);
+  gev_ctx *ctx = s->ctx;
   delete s;
+  if (ctx) ctx_release(ctx);
   return GEV_OK;
 }
 

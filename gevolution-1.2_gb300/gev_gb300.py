@@ -442,3 +442,29 @@ class _BorrowedParticles(Particles):
 
     def __del__(self):
         pass
+
+
+class ICParams(ctypes.Structure):
+    _fields_ = [(n, _d) for n in ("h", "Omega_cdm", "Omega_b", "n_s", "sigma8", "z_in", "boxsize", "Cf",
+                                  "steplimit")] + [("seed", ctypes.c_uint64), ("ksphere", _i)]
+
+
+def ic_params(boxsize, seed=1, z_in=100.0, Cf=48.0, steplimit=0.04, Omega_cdm=0.27, Omega_b=0.05, sigma8=0.81,
+              n_s=0.96, h=0.67, ksphere=1):
+    """The initial-condition settings of the benchmark configurations (BBKS, z_in = 100)."""
+    return dict(h=h, Omega_cdm=Omega_cdm, Omega_b=Omega_b, n_s=n_s, sigma8=sigma8, z_in=z_in, boxsize=boxsize, Cf=Cf,
+                steplimit=steplimit, seed=seed, ksphere=ksphere)
+
+
+def sim_ic_generate(sim, **params):
+    L = _sim_lib()
+    if not getattr(L, "_ic_ready", False):
+        L.gev_sim_ic_generate.argtypes = [_vp, ctypes.POINTER(ICParams)]
+        L.gev_sim_ic_generate.restype = ctypes.c_int
+        L._ic_ready = True
+    p = ICParams(**params)
+    _check(L.gev_sim_ic_generate(sim.handle, ctypes.byref(p)), sim.ctx, "gev_sim_ic_generate")
+    return sim
+
+
+Sim.ic_generate = sim_ic_generate

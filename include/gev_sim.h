@@ -51,6 +51,18 @@ int gev_sim_particles(gev_sim *s, gev_pcls **out);
 /* one cycle: deposits, phi / chi / B solves, kick, drift, background, next dtau */
 int gev_sim_step(gev_sim *s);
 
+/* Zel'dovich initial conditions at z_in generated on the device, following the
+ * power-spectrum branch of generateIC_basic (ic_basic.hpp:1626-2259): sc1
+ * template tiled N/4 times, BBKS spectrum normalised to sigma8, baryons folded
+ * into CDM, no radiation.  Requires N % 4 == 0 and capacity >= N^3.  Sets the
+ * whole state (a, tau, dtau, dtau_old = 0, fourpiG, cosmology, particle mass). */
+typedef struct {
+  double h, Omega_cdm, Omega_b, n_s, sigma8, z_in, boxsize, Cf, steplimit;
+  uint64_t seed;
+  int ksphere; /* 1: k-domain = sphere */
+} gev_ic_params;
+int gev_sim_ic_generate(gev_sim *s, const gev_ic_params *ic);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,96 @@
+"""Device-generated initial conditions against the oracle's, and the
+mixed-precision form (FP32 fields and FFTs, FP64 positions, int64 fixed-point
+deposits) against the FP64 form."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300))
+
+
+@pytest.mark.parametrize("N", [16, 32])
+def test_device_ic_matches_oracle(gpu, oracle, N):
+    L = 5.0 * N
+    o = oracle.Sim(N).ic(**oracle.default_icparams(N, L, seed=21))
+    ctx = gpu.Context(N)
+    s = gpu.Sim(ctx, N ** 3)
+    s.ic_generate(**gpu.ic_params(L, seed=21))
+    st = s.state()
+    for k in ("a", "dtau", "fourpiG", "mass"):
+        assert abs(st[k] - o.scalars()[k]) <= 1e-14 * abs(o.scalars()[k]), k
+    assert abs(st["tau"] - o.s.tau) <= 1e-12 * o.s.tau
+    got = s.particles().download()
+    ref = o.particles
+    assert (got["ID"] == ref["ID"]).all()
+    assert np.abs(got["pos"] - ref["pos"]).max() * N < 1e-12
+    assert rel(got["vel"], ref["vel"]) < 1e-11
+    for name in ("phi", "chi", "Bi"):
+        assert rel(s.field(name).download(), o.field(name)) < 1e-11, name
+    assert rel(s.field("BiFT").download(), o.spectrum("BiFT")) < 1e-11
+
+
+@pytest.mark.parametrize("N", [16, 32, 48])
+def test_mixed_operators_against_fp64(gpu, oracle, N):
+    rng = np.random.default_rng(7 + N)
+    c64, c32 = gpu.Context(N, gpu.PREC_FP64), gpu.Context(N, gpu.PREC_MIXED)
+    x = rng.standard_normal((6, N, N, N))
+    out = {}
+    for c in (c64, c32):
+        r = c.real(6).upload(x)
+        sp = c.spectrum(6)
+        gpu.fft_r2c(r, sp)
+        one = c.spectrum(1)
+        gpu.project_scalar(sp, one, 0)
+        back = c.real(1)
+        gpu.fft_c2r(one, back)
+        out[c.precision] = (sp.download(), back.download())
+    assert rel(out[1][0], out[0][0]) < 1e-5
+    assert rel(out[1][1], out[0][1]) < 1e-4
+
+
+@pytest.mark.parametrize("N", [16, 32])
+def test_mixed_deposits_reproducible_and_close(gpu, oracle, N):
+    rng = np.random.default_rng(3 * N)
+    n = N ** 3
+    p = np.zeros(n, oracle.PART)
+    p["pos"] = rng.random((n, 3))
+    p["pos"][:300] = 0.25 + rng.random((300, 3)) * (0.4 / N)  # a dense clump
+    p["vel"] = rng.standard_normal((n, 3)) * 1e-3
+    p["ID"] = np.arange(n)
+    phi_h = rng.standard_normal((1, N, N, N)) * 1e-5
+    res = {}
+    for prec in (gpu.PREC_FP64, gpu.PREC_MIXED):
+        c = gpu.Context(N, prec)
+        pc = c.particles(n, 1.0 / n).upload(p)
+        phi = c.real(1).upload(phi_h)
+        fs = []
+        for _ in range(2):
+            T = c.real(6)
+            gpu.projection_Tij(pc, T, 0.05, phi)
+            f0 = c.real(1)
+            gpu.projection_T00(pc, f0, 0.05, phi)
+            fs.append((f0.download(), T.download()))
+        assert np.array_equal(fs[0][0], fs[1][0]) and np.array_equal(fs[0][1], fs[1][1])
+        res[prec] = fs[0]
+    assert rel(res[1][0], res[0][0]) < 1e-6
+    assert rel(res[1][1], res[0][1]) < 1e-5
+
+
+def test_mixed_cycles_track_fp64(gpu, oracle):
+    """A few cycles from the same device IC: mixed positions stay within 1e-4 of a cell."""
+    N = 32
+    sims = {}
+    for prec in (gpu.PREC_FP64, gpu.PREC_MIXED):
+        c = gpu.Context(N, prec)
+        s = gpu.Sim(c, N ** 3)
+        s.ic_generate(**gpu.ic_params(160.0, seed=4))
+        for _ in range(8):
+            s.step()
+        sims[prec] = (c, s, s.particles().download())
+    a, b = sims[0][2], sims[1][2]
+    order_a, order_b = np.argsort(a["ID"]), np.argsort(b["ID"])
+    d = (a["pos"][order_a] - b["pos"][order_b] + 0.5) % 1.0 - 0.5
+    assert np.abs(d).max() * N < 1e-4
