@@ -46,7 +46,7 @@ FALLBACK_HBM_GBS = 6800.0
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--steps", type=int, default=20)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--grid", type=int, default=512)
@@ -200,31 +200,36 @@ def run_ours(args, rank, world, local):
                 e2e=e2e, box=box)
 
 
+# DRAM traffic per launch of the column pass from the committed ncu captures
+# (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (grid, precision);
+# see profiles/fft_cols_*.md for the command and the raw figures
+COLS_TRAFFIC = {}
+
+
 def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
+    """The FFT column pass (k_fft_cols, the y / z passes of every transform) is the
+    largest share of the cycle in the ncu launch list.  One launch transforms one
+    spectrum component along y or z in place: its algorithmic bytes are one read
+    and one write of the component, 2 * N^2 (N/2+1) * sizeof(complex)."""
     import torch
-    r = 8 if prec == "fp64" else 4
-    pcls = sim.particles()
-    Sij = sim.field("Sij")
-    phi = sim.field("phi")
-    st = sim.state()
-    reps = 3
+    csz = 16 if prec == "fp64" else 8
+    spec = sim.field("scalarFT")
+    reps = 6
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    gpu.projection_Tij(pcls, Sij, st["a"], phi, 1.0)
+    gpu.fft_axis(spec, 1, -1)
     ctx.sync()
     e0.record(stream)
-    for _ in range(reps):
-        gpu.projection_Tij(pcls, Sij, st["a"], phi, 1.0)
+    for i in range(reps):
+        gpu.fft_axis(spec, 1 + (i & 1), -1)
     e1.record(stream)
     e1.synchronize()
     ms = e0.elapsed_time(e1) / reps
-    V = N ** 3
-    # algorithmic bytes: particle pos+vel read once, phi read once, 6 components read-modify-written
-    alg = V * (3 * 8 + 3 * r) + V * r + 6 * V * r * 2
+    alg = 2 * N * N * (N // 2 + 1) * csz
     peak, kind = hbm_peak()
     achieved = alg / (ms / 1e3) / 1e9
-    return {"kernel": "projection_Tij (deposit of T_ij, both passes)", "bound": "hbm", "achieved": achieved,
-            "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None, "peak_kind": kind,
-            "ms_per_launch": ms, "alg_bytes": alg}
+    return {"kernel": "k_fft_cols (one y or z pass of the 3-D FFT over one spectrum component)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": COLS_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
 
 
 def run_e2e(gpu, ctx, sim, stream, N, steps, torch):
@@ -235,13 +240,13 @@ def run_e2e(gpu, ctx, sim, stream, N, steps, torch):
     arr = host.numpy().view(gpu.PART)
     back = torch.empty(n * 56, dtype=torch.uint8, pin_memory=True)
     barr = back.numpy().view(gpu.PART)
-    arr[:] = pcls.download()
+    pcls.download(out=arr)
     ctx.sync()
     t0 = time.perf_counter()
     for _ in range(steps):
         pcls.upload(arr)
         sim.step()
-        barr[:] = pcls.download()  # download synchronises the stream
+        pcls.download(out=barr)  # into pinned memory; synchronises the stream
     dt = time.perf_counter() - t0
     return {"value": n * steps / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 56,
             "d2h_bytes_per_step": n * 56}

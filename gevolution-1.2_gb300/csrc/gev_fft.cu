@@ -408,3 +408,21 @@ int fft_c2r_comp(gev_ctx *ctx, const void *spec, void *real, void *scratch) {
   return ctx->prec == GEV_PREC_FP64 ? c2r_comp<double>(ctx, spec, real, scratch)
                                     : c2r_comp<float>(ctx, spec, real, scratch);
 }
+
+extern "C" int gev_fft_axis(gev_ctx *ctx, gev_field *spec, int axis, int sign) {
+  if (!ctx || !spec || spec->ctx != ctx || spec->kind != GEV_FIELD_SPECTRUM || (axis != 1 && axis != 2) ||
+      (sign != -1 && sign != 1))
+    return gev_fail(ctx, GEV_EINVAL, "fft_axis: spectrum, axis 1 (y) or 2 (z), sign -1 or +1");
+  const int N = ctx->N, NH = N / 2 + 1;
+  const long ls = axis == 1 ? NH : (long)N * NH, ps = axis == 1 ? (long)N * NH : NH;
+  for (int c = 0; c < spec->ncomp; ++c) {
+    void *d = (char *)spec->d + c * spec->comp_elems * spec->elem_bytes;
+    int rc;
+    if (ctx->prec == GEV_PREC_FP64)
+      rc = sign < 0 ? run_cols<double, -1>(ctx, d, d, ls, ps) : run_cols<double, +1>(ctx, d, d, ls, ps);
+    else
+      rc = sign < 0 ? run_cols<float, -1>(ctx, d, d, ls, ps) : run_cols<float, +1>(ctx, d, d, ls, ps);
+    if (rc) return rc;
+  }
+  return GEV_OK;
+}

@@ -262,108 +262,182 @@ __device__ __forceinline__ T F(const T *__restrict__ f, int x, int y, int z, int
   return __ldg(&f[sidx(wrapi(x, N), wrapi(y, N), wrapi(z, N), N)]);
 }
 
-// update_q, gevolution.hpp:570-678 (GRADIENT_ORDER 1).  The field values at the
-// particle's cell corners are gathered once; ref_dist = pos*N - cell.
-template <typename T, typename V, int KIND>
-__global__ void __launch_bounds__(256) k_update_q(PclsArrays P, long n, const T *__restrict__ phi,
-                                                  const T *__restrict__ chi, const T *__restrict__ Bi, Params pr,
-                                                  unsigned long long *maxbits) {
+// The per-particle physics of update_q (gevolution.hpp:570-678, GRADIENT_ORDER 1)
+// and update_pos (810-871), on the particle's linked cell (cx, cy, cz) and its
+// in-cell offset r = pos*N - cell (ref_dist of the reference).  Field values are
+// gathered with periodic wrap.
+
+// q -> q - dtau e grad / dx (GR) or q - dtau a grad / dx (Newton)
+template <typename T, int KIND>
+__device__ __forceinline__ void kick_one(const T *__restrict__ phi, const T *__restrict__ chi,
+                                         const T *__restrict__ Bi, const Params &pr, int cx, int cy, int cz, T r0, T r1,
+                                         T r2, T &q0, T &q1, T &q2) {
   const int N = pr.N;
   const size_t NV = (size_t)N * N * N;
-  T vmax = (T)0;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const uint32_t c = P.cell[i];
-    const int cx = (int)(c % N), cy = (int)((c / N) % N), cz = (int)(c / ((uint32_t)N * N));
-    T r0, r1, r2;
-    if constexpr (sizeof(T) == 4) {
-      r0 = P.rx[i];
-      r1 = P.ry[i];
-      r2 = P.rz[i];
-    } else {
-      r0 = (T)(P.px[i] * (double)N - cx);
-      r1 = (T)(P.py[i] * (double)N - cy);
-      r2 = (T)(P.pz[i] * (double)N - cz);
-    }
-    T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
-    const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
-    T g0, g1, g2;
-    {
-      const T f000 = F(phi, cx, cy, cz, N), f100 = F(phi, cx + 1, cy, cz, N), f010 = F(phi, cx, cy + 1, cz, N),
-              f110 = F(phi, cx + 1, cy + 1, cz, N), f001 = F(phi, cx, cy, cz + 1, N),
-              f101 = F(phi, cx + 1, cy, cz + 1, N), f011 = F(phi, cx, cy + 1, cz + 1, N),
-              f111 = F(phi, cx + 1, cy + 1, cz + 1, N);
-      g0 = s1 * s2 * (f100 - f000) + r1 * s2 * (f110 - f010) + s1 * r2 * (f101 - f001) + r1 * r2 * (f111 - f011);
-      g1 = s0 * s2 * (f010 - f000) + r0 * s2 * (f110 - f100) + s0 * r2 * (f011 - f001) + r0 * r2 * (f111 - f101);
-      g2 = s0 * s1 * (f001 - f000) + r0 * s1 * (f101 - f100) + s0 * r1 * (f011 - f010) + r0 * r1 * (f111 - f110);
-    }
-    const T a = (T)pr.a;
-    T e2 = (T)0, e = (T)0, inv_e = (T)0;
-    if (KIND == GEV_GR) {
-      const T v2 = q0 * q0 + q1 * q1 + q2 * q2;
-      e2 = v2 + a * a;
-      const T fac = (v2 + e2) / e2;
-      g0 *= fac;
-      g1 *= fac;
-      g2 *= fac;
-    }
-    if (pr.nfield >= 2 && chi != nullptr) {
-      const T f000 = F(chi, cx, cy, cz, N), f100 = F(chi, cx + 1, cy, cz, N), f010 = F(chi, cx, cy + 1, cz, N),
-              f110 = F(chi, cx + 1, cy + 1, cz, N), f001 = F(chi, cx, cy, cz + 1, N),
-              f101 = F(chi, cx + 1, cy, cz + 1, N), f011 = F(chi, cx, cy + 1, cz + 1, N),
-              f111 = F(chi, cx + 1, cy + 1, cz + 1, N);
-      g0 -= s1 * s2 * (f100 - f000) + r1 * s2 * (f110 - f010) + s1 * r2 * (f101 - f001) + r1 * r2 * (f111 - f011);
-      g1 -= s0 * s2 * (f010 - f000) + r0 * s2 * (f110 - f100) + s0 * r2 * (f011 - f001) + r0 * r2 * (f111 - f101);
-      g2 -= s0 * s1 * (f001 - f000) + r0 * s1 * (f101 - f100) + s0 * r1 * (f011 - f010) + r0 * r1 * (f111 - f110);
-    }
-    if (KIND == GEV_GR) {
-      e = sqrt(e2);
-      inv_e = (T)1 / e;
-      if (pr.nfield >= 3 && Bi != nullptr) {
-        const T *B0 = Bi, *B1 = Bi + NV, *B2 = Bi + 2 * NV;
-        const T t0 = (T)2 * r0, t1 = (T)2 * r1, t2 = (T)2 * r2;
-        T p0, p1, p2;
-        p0 = (s2 * (F(B1, cx + 1, cy, cz, N) - F(B1, cx, cy, cz, N)) +
-              r2 * (F(B1, cx + 1, cy, cz + 1, N) - F(B1, cx, cy, cz + 1, N))) * q1;
-        p0 += (s1 * (F(B2, cx + 1, cy, cz, N) - F(B2, cx, cy, cz, N)) +
-               r1 * (F(B2, cx + 1, cy + 1, cz, N) - F(B2, cx, cy + 1, cz, N))) * q2;
-        p0 += (s1 * s2 * ((r0 - (T)1) * F(B0, cx - 1, cy, cz, N) + ((T)1 - t0) * F(B0, cx, cy, cz, N) + r0 * F(B0, cx + 1, cy, cz, N)) +
-               r1 * s2 * ((r0 - (T)1) * F(B0, cx - 1, cy + 1, cz, N) + ((T)1 - t0) * F(B0, cx, cy + 1, cz, N) + r0 * F(B0, cx + 1, cy + 1, cz, N)) +
-               s1 * r2 * ((r0 - (T)1) * F(B0, cx - 1, cy, cz + 1, N) + ((T)1 - t0) * F(B0, cx, cy, cz + 1, N) + r0 * F(B0, cx + 1, cy, cz + 1, N)) +
-               r1 * r2 * ((r0 - (T)1) * F(B0, cx - 1, cy + 1, cz + 1, N) + ((T)1 - t0) * F(B0, cx, cy + 1, cz + 1, N) + r0 * F(B0, cx + 1, cy + 1, cz + 1, N))) * q0;
-        p1 = (s0 * (F(B2, cx, cy + 1, cz, N) - F(B2, cx, cy, cz, N)) +
-              r0 * (F(B2, cx + 1, cy + 1, cz, N) - F(B2, cx + 1, cy, cz, N))) * q2;
-        p1 += (s2 * (F(B0, cx, cy + 1, cz, N) - F(B0, cx, cy, cz, N)) +
-               r2 * (F(B0, cx, cy + 1, cz + 1, N) - F(B0, cx, cy, cz + 1, N))) * q0;
-        p1 += (s0 * s2 * ((r1 - (T)1) * F(B1, cx, cy - 1, cz, N) + ((T)1 - t1) * F(B1, cx, cy, cz, N) + r1 * F(B1, cx, cy + 1, cz, N)) +
-               r0 * s2 * ((r1 - (T)1) * F(B1, cx + 1, cy - 1, cz, N) + ((T)1 - t1) * F(B1, cx + 1, cy, cz, N) + r1 * F(B1, cx + 1, cy + 1, cz, N)) +
-               s0 * r2 * ((r1 - (T)1) * F(B1, cx, cy - 1, cz + 1, N) + ((T)1 - t1) * F(B1, cx, cy, cz + 1, N) + r1 * F(B1, cx, cy + 1, cz + 1, N)) +
-               r0 * r2 * ((r1 - (T)1) * F(B1, cx + 1, cy - 1, cz + 1, N) + ((T)1 - t1) * F(B1, cx + 1, cy, cz + 1, N) + r1 * F(B1, cx + 1, cy + 1, cz + 1, N))) * q1;
-        p2 = (s1 * (F(B0, cx, cy, cz + 1, N) - F(B0, cx, cy, cz, N)) +
-              r1 * (F(B0, cx, cy + 1, cz + 1, N) - F(B0, cx, cy + 1, cz, N))) * q0;
-        p2 += (s0 * (F(B1, cx, cy, cz + 1, N) - F(B1, cx, cy, cz, N)) +
-               r0 * (F(B1, cx + 1, cy, cz + 1, N) - F(B1, cx + 1, cy, cz, N))) * q1;
-        p2 += (s0 * s1 * ((r2 - (T)1) * F(B2, cx, cy, cz - 1, N) + ((T)1 - t2) * F(B2, cx, cy, cz, N) + r2 * F(B2, cx, cy, cz + 1, N)) +
-               r0 * s1 * ((r2 - (T)1) * F(B2, cx + 1, cy, cz - 1, N) + ((T)1 - t2) * F(B2, cx + 1, cy, cz, N) + r2 * F(B2, cx + 1, cy, cz + 1, N)) +
-               s0 * r1 * ((r2 - (T)1) * F(B2, cx, cy + 1, cz - 1, N) + ((T)1 - t2) * F(B2, cx, cy + 1, cz, N) + r2 * F(B2, cx, cy + 1, cz + 1, N)) +
-               r0 * r1 * ((r2 - (T)1) * F(B2, cx + 1, cy + 1, cz - 1, N) + ((T)1 - t2) * F(B2, cx + 1, cy + 1, cz, N) + r2 * F(B2, cx + 1, cy + 1, cz + 1, N))) * q2;
-        const T k = (T)pr.inv_a2N * inv_e;
-        g0 += p0 * k;
-        g1 += p1 * k;
-        g2 += p2 * k;
-      }
-    }
-    // vel -= dtau * e * grad / dx   (GR);  vel -= dtau * a * grad / dx   (Newton)
-    const T m = (T)pr.dtau * (KIND == GEV_GR ? e : a) * (T)N;
-    q0 -= m * g0;
-    q1 -= m * g1;
-    q2 -= m * g2;
-    ((V *)P.vx)[i] = (V)q0;
-    ((V *)P.vy)[i] = (V)q1;
-    ((V *)P.vz)[i] = (V)q2;
-    const T v2 = (q0 * q0 + q1 * q1 + q2 * q2) * (T)pr.inv_a2;
-    vmax = v2 > vmax ? v2 : vmax;
+  const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
+  T g0, g1, g2;
+  {
+    const T f000 = F(phi, cx, cy, cz, N), f100 = F(phi, cx + 1, cy, cz, N), f010 = F(phi, cx, cy + 1, cz, N),
+            f110 = F(phi, cx + 1, cy + 1, cz, N), f001 = F(phi, cx, cy, cz + 1, N), f101 = F(phi, cx + 1, cy, cz + 1, N),
+            f011 = F(phi, cx, cy + 1, cz + 1, N), f111 = F(phi, cx + 1, cy + 1, cz + 1, N);
+    g0 = s1 * s2 * (f100 - f000) + r1 * s2 * (f110 - f010) + s1 * r2 * (f101 - f001) + r1 * r2 * (f111 - f011);
+    g1 = s0 * s2 * (f010 - f000) + r0 * s2 * (f110 - f100) + s0 * r2 * (f011 - f001) + r0 * r2 * (f111 - f101);
+    g2 = s0 * s1 * (f001 - f000) + r0 * s1 * (f101 - f100) + s0 * r1 * (f011 - f010) + r0 * r1 * (f111 - f110);
   }
-  // max over the block, then one atomic on the bit pattern (non-negative doubles order as integers)
+  const T a = (T)pr.a;
+  T e = (T)0, inv_e = (T)0;
+  if (KIND == GEV_GR) {
+    const T v2 = q0 * q0 + q1 * q1 + q2 * q2;
+    const T e2 = v2 + a * a;
+    const T fac = (v2 + e2) / e2;
+    g0 *= fac;
+    g1 *= fac;
+    g2 *= fac;
+    e = sqrt(e2);
+    inv_e = (T)1 / e;
+  }
+  if (pr.nfield >= 2 && chi != nullptr) {
+    const T f000 = F(chi, cx, cy, cz, N), f100 = F(chi, cx + 1, cy, cz, N), f010 = F(chi, cx, cy + 1, cz, N),
+            f110 = F(chi, cx + 1, cy + 1, cz, N), f001 = F(chi, cx, cy, cz + 1, N), f101 = F(chi, cx + 1, cy, cz + 1, N),
+            f011 = F(chi, cx, cy + 1, cz + 1, N), f111 = F(chi, cx + 1, cy + 1, cz + 1, N);
+    g0 -= s1 * s2 * (f100 - f000) + r1 * s2 * (f110 - f010) + s1 * r2 * (f101 - f001) + r1 * r2 * (f111 - f011);
+    g1 -= s0 * s2 * (f010 - f000) + r0 * s2 * (f110 - f100) + s0 * r2 * (f011 - f001) + r0 * r2 * (f111 - f101);
+    g2 -= s0 * s1 * (f001 - f000) + r0 * s1 * (f101 - f100) + s0 * r1 * (f011 - f010) + r0 * r1 * (f111 - f110);
+  }
+  if (KIND == GEV_GR && pr.nfield >= 3 && Bi != nullptr) {
+    const T *B0 = Bi, *B1 = Bi + NV, *B2 = Bi + 2 * NV;
+    const T t0 = (T)2 * r0, t1 = (T)2 * r1, t2 = (T)2 * r2;
+    T p0, p1, p2;
+    p0 = (s2 * (F(B1, cx + 1, cy, cz, N) - F(B1, cx, cy, cz, N)) +
+          r2 * (F(B1, cx + 1, cy, cz + 1, N) - F(B1, cx, cy, cz + 1, N))) * q1;
+    p0 += (s1 * (F(B2, cx + 1, cy, cz, N) - F(B2, cx, cy, cz, N)) +
+           r1 * (F(B2, cx + 1, cy + 1, cz, N) - F(B2, cx, cy + 1, cz, N))) * q2;
+    p0 += (s1 * s2 * ((r0 - (T)1) * F(B0, cx - 1, cy, cz, N) + ((T)1 - t0) * F(B0, cx, cy, cz, N) + r0 * F(B0, cx + 1, cy, cz, N)) +
+           r1 * s2 * ((r0 - (T)1) * F(B0, cx - 1, cy + 1, cz, N) + ((T)1 - t0) * F(B0, cx, cy + 1, cz, N) + r0 * F(B0, cx + 1, cy + 1, cz, N)) +
+           s1 * r2 * ((r0 - (T)1) * F(B0, cx - 1, cy, cz + 1, N) + ((T)1 - t0) * F(B0, cx, cy, cz + 1, N) + r0 * F(B0, cx + 1, cy, cz + 1, N)) +
+           r1 * r2 * ((r0 - (T)1) * F(B0, cx - 1, cy + 1, cz + 1, N) + ((T)1 - t0) * F(B0, cx, cy + 1, cz + 1, N) + r0 * F(B0, cx + 1, cy + 1, cz + 1, N))) * q0;
+    p1 = (s0 * (F(B2, cx, cy + 1, cz, N) - F(B2, cx, cy, cz, N)) +
+          r0 * (F(B2, cx + 1, cy + 1, cz, N) - F(B2, cx + 1, cy, cz, N))) * q2;
+    p1 += (s2 * (F(B0, cx, cy + 1, cz, N) - F(B0, cx, cy, cz, N)) +
+           r2 * (F(B0, cx, cy + 1, cz + 1, N) - F(B0, cx, cy, cz + 1, N))) * q0;
+    p1 += (s0 * s2 * ((r1 - (T)1) * F(B1, cx, cy - 1, cz, N) + ((T)1 - t1) * F(B1, cx, cy, cz, N) + r1 * F(B1, cx, cy + 1, cz, N)) +
+           r0 * s2 * ((r1 - (T)1) * F(B1, cx + 1, cy - 1, cz, N) + ((T)1 - t1) * F(B1, cx + 1, cy, cz, N) + r1 * F(B1, cx + 1, cy + 1, cz, N)) +
+           s0 * r2 * ((r1 - (T)1) * F(B1, cx, cy - 1, cz + 1, N) + ((T)1 - t1) * F(B1, cx, cy, cz + 1, N) + r1 * F(B1, cx, cy + 1, cz + 1, N)) +
+           r0 * r2 * ((r1 - (T)1) * F(B1, cx + 1, cy - 1, cz + 1, N) + ((T)1 - t1) * F(B1, cx + 1, cy, cz + 1, N) + r1 * F(B1, cx + 1, cy + 1, cz + 1, N))) * q1;
+    p2 = (s1 * (F(B0, cx, cy, cz + 1, N) - F(B0, cx, cy, cz, N)) +
+          r1 * (F(B0, cx, cy + 1, cz + 1, N) - F(B0, cx, cy + 1, cz, N))) * q0;
+    p2 += (s0 * (F(B1, cx, cy, cz + 1, N) - F(B1, cx, cy, cz, N)) +
+           r0 * (F(B1, cx + 1, cy, cz + 1, N) - F(B1, cx + 1, cy, cz, N))) * q1;
+    p2 += (s0 * s1 * ((r2 - (T)1) * F(B2, cx, cy, cz - 1, N) + ((T)1 - t2) * F(B2, cx, cy, cz, N) + r2 * F(B2, cx, cy, cz + 1, N)) +
+           r0 * s1 * ((r2 - (T)1) * F(B2, cx + 1, cy, cz - 1, N) + ((T)1 - t2) * F(B2, cx + 1, cy, cz, N) + r2 * F(B2, cx + 1, cy, cz + 1, N)) +
+           s0 * r1 * ((r2 - (T)1) * F(B2, cx, cy + 1, cz - 1, N) + ((T)1 - t2) * F(B2, cx, cy + 1, cz, N) + r2 * F(B2, cx, cy + 1, cz + 1, N)) +
+           r0 * r1 * ((r2 - (T)1) * F(B2, cx + 1, cy + 1, cz - 1, N) + ((T)1 - t2) * F(B2, cx + 1, cy + 1, cz, N) + r2 * F(B2, cx + 1, cy + 1, cz + 1, N))) * q2;
+    const T k = (T)pr.inv_a2N * inv_e;
+    g0 += p0 * k;
+    g1 += p1 * k;
+    g2 += p2 * k;
+  }
+  const T m = (T)pr.dtau * (KIND == GEV_GR ? e : a) * (T)N;
+  q0 -= m * g0;
+  q1 -= m * g1;
+  q2 -= m * g2;
+}
+
+// the coordinate velocity of update_pos (GR): q (1 + (3 - q^2/e^2) phi - chi) / e + b / (a^2 N)
+template <typename T>
+__device__ __forceinline__ void drift_vel(const T *__restrict__ phi, const T *__restrict__ chi,
+                                          const T *__restrict__ Bi, const Params &pr, int cx, int cy, int cz, T r0,
+                                          T r1, T r2, T q0, T q1, T q2, T &v0, T &v1, T &v2) {
+  const int N = pr.N;
+  const size_t NV = (size_t)N * N * N;
+  const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
+  const T a = (T)pr.a;
+  const T qq = q0 * q0 + q1 * q1 + q2 * q2;
+  const T e2 = qq + a * a;
+  T ph = (T)0, ch = (T)0;
+  const T w000 = s0 * s1 * s2, w100 = r0 * s1 * s2, w010 = s0 * r1 * s2, w110 = r0 * r1 * s2;
+  const T w001 = s0 * s1 * r2, w101 = r0 * s1 * r2, w011 = s0 * r1 * r2, w111 = r0 * r1 * r2;
+  if (pr.nfield >= 1)
+    ph = F(phi, cx, cy, cz, N) * w000 + F(phi, cx + 1, cy, cz, N) * w100 + F(phi, cx, cy + 1, cz, N) * w010 +
+         F(phi, cx + 1, cy + 1, cz, N) * w110 + F(phi, cx, cy, cz + 1, N) * w001 + F(phi, cx + 1, cy, cz + 1, N) * w101 +
+         F(phi, cx, cy + 1, cz + 1, N) * w011 + F(phi, cx + 1, cy + 1, cz + 1, N) * w111;
+  if (pr.nfield >= 2)
+    ch = F(chi, cx, cy, cz, N) * w000 + F(chi, cx + 1, cy, cz, N) * w100 + F(chi, cx, cy + 1, cz, N) * w010 +
+         F(chi, cx + 1, cy + 1, cz, N) * w110 + F(chi, cx, cy, cz + 1, N) * w001 + F(chi, cx + 1, cy, cz + 1, N) * w101 +
+         F(chi, cx, cy + 1, cz + 1, N) * w011 + F(chi, cx + 1, cy + 1, cz + 1, N) * w111;
+  const T inv_e2 = (T)1 / e2;
+  const T fac = ((T)1 + ((T)3 - qq * inv_e2) * ph - ch) * sqrt(inv_e2);
+  v0 = q0 * fac;
+  v1 = q1 * fac;
+  v2 = q2 * fac;
+  if (pr.nfield >= 3) {
+    const T *B0 = Bi, *B1 = Bi + NV, *B2 = Bi + 2 * NV;
+    const T b0 = F(B0, cx, cy, cz, N) * s1 * s2 + F(B0, cx, cy + 1, cz, N) * r1 * s2 + F(B0, cx, cy, cz + 1, N) * s1 * r2 +
+                 F(B0, cx, cy + 1, cz + 1, N) * r1 * r2;
+    const T b1 = F(B1, cx, cy, cz, N) * s0 * s2 + F(B1, cx + 1, cy, cz, N) * r0 * s2 + F(B1, cx, cy, cz + 1, N) * s0 * r2 +
+                 F(B1, cx + 1, cy, cz + 1, N) * r0 * r2;
+    const T b2 = F(B2, cx, cy, cz, N) * s0 * s1 + F(B2, cx + 1, cy, cz, N) * r0 * s1 + F(B2, cx, cy + 1, cz, N) * s0 * r1 +
+                 F(B2, cx + 1, cy + 1, cz, N) * r0 * r1;
+    const T ib = (T)pr.inv_a2N;
+    v0 += b0 * ib;
+    v1 += b1 * ib;
+    v2 += b2 * ib;
+  }
+}
+
+// the particle's linked cell and in-cell offset (the FP32 copy in the mixed form)
+template <typename T>
+__device__ __forceinline__ void load_cell(const PclsArrays &P, long i, int N, int &cx, int &cy, int &cz, T &r0, T &r1,
+                                          T &r2) {
+  const uint32_t c = P.cell[i];
+  cx = (int)(c % N);
+  cy = (int)((c / N) % N);
+  cz = (int)(c / ((uint32_t)N * N));
+  if constexpr (sizeof(T) == 4) {
+    r0 = P.rx[i];
+    r1 = P.ry[i];
+    r2 = P.rz[i];
+  } else {
+    r0 = (T)(P.px[i] * (double)N - cx);
+    r1 = (T)(P.py[i] * (double)N - cy);
+    r2 = (T)(P.pz[i] * (double)N - cz);
+  }
+}
+
+// pos += dtau v, periodic wrap into [0, 1), new cell key (and offset) for the relink
+template <typename T>
+__device__ __forceinline__ void move_store(PclsArrays &P, long i, double dtau, T v0, T v1, T v2, int N, int lg) {
+  double x = P.px[i], y = P.py[i], z = P.pz[i];
+  if constexpr (sizeof(T) == 4) {
+    const float dt = (float)dtau;
+    x += (double)(dt * v0);
+    y += (double)(dt * v1);
+    z += (double)(dt * v2);
+    x = wrap01_bits(x);
+    y = wrap01_bits(y);
+    z = wrap01_bits(z);
+    int cx, cy, cz;
+    float r0, r1, r2;
+    pos_split(x, N, lg, cx, r0);
+    pos_split(y, N, lg, cy, r1);
+    pos_split(z, N, lg, cz, r2);
+    P.rx[i] = r0;
+    P.ry[i] = r1;
+    P.rz[i] = r2;
+    P.cell[i] = (uint32_t)cx + (uint32_t)N * ((uint32_t)cy + (uint32_t)N * (uint32_t)cz);
+  } else {
+    x = wrap01(x + dtau * (double)v0);
+    y = wrap01(y + dtau * (double)v1);
+    z = wrap01(z + dtau * (double)v2);
+    P.cell[i] = cell_key(x, y, z, N);
+  }
+  P.px[i] = x;
+  P.py[i] = y;
+  P.pz[i] = z;
+}
+
+template <typename T>
+__device__ __forceinline__ void block_max_to(T vmax, unsigned long long *maxbits) {
   for (int o = 16; o > 0; o >>= 1) {
     const T other = __shfl_xor_sync(0xffffffffu, vmax, o);
     vmax = other > vmax ? other : vmax;
@@ -378,101 +452,73 @@ __global__ void __launch_bounds__(256) k_update_q(PclsArrays P, long n, const T 
   }
 }
 
-// update_pos, gevolution.hpp:810-871, and update_pos_Newton, 900-903; then the
-// periodic wrap and the new cell key for the relink
+// Particles::updateVel(update_q | update_q_Newton); the reduction is max q^2 / a^2
+template <typename T, typename V, int KIND>
+__global__ void __launch_bounds__(256) k_update_q(PclsArrays P, long n, const T *__restrict__ phi,
+                                                  const T *__restrict__ chi, const T *__restrict__ Bi, Params pr,
+                                                  unsigned long long *maxbits) {
+  T vmax = (T)0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    int cx, cy, cz;
+    T r0, r1, r2;
+    load_cell<T>(P, i, pr.N, cx, cy, cz, r0, r1, r2);
+    T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
+    kick_one<T, KIND>(phi, chi, Bi, pr, cx, cy, cz, r0, r1, r2, q0, q1, q2);
+    ((V *)P.vx)[i] = (V)q0;
+    ((V *)P.vy)[i] = (V)q1;
+    ((V *)P.vz)[i] = (V)q2;
+    const T v2 = (q0 * q0 + q1 * q1 + q2 * q2) * (T)pr.inv_a2;
+    vmax = v2 > vmax ? v2 : vmax;
+  }
+  block_max_to<T>(vmax, maxbits);
+}
+
+// Particles::moveParticles(update_pos | update_pos_Newton), then the wrap and the new key
 template <typename T, typename V, int KIND>
 __global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const T *__restrict__ phi,
                                                     const T *__restrict__ chi, const T *__restrict__ Bi, Params pr) {
-  const int N = pr.N;
-  const size_t NV = (size_t)N * N * N;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    double x = P.px[i], y = P.py[i], z = P.pz[i];
     const T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
-    if (KIND == GEV_NEWTON) {
-      const double f = pr.dtau / pr.a;
-      x += (double)q0 * f;
-      y += (double)q1 * f;
-      z += (double)q2 * f;
+    T v0, v1, v2;
+    if (KIND == GEV_NEWTON) {  // update_pos_Newton: dtau q / a
+      const T ia = (T)(1.0 / pr.a);
+      v0 = q0 * ia;
+      v1 = q1 * ia;
+      v2 = q2 * ia;
     } else {
-      const uint32_t c = P.cell[i];
-      const int cx = (int)(c % N), cy = (int)((c / N) % N), cz = (int)(c / ((uint32_t)N * N));
-      T r0, r1, r2;
-      if constexpr (sizeof(T) == 4) {
-        r0 = P.rx[i];
-        r1 = P.ry[i];
-        r2 = P.rz[i];
-      } else {
-        r0 = (T)(x * (double)N - cx);
-        r1 = (T)(y * (double)N - cy);
-        r2 = (T)(z * (double)N - cz);
-      }
-      const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
-      const T a = (T)pr.a;
-      const T v2 = q0 * q0 + q1 * q1 + q2 * q2;
-      const T e2 = v2 + a * a;
-      T ph = (T)0, ch = (T)0;
-      const T w000 = s0 * s1 * s2, w100 = r0 * s1 * s2, w010 = s0 * r1 * s2, w110 = r0 * r1 * s2;
-      const T w001 = s0 * s1 * r2, w101 = r0 * s1 * r2, w011 = s0 * r1 * r2, w111 = r0 * r1 * r2;
-      if (pr.nfield >= 1)
-        ph = F(phi, cx, cy, cz, N) * w000 + F(phi, cx + 1, cy, cz, N) * w100 + F(phi, cx, cy + 1, cz, N) * w010 +
-             F(phi, cx + 1, cy + 1, cz, N) * w110 + F(phi, cx, cy, cz + 1, N) * w001 +
-             F(phi, cx + 1, cy, cz + 1, N) * w101 + F(phi, cx, cy + 1, cz + 1, N) * w011 +
-             F(phi, cx + 1, cy + 1, cz + 1, N) * w111;
-      if (pr.nfield >= 2)
-        ch = F(chi, cx, cy, cz, N) * w000 + F(chi, cx + 1, cy, cz, N) * w100 + F(chi, cx, cy + 1, cz, N) * w010 +
-             F(chi, cx + 1, cy + 1, cz, N) * w110 + F(chi, cx, cy, cz + 1, N) * w001 +
-             F(chi, cx + 1, cy, cz + 1, N) * w101 + F(chi, cx, cy + 1, cz + 1, N) * w011 +
-             F(chi, cx + 1, cy + 1, cz + 1, N) * w111;
-      const T inv_e2 = (T)1 / e2;
-      const T fac = ((T)1 + ((T)3 - v2 * inv_e2) * ph - ch) * sqrt(inv_e2);
-      T v0 = q0 * fac, v1 = q1 * fac, vv2 = q2 * fac;
-      if (pr.nfield >= 3) {
-        const T *B0 = Bi, *B1 = Bi + NV, *B2 = Bi + 2 * NV;
-        T b0 = F(B0, cx, cy, cz, N) * s1 * s2 + F(B0, cx, cy + 1, cz, N) * r1 * s2 + F(B0, cx, cy, cz + 1, N) * s1 * r2 +
-               F(B0, cx, cy + 1, cz + 1, N) * r1 * r2;
-        T b1 = F(B1, cx, cy, cz, N) * s0 * s2 + F(B1, cx + 1, cy, cz, N) * r0 * s2 + F(B1, cx, cy, cz + 1, N) * s0 * r2 +
-               F(B1, cx + 1, cy, cz + 1, N) * r0 * r2;
-        T b2 = F(B2, cx, cy, cz, N) * s0 * s1 + F(B2, cx + 1, cy, cz, N) * r0 * s1 + F(B2, cx, cy + 1, cz, N) * s0 * r1 +
-               F(B2, cx + 1, cy + 1, cz, N) * r0 * r1;
-        const T ib = (T)pr.inv_a2N;
-        v0 += b0 * ib;
-        v1 += b1 * ib;
-        vv2 += b2 * ib;
-      }
-      if constexpr (sizeof(T) == 4) {
-        const float dt = (float)pr.dtau;
-        x += (double)(dt * v0);
-        y += (double)(dt * v1);
-        z += (double)(dt * vv2);
-      } else {
-        x += pr.dtau * (double)v0;
-        y += pr.dtau * (double)v1;
-        z += pr.dtau * (double)vv2;
-      }
-    }
-    if constexpr (sizeof(T) == 4) {
-      x = wrap01_bits(x);
-      y = wrap01_bits(y);
-      z = wrap01_bits(z);
       int cx, cy, cz;
-      float r0, r1, r2;
-      pos_split(x, N, pr.lg, cx, r0);
-      pos_split(y, N, pr.lg, cy, r1);
-      pos_split(z, N, pr.lg, cz, r2);
-      P.rx[i] = r0;
-      P.ry[i] = r1;
-      P.rz[i] = r2;
-      P.cell[i] = (uint32_t)cx + (uint32_t)N * ((uint32_t)cy + (uint32_t)N * (uint32_t)cz);
-    } else {
-      x = wrap01(x);
-      y = wrap01(y);
-      z = wrap01(z);
-      P.cell[i] = cell_key(x, y, z, N);
+      T r0, r1, r2;
+      load_cell<T>(P, i, pr.N, cx, cy, cz, r0, r1, r2);
+      drift_vel<T>(phi, chi, Bi, pr, cx, cy, cz, r0, r1, r2, q0, q1, q2, v0, v1, v2);
     }
-    P.px[i] = x;
-    P.py[i] = y;
-    P.pz[i] = z;
+    move_store<T>(P, i, pr.dtau, v0, v1, v2, pr.N, pr.lg);
   }
+}
+
+// updateVel(update_q) followed by moveParticles(update_pos) (main.cpp:775-798)
+// in one pass: both read the same cell and the same phi / chi / B values.  The
+// drift's scale factor (after the background half step) comes in pd.
+template <typename T, typename V>
+__global__ void __launch_bounds__(256) k_kick_drift(PclsArrays P, long n, const T *__restrict__ phi,
+                                                    const T *__restrict__ chi, const T *__restrict__ Bi, Params pk,
+                                                    Params pd, unsigned long long *maxbits) {
+  T vmax = (T)0;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    int cx, cy, cz;
+    T r0, r1, r2;
+    load_cell<T>(P, i, pk.N, cx, cy, cz, r0, r1, r2);
+    T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
+    kick_one<T, GEV_GR>(phi, chi, Bi, pk, cx, cy, cz, r0, r1, r2, q0, q1, q2);
+    ((V *)P.vx)[i] = (V)q0;
+    ((V *)P.vy)[i] = (V)q1;
+    ((V *)P.vz)[i] = (V)q2;
+    const T vv = (q0 * q0 + q1 * q1 + q2 * q2) * (T)pk.inv_a2;
+    vmax = vv > vmax ? vv : vmax;
+    T v0, v1, v2;
+    drift_vel<T>(phi, chi, Bi, pd, cx, cy, cz, r0, r1, r2, q0, q1, q2, v0, v1, v2);
+    move_store<T>(P, i, pd.dtau, v0, v1, v2, pd.N, pd.lg);
+  }
+  block_max_to<T>(vmax, maxbits);
 }
 
 template <typename V>
@@ -569,6 +615,27 @@ int pcls_kick_async(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_
   return ctx->prec == GEV_PREC_FP64
              ? launch_update_q<double, double>(ctx, p, kind, dtau, phi, chi, Bi, nfield, a, a2N, maxbits_dev)
              : launch_update_q<float, float>(ctx, p, kind, dtau, phi, chi, Bi, nfield, a, a2N, maxbits_dev);
+}
+
+int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, int nfield_k, double dtau_d,
+                          double a_d, int nfield_d, const gev_field *phi, const gev_field *chi, const gev_field *Bi,
+                          unsigned long long *maxbits_dev) {
+  const int N = ctx->N, lg = lg_pow2(N);
+  const double a2N_k = a_k * a_k * N, a2N_d = a_d * a_d * N;
+  Params pk{dtau_k, a_k, a2N_k, 1.0 / (a_k * a_k), 1.0 / a2N_k, nfield_k, N, lg};
+  Params pd{dtau_d, a_d, a2N_d, 1.0 / (a_d * a_d), 1.0 / a2N_d, nfield_d, N, lg};
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(maxbits_dev, 0, sizeof(unsigned long long), ctx->stream));
+  const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
+  if (ctx->prec == GEV_PREC_FP64)
+    k_kick_drift<double, double><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, (const double *)phi->d,
+                                                                  (const double *)chi->d, (const double *)Bi->d, pk, pd,
+                                                                  maxbits_dev);
+  else
+    k_kick_drift<float, float><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, (const float *)phi->d,
+                                                                (const float *)chi->d, (const float *)Bi->d, pk, pd,
+                                                                maxbits_dev);
+  GEV_LAUNCH_CHECK(ctx);
+  return pcls_relink(ctx, p);
 }
 
 int pcls_relink(gev_ctx *ctx, gev_pcls *p) {

@@ -77,8 +77,9 @@ int sum_async(gev_sim *s, const gev_field *f, double *dst_dev) {
 
 }  // namespace
 
-int pcls_kick_async(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
-                    const gev_field *Bi, int nfield, double a, double a2N, unsigned long long *maxbits_dev);
+int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, int nfield_k, double dtau_d,
+                          double a_d, int nfield_d, const gev_field *phi, const gev_field *chi, const gev_field *Bi,
+                          unsigned long long *maxbits_dev);
 
 extern "C" {
 
@@ -217,13 +218,16 @@ int gev_sim_step(gev_sim *s) {
   }
   RC(gev_fft_c2r(ctx, s->BiFT, s->Bi));
 
-  // particles (main.cpp:764-822)
+  // particles (main.cpp:764-822): the kick at a, the background half step, the
+  // drift at the new a -- the host runs the RK4 first so that one fused pass
+  // does both particle updates, then the relink
   const double dtau = st.dtau;
-  RC(pcls_kick_async(ctx, s->pcls, GEV_GR, (dtau + st.dtau_old) / 2., s->phi, s->chi, s->Bi,
-                     (1. / a < st.z_relax + 1. ? 3 : 2), a, a * a * N, (unsigned long long *)(s->dev_words + 1)));
+  const double a_kick = a;
+  const int nf_kick = 1. / a_kick < st.z_relax + 1. ? 3 : 2;
   rk4bg(a, fourpiG, cm, 0.5 * dtau);
-  RC(gev_update_pos(ctx, s->pcls, GEV_GR, dtau, s->phi, s->chi, s->Bi, (1. / a < st.z_relax + 1. ? 3 : 0), a,
-                    a * a * N));
+  const int nf_drift = 1. / a < st.z_relax + 1. ? 3 : 0;
+  RC(pcls_kick_drift_async(ctx, s->pcls, (dtau + st.dtau_old) / 2., a_kick, nf_kick, dtau, a, nf_drift, s->phi, s->chi,
+                           s->Bi, (unsigned long long *)(s->dev_words + 1)));
   rk4bg(a, fourpiG, cm, 0.5 * dtau);
   GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(s->host_words, s->dev_words, 4 * sizeof(double), cudaMemcpyDeviceToHost,
                                       ctx->stream));

@@ -61,6 +61,7 @@ _SIGS = {
     "gev_prepare_source_scalar": [_vp, _vp, _vp, _vp, _d, _vp, _d, _d, _d],
     "gev_fft_r2c": [_vp, _vp, _vp],
     "gev_fft_c2r": [_vp, _vp, _vp],
+    "gev_fft_axis": [_vp, _vp, _i, _i],
     "gev_solve_poisson": [_vp, _vp, _vp, _d, _d],
     "gev_project_scalar": [_vp, _vp, _vp, _i],
     "gev_evolve_vector": [_vp, _vp, _vp, _d],
@@ -237,8 +238,10 @@ class Particles:
         _check(lib().gev_pcls_count(self.handle, ctypes.byref(n)), self.ctx, "gev_pcls_count")
         return n.value
 
-    def download(self):
-        out = np.empty(self.count(), PART)
+    def download(self, out=None):
+        """Particle records in (cell, ID) order, into `out` (e.g. pinned memory) when given."""
+        if out is None:
+            out = np.empty(self.count(), PART)
         n = _l()
         _check(lib().gev_pcls_download(self.handle, out.ctypes.data if len(out) else None, ctypes.byref(n)),
                self.ctx, "gev_pcls_download")
@@ -281,6 +284,11 @@ def fft_r2c(real, spec):
 
 def fft_c2r(spec, real):
     _check(lib().gev_fft_c2r(spec.ctx.handle, spec.handle, real.handle), spec.ctx, "gev_fft_c2r")
+
+
+def fft_axis(spec, axis, sign):
+    """One pass of the 3-D transform: 1-D FFT along y (axis 1) or z (axis 2), in place."""
+    _check(lib().gev_fft_axis(spec.ctx.handle, spec.handle, axis, sign), spec.ctx, "gev_fft_axis")
 
 
 def solve_poisson(srcFT, potFT, coeff, modif=0.0):

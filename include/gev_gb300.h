@@ -109,6 +109,9 @@ int gev_prepare_source_scalar(gev_ctx *ctx, const gev_field *phi, const gev_fiel
 int gev_fft_r2c(gev_ctx *ctx, const gev_field *real, gev_field *spectrum);
 /* backward transform; never modifies its input spectrum */
 int gev_fft_c2r(gev_ctx *ctx, const gev_field *spectrum, gev_field *real);
+/* one unnormalised 1-D transform of a half spectrum along y (axis 1) or z (axis 2), in place,
+ * sign -1 forward / +1 backward: one of the passes of the 3-D transforms above */
+int gev_fft_axis(gev_ctx *ctx, gev_field *spectrum, int axis, int sign);
 
 /* ---- k-space operators ---- */
 int gev_solve_poisson(gev_ctx *ctx, const gev_field *srcFT, gev_field *potFT, double coeff,
