@@ -139,6 +139,30 @@ int gev_update_pos(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_f
 /* sum of one component over all cells (T00hom, main.cpp:459-463); deterministic order */
 int gev_field_sum(gev_ctx *ctx, const gev_field *f, int comp, double *out);
 
+/* ---- reduction that allocates nothing (no counterpart in gevolution-1.2) ----
+ * For host codes that must not allocate device memory while they run: their
+ * fields fill the GPU and all device memory belongs to their own pool (or to
+ * PyTorch's caching allocator), where a cudaMalloc behind the pool's back can
+ * fail, and cudaMalloc / cudaFree may synchronise the device in the middle of a
+ * queued time step.  Needs no context and calls no allocating routine.
+ *
+ * Sums the n values at device pointer `data` (double for GEV_PREC_FP64, float for
+ * GEV_PREC_MIXED) in FP64 and a fixed order that depends only on n, and writes
+ * the sum to out[0] (device memory) on `cuda_stream` (NULL: the legacy default
+ * stream) of GPU `device`.  Returns when the work is enqueued; the caller
+ * synchronises.  n may be 0 (sum 0); n above GEV_SUM_NOALLOC_MAX_N is rejected
+ * with GEV_EINVAL.  On error a message goes to errbuf (may be NULL).
+ *
+ * Scratch: 1 MiB of partial sums in a static device array, held on every GPU
+ * that loads the library until the process exits.  The first call on a device
+ * looks up that array's device address (cudaGetSymbolAddress), so make it before
+ * any stream capture.  All calls on a GPU share the one array: calls whose work
+ * overlaps on that GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  Nothing in it has to start at zero. */
+#define GEV_SUM_NOALLOC_MAX_N 1073741824LL /* 2^30 values, e.g. one component of a 1024^3 field */
+int gev_sum_noalloc(int device, const void *data, int precision, size_t n, double *out, void *cuda_stream,
+                    char *errbuf, size_t errbuf_len);
+
 #ifdef __cplusplus
 }
 #endif
