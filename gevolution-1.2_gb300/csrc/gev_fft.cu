@@ -26,6 +26,7 @@
 // power of two) or an exact multiply-high division.
 #include <vector>
 
+#include "gev_fft_bfly.cuh"
 #include "gev_internal.cuh"
 
 namespace {
@@ -41,64 +42,6 @@ inline FastDiv make_div(unsigned d) {
   return f;
 }
 __device__ __forceinline__ unsigned fdiv(unsigned t, const FastDiv &f) { return __umulhi(t, f.m); }
-
-template <typename T, int SIGN>
-struct Bfly {
-  typedef typename CT<T>::C C;
-  // multiply by SIGN * i
-  static __device__ __forceinline__ C mi(C a) { return SIGN < 0 ? cmk<C>(a.y, -a.x) : cmk<C>(-a.y, a.x); }
-  static __device__ __forceinline__ void r2(C *v) {
-    C a = v[0];
-    v[0] = cadd(a, v[1]);
-    v[1] = csub(a, v[1]);
-  }
-  static __device__ __forceinline__ void r4(C *v) {
-    C a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]), a2 = cadd(v[1], v[3]), a3 = mi(csub(v[1], v[3]));
-    v[0] = cadd(a0, a2);
-    v[2] = csub(a0, a2);
-    v[1] = cadd(a1, a3);
-    v[3] = csub(a1, a3);
-  }
-  static __device__ __forceinline__ void r8(C *v) {
-    const T c = (T)0.707106781186547524400844362104849039;
-    C b[4], d[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-      b[r] = cadd(v[r], v[r + 4]);
-      d[r] = csub(v[r], v[r + 4]);
-    }
-    // d[r] *= e^{SIGN 2 pi i r / 8}
-    d[1] = cmk<C>(c * (d[1].x - (T)SIGN * d[1].y), c * (d[1].y + (T)SIGN * d[1].x));
-    d[2] = mi(d[2]);
-    d[3] = cmk<C>(c * (-d[3].x - (T)SIGN * d[3].y), c * ((T)SIGN * d[3].x - d[3].y));
-    r4(b);
-    r4(d);
-    v[0] = b[0];
-    v[2] = b[1];
-    v[4] = b[2];
-    v[6] = b[3];
-    v[1] = d[0];
-    v[3] = d[1];
-    v[5] = d[2];
-    v[7] = d[3];
-  }
-  static __device__ __forceinline__ void r3(C *v) {
-    const T s = (T)0.866025403784438646763723170752936183;
-    C t1 = cadd(v[1], v[2]);
-    C t2 = csub(v[0], cscale((T)0.5, t1));
-    C t3 = cscale(s, mi(csub(v[1], v[2])));
-    v[0] = cadd(v[0], t1);
-    v[1] = cadd(t2, t3);
-    v[2] = csub(t2, t3);
-  }
-  template <int R>
-  static __device__ __forceinline__ void run(C *v) {
-    if (R == 2) r2(v);
-    if (R == 3) r3(v);
-    if (R == 4) r4(v);
-    if (R == 8) r8(v);
-  }
-};
 
 // One decimation-in-frequency stage of radix R over the B lines of a batch
 // (element-major, element stride LD), in place.  span = current sub-transform
@@ -306,6 +249,7 @@ template <typename T, int SIGN>
 int run_cols(gev_ctx *ctx, const void *in, void *out, long line_stride, long plane_stride) {
   typedef typename CT<T>::C C;
   const int N = ctx->N, NH = N / 2 + 1;
+  if (fft_reg_ok(N)) return fft_cols_reg(ctx, in, out, line_stride, plane_stride, SIGN);
   int lgB = batch_lg(N, sizeof(C), 2, 16, 32768);
   while ((1 << lgB) > NH && lgB > 0) --lgB;
   const int B = 1 << lgB;
@@ -324,6 +268,13 @@ int r2c_comp(gev_ctx *ctx, const void *real, void *spec) {
   typedef typename CT<T>::C C;
   const int N = ctx->N, NH = N / 2 + 1, M = N / 2;
   const long nrows = (long)N * N;
+  if (fft_reg_ok(M)) {
+    int rc = fft_r2c_rows_reg(ctx, real, spec);
+    if (rc) return rc;
+    rc = run_cols<T, -1>(ctx, spec, spec, NH, (long)N * NH);
+    if (rc) return rc;
+    return run_cols<T, -1>(ctx, spec, spec, (long)N * NH, NH);
+  }
   const int lgB = batch_lg(M, sizeof(C), 1, 64, 32768), B = 1 << lgB;
   const size_t smem = ((size_t)M + (size_t)M * (B + 1)) * sizeof(C) + (size_t)M * 2;
   k_fft_r2c_rows<T><<<(unsigned)((nrows + B - 1) / B), 256, smem, ctx->stream>>>(
@@ -343,6 +294,7 @@ int c2r_comp(gev_ctx *ctx, const void *spec, void *real, void *scratch) {
   if (rc) return rc;
   rc = run_cols<T, +1>(ctx, scratch, scratch, NH, (long)N * NH);  // y, in place
   if (rc) return rc;
+  if (fft_reg_ok(M)) return fft_c2r_rows_reg(ctx, scratch, real);
   const long nrows = (long)N * N;
   const int lgB = batch_lg(M, sizeof(C), 1, 64, 32768), B = 1 << lgB;
   const size_t smem = ((size_t)M + (size_t)M * (B + 1) + (size_t)B * (M + 1)) * sizeof(C) + (size_t)M * 2;

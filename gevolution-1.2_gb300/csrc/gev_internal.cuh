@@ -239,6 +239,11 @@ inline int grid_for(const gev_ctx *ctx, size_t work, int threads, int per_sm = 8
 int fft_build_plan(int L, FftPlan *pl);
 int fft_r2c_comp(gev_ctx *ctx, const void *real, void *spec);
 int fft_c2r_comp(gev_ctx *ctx, const void *spec, void *real, void *scratch);
+// register-resident passes for power-of-two lengths 8..1024 (gev_fft_reg.cu)
+bool fft_reg_ok(int L);
+int fft_cols_reg(gev_ctx *ctx, const void *in, void *out, long ES, long PS, int sign);
+int fft_r2c_rows_reg(gev_ctx *ctx, const void *real, void *spec);
+int fft_c2r_rows_reg(gev_ctx *ctx, const void *spec, void *real);
 int pcls_relink(gev_ctx *ctx, gev_pcls *p);
 int ctx_ensure_cube(gev_ctx *ctx, size_t bytes);
 int ctx_ensure_red(gev_ctx *ctx, size_t elems);
