@@ -29,7 +29,7 @@ constexpr int FX_NC[4] = {1, 3, 6, 1};
 constexpr int TX = 32, TY = 16, TZ = 32, FX_THREADS = 256;
 
 struct FxParams {
-  int N;
+  int N, lg;  // lg = log2 N for a power of two, else -1
   float mass, a;
   float scale;  // 2^k
   double inv_scale;
@@ -84,16 +84,25 @@ __global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint3
   for (int i = threadIdx.x; i < 2 * NC * SL; i += blockDim.x) lay[i] = 0ull;
   int cur = 0;  // layer holding field z = zs; 1 - cur holds z = zs + 1
   for (int zs = z0; zs < z0 + nz; ++zs) {
-    if (threadIdx.x == 0) {
-      uint32_t acc = 0;
-      for (int yy = 0; yy < ny; ++yy) {
+    if (threadIdx.x < 32) {  // the layer's TY row runs: one lane per row, then a warp scan of the counts
+      const int yy = threadIdx.x;
+      uint32_t s = 0, cnt = 0;
+      if (yy < ny) {
         const long c0 = x0 + (long)N * (y0 + yy) + NN * zs;
-        const uint32_t s = start[c0], e = start[c0 + nx];
-        rowbase[yy] = s;
-        rowoff[yy] = acc;
-        acc += e - s;
+        s = start[c0];
+        cnt = start[c0 + nx] - s;
       }
-      rowoff[ny] = acc;
+      uint32_t inc = cnt;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, inc, o);
+        if (yy >= o) inc += v;
+      }
+      if (yy < ny) {
+        rowbase[yy] = s;
+        rowoff[yy] = inc - cnt;
+      }
+      if (yy == ny - 1) rowoff[ny] = inc;
     }
     __syncthreads();
     const uint32_t total = rowoff[ny];
@@ -103,7 +112,8 @@ __global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint3
       while (rowoff[yy + 1] <= t) ++yy;
       const uint32_t j = rowbase[yy] + (t - rowoff[yy]);
       const uint32_t cell = P.cell[j];
-      const int cx = (int)(cell % N), cy = (int)((cell / N) % N);
+      const int cx = p.lg >= 0 ? (int)(cell & (uint32_t)(N - 1)) : (int)(cell % N);
+      const int cy = p.lg >= 0 ? (int)((cell >> p.lg) & (uint32_t)(N - 1)) : (int)((cell / N) % N);
       const int lx = cx - x0, ly = cy - y0;
       const float u0 = P.rx[j], u1 = P.ry[j], u2 = P.rz[j];
       const float d0 = 1.f - u0, d1 = 1.f - u1, d2 = 1.f - u2;
@@ -262,6 +272,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   const int NC = FX_NC[kind];
   FxParams fp;
   fp.N = N;
+  fp.lg = lg_pow2(N);
   fp.mass = (float)mass;
   fp.a = (float)a;
   int e2 = 0;

@@ -255,36 +255,100 @@ __global__ void k_gather(PclsArrays src, PclsArrays dst, const uint32_t *__restr
 struct Params {
   double dtau, a, a2N, inv_a2, inv_a2N;
   int nfield, N, lg;
+  // the same values rounded to FP32 on the host (round to nearest, as the device
+  // conversion would), so the mixed form's loops convert nothing per particle
+  float dtau_f, a_f, inv_a2_f, inv_a2N_f, inv_a_f;
 };
-
+inline Params make_params(double dtau, double a, double a2N, int nfield, int N) {
+  Params p;
+  p.dtau = dtau;
+  p.a = a;
+  p.a2N = a2N;
+  p.inv_a2 = 1.0 / (a * a);
+  p.inv_a2N = 1.0 / a2N;
+  p.nfield = nfield;
+  p.N = N;
+  p.lg = lg_pow2(N);
+  p.dtau_f = (float)p.dtau;
+  p.a_f = (float)p.a;
+  p.inv_a2_f = (float)p.inv_a2;
+  p.inv_a2N_f = (float)p.inv_a2N;
+  p.inv_a_f = (float)(1.0 / a);
+  return p;
+}
+// a parameter in the kernel's real type
 template <typename T>
-__device__ __forceinline__ T F(const T *__restrict__ f, int x, int y, int z, int N) {
-  return __ldg(&f[sidx(wrapi(x, N), wrapi(y, N), wrapi(z, N), N)]);
+__device__ __forceinline__ T pv(double d, float f) {
+  if constexpr (sizeof(T) == 4)
+    return f;
+  else
+    return d;
+}
+
+// The linked cell of a particle and the index offsets (mod 2^32) of its six
+// periodic neighbours, computed once per particle: every stencil value is then
+// f[base + offsets], a few integer adds instead of a wrapped 3-D index.
+struct CellNb {
+  uint32_t base;  // x + N (y + N z)
+  uint32_t xm, xp, ym, yp, zm, zp;
+};
+__device__ __forceinline__ CellNb cell_nb(uint32_t c, int N, int lg, int &cx, int &cy, int &cz) {
+  if (lg >= 0) {
+    cx = (int)(c & (uint32_t)(N - 1));
+    cy = (int)((c >> lg) & (uint32_t)(N - 1));
+    cz = (int)(c >> (2 * lg));
+  } else {
+    cx = (int)(c % (uint32_t)N);
+    cy = (int)((c / (uint32_t)N) % (uint32_t)N);
+    cz = (int)(c / ((uint32_t)N * (uint32_t)N));
+  }
+  const uint32_t n1 = (uint32_t)N, n2 = n1 * n1, n3 = n2 * n1;
+  CellNb b;
+  b.base = c;
+  b.xm = cx == 0 ? n1 - 1u : 0u - 1u;
+  b.xp = cx == N - 1 ? 1u - n1 : 1u;
+  b.ym = cy == 0 ? n2 - n1 : 0u - n1;
+  b.yp = cy == N - 1 ? n1 - n2 : n1;
+  b.zm = cz == 0 ? n3 - n2 : 0u - n2;
+  b.zp = cz == N - 1 ? n2 - n3 : n2;
+  return b;
+}
+// f at the neighbour (DX, DY, DZ) in {-1, 0, 1}^3 of the cell
+template <int DX, int DY, int DZ, typename T>
+__device__ __forceinline__ T at(const T *__restrict__ f, const CellNb &b) {
+  uint32_t i = b.base;
+  if (DX < 0) i += b.xm;
+  if (DX > 0) i += b.xp;
+  if (DY < 0) i += b.ym;
+  if (DY > 0) i += b.yp;
+  if (DZ < 0) i += b.zm;
+  if (DZ > 0) i += b.zp;
+  return __ldg(f + i);
 }
 
 // The per-particle physics of update_q (gevolution.hpp:570-678, GRADIENT_ORDER 1)
-// and update_pos (810-871), on the particle's linked cell (cx, cy, cz) and its
+// and update_pos (810-871), on the particle's linked cell (its neighbours nb) and its
 // in-cell offset r = pos*N - cell (ref_dist of the reference).  Field values are
 // gathered with periodic wrap.
 
 // q -> q - dtau e grad / dx (GR) or q - dtau a grad / dx (Newton)
 template <typename T, int KIND>
 __device__ __forceinline__ void kick_one(const T *__restrict__ phi, const T *__restrict__ chi,
-                                         const T *__restrict__ Bi, const Params &pr, int cx, int cy, int cz, T r0, T r1,
+                                         const T *__restrict__ Bi, const Params &pr, const CellNb &nb, T r0, T r1,
                                          T r2, T &q0, T &q1, T &q2) {
   const int N = pr.N;
   const size_t NV = (size_t)N * N * N;
   const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
   T g0, g1, g2;
   {
-    const T f000 = F(phi, cx, cy, cz, N), f100 = F(phi, cx + 1, cy, cz, N), f010 = F(phi, cx, cy + 1, cz, N),
-            f110 = F(phi, cx + 1, cy + 1, cz, N), f001 = F(phi, cx, cy, cz + 1, N), f101 = F(phi, cx + 1, cy, cz + 1, N),
-            f011 = F(phi, cx, cy + 1, cz + 1, N), f111 = F(phi, cx + 1, cy + 1, cz + 1, N);
+    const T f000 = at<0, 0, 0>(phi, nb), f100 = at<1, 0, 0>(phi, nb), f010 = at<0, 1, 0>(phi, nb),
+            f110 = at<1, 1, 0>(phi, nb), f001 = at<0, 0, 1>(phi, nb), f101 = at<1, 0, 1>(phi, nb),
+            f011 = at<0, 1, 1>(phi, nb), f111 = at<1, 1, 1>(phi, nb);
     g0 = s1 * s2 * (f100 - f000) + r1 * s2 * (f110 - f010) + s1 * r2 * (f101 - f001) + r1 * r2 * (f111 - f011);
     g1 = s0 * s2 * (f010 - f000) + r0 * s2 * (f110 - f100) + s0 * r2 * (f011 - f001) + r0 * r2 * (f111 - f101);
     g2 = s0 * s1 * (f001 - f000) + r0 * s1 * (f101 - f100) + s0 * r1 * (f011 - f010) + r0 * r1 * (f111 - f110);
   }
-  const T a = (T)pr.a;
+  const T a = pv<T>(pr.a, pr.a_f);
   T e = (T)0, inv_e = (T)0;
   if (KIND == GEV_GR) {
     const T v2 = q0 * q0 + q1 * q1 + q2 * q2;
@@ -297,9 +361,9 @@ __device__ __forceinline__ void kick_one(const T *__restrict__ phi, const T *__r
     inv_e = (T)1 / e;
   }
   if (pr.nfield >= 2 && chi != nullptr) {
-    const T f000 = F(chi, cx, cy, cz, N), f100 = F(chi, cx + 1, cy, cz, N), f010 = F(chi, cx, cy + 1, cz, N),
-            f110 = F(chi, cx + 1, cy + 1, cz, N), f001 = F(chi, cx, cy, cz + 1, N), f101 = F(chi, cx + 1, cy, cz + 1, N),
-            f011 = F(chi, cx, cy + 1, cz + 1, N), f111 = F(chi, cx + 1, cy + 1, cz + 1, N);
+    const T f000 = at<0, 0, 0>(chi, nb), f100 = at<1, 0, 0>(chi, nb), f010 = at<0, 1, 0>(chi, nb),
+            f110 = at<1, 1, 0>(chi, nb), f001 = at<0, 0, 1>(chi, nb), f101 = at<1, 0, 1>(chi, nb),
+            f011 = at<0, 1, 1>(chi, nb), f111 = at<1, 1, 1>(chi, nb);
     g0 -= s1 * s2 * (f100 - f000) + r1 * s2 * (f110 - f010) + s1 * r2 * (f101 - f001) + r1 * r2 * (f111 - f011);
     g1 -= s0 * s2 * (f010 - f000) + r0 * s2 * (f110 - f100) + s0 * r2 * (f011 - f001) + r0 * r2 * (f111 - f101);
     g2 -= s0 * s1 * (f001 - f000) + r0 * s1 * (f101 - f100) + s0 * r1 * (f011 - f010) + r0 * r1 * (f111 - f110);
@@ -308,36 +372,36 @@ __device__ __forceinline__ void kick_one(const T *__restrict__ phi, const T *__r
     const T *B0 = Bi, *B1 = Bi + NV, *B2 = Bi + 2 * NV;
     const T t0 = (T)2 * r0, t1 = (T)2 * r1, t2 = (T)2 * r2;
     T p0, p1, p2;
-    p0 = (s2 * (F(B1, cx + 1, cy, cz, N) - F(B1, cx, cy, cz, N)) +
-          r2 * (F(B1, cx + 1, cy, cz + 1, N) - F(B1, cx, cy, cz + 1, N))) * q1;
-    p0 += (s1 * (F(B2, cx + 1, cy, cz, N) - F(B2, cx, cy, cz, N)) +
-           r1 * (F(B2, cx + 1, cy + 1, cz, N) - F(B2, cx, cy + 1, cz, N))) * q2;
-    p0 += (s1 * s2 * ((r0 - (T)1) * F(B0, cx - 1, cy, cz, N) + ((T)1 - t0) * F(B0, cx, cy, cz, N) + r0 * F(B0, cx + 1, cy, cz, N)) +
-           r1 * s2 * ((r0 - (T)1) * F(B0, cx - 1, cy + 1, cz, N) + ((T)1 - t0) * F(B0, cx, cy + 1, cz, N) + r0 * F(B0, cx + 1, cy + 1, cz, N)) +
-           s1 * r2 * ((r0 - (T)1) * F(B0, cx - 1, cy, cz + 1, N) + ((T)1 - t0) * F(B0, cx, cy, cz + 1, N) + r0 * F(B0, cx + 1, cy, cz + 1, N)) +
-           r1 * r2 * ((r0 - (T)1) * F(B0, cx - 1, cy + 1, cz + 1, N) + ((T)1 - t0) * F(B0, cx, cy + 1, cz + 1, N) + r0 * F(B0, cx + 1, cy + 1, cz + 1, N))) * q0;
-    p1 = (s0 * (F(B2, cx, cy + 1, cz, N) - F(B2, cx, cy, cz, N)) +
-          r0 * (F(B2, cx + 1, cy + 1, cz, N) - F(B2, cx + 1, cy, cz, N))) * q2;
-    p1 += (s2 * (F(B0, cx, cy + 1, cz, N) - F(B0, cx, cy, cz, N)) +
-           r2 * (F(B0, cx, cy + 1, cz + 1, N) - F(B0, cx, cy, cz + 1, N))) * q0;
-    p1 += (s0 * s2 * ((r1 - (T)1) * F(B1, cx, cy - 1, cz, N) + ((T)1 - t1) * F(B1, cx, cy, cz, N) + r1 * F(B1, cx, cy + 1, cz, N)) +
-           r0 * s2 * ((r1 - (T)1) * F(B1, cx + 1, cy - 1, cz, N) + ((T)1 - t1) * F(B1, cx + 1, cy, cz, N) + r1 * F(B1, cx + 1, cy + 1, cz, N)) +
-           s0 * r2 * ((r1 - (T)1) * F(B1, cx, cy - 1, cz + 1, N) + ((T)1 - t1) * F(B1, cx, cy, cz + 1, N) + r1 * F(B1, cx, cy + 1, cz + 1, N)) +
-           r0 * r2 * ((r1 - (T)1) * F(B1, cx + 1, cy - 1, cz + 1, N) + ((T)1 - t1) * F(B1, cx + 1, cy, cz + 1, N) + r1 * F(B1, cx + 1, cy + 1, cz + 1, N))) * q1;
-    p2 = (s1 * (F(B0, cx, cy, cz + 1, N) - F(B0, cx, cy, cz, N)) +
-          r1 * (F(B0, cx, cy + 1, cz + 1, N) - F(B0, cx, cy + 1, cz, N))) * q0;
-    p2 += (s0 * (F(B1, cx, cy, cz + 1, N) - F(B1, cx, cy, cz, N)) +
-           r0 * (F(B1, cx + 1, cy, cz + 1, N) - F(B1, cx + 1, cy, cz, N))) * q1;
-    p2 += (s0 * s1 * ((r2 - (T)1) * F(B2, cx, cy, cz - 1, N) + ((T)1 - t2) * F(B2, cx, cy, cz, N) + r2 * F(B2, cx, cy, cz + 1, N)) +
-           r0 * s1 * ((r2 - (T)1) * F(B2, cx + 1, cy, cz - 1, N) + ((T)1 - t2) * F(B2, cx + 1, cy, cz, N) + r2 * F(B2, cx + 1, cy, cz + 1, N)) +
-           s0 * r1 * ((r2 - (T)1) * F(B2, cx, cy + 1, cz - 1, N) + ((T)1 - t2) * F(B2, cx, cy + 1, cz, N) + r2 * F(B2, cx, cy + 1, cz + 1, N)) +
-           r0 * r1 * ((r2 - (T)1) * F(B2, cx + 1, cy + 1, cz - 1, N) + ((T)1 - t2) * F(B2, cx + 1, cy + 1, cz, N) + r2 * F(B2, cx + 1, cy + 1, cz + 1, N))) * q2;
-    const T k = (T)pr.inv_a2N * inv_e;
+    p0 = (s2 * (at<1, 0, 0>(B1, nb) - at<0, 0, 0>(B1, nb)) +
+          r2 * (at<1, 0, 1>(B1, nb) - at<0, 0, 1>(B1, nb))) * q1;
+    p0 += (s1 * (at<1, 0, 0>(B2, nb) - at<0, 0, 0>(B2, nb)) +
+           r1 * (at<1, 1, 0>(B2, nb) - at<0, 1, 0>(B2, nb))) * q2;
+    p0 += (s1 * s2 * ((r0 - (T)1) * at<-1, 0, 0>(B0, nb) + ((T)1 - t0) * at<0, 0, 0>(B0, nb) + r0 * at<1, 0, 0>(B0, nb)) +
+           r1 * s2 * ((r0 - (T)1) * at<-1, 1, 0>(B0, nb) + ((T)1 - t0) * at<0, 1, 0>(B0, nb) + r0 * at<1, 1, 0>(B0, nb)) +
+           s1 * r2 * ((r0 - (T)1) * at<-1, 0, 1>(B0, nb) + ((T)1 - t0) * at<0, 0, 1>(B0, nb) + r0 * at<1, 0, 1>(B0, nb)) +
+           r1 * r2 * ((r0 - (T)1) * at<-1, 1, 1>(B0, nb) + ((T)1 - t0) * at<0, 1, 1>(B0, nb) + r0 * at<1, 1, 1>(B0, nb))) * q0;
+    p1 = (s0 * (at<0, 1, 0>(B2, nb) - at<0, 0, 0>(B2, nb)) +
+          r0 * (at<1, 1, 0>(B2, nb) - at<1, 0, 0>(B2, nb))) * q2;
+    p1 += (s2 * (at<0, 1, 0>(B0, nb) - at<0, 0, 0>(B0, nb)) +
+           r2 * (at<0, 1, 1>(B0, nb) - at<0, 0, 1>(B0, nb))) * q0;
+    p1 += (s0 * s2 * ((r1 - (T)1) * at<0, -1, 0>(B1, nb) + ((T)1 - t1) * at<0, 0, 0>(B1, nb) + r1 * at<0, 1, 0>(B1, nb)) +
+           r0 * s2 * ((r1 - (T)1) * at<1, -1, 0>(B1, nb) + ((T)1 - t1) * at<1, 0, 0>(B1, nb) + r1 * at<1, 1, 0>(B1, nb)) +
+           s0 * r2 * ((r1 - (T)1) * at<0, -1, 1>(B1, nb) + ((T)1 - t1) * at<0, 0, 1>(B1, nb) + r1 * at<0, 1, 1>(B1, nb)) +
+           r0 * r2 * ((r1 - (T)1) * at<1, -1, 1>(B1, nb) + ((T)1 - t1) * at<1, 0, 1>(B1, nb) + r1 * at<1, 1, 1>(B1, nb))) * q1;
+    p2 = (s1 * (at<0, 0, 1>(B0, nb) - at<0, 0, 0>(B0, nb)) +
+          r1 * (at<0, 1, 1>(B0, nb) - at<0, 1, 0>(B0, nb))) * q0;
+    p2 += (s0 * (at<0, 0, 1>(B1, nb) - at<0, 0, 0>(B1, nb)) +
+           r0 * (at<1, 0, 1>(B1, nb) - at<1, 0, 0>(B1, nb))) * q1;
+    p2 += (s0 * s1 * ((r2 - (T)1) * at<0, 0, -1>(B2, nb) + ((T)1 - t2) * at<0, 0, 0>(B2, nb) + r2 * at<0, 0, 1>(B2, nb)) +
+           r0 * s1 * ((r2 - (T)1) * at<1, 0, -1>(B2, nb) + ((T)1 - t2) * at<1, 0, 0>(B2, nb) + r2 * at<1, 0, 1>(B2, nb)) +
+           s0 * r1 * ((r2 - (T)1) * at<0, 1, -1>(B2, nb) + ((T)1 - t2) * at<0, 1, 0>(B2, nb) + r2 * at<0, 1, 1>(B2, nb)) +
+           r0 * r1 * ((r2 - (T)1) * at<1, 1, -1>(B2, nb) + ((T)1 - t2) * at<1, 1, 0>(B2, nb) + r2 * at<1, 1, 1>(B2, nb))) * q2;
+    const T k = pv<T>(pr.inv_a2N, pr.inv_a2N_f) * inv_e;
     g0 += p0 * k;
     g1 += p1 * k;
     g2 += p2 * k;
   }
-  const T m = (T)pr.dtau * (KIND == GEV_GR ? e : a) * (T)N;
+  const T m = pv<T>(pr.dtau, pr.dtau_f) * (KIND == GEV_GR ? e : a) * (T)N;
   q0 -= m * g0;
   q1 -= m * g1;
   q2 -= m * g2;
@@ -346,25 +410,25 @@ __device__ __forceinline__ void kick_one(const T *__restrict__ phi, const T *__r
 // the coordinate velocity of update_pos (GR): q (1 + (3 - q^2/e^2) phi - chi) / e + b / (a^2 N)
 template <typename T>
 __device__ __forceinline__ void drift_vel(const T *__restrict__ phi, const T *__restrict__ chi,
-                                          const T *__restrict__ Bi, const Params &pr, int cx, int cy, int cz, T r0,
+                                          const T *__restrict__ Bi, const Params &pr, const CellNb &nb, T r0,
                                           T r1, T r2, T q0, T q1, T q2, T &v0, T &v1, T &v2) {
   const int N = pr.N;
   const size_t NV = (size_t)N * N * N;
   const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
-  const T a = (T)pr.a;
+  const T a = pv<T>(pr.a, pr.a_f);
   const T qq = q0 * q0 + q1 * q1 + q2 * q2;
   const T e2 = qq + a * a;
   T ph = (T)0, ch = (T)0;
   const T w000 = s0 * s1 * s2, w100 = r0 * s1 * s2, w010 = s0 * r1 * s2, w110 = r0 * r1 * s2;
   const T w001 = s0 * s1 * r2, w101 = r0 * s1 * r2, w011 = s0 * r1 * r2, w111 = r0 * r1 * r2;
   if (pr.nfield >= 1)
-    ph = F(phi, cx, cy, cz, N) * w000 + F(phi, cx + 1, cy, cz, N) * w100 + F(phi, cx, cy + 1, cz, N) * w010 +
-         F(phi, cx + 1, cy + 1, cz, N) * w110 + F(phi, cx, cy, cz + 1, N) * w001 + F(phi, cx + 1, cy, cz + 1, N) * w101 +
-         F(phi, cx, cy + 1, cz + 1, N) * w011 + F(phi, cx + 1, cy + 1, cz + 1, N) * w111;
+    ph = at<0, 0, 0>(phi, nb) * w000 + at<1, 0, 0>(phi, nb) * w100 + at<0, 1, 0>(phi, nb) * w010 +
+         at<1, 1, 0>(phi, nb) * w110 + at<0, 0, 1>(phi, nb) * w001 + at<1, 0, 1>(phi, nb) * w101 +
+         at<0, 1, 1>(phi, nb) * w011 + at<1, 1, 1>(phi, nb) * w111;
   if (pr.nfield >= 2)
-    ch = F(chi, cx, cy, cz, N) * w000 + F(chi, cx + 1, cy, cz, N) * w100 + F(chi, cx, cy + 1, cz, N) * w010 +
-         F(chi, cx + 1, cy + 1, cz, N) * w110 + F(chi, cx, cy, cz + 1, N) * w001 + F(chi, cx + 1, cy, cz + 1, N) * w101 +
-         F(chi, cx, cy + 1, cz + 1, N) * w011 + F(chi, cx + 1, cy + 1, cz + 1, N) * w111;
+    ch = at<0, 0, 0>(chi, nb) * w000 + at<1, 0, 0>(chi, nb) * w100 + at<0, 1, 0>(chi, nb) * w010 +
+         at<1, 1, 0>(chi, nb) * w110 + at<0, 0, 1>(chi, nb) * w001 + at<1, 0, 1>(chi, nb) * w101 +
+         at<0, 1, 1>(chi, nb) * w011 + at<1, 1, 1>(chi, nb) * w111;
   const T inv_e2 = (T)1 / e2;
   const T fac = ((T)1 + ((T)3 - qq * inv_e2) * ph - ch) * sqrt(inv_e2);
   v0 = q0 * fac;
@@ -372,13 +436,13 @@ __device__ __forceinline__ void drift_vel(const T *__restrict__ phi, const T *__
   v2 = q2 * fac;
   if (pr.nfield >= 3) {
     const T *B0 = Bi, *B1 = Bi + NV, *B2 = Bi + 2 * NV;
-    const T b0 = F(B0, cx, cy, cz, N) * s1 * s2 + F(B0, cx, cy + 1, cz, N) * r1 * s2 + F(B0, cx, cy, cz + 1, N) * s1 * r2 +
-                 F(B0, cx, cy + 1, cz + 1, N) * r1 * r2;
-    const T b1 = F(B1, cx, cy, cz, N) * s0 * s2 + F(B1, cx + 1, cy, cz, N) * r0 * s2 + F(B1, cx, cy, cz + 1, N) * s0 * r2 +
-                 F(B1, cx + 1, cy, cz + 1, N) * r0 * r2;
-    const T b2 = F(B2, cx, cy, cz, N) * s0 * s1 + F(B2, cx + 1, cy, cz, N) * r0 * s1 + F(B2, cx, cy + 1, cz, N) * s0 * r1 +
-                 F(B2, cx + 1, cy + 1, cz, N) * r0 * r1;
-    const T ib = (T)pr.inv_a2N;
+    const T b0 = at<0, 0, 0>(B0, nb) * s1 * s2 + at<0, 1, 0>(B0, nb) * r1 * s2 + at<0, 0, 1>(B0, nb) * s1 * r2 +
+                 at<0, 1, 1>(B0, nb) * r1 * r2;
+    const T b1 = at<0, 0, 0>(B1, nb) * s0 * s2 + at<1, 0, 0>(B1, nb) * r0 * s2 + at<0, 0, 1>(B1, nb) * s0 * r2 +
+                 at<1, 0, 1>(B1, nb) * r0 * r2;
+    const T b2 = at<0, 0, 0>(B2, nb) * s0 * s1 + at<1, 0, 0>(B2, nb) * r0 * s1 + at<0, 1, 0>(B2, nb) * s0 * r1 +
+                 at<1, 1, 0>(B2, nb) * r0 * r1;
+    const T ib = pv<T>(pr.inv_a2N, pr.inv_a2N_f);
     v0 += b0 * ib;
     v1 += b1 * ib;
     v2 += b2 * ib;
@@ -387,12 +451,9 @@ __device__ __forceinline__ void drift_vel(const T *__restrict__ phi, const T *__
 
 // the particle's linked cell and in-cell offset (the FP32 copy in the mixed form)
 template <typename T>
-__device__ __forceinline__ void load_cell(const PclsArrays &P, long i, int N, int &cx, int &cy, int &cz, T &r0, T &r1,
-                                          T &r2) {
-  const uint32_t c = P.cell[i];
-  cx = (int)(c % N);
-  cy = (int)((c / N) % N);
-  cz = (int)(c / ((uint32_t)N * N));
+__device__ __forceinline__ CellNb load_cell(const PclsArrays &P, long i, int N, int lg, T &r0, T &r1, T &r2) {
+  int cx, cy, cz;
+  const CellNb nb = cell_nb(P.cell[i], N, lg, cx, cy, cz);
   if constexpr (sizeof(T) == 4) {
     r0 = P.rx[i];
     r1 = P.ry[i];
@@ -402,14 +463,17 @@ __device__ __forceinline__ void load_cell(const PclsArrays &P, long i, int N, in
     r1 = (T)(P.py[i] * (double)N - cy);
     r2 = (T)(P.pz[i] * (double)N - cz);
   }
+  return nb;
 }
 
 // pos += dtau v, periodic wrap into [0, 1), new cell key (and offset) for the relink
 template <typename T>
-__device__ __forceinline__ void move_store(PclsArrays &P, long i, double dtau, T v0, T v1, T v2, int N, int lg) {
+__device__ __forceinline__ void move_store(PclsArrays &P, long i, const Params &pr, T v0, T v1, T v2) {
+  const int N = pr.N, lg = pr.lg;
+  const double dtau = pr.dtau;
   double x = P.px[i], y = P.py[i], z = P.pz[i];
   if constexpr (sizeof(T) == 4) {
-    const float dt = (float)dtau;
+    const float dt = pr.dtau_f;
     x += (double)(dt * v0);
     y += (double)(dt * v1);
     z += (double)(dt * v2);
@@ -459,15 +523,14 @@ __global__ void __launch_bounds__(256) k_update_q(PclsArrays P, long n, const T 
                                                   unsigned long long *maxbits) {
   T vmax = (T)0;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    int cx, cy, cz;
     T r0, r1, r2;
-    load_cell<T>(P, i, pr.N, cx, cy, cz, r0, r1, r2);
+    const CellNb nb = load_cell<T>(P, i, pr.N, pr.lg, r0, r1, r2);
     T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
-    kick_one<T, KIND>(phi, chi, Bi, pr, cx, cy, cz, r0, r1, r2, q0, q1, q2);
+    kick_one<T, KIND>(phi, chi, Bi, pr, nb, r0, r1, r2, q0, q1, q2);
     ((V *)P.vx)[i] = (V)q0;
     ((V *)P.vy)[i] = (V)q1;
     ((V *)P.vz)[i] = (V)q2;
-    const T v2 = (q0 * q0 + q1 * q1 + q2 * q2) * (T)pr.inv_a2;
+    const T v2 = (q0 * q0 + q1 * q1 + q2 * q2) * pv<T>(pr.inv_a2, pr.inv_a2_f);
     vmax = v2 > vmax ? v2 : vmax;
   }
   block_max_to<T>(vmax, maxbits);
@@ -481,17 +544,16 @@ __global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const 
     const T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
     T v0, v1, v2;
     if (KIND == GEV_NEWTON) {  // update_pos_Newton: dtau q / a
-      const T ia = (T)(1.0 / pr.a);
+      const T ia = pv<T>(1.0 / pr.a, pr.inv_a_f);
       v0 = q0 * ia;
       v1 = q1 * ia;
       v2 = q2 * ia;
     } else {
-      int cx, cy, cz;
       T r0, r1, r2;
-      load_cell<T>(P, i, pr.N, cx, cy, cz, r0, r1, r2);
-      drift_vel<T>(phi, chi, Bi, pr, cx, cy, cz, r0, r1, r2, q0, q1, q2, v0, v1, v2);
+      const CellNb nb = load_cell<T>(P, i, pr.N, pr.lg, r0, r1, r2);
+      drift_vel<T>(phi, chi, Bi, pr, nb, r0, r1, r2, q0, q1, q2, v0, v1, v2);
     }
-    move_store<T>(P, i, pr.dtau, v0, v1, v2, pr.N, pr.lg);
+    move_store<T>(P, i, pr, v0, v1, v2);
   }
 }
 
@@ -499,24 +561,23 @@ __global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const 
 // in one pass: both read the same cell and the same phi / chi / B values.  The
 // drift's scale factor (after the background half step) comes in pd.
 template <typename T, typename V>
-__global__ void __launch_bounds__(256) k_kick_drift(PclsArrays P, long n, const T *__restrict__ phi,
+__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_kick_drift(PclsArrays P, long n, const T *__restrict__ phi,
                                                     const T *__restrict__ chi, const T *__restrict__ Bi, Params pk,
                                                     Params pd, unsigned long long *maxbits) {
   T vmax = (T)0;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    int cx, cy, cz;
     T r0, r1, r2;
-    load_cell<T>(P, i, pk.N, cx, cy, cz, r0, r1, r2);
+    const CellNb nb = load_cell<T>(P, i, pk.N, pk.lg, r0, r1, r2);
     T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
-    kick_one<T, GEV_GR>(phi, chi, Bi, pk, cx, cy, cz, r0, r1, r2, q0, q1, q2);
+    kick_one<T, GEV_GR>(phi, chi, Bi, pk, nb, r0, r1, r2, q0, q1, q2);
     ((V *)P.vx)[i] = (V)q0;
     ((V *)P.vy)[i] = (V)q1;
     ((V *)P.vz)[i] = (V)q2;
-    const T vv = (q0 * q0 + q1 * q1 + q2 * q2) * (T)pk.inv_a2;
+    const T vv = (q0 * q0 + q1 * q1 + q2 * q2) * pv<T>(pk.inv_a2, pk.inv_a2_f);
     vmax = vv > vmax ? vv : vmax;
     T v0, v1, v2;
-    drift_vel<T>(phi, chi, Bi, pd, cx, cy, cz, r0, r1, r2, q0, q1, q2, v0, v1, v2);
-    move_store<T>(P, i, pd.dtau, v0, v1, v2, pd.N, pd.lg);
+    drift_vel<T>(phi, chi, Bi, pd, nb, r0, r1, r2, q0, q1, q2, v0, v1, v2);
+    move_store<T>(P, i, pd, v0, v1, v2);
   }
   block_max_to<T>(vmax, maxbits);
 }
@@ -575,7 +636,7 @@ int scan_cells(gev_ctx *ctx, gev_pcls *p) {
 template <typename T, typename V>
 int launch_update_q(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
                     const gev_field *Bi, int nfield, double a, double a2N, unsigned long long *mb) {
-  Params pr{dtau, a, a2N, 1.0 / (a * a), 1.0 / a2N, nfield, ctx->N, lg_pow2(ctx->N)};
+  const Params pr = make_params(dtau, a, a2N, nfield, ctx->N);
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(mb, 0, sizeof(unsigned long long), ctx->stream));
   const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
   const T *fphi = (const T *)phi->d, *fchi = chi ? (const T *)chi->d : nullptr, *fB = Bi ? (const T *)Bi->d : nullptr;
@@ -590,7 +651,7 @@ int launch_update_q(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_
 template <typename T, typename V>
 int update_pos_t(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
                  const gev_field *Bi, int nfield, double a, double a2N) {
-  Params pr{dtau, a, a2N, 1.0 / (a * a), 1.0 / a2N, nfield, ctx->N, lg_pow2(ctx->N)};
+  const Params pr = make_params(dtau, a, a2N, nfield, ctx->N);
   const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
   const T *fphi = phi ? (const T *)phi->d : nullptr, *fchi = chi ? (const T *)chi->d : nullptr,
           *fB = Bi ? (const T *)Bi->d : nullptr;
@@ -620,10 +681,10 @@ int pcls_kick_async(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_
 int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, int nfield_k, double dtau_d,
                           double a_d, int nfield_d, const gev_field *phi, const gev_field *chi, const gev_field *Bi,
                           unsigned long long *maxbits_dev) {
-  const int N = ctx->N, lg = lg_pow2(N);
+  const int N = ctx->N;
   const double a2N_k = a_k * a_k * N, a2N_d = a_d * a_d * N;
-  Params pk{dtau_k, a_k, a2N_k, 1.0 / (a_k * a_k), 1.0 / a2N_k, nfield_k, N, lg};
-  Params pd{dtau_d, a_d, a2N_d, 1.0 / (a_d * a_d), 1.0 / a2N_d, nfield_d, N, lg};
+  const Params pk = make_params(dtau_k, a_k, a2N_k, nfield_k, N);
+  const Params pd = make_params(dtau_d, a_d, a2N_d, nfield_d, N);
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(maxbits_dev, 0, sizeof(unsigned long long), ctx->stream));
   const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
   if (ctx->prec == GEV_PREC_FP64)
