@@ -207,8 +207,8 @@ COLS_TRAFFIC = {}
 
 
 def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
-    """The FFT column pass (k_fft_cols, the y / z passes of every transform) is the
-    largest share of the cycle in the ncu launch list.  One launch transforms one
+    """The FFT column pass (k_fft_cols_reg, the y / z passes of every transform) is
+    the largest kernel family of the cycle in the ncu launch list.  One launch transforms one
     spectrum component along y or z in place: its algorithmic bytes are one read
     and one write of the component, 2 * N^2 (N/2+1) * sizeof(complex)."""
     import torch
@@ -227,7 +227,7 @@ def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
     alg = 2 * N * N * (N // 2 + 1) * csz
     peak, kind = hbm_peak()
     achieved = alg / (ms / 1e3) / 1e9
-    return {"kernel": "k_fft_cols (one y or z pass of the 3-D FFT over one spectrum component)", "bound": "hbm",
+    return {"kernel": "k_fft_cols_reg (one y or z pass of the 3-D FFT over one spectrum component)", "bound": "hbm",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": COLS_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
 

@@ -17,7 +17,7 @@
 #include "gev_internal.cuh"
 
 int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass, double a, const gev_field *phi,
-               double bound);
+               double bound, bool overwrite);
 
 namespace {
 
@@ -205,7 +205,8 @@ double contribution_bound(int kind, double mass, double a, double vmax_hint) {
 }
 
 template <int KIND>
-int run_deposit(gev_ctx *ctx, gev_pcls *p, gev_field *out, double a, const gev_field *phi, double coeff) {
+int run_deposit(gev_ctx *ctx, gev_pcls *p, gev_field *out, double a, const gev_field *phi, double coeff,
+                bool overwrite = false) {
   const int N = ctx->N;
   const size_t C = (size_t)N * N * N;
   const double dx = 1.0 / N;
@@ -218,6 +219,10 @@ int run_deposit(gev_ctx *ctx, gev_pcls *p, gev_field *out, double a, const gev_f
   if (ctx->prec == GEV_PREC_FP64) {
     int rc = ctx_ensure_cube(ctx, (size_t)NVAL[KIND] * C * 8);
     if (rc) return rc;
+    if (overwrite) {
+      rc = gev_field_zero(out);
+      if (rc) return rc;
+    }
     k_cube_fp64<KIND><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->start, phi ? (const double *)phi->d : nullptr, dp,
                                                        (double *)ctx->d_cube);
     GEV_LAUNCH_CHECK(ctx);
@@ -227,7 +232,7 @@ int run_deposit(gev_ctx *ctx, gev_pcls *p, gev_field *out, double a, const gev_f
     // fixed-point scale: all particles at the contribution bound in one cell stay below 2^62
     const double vmax = 0.05;  // |q| bound for the scale; CDM momenta q = a v stay far below it
     const double bound = contribution_bound(KIND, mass, a, vmax) * (double)(p->n > 0 ? p->n : 1) * 8.;
-    int rc = deposit_fx(ctx, p, out, KIND, mass, a, phi, bound);
+    int rc = deposit_fx(ctx, p, out, KIND, mass, a, phi, bound, overwrite);
     if (rc) return rc;
   }
   return GEV_OK;
@@ -238,6 +243,20 @@ bool ok_field(gev_ctx *ctx, const gev_field *f, int ncomp) {
 }
 
 }  // namespace
+
+// projection_init followed by the deposit, in one pass for the mixed form
+int projection_replace(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double a, const gev_field *phi) {
+  switch (kind) {
+    case DEP_T00:
+      return run_deposit<DEP_T00>(ctx, p, out, a, phi, 1., true);
+    case DEP_T0I:
+      return run_deposit<DEP_T0I>(ctx, p, out, 1., phi, 1., true);
+    case DEP_TIJ:
+      return run_deposit<DEP_TIJ>(ctx, p, out, a, phi, 1., true);
+    default:
+      return run_deposit<DEP_MASS>(ctx, p, out, 1., nullptr, 1., true);
+  }
+}
 
 extern "C" {
 

@@ -31,9 +31,10 @@ constexpr int TX = 32, TY = 16, TZ = 32, FX_THREADS = 256;
 struct FxParams {
   int N, lg;  // lg = log2 N for a power of two, else -1
   float mass, a;
-  float scale;  // 2^k
-  double inv_scale;
+  float scale;  // 2^kshift
+  int kshift;
   long nPX, nPY, nPZ;  // face planes per direction
+  int overwrite;       // 1: the target's previous contents are replaced instead of added to
 };
 
 __device__ __forceinline__ long face_index(int x, int y, int z, const FxParams &p) {
@@ -78,6 +79,7 @@ __global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint3
   const long C = (long)N * N * N;
   const long NN = (long)N * N;
   const int ntx = (N + TX - 1) / TX, nty = (N + TY - 1) / TY;
+  const long fstride = (p.nPX + p.nPY + p.nPZ) * NN;  // face entries per component
   const int bx = blockIdx.x % ntx, by = (blockIdx.x / ntx) % nty, bz = blockIdx.x / (ntx * nty);
   const int x0 = bx * TX, y0 = by * TY, z0 = bz * TZ;
   const int nx = min(TX, N - x0), ny = min(TY, N - y0), nz = min(TZ, N - z0);
@@ -194,22 +196,29 @@ __global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint3
       }
     }
     __syncthreads();
-    // flush field layer zs (complete now) and clear it
-    for (int i = threadIdx.x; i < NC * SL; i += blockDim.x) {
-      const int comp = i / SL, r = i - comp * SL, ly = r / SX, lx = r - ly * SX;
+    // flush field layer zs (complete now) and clear it: one cell of the layer per
+    // thread, its components in turn (the output component index equals the slot)
+    for (int ci = threadIdx.x; ci < SL; ci += blockDim.x) {
+      const int ly = ci / SX, lx = ci - ly * SX;
       if (lx > nx || ly > ny) continue;
-      const unsigned long long v = A[i];
-      if (v == 0ull) continue;
-      A[i] = 0ull;
       int x = x0 + lx, y = y0 + ly;
       if (x == N) x = 0;
       if (y == N) y = 0;
       const bool onface = lx == 0 || lx == nx || ly == 0 || ly == ny || zs == z0;
-      const int oc = KIND == FX_TIJ ? comp : comp;  // output component index equals the slot
-      if (onface)
-        atomicAdd(&face[(long)oc * (p.nPX + p.nPY + p.nPZ) * NN + face_index(x, y, zs, p)], v);
-      else
-        out[(long)oc * C + sidx(x, y, zs, N)] += (float)((double)(long long)v * p.inv_scale);
+      const long fi = onface ? face_index(x, y, zs, p) : 0;
+      const size_t gi = sidx(x, y, zs, N);
+#pragma unroll
+      for (int comp = 0; comp < NC; ++comp) {
+        const unsigned long long v = A[comp * SL + ci];
+        if (v != 0ull) A[comp * SL + ci] = 0ull;
+        if (onface) {
+          if (v != 0ull) atomicAdd(&face[(long)comp * fstride + fi], v);
+        } else if (p.overwrite) {
+          out[(long)comp * C + gi] = float_of_fixed((long long)v, p.kshift);
+        } else if (v != 0ull) {
+          out[(long)comp * C + gi] += float_of_fixed((long long)v, p.kshift);
+        }
+      }
     }
     __syncthreads();
     cur = 1 - cur;
@@ -219,28 +228,34 @@ __global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint3
     unsigned long long *A = lay + cur * NC * SL;
     int zf = z0 + nz;
     if (zf == N) zf = 0;
-    for (int i = threadIdx.x; i < NC * SL; i += blockDim.x) {
-      const int comp = i / SL, r = i - comp * SL, ly = r / SX, lx = r - ly * SX;
+    for (int ci = threadIdx.x; ci < SL; ci += blockDim.x) {
+      const int ly = ci / SX, lx = ci - ly * SX;
       if (lx > nx || ly > ny) continue;
-      const unsigned long long v = A[i];
-      if (v == 0ull) continue;
       int x = x0 + lx, y = y0 + ly;
       if (x == N) x = 0;
       if (y == N) y = 0;
-      atomicAdd(&face[(long)comp * (p.nPX + p.nPY + p.nPZ) * NN + face_index(x, y, zf, p)], v);
+      const long fi = face_index(x, y, zf, p);
+#pragma unroll
+      for (int comp = 0; comp < NC; ++comp) {
+        const unsigned long long v = A[comp * SL + ci];
+        if (v != 0ull) atomicAdd(&face[(long)comp * fstride + fi], v);
+      }
     }
   }
 }
 
-// add the face accumulators into the field and clear them
+// add the face accumulators into the field (or, with p.overwrite, store them) and
+// clear them.  A cell on several face planes has one entry, on the first of its
+// x, y, z planes (face_index); in overwrite mode the other planes' entries for it
+// (always zero) are skipped so that they do not overwrite the cell.
 __global__ void k_face_fix(unsigned long long *face, float *out, int ncomp, FxParams p) {
   const int N = p.N;
   const long NN = (long)N * N, C = NN * N;
   const long per = (p.nPX + p.nPY + p.nPZ) * NN;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < per * ncomp; i += (long)gridDim.x * blockDim.x) {
     const unsigned long long v = face[i];
-    if (v == 0ull) continue;
-    face[i] = 0ull;
+    if (v == 0ull && !p.overwrite) continue;
+    if (v != 0ull) face[i] = 0ull;
     const long comp = i / per, r = i - comp * per;
     int x, y, z;
     if (r < p.nPX * NN) {
@@ -259,15 +274,22 @@ __global__ void k_face_fix(unsigned long long *face, float *out, int ncomp, FxPa
       y = (int)(q / N);
       x = (int)(q - (long)y * N);
     }
-    out[comp * C + sidx(x, y, z, N)] += (float)((double)(long long)v * p.inv_scale);
+    if (p.overwrite) {
+      const bool canonical = r < p.nPX * NN || (x % TX != 0 && (r < (p.nPX + p.nPY) * NN || y % TY != 0));
+      if (canonical) out[comp * C + sidx(x, y, z, N)] = float_of_fixed((long long)v, p.kshift);
+    } else {
+      out[comp * C + sidx(x, y, z, N)] += float_of_fixed((long long)v, p.kshift);
+    }
   }
 }
 
 }  // namespace
 
-// the fixed-point deposit of the mixed form; kind: 0 T00, 1 T0i, 2 Tij, 3 mass
+// the fixed-point deposit of the mixed form; kind: 0 T00, 1 T0i, 2 Tij, 3 mass.
+// overwrite: every cell of the target is written (the sum of this deposit alone),
+// which spares the caller zeroing it first and the kernel reading it back.
 int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass, double a, const gev_field *phi,
-               double bound) {
+               double bound, bool overwrite) {
   const int N = ctx->N;
   const int NC = FX_NC[kind];
   FxParams fp;
@@ -278,11 +300,13 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   int e2 = 0;
   frexp(bound, &e2);  // bound < 2^e2
   const int k = 62 - e2;
+  if (k < 0 || k > 62) return gev_fail(ctx, GEV_EINVAL, "deposit: contribution bound outside the fixed-point range");
   fp.scale = ldexpf(1.f, k);
-  fp.inv_scale = ldexp(1.0, -k);
+  fp.kshift = k;
   fp.nPX = (N + TX - 1) / TX;
   fp.nPY = (N + TY - 1) / TY;
   fp.nPZ = (N + TZ - 1) / TZ;
+  fp.overwrite = overwrite ? 1 : 0;
   const size_t face_elems = (size_t)(fp.nPX + fp.nPY + fp.nPZ) * N * N * NC;
   // the face buffer lives behind the deposit scratch pointer, kept zeroed between uses
   if (ctx->cube_bytes < face_elems * 8) {

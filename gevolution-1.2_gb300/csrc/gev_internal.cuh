@@ -97,6 +97,8 @@ struct gev_pcls {
   uint32_t *big = nullptr;    // list of cells needing the block-wide ID sort (+1 counter)
   uint32_t *scan_tmp = nullptr;
   size_t scan_tmp_elems = 0;
+  // false after a mixed-form relink that left each cell's run in atomic order
+  bool id_order = true;
 };
 
 // one simulation (include/gev_sim.h)
@@ -226,6 +228,23 @@ __device__ __forceinline__ double wrap01_bits(double x) {
   return x;
 }
 
+// v * 2^-k rounded once to the nearest FP32 (ties to even), with integer
+// instructions only: the int64 -> FP64 -> FP32 route issues three instructions
+// on the FP64 pipe (1/64 of the FP32 rate on GB300).  The result is normal for
+// |v| >= 1 whenever 0 <= k <= 62 (exponent 63 - clz - k + 127 in [65, 190]).
+__device__ __forceinline__ float float_of_fixed(long long v, int k) {
+  if (v == 0) return 0.f;
+  const unsigned sign = v < 0 ? 0x80000000u : 0u;
+  const unsigned long long a = v < 0 ? 0ull - (unsigned long long)v : (unsigned long long)v;
+  const int lz = __clzll((long long)a);
+  const unsigned long long n = a << lz;  // leading one at bit 63
+  const unsigned mant = (unsigned)(n >> 40);
+  const unsigned long long rest = n & ((1ull << 40) - 1ull), half = 1ull << 39;
+  unsigned bits = sign | ((unsigned)(63 - lz - k + 127) << 23) | (mant & 0x7fffffu);
+  if (rest > half || (rest == half && (mant & 1u))) bits += 1u;  // a carry moves into the exponent
+  return __uint_as_float(bits);
+}
+
 inline int grid_for(const gev_ctx *ctx, size_t work, int threads, int per_sm = 8) {
   size_t blocks = (work + threads - 1) / threads;
   size_t cap = (size_t)ctx->sms * per_sm;
@@ -245,5 +264,9 @@ int fft_cols_reg(gev_ctx *ctx, const void *in, void *out, long ES, long PS, int 
 int fft_r2c_rows_reg(gev_ctx *ctx, const void *real, void *spec);
 int fft_c2r_rows_reg(gev_ctx *ctx, const void *spec, void *real);
 int pcls_relink(gev_ctx *ctx, gev_pcls *p);
+int pcls_id_order(gev_ctx *ctx, gev_pcls *p);
 int ctx_ensure_cube(gev_ctx *ctx, size_t bytes);
 int ctx_ensure_red(gev_ctx *ctx, size_t elems);
+// the deposit of kind 0 T00, 1 T0i, 2 Tij, 3 mass (coefficient 1) replacing the
+// target's contents: projection_init + projection_*_project + _comm in one call
+int projection_replace(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double a, const gev_field *phi);

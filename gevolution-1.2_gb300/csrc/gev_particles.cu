@@ -251,6 +251,38 @@ __global__ void k_gather(PclsArrays src, PclsArrays dst, const uint32_t *__restr
   }
 }
 
+// relink without the ID order: particle i goes to start[cell] + rank, its rank
+// among the particles of its cell taken by the atomic histogram.  The order
+// inside a cell then follows atomic timing, which changes no result of the mixed
+// form (its deposits add integers, the updates are per particle); downloads
+// restore the (cell, ID) order first.
+template <typename V>
+__global__ void k_move(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ start,
+                       const uint32_t *__restrict__ rank, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t c = src.cell[i];
+    const uint32_t j = start[c] + rank[i];
+    dst.px[j] = src.px[i];
+    dst.py[j] = src.py[i];
+    dst.pz[j] = src.pz[i];
+    ((V *)dst.vx)[j] = ((const V *)src.vx)[i];
+    ((V *)dst.vy)[j] = ((const V *)src.vy)[i];
+    ((V *)dst.vz)[j] = ((const V *)src.vz)[i];
+    dst.id[j] = src.id[i];
+    dst.cell[j] = c;
+    if (sizeof(V) == 4) {
+      dst.rx[j] = src.rx[i];
+      dst.ry[j] = src.ry[i];
+      dst.rz[j] = src.rz[i];
+    }
+  }
+}
+
+__global__ void k_iota(uint32_t *perm, long n) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    perm[i] = (uint32_t)i;
+}
+
 // ------------------------------------------------------- particle updates --
 struct Params {
   double dtau, a, a2N, inv_a2, inv_a2N;
@@ -275,6 +307,15 @@ inline Params make_params(double dtau, double a, double a2N, int nfield, int N) 
   p.inv_a2N_f = (float)p.inv_a2N;
   p.inv_a_f = (float)(1.0 / a);
   return p;
+}
+// square root in the kernel's real type (sqrt of a float argument would otherwise
+// resolve to the double overload and run on the FP64 pipe)
+template <typename T>
+__device__ __forceinline__ T tsqrt(T x) {
+  if constexpr (sizeof(T) == 4)
+    return sqrtf(x);
+  else
+    return sqrt(x);
 }
 // a parameter in the kernel's real type
 template <typename T>
@@ -357,7 +398,7 @@ __device__ __forceinline__ void kick_one(const T *__restrict__ phi, const T *__r
     g0 *= fac;
     g1 *= fac;
     g2 *= fac;
-    e = sqrt(e2);
+    e = tsqrt<T>(e2);
     inv_e = (T)1 / e;
   }
   if (pr.nfield >= 2 && chi != nullptr) {
@@ -430,7 +471,7 @@ __device__ __forceinline__ void drift_vel(const T *__restrict__ phi, const T *__
          at<1, 1, 0>(chi, nb) * w110 + at<0, 0, 1>(chi, nb) * w001 + at<1, 0, 1>(chi, nb) * w101 +
          at<0, 1, 1>(chi, nb) * w011 + at<1, 1, 1>(chi, nb) * w111;
   const T inv_e2 = (T)1 / e2;
-  const T fac = ((T)1 + ((T)3 - qq * inv_e2) * ph - ch) * sqrt(inv_e2);
+  const T fac = ((T)1 + ((T)3 - qq * inv_e2) * ph - ch) * tsqrt<T>(inv_e2);
   v0 = q0 * fac;
   v1 = q1 * fac;
   v2 = q2 * fac;
@@ -468,10 +509,11 @@ __device__ __forceinline__ CellNb load_cell(const PclsArrays &P, long i, int N, 
 
 // pos += dtau v, periodic wrap into [0, 1), new cell key (and offset) for the relink
 template <typename T>
-__device__ __forceinline__ void move_store(PclsArrays &P, long i, const Params &pr, T v0, T v1, T v2) {
+__device__ __forceinline__ uint32_t move_store(PclsArrays &P, long i, const Params &pr, T v0, T v1, T v2) {
   const int N = pr.N, lg = pr.lg;
   const double dtau = pr.dtau;
   double x = P.px[i], y = P.py[i], z = P.pz[i];
+  uint32_t key;
   if constexpr (sizeof(T) == 4) {
     const float dt = pr.dtau_f;
     x += (double)(dt * v0);
@@ -488,16 +530,18 @@ __device__ __forceinline__ void move_store(PclsArrays &P, long i, const Params &
     P.rx[i] = r0;
     P.ry[i] = r1;
     P.rz[i] = r2;
-    P.cell[i] = (uint32_t)cx + (uint32_t)N * ((uint32_t)cy + (uint32_t)N * (uint32_t)cz);
+    key = (uint32_t)cx + (uint32_t)N * ((uint32_t)cy + (uint32_t)N * (uint32_t)cz);
   } else {
     x = wrap01(x + dtau * (double)v0);
     y = wrap01(y + dtau * (double)v1);
     z = wrap01(z + dtau * (double)v2);
-    P.cell[i] = cell_key(x, y, z, N);
+    key = cell_key(x, y, z, N);
   }
+  P.cell[i] = key;
   P.px[i] = x;
   P.py[i] = y;
   P.pz[i] = z;
+  return key;
 }
 
 template <typename T>
@@ -563,7 +607,8 @@ __global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const 
 template <typename T, typename V>
 __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_kick_drift(PclsArrays P, long n, const T *__restrict__ phi,
                                                     const T *__restrict__ chi, const T *__restrict__ Bi, Params pk,
-                                                    Params pd, unsigned long long *maxbits) {
+                                                    Params pd, unsigned long long *maxbits, uint32_t *count,
+                                                    uint32_t *rank) {
   T vmax = (T)0;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
     T r0, r1, r2;
@@ -577,7 +622,8 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_kick_drift(Pcls
     vmax = vv > vmax ? vv : vmax;
     T v0, v1, v2;
     drift_vel<T>(phi, chi, Bi, pd, nb, r0, r1, r2, q0, q1, q2, v0, v1, v2);
-    move_store<T>(P, i, pd, v0, v1, v2);
+    const uint32_t key = move_store<T>(P, i, pd, v0, v1, v2);
+    if (count) rank[i] = atomicAdd(&count[key], 1u);  // the histogram of the relink, fused
   }
   block_max_to<T>(vmax, maxbits);
 }
@@ -687,16 +733,50 @@ int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, 
   const Params pd = make_params(dtau_d, a_d, a2N_d, nfield_d, N);
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(maxbits_dev, 0, sizeof(unsigned long long), ctx->stream));
   const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
-  if (ctx->prec == GEV_PREC_FP64)
+  if (ctx->prec == GEV_PREC_FP64) {
     k_kick_drift<double, double><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, (const double *)phi->d,
                                                                   (const double *)chi->d, (const double *)Bi->d, pk, pd,
-                                                                  maxbits_dev);
-  else
-    k_kick_drift<float, float><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, (const float *)phi->d,
-                                                                (const float *)chi->d, (const float *)Bi->d, pk, pd,
-                                                                maxbits_dev);
+                                                                  maxbits_dev, nullptr, nullptr);
+    GEV_LAUNCH_CHECK(ctx);
+    return pcls_relink(ctx, p);
+  }
+  // mixed form: histogram in the update, then scan and one move (no ID order)
+  const long C = (long)N * N * N;
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->count, 0, C * sizeof(uint32_t), ctx->stream));
+  k_kick_drift<float, float><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, (const float *)phi->d,
+                                                              (const float *)chi->d, (const float *)Bi->d, pk, pd,
+                                                              maxbits_dev, p->count, p->rank);
   GEV_LAUNCH_CHECK(ctx);
-  return pcls_relink(ctx, p);
+  if (p->n == 0) return GEV_OK;
+  int rc = scan_cells(ctx, p);
+  if (rc) return rc;
+  k_move<float><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->alt, p->start, p->rank, p->n);
+  GEV_LAUNCH_CHECK(ctx);
+  std::swap(p->cur, p->alt);
+  p->id_order = false;
+  return GEV_OK;
+}
+
+// restore the (cell, ID) order after moves that skipped it
+int pcls_id_order(gev_ctx *ctx, gev_pcls *p) {
+  if (p->id_order || p->n == 0) return GEV_OK;
+  const long C = (long)ctx->N * ctx->N * ctx->N;
+  const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->big, 0, sizeof(uint32_t), ctx->stream));
+  k_iota<<<pb, 256, 0, ctx->stream>>>(p->perm, p->n);
+  GEV_LAUNCH_CHECK(ctx);
+  k_canon<<<grid_for(ctx, (size_t)C, 256, 16), 256, 0, ctx->stream>>>(p->start, C, p->cur.id, p->perm, p->big);
+  GEV_LAUNCH_CHECK(ctx);
+  k_canon_big<<<ctx->sms * 2, 256, 0, ctx->stream>>>(p->start, p->cur.id, p->perm, p->rank, p->big);
+  GEV_LAUNCH_CHECK(ctx);
+  if (ctx->prec == GEV_PREC_FP64)
+    k_gather<double><<<pb, 256, 0, ctx->stream>>>(p->cur, p->alt, p->perm, p->n);
+  else
+    k_gather<float><<<pb, 256, 0, ctx->stream>>>(p->cur, p->alt, p->perm, p->n);
+  GEV_LAUNCH_CHECK(ctx);
+  std::swap(p->cur, p->alt);
+  p->id_order = true;
+  return GEV_OK;
 }
 
 int pcls_relink(gev_ctx *ctx, gev_pcls *p) {
@@ -724,6 +804,7 @@ int pcls_relink(gev_ctx *ctx, gev_pcls *p) {
     k_gather<float><<<pb, 256, 0, ctx->stream>>>(p->cur, p->alt, p->perm, p->n);
   GEV_LAUNCH_CHECK(ctx);
   std::swap(p->cur, p->alt);
+  p->id_order = true;
   return GEV_OK;
 }
 
@@ -800,6 +881,8 @@ int gev_pcls_download(gev_pcls *p, gev_part *host, long *n) {
   if (!p || (!host && p->n > 0)) return gev_fail(p ? p->ctx : nullptr, GEV_EINVAL, "pcls_download: null buffer");
   gev_ctx *ctx = p->ctx;
   if (n) *n = p->n;
+  int rc = pcls_id_order(ctx, p);
+  if (rc) return rc;
   if (p->n > 0) {
     gev_part *d = nullptr;
     GEV_CHECK_CUDA(ctx, cudaMallocAsync(&d, p->n * sizeof(gev_part), ctx->stream));

@@ -178,14 +178,10 @@ int gev_sim_step(gev_sim *s) {
   const gev_cosmology &cm = st.cosmo;
 
   // stress-energy (main.cpp:378-450)
-  RC(gev_field_zero(s->source));
-  RC(gev_projection_T00(ctx, s->pcls, s->source, a, s->phi, 1.));
-  if (st.vector_elliptic) {
-    RC(gev_field_zero(s->Bi));
-    RC(gev_projection_T0i(ctx, s->pcls, s->Bi, s->phi, 1.));
-  }
-  RC(gev_field_zero(s->Sij));
-  RC(gev_projection_Tij(ctx, s->pcls, s->Sij, a, s->phi, 1.));
+  // (projection_init + projection_*: the target is replaced, not zeroed and re-read)
+  RC(projection_replace(ctx, s->pcls, s->source, 0, a, s->phi));
+  if (st.vector_elliptic) RC(projection_replace(ctx, s->pcls, s->Bi, 1, 1., s->phi));
+  RC(projection_replace(ctx, s->pcls, s->Sij, 2, a, s->phi));
   RC(sum_async(s, s->source, s->dev_words + 0));  // T00hom, main.cpp:459-463
 
   // phi (main.cpp:470-491)

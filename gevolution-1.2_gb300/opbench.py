@@ -33,6 +33,26 @@ def main():
 
     N = args.grid
     ctx = gpu.Context(N, gpu.PREC_MIXED if args.prec == "mixed" else gpu.PREC_FP64)
+    if args.only in ("fft_axis_y", "fft_axis_z"):
+        # one spectrum component of random values and nothing else (small enough for a
+        # full profiler capture at 512^3): the same kernel as inside the cycle
+        import numpy as np
+        rng = np.random.default_rng(1)
+        spec = ctx.spectrum(1)
+        spec.upload(rng.standard_normal(spec.shape) + 1j * rng.standard_normal(spec.shape))
+        axis = 1 if args.only == "fft_axis_y" else 2
+        st = torch.cuda.ExternalStream(ctx.stream())
+        gpu.fft_axis(spec, axis, -1)
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.reps):
+            gpu.fft_axis(spec, axis, -1)
+        e1.record(st)
+        e1.synchronize()
+        print("grid %d^3, %s form, one spectrum component; %s %.3f ms per call (CUDA events), %d calls"
+              % (N, args.prec, args.only, e0.elapsed_time(e1) / args.reps, args.reps))
+        return
     s = gpu.Sim(ctx, N ** 3)
     s.ic_generate(**gpu.ic_params(1000.0 * N / 512, seed=1))
     for _ in range(2):
