@@ -248,37 +248,43 @@ __global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint3
 // clear them.  A cell on several face planes has one entry, on the first of its
 // x, y, z planes (face_index); in overwrite mode the other planes' entries for it
 // (always zero) are skipped so that they do not overwrite the cell.
-__global__ void k_face_fix(unsigned long long *face, float *out, int ncomp, FxParams p) {
+__global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, float *out, int ncomp, FxParams p) {
   const int N = p.N;
   const long NN = (long)N * N, C = NN * N;
-  const long per = (p.nPX + p.nPY + p.nPZ) * NN;
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < per * ncomp; i += (long)gridDim.x * blockDim.x) {
-    const unsigned long long v = face[i];
-    if (v == 0ull && !p.overwrite) continue;
-    if (v != 0ull) face[i] = 0ull;
-    const long comp = i / per, r = i - comp * per;
-    int x, y, z;
-    if (r < p.nPX * NN) {
-      const long pl = r / NN, q = r - pl * NN;
-      x = (int)pl * TX;
-      z = (int)(q / N);
-      y = (int)(q - (long)z * N);
-    } else if (r < (p.nPX + p.nPY) * NN) {
-      const long rr = r - p.nPX * NN, pl = rr / NN, q = rr - pl * NN;
-      y = (int)pl * TY;
-      z = (int)(q / N);
-      x = (int)(q - (long)z * N);
-    } else {
-      const long rr = r - (p.nPX + p.nPY) * NN, pl = rr / NN, q = rr - pl * NN;
-      z = (int)pl * TZ;
-      y = (int)(q / N);
-      x = (int)(q - (long)y * N);
-    }
-    if (p.overwrite) {
-      const bool canonical = r < p.nPX * NN || (x % TX != 0 && (r < (p.nPX + p.nPY) * NN || y % TY != 0));
-      if (canonical) out[comp * C + sidx(x, y, z, N)] = float_of_fixed((long long)v, p.kshift);
-    } else {
-      out[comp * C + sidx(x, y, z, N)] += float_of_fixed((long long)v, p.kshift);
+  const int planes = (int)(p.nPX + p.nPY + p.nPZ);
+  const long rows = (long)ncomp * planes * N;  // face entries come in rows of N (face_index)
+  for (long row = blockIdx.x; row < rows; row += gridDim.x) {
+    const int comp = (int)(row / ((long)planes * N));
+    const int rr = (int)(row - (long)comp * planes * N);
+    const int pl = rr / N, q = rr - pl * N;
+    unsigned long long *f = face + row * N;
+    float *o = out + comp * C;
+    for (int t = threadIdx.x; t < N; t += blockDim.x) {
+      const unsigned long long v = f[t];
+      if (v == 0ull && !p.overwrite) continue;
+      if (v != 0ull) f[t] = 0ull;
+      int x, y, z;
+      bool canonical = true;
+      if (pl < p.nPX) {  // x plane: rows z, columns y
+        x = pl * TX;
+        z = q;
+        y = t;
+      } else if (pl < p.nPX + p.nPY) {  // y plane: rows z, columns x
+        y = (int)(pl - p.nPX) * TY;
+        z = q;
+        x = t;
+        canonical = x % TX != 0;
+      } else {  // z plane: rows y, columns x
+        z = (int)(pl - p.nPX - p.nPY) * TZ;
+        y = q;
+        x = t;
+        canonical = x % TX != 0 && y % TY != 0;
+      }
+      if (p.overwrite) {
+        if (canonical) o[sidx(x, y, z, N)] = float_of_fixed((long long)v, p.kshift);
+      } else {
+        o[sidx(x, y, z, N)] += float_of_fixed((long long)v, p.kshift);
+      }
     }
   }
 }
@@ -338,7 +344,9 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
       k_dep_fx<FX_MASS><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, nullptr, fo, face, fp);
   }
   GEV_LAUNCH_CHECK(ctx);
-  k_face_fix<<<grid_for(ctx, face_elems, 256, 16), 256, 0, ctx->stream>>>(face, fo, NC, fp);
+  const long face_rows = (long)NC * (fp.nPX + fp.nPY + fp.nPZ) * N;
+  const long ff_blocks = face_rows < (long)ctx->sms * 16 ? face_rows : (long)ctx->sms * 16;
+  k_face_fix<<<(unsigned)ff_blocks, 256, 0, ctx->stream>>>(face, fo, NC, fp);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }

@@ -180,6 +180,38 @@ __host__ __device__ inline int lg_pow2(int N) {
   return (1 << l) == N ? l : -1;
 }
 
+// f * 2^-24 for a 24-bit f, built from bits (an int -> float conversion issues on
+// the FP64 pipe on GB300): (f >> 1) * 2^-23 = (1 + (f >> 1) 2^-23) - 1 exactly, plus
+// the last bit; every step is exact, so the result equals (float)f * 2^-24.
+__device__ __forceinline__ float frac24(unsigned f) {
+  float r = __uint_as_float(0x3F800000u | (f >> 1)) - 1.0f;
+  if (f & 1u) r += 5.9604644775390625e-8f;
+  return r;
+}
+
+// (double)f from bits, without the float -> double conversion instruction
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned long long s = (unsigned long long)(b >> 31) << 63;
+  unsigned long long m = b & 0x7fffffu;
+  unsigned long long d;
+  if (e == 0u) {
+    if (m == 0ull) {
+      d = s;
+    } else {  // subnormal float: normalise (a normal double)
+      const int sh = __clz((int)m) - 8;
+      m = (m << sh) & 0x7fffffull;
+      d = s | ((unsigned long long)(1023 - 126 - sh) << 52) | (m << 29);
+    }
+  } else if (e == 0xffu) {
+    d = s | (0x7ffull << 52) | (m << 29);
+  } else {
+    d = s | ((unsigned long long)(e - 127u + 1023u) << 52) | (m << 29);
+  }
+  return __longlong_as_double((long long)d);
+}
+
 // cell = floor(x N) (clamped to N-1) and r = x N - cell as FP32, for x in [0, 1).
 // With N = 2^lg the split reads the double's bits (x N is an exact exponent
 // shift), so it issues no FP64 instruction; r keeps the leading 24 bits of the
@@ -197,11 +229,11 @@ __device__ __forceinline__ void pos_split(double x, int N, int lg, int &c, float
     const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | 0x10000000000000ull;
     if (sh >= 64) {
       c = 0;
-      r = (float)(unsigned)(m >> (sh - 24)) * 5.9604644775390625e-8f;
+      r = frac24((unsigned)(m >> (sh - 24)));
     } else {
       c = (int)(m >> sh);
       const unsigned long long frac = m & ((1ull << sh) - 1ull);
-      r = (float)(unsigned)(frac >> (sh - 24)) * 5.9604644775390625e-8f;
+      r = frac24((unsigned)(frac >> (sh - 24)));
     }
     if (c >= N) {
       c = N - 1;

@@ -256,25 +256,64 @@ __global__ void k_gather(PclsArrays src, PclsArrays dst, const uint32_t *__restr
 // inside a cell then follows atomic timing, which changes no result of the mixed
 // form (its deposits add integers, the updates are per particle); downloads
 // restore the (cell, ID) order first.
-template <typename V>
-__global__ void k_move(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ start,
-                       const uint32_t *__restrict__ rank, long n) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const uint32_t c = src.cell[i];
-    const uint32_t j = start[c] + rank[i];
-    dst.px[j] = src.px[i];
-    dst.py[j] = src.py[i];
-    dst.pz[j] = src.pz[i];
-    ((V *)dst.vx)[j] = ((const V *)src.vx)[i];
-    ((V *)dst.vy)[j] = ((const V *)src.vy)[i];
-    ((V *)dst.vz)[j] = ((const V *)src.vz)[i];
-    dst.id[j] = src.id[i];
-    dst.cell[j] = c;
-    if (sizeof(V) == 4) {
-      dst.rx[j] = src.rx[i];
-      dst.ry[j] = src.ry[i];
-      dst.rz[j] = src.rz[i];
+// Mixed form (FP32 momenta and offsets).  Four consecutive particles per thread,
+// read with 16-byte vector loads (cudaMalloc'd arrays, index a multiple of 4), so
+// that each thread has its whole payload in flight before the scattered stores.
+__global__ void __launch_bounds__(256) k_move(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ start,
+                                              const uint32_t *__restrict__ rank, long n) {
+  const long n4 = n >> 2;
+  const float *svx = (const float *)src.vx, *svy = (const float *)src.vy, *svz = (const float *)src.vz;
+  float *dvx = (float *)dst.vx, *dvy = (float *)dst.vy, *dvz = (float *)dst.vz;
+  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
+    const long i = q << 2;
+    const uint4 c = *reinterpret_cast<const uint4 *>(src.cell + i);
+    const uint4 rk = *reinterpret_cast<const uint4 *>(rank + i);
+    const double2 x01 = *reinterpret_cast<const double2 *>(src.px + i), x23 = *reinterpret_cast<const double2 *>(src.px + i + 2);
+    const double2 y01 = *reinterpret_cast<const double2 *>(src.py + i), y23 = *reinterpret_cast<const double2 *>(src.py + i + 2);
+    const double2 z01 = *reinterpret_cast<const double2 *>(src.pz + i), z23 = *reinterpret_cast<const double2 *>(src.pz + i + 2);
+    const longlong2 d01 = *reinterpret_cast<const longlong2 *>(src.id + i), d23 = *reinterpret_cast<const longlong2 *>(src.id + i + 2);
+    const float4 vx = *reinterpret_cast<const float4 *>(svx + i), vy = *reinterpret_cast<const float4 *>(svy + i),
+                 vz = *reinterpret_cast<const float4 *>(svz + i);
+    const float4 rx = *reinterpret_cast<const float4 *>(src.rx + i), ry = *reinterpret_cast<const float4 *>(src.ry + i),
+                 rz = *reinterpret_cast<const float4 *>(src.rz + i);
+    const uint32_t j[4] = {start[c.x] + rk.x, start[c.y] + rk.y, start[c.z] + rk.z, start[c.w] + rk.w};
+    const uint32_t cc[4] = {c.x, c.y, c.z, c.w};
+    const double X[4] = {x01.x, x01.y, x23.x, x23.y}, Y[4] = {y01.x, y01.y, y23.x, y23.y},
+                 Z[4] = {z01.x, z01.y, z23.x, z23.y};
+    const long long D[4] = {d01.x, d01.y, d23.x, d23.y};
+    const float VX[4] = {vx.x, vx.y, vx.z, vx.w}, VY[4] = {vy.x, vy.y, vy.z, vy.w}, VZ[4] = {vz.x, vz.y, vz.z, vz.w};
+    const float RX[4] = {rx.x, rx.y, rx.z, rx.w}, RY[4] = {ry.x, ry.y, ry.z, ry.w}, RZ[4] = {rz.x, rz.y, rz.z, rz.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const uint32_t t = j[k];
+      dst.px[t] = X[k];
+      dst.py[t] = Y[k];
+      dst.pz[t] = Z[k];
+      dvx[t] = VX[k];
+      dvy[t] = VY[k];
+      dvz[t] = VZ[k];
+      dst.id[t] = D[k];
+      dst.cell[t] = cc[k];
+      dst.rx[t] = RX[k];
+      dst.ry[t] = RY[k];
+      dst.rz[t] = RZ[k];
     }
+  }
+  // the last n % 4 particles
+  for (long i = (n4 << 2) + blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t c = src.cell[i];
+    const uint32_t t = start[c] + rank[i];
+    dst.px[t] = src.px[i];
+    dst.py[t] = src.py[i];
+    dst.pz[t] = src.pz[i];
+    dvx[t] = svx[i];
+    dvy[t] = svy[i];
+    dvz[t] = svz[i];
+    dst.id[t] = src.id[i];
+    dst.cell[t] = c;
+    dst.rx[t] = src.rx[i];
+    dst.ry[t] = src.ry[i];
+    dst.rz[t] = src.rz[i];
   }
 }
 
@@ -289,7 +328,7 @@ struct Params {
   int nfield, N, lg;
   // the same values rounded to FP32 on the host (round to nearest, as the device
   // conversion would), so the mixed form's loops convert nothing per particle
-  float dtau_f, a_f, inv_a2_f, inv_a2N_f, inv_a_f;
+  float dtau_f, a_f, inv_a2_f, inv_a2N_f, inv_a_f, N_f;
 };
 inline Params make_params(double dtau, double a, double a2N, int nfield, int N) {
   Params p;
@@ -306,6 +345,7 @@ inline Params make_params(double dtau, double a, double a2N, int nfield, int N) 
   p.inv_a2_f = (float)p.inv_a2;
   p.inv_a2N_f = (float)p.inv_a2N;
   p.inv_a_f = (float)(1.0 / a);
+  p.N_f = (float)N;
   return p;
 }
 // square root in the kernel's real type (sqrt of a float argument would otherwise
@@ -442,7 +482,7 @@ __device__ __forceinline__ void kick_one(const T *__restrict__ phi, const T *__r
     g1 += p1 * k;
     g2 += p2 * k;
   }
-  const T m = pv<T>(pr.dtau, pr.dtau_f) * (KIND == GEV_GR ? e : a) * (T)N;
+  const T m = pv<T>(pr.dtau, pr.dtau_f) * (KIND == GEV_GR ? e : a) * pv<T>((double)N, pr.N_f);
   q0 -= m * g0;
   q1 -= m * g1;
   q2 -= m * g2;
@@ -516,9 +556,9 @@ __device__ __forceinline__ uint32_t move_store(PclsArrays &P, long i, const Para
   uint32_t key;
   if constexpr (sizeof(T) == 4) {
     const float dt = pr.dtau_f;
-    x += (double)(dt * v0);
-    y += (double)(dt * v1);
-    z += (double)(dt * v2);
+    x += f2d_bits(dt * v0);
+    y += f2d_bits(dt * v1);
+    z += f2d_bits(dt * v2);
     x = wrap01_bits(x);
     y = wrap01_bits(y);
     z = wrap01_bits(z);
@@ -750,7 +790,8 @@ int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, 
   if (p->n == 0) return GEV_OK;
   int rc = scan_cells(ctx, p);
   if (rc) return rc;
-  k_move<float><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->alt, p->start, p->rank, p->n);
+  k_move<<<grid_for(ctx, (size_t)(p->n + 3) / 4, 256, 16), 256, 0, ctx->stream>>>(p->cur, p->alt, p->start, p->rank,
+                                                                                  p->n);
   GEV_LAUNCH_CHECK(ctx);
   std::swap(p->cur, p->alt);
   p->id_order = false;

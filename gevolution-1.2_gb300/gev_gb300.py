@@ -70,6 +70,7 @@ _SIGS = {
     "gev_update_q": [_vp, _vp, _i, _d, _vp, _vp, _vp, _i, _d, _d, ctypes.POINTER(_d)],
     "gev_update_pos": [_vp, _vp, _i, _d, _vp, _vp, _vp, _i, _d, _d],
     "gev_field_sum": [_vp, _vp, _i, ctypes.POINTER(_d)],
+    "gev_cross_spectrum": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _i, _i],
 }
 
 
@@ -289,6 +290,19 @@ def fft_c2r(spec, real):
 def fft_axis(spec, axis, sign):
     """One pass of the 3-D transform: 1-D FFT along y (axis 1) or z (axis 2), in place."""
     _check(lib().gev_fft_axis(spec.ctx.handle, spec.handle, axis, sign), spec.ctx, "gev_fft_axis")
+
+
+def cross_spectrum(f1, f2=None, numbins=32, deconvolve=True, ktype=1, symmetric=False, comp1=-1, comp2=-1):
+    """extractCrossSpectrum / extractPowerSpectrum (tools.hpp:53-240) on the device:
+    returns (kbin, power, kscatter, pscatter, occupation), numbins entries each."""
+    import numpy as np
+    f2 = f1 if f2 is None else f2
+    out = [np.zeros(numbins) for _ in range(4)]
+    occ = np.zeros(numbins, np.int32)
+    _check(lib().gev_cross_spectrum(f1.ctx.handle, f1.handle, f2.handle, *(o.ctypes.data for o in out), occ.ctypes.data,
+                                    numbins, int(bool(deconvolve)), ktype, int(bool(symmetric)), comp1, comp2), f1.ctx,
+           "gev_cross_spectrum")
+    return out[0], out[1], out[2], out[3], occ
 
 
 def solve_poisson(srcFT, potFT, coeff, modif=0.0):

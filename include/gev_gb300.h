@@ -139,6 +139,20 @@ int gev_update_pos(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_f
 /* sum of one component over all cells (T00hom, main.cpp:459-463); deterministic order */
 int gev_field_sum(gev_ctx *ctx, const gev_field *f, int comp, double *out);
 
+/* ---- spectra ---- */
+/* extractCrossSpectrum (tools.hpp:53-212) / extractPowerSpectrum (237-240) over device
+ * spectra, without copying them to the host: numbins bins of |k| up to sqrt(3) k_Nyquist,
+ * linear k (ktype 1, KTYPE_LINEAR) or grid k (ktype 0, KTYPE_GRID), the CIC window
+ * deconvolved when deconvolve != 0.  comp1, comp2 >= 0 correlate one component of each
+ * field; otherwise all components are summed (f1 and f2 with equal counts) and
+ * symmetric != 0 reads 6 components as the symmetric tensor 00 01 02 11 12 22 with the
+ * off-diagonal terms counted twice.  f2 may be f1.  Fills host arrays of numbins entries
+ * as the reference does: mean k, mean power, k scatter, power scatter, modes per bin.
+ * The per-bin sums are exact integer sums (bit-reproducible); waits for the stream. */
+int gev_cross_spectrum(gev_ctx *ctx, const gev_field *f1, const gev_field *f2, double *kbin, double *power,
+                       double *kscatter, double *pscatter, int *occupation, int numbins, int deconvolve, int ktype,
+                       int symmetric, int comp1, int comp2);
+
 /* ---- reduction that allocates nothing (no counterpart in gevolution-1.2) ----
  * For host codes that must not allocate device memory while they run: their
  * fields fill the GPU and all device memory belongs to their own pool (or to
