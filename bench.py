@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-pk-check", action="store_true", help="skip the FP64-form run and spectrum comparison")
     return ap.parse_args()
 
 
@@ -188,22 +189,79 @@ def run_ours(args, rank, world, local):
     ms_max = float(t.item())
     value = N ** 3 * args.steps * world / (ms_max / 1e3)
     st = sim.state()
+    pk = None
+    if not args.no_pk_check and prec == gpu.PREC_MIXED and world == 1:
+        pk = spectra_of(gpu, ctx, sim)
 
-    # dominant-kernel roofline: the deposit of T_ij (see the design doc for the per-kernel bytes)
+    # dominant-kernel roofline: one FFT column pass
     roof = dominant_kernel_roofline(gpu, ctx, sim, stream, N, args.prec)
 
     # e2e: particle state from pinned host memory in, cycle, particle state out
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(gpu, ctx, sim, stream, N, args.steps, torch)
+    fp64 = None
+    if pk is not None:
+        del sim, ctx
+        fp64 = fp64_form_check(args, gpu, N, box, local, pk, torch)
     return dict(value=value, ms=ms_max / args.steps, launches=launches, clocks=clk, state=st, roofline=roof,
-                e2e=e2e, box=box)
+                e2e=e2e, box=box, fp64=fp64)
 
 
-# DRAM traffic per launch of the column pass from the committed ncu captures
-# (dram__bytes_read.sum + dram__bytes_write.sum), keyed by (grid, precision);
-# see profiles/fft_cols_*.md for the command and the raw figures
-COLS_TRAFFIC = {}
+PK_FIELDS = (("phi", 1), ("chi", 1), ("Bi", 3), ("source", 1))
+PK_BINS = 64
+
+
+def spectra_of(gpu, ctx, sim):
+    """Power spectra (device FFT + gev_cross_spectrum) of phi, chi, B_i and the
+    source field of a simulation."""
+    out = {}
+    for name, nc in PK_FIELDS:
+        sp = ctx.spectrum(nc)
+        gpu.fft_r2c(sim.field(name), sp)
+        out[name] = gpu.cross_spectrum(sp, numbins=PK_BINS)
+        del sp
+    return out
+
+
+def fp64_form_check(args, gpu, N, box, local, pk_mixed, torch):
+    """The plain FP64 form from the same initial conditions for the same cycles:
+    its device-timed throughput, and the largest per-bin relative deviation of the
+    mixed form's power spectra from it up to k_Nyquist / 2 (criterion 1e-3)."""
+    import numpy as np
+    ctx = gpu.Context(N, gpu.PREC_FP64, device=local)
+    sim = gpu.Sim(ctx, N ** 3)
+    sim.ic_generate(**gpu.ic_params(box, seed=args.seed))
+    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
+    for _ in range(args.warmup):
+        sim.step()
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        sim.step()
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    pk64 = spectra_of(gpu, ctx, sim)
+    dev = {}
+    for name, _ in PK_FIELDS:
+        kb, p64, _, _, occ = pk64[name]
+        p32 = pk_mixed[name][1]
+        m = (occ > 0) & (kb <= 0.5 * np.pi * N)
+        dev[name] = float(np.max(np.abs(p32[m] - p64[m]) / np.maximum(np.abs(p64[m]), 1e-300)))
+    return {"fp64_form": {"value": N ** 3 * args.steps / (ms / 1e3), "unit": "particle-steps/s",
+                          "ms_per_step": ms / args.steps},
+            "pk_check": {"against": "the FP64 form on the GPU, same initial conditions, %d cycles"
+                         % (args.warmup + args.steps), "numbins": PK_BINS, "k_max": "k_Nyquist/2",
+                         "max_rel_dev": dev, "tolerance": 1e-3, "pass": all(v <= 1e-3 for v in dev.values())}}
+
+
+# DRAM traffic per launch of the column pass (dram__bytes_read.sum +
+# dram__bytes_write.sum) from an ncu capture of the same kernel on one 512^3
+# spectrum component (gevolution-1.2_gb300/opbench.py --only fft_axis_z), keyed by
+# (grid, precision): 556.2 MB read + 511.3 MB written
+COLS_TRAFFIC = {(512, "mixed"): 1.0675e9}
 
 
 def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
@@ -331,6 +389,8 @@ def main():
             "roofline": res["roofline"], "cpu_baseline": cpu, "e2e": res["e2e"], "gpu_launches": res["launches"],
             "clocks": res["clocks"], "bytes_per_cycle_alg": cycle_bytes(N, args.prec),
             "final_a": res["state"]["a"]}
+    if res.get("fp64"):
+        line.update(res["fp64"])
     print(json.dumps(line))
 
 

@@ -17,7 +17,7 @@
 #include "gev_internal.cuh"
 
 int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass, double a, const gev_field *phi,
-               double bound, bool overwrite);
+               bool overwrite);
 
 namespace {
 
@@ -187,23 +187,6 @@ __global__ void __launch_bounds__(256) k_gather(const A *__restrict__ cube, T *o
   }
 }
 
-// bound on |per-particle contribution| for the fixed-point scale of the mixed form
-double contribution_bound(int kind, double mass, double a, double vmax_hint) {
-  // weights <= 1, |phi| << 1 (|1 + f phi| <= 2), e <= sqrt(q^2 + a^2)
-  const double q2 = vmax_hint * vmax_hint;
-  const double e = sqrt(q2 + a * a);
-  switch (kind) {
-    case DEP_MASS:
-      return mass;
-    case DEP_T00:
-      return mass * (e + (3. * e + q2 / e) * 0.1) + mass * e;
-    case DEP_T0I:
-      return mass * sqrt(q2) * 2. + mass;
-    default:
-      return mass * q2 / (e > 0 ? e : 1.) * 3. + mass;
-  }
-}
-
 template <int KIND>
 int run_deposit(gev_ctx *ctx, gev_pcls *p, gev_field *out, double a, const gev_field *phi, double coeff,
                 bool overwrite = false) {
@@ -229,10 +212,7 @@ int run_deposit(gev_ctx *ctx, gev_pcls *p, gev_field *out, double a, const gev_f
     k_gather<KIND, double, double><<<blocks, 256, 0, ctx->stream>>>((const double *)ctx->d_cube, (double *)out->d, N, 1.);
     GEV_LAUNCH_CHECK(ctx);
   } else {
-    // fixed-point scale: all particles at the contribution bound in one cell stay below 2^62
-    const double vmax = 0.05;  // |q| bound for the scale; CDM momenta q = a v stay far below it
-    const double bound = contribution_bound(KIND, mass, a, vmax) * (double)(p->n > 0 ? p->n : 1) * 8.;
-    int rc = deposit_fx(ctx, p, out, KIND, mass, a, phi, bound, overwrite);
+    int rc = deposit_fx(ctx, p, out, KIND, mass, a, phi, overwrite);
     if (rc) return rc;
   }
   return GEV_OK;

@@ -31,8 +31,6 @@ constexpr int TX = 32, TY = 16, TZ = 32, FX_THREADS = 256;
 struct FxParams {
   int N, lg;  // lg = log2 N for a power of two, else -1
   float mass, a;
-  float scale;  // 2^kshift
-  int kshift;
   long nPX, nPY, nPZ;  // face planes per direction
   int overwrite;       // 1: the target's previous contents are replaced instead of added to
 };
@@ -67,11 +65,66 @@ __device__ __forceinline__ void sadd(unsigned long long *a, float v, float s) {
   if (q != 0) atomicAdd(a, (unsigned long long)q);
 }
 
+// The fixed-point scale comes from the data, on the device: max |q|^2 over the
+// particles and the most particles in one cell.  A cell's sum has at most 8 x that
+// many contributions (its 8 neighbouring cells), each below c_max of the kind, and
+// must stay below 2^62; max reductions do not depend on order, so neither does the
+// scale.
+__global__ void __launch_bounds__(256) k_fx_bounds(const float *__restrict__ vx, const float *__restrict__ vy,
+                                                   const float *__restrict__ vz, long n,
+                                                   const uint32_t *__restrict__ count, long C, uint32_t *bounds) {
+  float q2 = 0.f;
+  uint32_t mc = 0u;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    q2 = fmaxf(q2, vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < C; c += (long)gridDim.x * blockDim.x)
+    mc = max(mc, count[c]);
+  for (int o = 16; o > 0; o >>= 1) {
+    q2 = fmaxf(q2, __shfl_xor_sync(0xffffffffu, q2, o));
+    mc = max(mc, __shfl_xor_sync(0xffffffffu, mc, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicMax(&bounds[0], __float_as_uint(q2));  // q2 >= 0: the bit patterns order as the values
+    atomicMax(&bounds[1], mc);
+  }
+}
+
+// per-particle contribution bounds, |phi| <= 1 taken for the (1 + f phi) factors:
+// T00 m (e + (3e + q^2/e)|phi|) <= m (4e + q^2/a); T0i m |q_i| (1 + 2|phi|) <= 3 m |q|;
+// Tij m q_i q_j / e (1 + 5|phi|) <= 6 m q^2 / a; mass m.  Writes the power k of the
+// scale 2^k into bounds[2], kept in [-60, 100] (FP32 scale and float_of_fixed stay exact).
+__global__ void k_fx_scale(uint32_t *bounds, int kind, double mass, double a) {
+  const double q2 = (double)__uint_as_float(bounds[0]);
+  const double mc = (double)(bounds[1] > 0u ? bounds[1] : 1u);
+  const double e = sqrt(q2 + a * a);
+  double c;
+  if (kind == FX_MASS)
+    c = mass;
+  else if (kind == FX_T00)
+    c = mass * (4. * e + q2 / a);
+  else if (kind == FX_T0I)
+    c = 3. * mass * sqrt(q2);
+  else
+    c = 6. * mass * q2 / a;
+  const double bound = fabs(c) * 8. * mc;
+  int k = 100;
+  if (bound > 0.) {
+    int e2 = 0;
+    frexp(bound, &e2);  // bound < 2^e2
+    k = 62 - e2;
+  }
+  k = k < -60 ? -60 : (k > 100 ? 100 : k);
+  bounds[2] = (uint32_t)k;
+}
+
 template <int KIND>
 __global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint32_t *__restrict__ start,
                                                        const float *__restrict__ phi, float *out,
-                                                       unsigned long long *face, FxParams p) {
+                                                       unsigned long long *face, FxParams p,
+                                                       const uint32_t *__restrict__ fxb) {
   constexpr int NC = FX_NC[KIND];
+  const int ks = (int)fxb[2];
+  const float scale = __int_as_float((127 + ks) << 23);  // 2^ks
   constexpr int SX = TX + 1, SY = TY + 1, SL = SX * SY;  // one shared layer per component
   extern __shared__ __align__(16) unsigned long long lay[];  // [2][NC][SY][SX]
   __shared__ uint32_t rowoff[TY + 1], rowbase[TY];
@@ -139,7 +192,7 @@ __global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint3
       // corner k = 4 dx + 2 dy + dz goes to layer dz at (ly + dy, lx + dx)
       const int o00 = ly * SX + lx, o01 = (ly + 1) * SX + lx, o10 = ly * SX + lx + 1, o11 = (ly + 1) * SX + lx + 1;
       const int off[8] = {o00, o00, o01, o01, o10, o10, o11, o11};
-      const float s = p.scale, m = p.mass, a = p.a;
+      const float s = scale, m = p.mass, a = p.a;
       if (KIND == FX_MASS || KIND == FX_T00) {
         float ee = a, ff = 0.f;
         if (KIND == FX_T00 && phi != nullptr) {
@@ -214,9 +267,9 @@ __global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint3
         if (onface) {
           if (v != 0ull) atomicAdd(&face[(long)comp * fstride + fi], v);
         } else if (p.overwrite) {
-          out[(long)comp * C + gi] = float_of_fixed((long long)v, p.kshift);
+          out[(long)comp * C + gi] = float_of_fixed((long long)v, ks);
         } else if (v != 0ull) {
-          out[(long)comp * C + gi] += float_of_fixed((long long)v, p.kshift);
+          out[(long)comp * C + gi] += float_of_fixed((long long)v, ks);
         }
       }
     }
@@ -248,8 +301,10 @@ __global__ void __launch_bounds__(FX_THREADS) k_dep_fx(PclsArrays P, const uint3
 // clear them.  A cell on several face planes has one entry, on the first of its
 // x, y, z planes (face_index); in overwrite mode the other planes' entries for it
 // (always zero) are skipped so that they do not overwrite the cell.
-__global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, float *out, int ncomp, FxParams p) {
+__global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, float *out, int ncomp, FxParams p,
+                                                  const uint32_t *__restrict__ fxb) {
   const int N = p.N;
+  const int ks = (int)fxb[2];
   const long NN = (long)N * N, C = NN * N;
   const int planes = (int)(p.nPX + p.nPY + p.nPZ);
   const long rows = (long)ncomp * planes * N;  // face entries come in rows of N (face_index)
@@ -281,9 +336,9 @@ __global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, floa
         canonical = x % TX != 0 && y % TY != 0;
       }
       if (p.overwrite) {
-        if (canonical) o[sidx(x, y, z, N)] = float_of_fixed((long long)v, p.kshift);
+        if (canonical) o[sidx(x, y, z, N)] = float_of_fixed((long long)v, ks);
       } else {
-        o[sidx(x, y, z, N)] += float_of_fixed((long long)v, p.kshift);
+        o[sidx(x, y, z, N)] += float_of_fixed((long long)v, ks);
       }
     }
   }
@@ -295,7 +350,7 @@ __global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, floa
 // overwrite: every cell of the target is written (the sum of this deposit alone),
 // which spares the caller zeroing it first and the kernel reading it back.
 int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass, double a, const gev_field *phi,
-               double bound, bool overwrite) {
+               bool overwrite) {
   const int N = ctx->N;
   const int NC = FX_NC[kind];
   FxParams fp;
@@ -303,12 +358,6 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   fp.lg = lg_pow2(N);
   fp.mass = (float)mass;
   fp.a = (float)a;
-  int e2 = 0;
-  frexp(bound, &e2);  // bound < 2^e2
-  const int k = 62 - e2;
-  if (k < 0 || k > 62) return gev_fail(ctx, GEV_EINVAL, "deposit: contribution bound outside the fixed-point range");
-  fp.scale = ldexpf(1.f, k);
-  fp.kshift = k;
   fp.nPX = (N + TX - 1) / TX;
   fp.nPY = (N + TY - 1) / TY;
   fp.nPZ = (N + TZ - 1) / TZ;
@@ -326,27 +375,34 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   const float *fphi = phi ? (const float *)phi->d : nullptr;
   float *fo = (float *)out->d;
   const unsigned blocks = (unsigned)(ntx * nty * ntz);
+  const long C = (long)N * N * N;
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->bounds, 0, 2 * sizeof(uint32_t), ctx->stream));
+  k_fx_bounds<<<grid_for(ctx, (size_t)(p->n > C ? p->n : C), 256, 8), 256, 0, ctx->stream>>>(
+      (const float *)p->cur.vx, (const float *)p->cur.vy, (const float *)p->cur.vz, p->n, p->count, C, p->bounds);
+  GEV_LAUNCH_CHECK(ctx);
+  k_fx_scale<<<1, 1, 0, ctx->stream>>>(p->bounds, kind, mass, a);
+  GEV_LAUNCH_CHECK(ctx);
   switch (kind) {
     case FX_T00:
       cudaFuncSetAttribute(k_dep_fx<FX_T00>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_dep_fx<FX_T00><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, fphi, fo, face, fp);
+      k_dep_fx<FX_T00><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, fphi, fo, face, fp, p->bounds);
       break;
     case FX_T0I:
       cudaFuncSetAttribute(k_dep_fx<FX_T0I>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_dep_fx<FX_T0I><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, fphi, fo, face, fp);
+      k_dep_fx<FX_T0I><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, fphi, fo, face, fp, p->bounds);
       break;
     case FX_TIJ:
       cudaFuncSetAttribute(k_dep_fx<FX_TIJ>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_dep_fx<FX_TIJ><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, fphi, fo, face, fp);
+      k_dep_fx<FX_TIJ><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, fphi, fo, face, fp, p->bounds);
       break;
     default:
       cudaFuncSetAttribute(k_dep_fx<FX_MASS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      k_dep_fx<FX_MASS><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, nullptr, fo, face, fp);
+      k_dep_fx<FX_MASS><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, nullptr, fo, face, fp, p->bounds);
   }
   GEV_LAUNCH_CHECK(ctx);
   const long face_rows = (long)NC * (fp.nPX + fp.nPY + fp.nPZ) * N;
   const long ff_blocks = face_rows < (long)ctx->sms * 16 ? face_rows : (long)ctx->sms * 16;
-  k_face_fix<<<(unsigned)ff_blocks, 256, 0, ctx->stream>>>(face, fo, NC, fp);
+  k_face_fix<<<(unsigned)ff_blocks, 256, 0, ctx->stream>>>(face, fo, NC, fp, p->bounds);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }

@@ -99,6 +99,9 @@ struct gev_pcls {
   size_t scan_tmp_elems = 0;
   // false after a mixed-form relink that left each cell's run in atomic order
   bool id_order = true;
+  // mixed-form deposit scale: [0] max |q|^2 (FP32 bits), [1] max particles in a cell,
+  // [2] the power of two of the last deposit's fixed-point scale
+  uint32_t *bounds = nullptr;
 };
 
 // one simulation (include/gev_sim.h)

@@ -27,9 +27,19 @@ __global__ void k_source_tensor(const T *__restrict__ phi, const T *Tij, T *Sij,
     Sij[i] = coeff * t00 + h * (pxp - pxm) * (pxp - pxm);
     Sij[3 * V + i] = coeff * t11 + h * (pyp - pym) * (pyp - pym);
     Sij[5 * V + i] = coeff * t22 + h * (pzp - pzm) * (pzp - pzm);
-    Sij[V + i] = coeff * t01 + (pxp * pyp - p * pxy) + h * p * p - h * pxp * pxp - h * pyp * pyp + h * pxy * pxy;
-    Sij[2 * V + i] = coeff * t02 + (pxp * pzp - p * pxz) + h * p * p - h * pxp * pxp - h * pzp * pzp + h * pxz * pxz;
-    Sij[4 * V + i] = coeff * t12 + (pyp * pzp - p * pyz) + h * p * p - h * pyp * pyp - h * pzp * pzp + h * pyz * pyz;
+    if constexpr (sizeof(T) == 8) {  // the reference's expression, term by term
+      Sij[V + i] = coeff * t01 + (pxp * pyp - p * pxy) + h * p * p - h * pxp * pxp - h * pyp * pyp + h * pxy * pxy;
+      Sij[2 * V + i] = coeff * t02 + (pxp * pzp - p * pxz) + h * p * p - h * pxp * pxp - h * pzp * pzp + h * pxz * pxz;
+      Sij[4 * V + i] = coeff * t12 + (pyp * pzp - p * pyz) + h * p * p - h * pyp * pyp - h * pzp * pzp + h * pyz * pyz;
+    } else {
+      // FP32: with a = phi(x), b = phi(x+i), c = phi(x+j), d = phi(x+i+j) the sum
+      // bc - ad + a^2/2 - b^2/2 - c^2/2 + d^2/2 equals ((a-d) - (b-c)) ((a-d) + (b-c)) / 2,
+      // which never forms the O(phi^2) terms that cancel down to O((grad phi)^2)
+      const T dxy = p - pxy, exy = pxp - pyp, dxz = p - pxz, exz = pxp - pzp, dyz = p - pyz, eyz = pyp - pzp;
+      Sij[V + i] = coeff * t01 + h * (dxy - exy) * (dxy + exy);
+      Sij[2 * V + i] = coeff * t02 + h * (dxz - exz) * (dxz + exz);
+      Sij[4 * V + i] = coeff * t12 + h * (dyz - eyz) * (dyz + eyz);
+    }
   }
 }
 

@@ -79,6 +79,39 @@ def test_mixed_deposits_reproducible_and_close(gpu, oracle, N):
     assert rel(res[1][1], res[0][1]) < 1e-5
 
 
+@pytest.mark.parametrize("qscale", [1e-8, 1e-6, 1e-2])
+def test_mixed_deposit_scale_follows_momenta(gpu, oracle, qscale):
+    """The fixed-point scale comes from the particles' largest |q| and the fullest
+    cell: with the momenta of a high-redshift start (|q| ~ 1e-6) and with large
+    ones, every component of T0i and Tij (which carry q and q^2) stays at FP32
+    accuracy against the FP64 form, in rms and per cell."""
+    N = 32
+    rng = np.random.default_rng(17)
+    n = N ** 3
+    p = np.zeros(n, oracle.PART)
+    p["pos"] = rng.random((n, 3))
+    p["pos"][:500] = 0.5 + rng.random((500, 3)) * (0.5 / N)  # one crowded cell region
+    p["vel"] = rng.standard_normal((n, 3)) * qscale
+    p["ID"] = np.arange(n)
+    phi_h = rng.standard_normal((1, N, N, N)) * 1e-5
+    res = {}
+    for prec in (gpu.PREC_FP64, gpu.PREC_MIXED):
+        c = gpu.Context(N, prec)
+        pc = c.particles(n, 1.0 / n).upload(p)
+        phi = c.real(1).upload(phi_h)
+        T = c.real(6)
+        gpu.projection_Tij(pc, T, 0.02, phi)
+        B = c.real(3)
+        gpu.projection_T0i(pc, B, phi)
+        res[prec] = (T.download(), B.download())
+    for k in range(2):
+        got, ref = res[gpu.PREC_MIXED][k], res[gpu.PREC_FP64][k]
+        for comp in range(ref.shape[0]):
+            d, r = got[comp] - ref[comp], ref[comp]
+            assert np.sqrt((d ** 2).mean() / (r ** 2).mean()) < 1e-6, (k, comp)
+            assert np.abs(d).max() <= 1e-5 * np.abs(r).max(), (k, comp)
+
+
 def test_mixed_cycles_track_fp64(gpu, oracle):
     """A few cycles from the same device IC: mixed positions stay within 1e-4 of a cell."""
     N = 32
