@@ -17,7 +17,7 @@
 #include "gev_internal.cuh"
 
 int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass, double a, const gev_field *phi,
-               bool overwrite);
+               bool overwrite, gev_field *out2 = nullptr);
 
 namespace {
 
@@ -223,6 +223,19 @@ bool ok_field(gev_ctx *ctx, const gev_field *f, int ncomp) {
 }
 
 }  // namespace
+
+// projection_init + projection_T00 and projection_init + projection_Tij (coefficient
+// 1); the mixed form deposits both in one sweep over the particles
+int projection_replace_t00_tij(gev_ctx *ctx, gev_pcls *p, gev_field *T00, gev_field *Tij, double a,
+                               const gev_field *phi) {
+  if (ctx->prec == GEV_PREC_FP64) {
+    int rc = run_deposit<DEP_T00>(ctx, p, T00, a, phi, 1., true);
+    return rc ? rc : run_deposit<DEP_TIJ>(ctx, p, Tij, a, phi, 1., true);
+  }
+  const double dx = 1.0 / ctx->N;
+  const double mass = 1. / (dx * dx * dx) * p->mass / a;  // as run_deposit: coeff / dx^3 * m / a
+  return deposit_fx(ctx, p, T00, 4, mass, a, phi, true, Tij);
+}
 
 // projection_init followed by the deposit, in one pass for the mixed form
 int projection_replace(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double a, const gev_field *phi) {

@@ -99,8 +99,9 @@ struct gev_pcls {
   size_t scan_tmp_elems = 0;
   // false after a mixed-form relink that left each cell's run in atomic order
   bool id_order = true;
-  // mixed-form deposit scale: [0] max |q|^2 (FP32 bits), [1] max particles in a cell,
-  // [2] the power of two of the last deposit's fixed-point scale
+  // mixed-form deposit scales (16 words): [0] max |q|^2 and [4] max |phi| (FP32 bits),
+  // [1] max particles in a cell, [2], [3] the accumulator scale powers of the last
+  // deposit's groups, [5..8] their prefactor and weight-factor powers
   uint32_t *bounds = nullptr;
 };
 
@@ -305,3 +306,5 @@ int ctx_ensure_red(gev_ctx *ctx, size_t elems);
 // the deposit of kind 0 T00, 1 T0i, 2 Tij, 3 mass (coefficient 1) replacing the
 // target's contents: projection_init + projection_*_project + _comm in one call
 int projection_replace(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double a, const gev_field *phi);
+int projection_replace_t00_tij(gev_ctx *ctx, gev_pcls *p, gev_field *T00, gev_field *Tij, double a,
+                               const gev_field *phi);

@@ -867,7 +867,7 @@ int gev_pcls_create(gev_ctx *ctx, long capacity, double mass, gev_pcls **out) {
     p->scan_tmp_elems = (size_t)((C + SCAN_TILE - 1) / SCAN_TILE) + 1;
     if (cudaMalloc(&p->count, C * 4) != cudaSuccess || cudaMalloc(&p->start, (C + 1) * 4) != cudaSuccess ||
         cudaMalloc(&p->rank, cap * 4) != cudaSuccess || cudaMalloc(&p->perm, cap * 4) != cudaSuccess ||
-        cudaMalloc(&p->big, (C + 1) * 4) != cudaSuccess || cudaMalloc(&p->bounds, 4 * 4) != cudaSuccess ||
+        cudaMalloc(&p->big, (C + 1) * 4) != cudaSuccess || cudaMalloc(&p->bounds, 16 * 4) != cudaSuccess ||
         cudaMalloc(&p->scan_tmp, p->scan_tmp_elems * 4) != cudaSuccess)
       rc = gev_fail(ctx, GEV_ENOMEM, "pcls_create: device allocation failed");
     else

@@ -179,9 +179,9 @@ int gev_sim_step(gev_sim *s) {
 
   // stress-energy (main.cpp:378-450)
   // (projection_init + projection_*: the target is replaced, not zeroed and re-read)
-  RC(projection_replace(ctx, s->pcls, s->source, 0, a, s->phi));
+  // (T00 and Tij read the same particles and phi: one sweep deposits both)
+  RC(projection_replace_t00_tij(ctx, s->pcls, s->source, s->Sij, a, s->phi));
   if (st.vector_elliptic) RC(projection_replace(ctx, s->pcls, s->Bi, 1, 1., s->phi));
-  RC(projection_replace(ctx, s->pcls, s->Sij, 2, a, s->phi));
   RC(sum_async(s, s->source, s->dev_words + 0));  // T00hom, main.cpp:459-463
 
   // phi (main.cpp:470-491)
