@@ -153,7 +153,8 @@ const char *gev_strerror(int s) {
 int gev_ctx_create(int device, int N, int precision, gev_ctx **out) {
   if (!out) return GEV_EINVAL;
   *out = nullptr;
-  if (N < 8 || N > 2048 || N % 2 != 0 || (precision != GEV_PREC_FP64 && precision != GEV_PREC_MIXED))
+  // N^3 < 2^32: cell keys and field indices are 32-bit
+  if (N < 8 || N > 1536 || N % 2 != 0 || (precision != GEV_PREC_FP64 && precision != GEV_PREC_MIXED))
     return GEV_EINVAL;
   FftPlan pN, pH;
   if (fft_build_plan(N, &pN) != GEV_OK || fft_build_plan(N / 2, &pH) != GEV_OK) return GEV_EINVAL;

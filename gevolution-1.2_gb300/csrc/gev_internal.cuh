@@ -252,16 +252,16 @@ __device__ __forceinline__ void pos_split(double x, int N, int lg, int &c, float
   }
 }
 
-// periodic wrap into [0, 1) deciding on the bit pattern (integer compares)
+// periodic wrap into [0, 1), deciding on the bit pattern (integer compares) and
+// with one FP64 add whose addend is selected (+1 below 0, -1 at 1 and above, 0
+// otherwise: x + 0 is x), so that no predicated FP64 instructions are issued; a
+// tiny negative x whose x + 1 rounds to 1 gives 0, as moveParticles' second test does
 __device__ __forceinline__ double wrap01_bits(double x) {
   const long long b = __double_as_longlong(x);
-  if (b < 0) {  // negative (or -0)
-    x += 1.0;
-    if (__double_as_longlong(x) >= 0x3FF0000000000000ll) x -= 1.0;
-  } else if (b >= 0x3FF0000000000000ll) {  // >= 1
-    x -= 1.0;
-  }
-  return x;
+  const bool neg = b < 0, big = b >= 0x3FF0000000000000ll;  // sign bit set (incl. -0) / x >= 1
+  double y = x + (neg ? 1.0 : (big ? -1.0 : 0.0));
+  if (neg && __double_as_longlong(y) >= 0x3FF0000000000000ll) y = 0.0;
+  return y;
 }
 
 // v * 2^-k rounded once to the nearest FP32 (ties to even), with integer
@@ -279,6 +279,58 @@ __device__ __forceinline__ float float_of_fixed(long long v, int k) {
   unsigned bits = sign | ((unsigned)(63 - lz - k + 127) << 23) | (mant & 0x7fffffu);
   if (rest > half || (rest == half && (mant & 1u))) bits += 1u;  // a carry moves into the exponent
   return __uint_as_float(bits);
+}
+
+// n / d for every 32-bit n with one multiply-high (division by an invariant
+// integer, round-up method): m = floor(2^32 (2^l - d) / d) + 1, l = ceil(log2 d)
+struct Div32 {
+  unsigned d = 1, m = 1;
+  int s1 = 0, s2 = 0;
+};
+inline Div32 make_div32(unsigned d) {
+  Div32 v;
+  v.d = d;
+  int l = 0;
+  while ((1ull << l) < d) ++l;
+  v.m = (unsigned)((((1ull << 32) * ((1ull << l) - d)) / d) + 1);
+  v.s1 = l < 1 ? l : 1;
+  v.s2 = l - 1 > 0 ? l - 1 : 0;
+  return v;
+}
+__device__ __forceinline__ unsigned div32(unsigned n, const Div32 &v) {
+  const unsigned t = __umulhi(v.m, n);
+  return (t + ((n - t) >> v.s1)) >> v.s2;
+}
+
+// the periodic neighbours of cell i = x + N (y + N z) as index offsets modulo 2^32
+// (N^3 < 2^32): f[i + xp] is f(x + 1, y, z) and so on
+struct Nb3 {
+  unsigned i, xm, xp, ym, yp, zm, zp;
+};
+__device__ __forceinline__ Nb3 nb3(unsigned i, int x, int y, int z, int N) {
+  const unsigned n1 = (unsigned)N, n2 = n1 * n1, n3 = n2 * n1;
+  Nb3 b;
+  b.i = i;
+  b.xm = x == 0 ? n1 - 1u : 0u - 1u;
+  b.xp = x == N - 1 ? 1u - n1 : 1u;
+  b.ym = y == 0 ? n2 - n1 : 0u - n1;
+  b.yp = y == N - 1 ? n1 - n2 : n1;
+  b.zm = z == 0 ? n3 - n2 : 0u - n2;
+  b.zp = z == N - 1 ? n2 - n3 : n2;
+  return b;
+}
+// x, y, z of cell i: shifts for a power-of-two N, else two invariant divisions
+__device__ __forceinline__ void cell_xyz(unsigned i, int N, int lg, const Div32 &dN, int &x, int &y, int &z) {
+  if (lg >= 0) {
+    x = (int)(i & (unsigned)(N - 1));
+    y = (int)((i >> lg) & (unsigned)(N - 1));
+    z = (int)(i >> (2 * lg));
+  } else {
+    const unsigned r = div32(i, dN), q = div32(r, dN);
+    x = (int)(i - r * (unsigned)N);
+    y = (int)(r - q * (unsigned)N);
+    z = (int)q;
+  }
 }
 
 inline int grid_for(const gev_ctx *ctx, size_t work, int threads, int per_sm = 8) {

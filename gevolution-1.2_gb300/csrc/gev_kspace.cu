@@ -17,24 +17,39 @@ struct KIdx {
   size_t id;
 };
 
+// grid sizes and their invariant divisors (N^2 (N/2+1) < 2^32)
+struct KDim {
+  int N, NH;
+  Div32 dNH, dN;
+};
+inline KDim make_kdim(int N) {
+  KDim d;
+  d.N = N;
+  d.NH = N / 2 + 1;
+  d.dNH = make_div32((unsigned)d.NH);
+  d.dN = make_div32((unsigned)N);
+  return d;
+}
+
 template <typename T>
-__device__ __forceinline__ bool kidx(size_t id, int N, int NH, KIdx<T> &k) {
+__device__ __forceinline__ bool kidx(size_t id, const KDim &kd, KIdx<T> &k) {
   k.id = id;
-  k.kx = (int)(id % NH);
-  const size_t r = id / NH;
-  k.ky = (int)(r % N);
-  k.kz = (int)(r / N);
+  const unsigned i = (unsigned)id, r = div32(i, kd.dNH), q = div32(r, kd.dN);
+  k.kx = (int)(i - r * (unsigned)kd.NH);
+  k.ky = (int)(r - q * (unsigned)kd.N);
+  k.kz = (int)q;
   return true;
 }
 
 // solveModifiedPoissonFT, gevolution.hpp:501-535; coeff already divided by -N^3
 template <typename T>
 __global__ void k_poisson(const typename CT<T>::C *src, typename CT<T>::C *pot, const T *__restrict__ gk2, T coeff,
-                          T modif, int N, int NH, size_t n) {
+                          T modif, KDim kd, size_t n) {
+  const int N = kd.N, NH = kd.NH;
   typedef typename CT<T>::C C;
   for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < n; id += (size_t)gridDim.x * blockDim.x) {
     KIdx<T> k;
-    kidx<T>(id, N, NH, k);
+    kidx<T>(id, kd, k);
     const C s = src[id];
     C out;
     if (id == 0) {
@@ -50,8 +65,9 @@ __global__ void k_poisson(const typename CT<T>::C *src, typename CT<T>::C *pot, 
 // projectFTscalar, gevolution.hpp:211-265
 template <typename T>
 __global__ void k_project_scalar(const typename CT<T>::C *__restrict__ S, typename CT<T>::C *chi,
-                                 const T *__restrict__ gk2, const typename CT<T>::C *__restrict__ ks, int add, int N,
-                                 int NH, size_t n) {
+                                 const T *__restrict__ gk2, const typename CT<T>::C *__restrict__ ks, int add, KDim kd,
+                                 size_t n) {
+  const int N = kd.N, NH = kd.NH;
   typedef typename CT<T>::C C;
   for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < n; id += (size_t)gridDim.x * blockDim.x) {
     if (id == 0) {
@@ -59,7 +75,7 @@ __global__ void k_project_scalar(const typename CT<T>::C *__restrict__ S, typena
       continue;
     }
     KIdx<T> k;
-    kidx<T>(id, N, NH, k);
+    kidx<T>(id, kd, k);
     const T g0 = gk2[k.kx], g1 = gk2[k.ky], g2 = gk2[k.kz];
     const C k0 = ks[k.kx], k1 = ks[k.ky], k2 = ks[k.kz];
     const C S00 = S[id], S01 = S[n + id], S02 = S[2 * n + id], S11 = S[3 * n + id], S12 = S[4 * n + id],
@@ -79,8 +95,9 @@ __global__ void k_project_scalar(const typename CT<T>::C *__restrict__ S, typena
 // evolveFTvector, gevolution.hpp:284-330 (B += ...)
 template <typename T>
 __global__ void k_evolve_vector(const typename CT<T>::C *__restrict__ S, typename CT<T>::C *B,
-                                const T *__restrict__ gk2, const typename CT<T>::C *__restrict__ ks, T a2dtau, int N,
-                                int NH, size_t n) {
+                                const T *__restrict__ gk2, const typename CT<T>::C *__restrict__ ks, T a2dtau, KDim kd,
+                                size_t n) {
+  const int N = kd.N, NH = kd.NH;
   typedef typename CT<T>::C C;
   for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < n; id += (size_t)gridDim.x * blockDim.x) {
     if (id == 0) {
@@ -88,7 +105,7 @@ __global__ void k_evolve_vector(const typename CT<T>::C *__restrict__ S, typenam
       continue;
     }
     KIdx<T> k;
-    kidx<T>(id, N, NH, k);
+    kidx<T>(id, kd, k);
     const T g0 = gk2[k.kx], g1 = gk2[k.ky], g2 = gk2[k.kz];
     const C k0 = ks[k.kx], k1 = ks[k.ky], k2 = ks[k.kz];
     const C S00 = S[id], S01 = S[n + id], S02 = S[2 * n + id], S11 = S[3 * n + id], S12 = S[4 * n + id],
@@ -112,7 +129,8 @@ __global__ void k_evolve_vector(const typename CT<T>::C *__restrict__ S, typenam
 // projectFTvector, gevolution.hpp:350-392 (S may equal B)
 template <typename T>
 __global__ void k_project_vector(const typename CT<T>::C *S, typename CT<T>::C *B, const T *__restrict__ gk2,
-                                 const typename CT<T>::C *__restrict__ ks, T coeff, T modif, int N, int NH, size_t n) {
+                                 const typename CT<T>::C *__restrict__ ks, T coeff, T modif, KDim kd, size_t n) {
+  const int N = kd.N, NH = kd.NH;
   typedef typename CT<T>::C C;
   for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < n; id += (size_t)gridDim.x * blockDim.x) {
     if (id == 0) {
@@ -120,7 +138,7 @@ __global__ void k_project_vector(const typename CT<T>::C *S, typename CT<T>::C *
       continue;
     }
     KIdx<T> k;
-    kidx<T>(id, N, NH, k);
+    kidx<T>(id, kd, k);
     const T g0 = gk2[k.kx], g1 = gk2[k.ky], g2 = gk2[k.kz];
     const C k0 = ks[k.kx], k1 = ks[k.ky], k2 = ks[k.kz];
     const C S0 = S[id], S1 = S[n + id], S2 = S[2 * n + id];
@@ -136,7 +154,8 @@ __global__ void k_project_vector(const typename CT<T>::C *S, typename CT<T>::C *
 // projectFTtensor, gevolution.hpp:411-482 (S may equal h)
 template <typename T>
 __global__ void k_project_tensor(const typename CT<T>::C *S, typename CT<T>::C *h, const T *__restrict__ gk2,
-                                 const typename CT<T>::C *__restrict__ ks, int N, int NH, size_t n) {
+                                 const typename CT<T>::C *__restrict__ ks, KDim kd, size_t n) {
+  const int N = kd.N, NH = kd.NH;
   typedef typename CT<T>::C C;
   for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < n; id += (size_t)gridDim.x * blockDim.x) {
     if (id == 0) {
@@ -144,7 +163,7 @@ __global__ void k_project_tensor(const typename CT<T>::C *S, typename CT<T>::C *
       continue;
     }
     KIdx<T> k;
-    kidx<T>(id, N, NH, k);
+    kidx<T>(id, kd, k);
     const T g0 = gk2[k.kx], g1 = gk2[k.ky], g2 = gk2[k.kz];
     const C k0 = ks[k.kx], k1 = ks[k.ky], k2 = ks[k.kz];
     const C c0 = cconj(k0), c1 = cconj(k1), c2 = cconj(k2);
@@ -203,20 +222,20 @@ int launch_kspace(gev_ctx *ctx, int op, const void *in, void *out, double p1, do
   const C *ks = (const C *)ctx->d_kshift;
   switch (op) {
     case 0:
-      k_poisson<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, (T)p1, (T)p2, N, NH, n);
+      k_poisson<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, (T)p1, (T)p2, make_kdim(N), n);
       break;
     case 1:
-      k_project_scalar<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, ks, add, N, NH, n);
+      k_project_scalar<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, ks, add, make_kdim(N), n);
       break;
     case 2:
-      k_evolve_vector<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, ks, (T)p1, N, NH, n);
+      k_evolve_vector<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, ks, (T)p1, make_kdim(N), n);
       break;
     case 3:
-      k_project_vector<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, ks, (T)p1, (T)p2, N, NH,
-                                                               n);
+      k_project_vector<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, ks, (T)p1, (T)p2,
+                                                               make_kdim(N), n);
       break;
     default:
-      k_project_tensor<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, ks, N, NH, n);
+      k_project_tensor<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, ks, make_kdim(N), n);
   }
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;

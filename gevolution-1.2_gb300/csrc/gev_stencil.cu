@@ -10,17 +10,17 @@ namespace {
 // ORIGINALMETRIC.  T and S may be the same array (each cell reads its own
 // components before writing them).
 template <typename T>
-__global__ void k_source_tensor(const T *__restrict__ phi, const T *Tij, T *Sij, T coeff, int N) {
-  const size_t V = (size_t)N * N * N;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((size_t)N * N));
-    const int xp = wrapi(x + 1, N), xm = wrapi(x - 1, N), yp = wrapi(y + 1, N), ym = wrapi(y - 1, N);
-    const int zp = wrapi(z + 1, N), zm = wrapi(z - 1, N);
+__global__ void k_source_tensor(const T *__restrict__ phi, const T *Tij, T *Sij, T coeff, int N, int lg, Div32 dN) {
+  const unsigned V = (unsigned)N * N * N;  // < 2^32
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x) {
+    int x, y, z;
+    cell_xyz(i, N, lg, dN, x, y, z);
+    const Nb3 b = nb3(i, x, y, z, N);
     const T p = phi[i];
-    const T pxp = phi[sidx(xp, y, z, N)], pxm = phi[sidx(xm, y, z, N)];
-    const T pyp = phi[sidx(x, yp, z, N)], pym = phi[sidx(x, ym, z, N)];
-    const T pzp = phi[sidx(x, y, zp, N)], pzm = phi[sidx(x, y, zm, N)];
-    const T pxy = phi[sidx(xp, yp, z, N)], pxz = phi[sidx(xp, y, zp, N)], pyz = phi[sidx(x, yp, zp, N)];
+    const T pxp = phi[i + b.xp], pxm = phi[i + b.xm];
+    const T pyp = phi[i + b.yp], pym = phi[i + b.ym];
+    const T pzp = phi[i + b.zp], pzm = phi[i + b.zm];
+    const T pxy = phi[i + b.xp + b.yp], pxz = phi[i + b.xp + b.zp], pyz = phi[i + b.yp + b.zp];
     const T h = (T)0.5;
     const T t00 = Tij[i], t01 = Tij[V + i], t02 = Tij[2 * V + i], t11 = Tij[3 * V + i], t12 = Tij[4 * V + i],
             t22 = Tij[5 * V + i];
@@ -46,14 +46,16 @@ __global__ void k_source_tensor(const T *__restrict__ phi, const T *Tij, T *Sij,
 // prepareFTsource (scalar), gevolution.hpp:169-192; result may equal source
 template <typename T>
 __global__ void k_source_scalar(const T *__restrict__ phi, const T *__restrict__ chi, const T *source, T bgmodel,
-                                T *result, T coeff, T coeff2, T coeff3, int N) {
-  const size_t V = (size_t)N * N * N;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < V; i += (size_t)gridDim.x * blockDim.x) {
-    const int x = (int)(i % N), y = (int)((i / N) % N), z = (int)(i / ((size_t)N * N));
+                                T *result, T coeff, T coeff2, T coeff3, int N, int lg, Div32 dN) {
+  const unsigned V = (unsigned)N * N * N;  // < 2^32
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x) {
+    int x, y, z;
+    cell_xyz(i, N, lg, dN, x, y, z);
+    const Nb3 b = nb3(i, x, y, z, N);
     const T p = phi[i];
-    const T dx = phi[sidx(wrapi(x - 1, N), y, z, N)] - phi[sidx(wrapi(x + 1, N), y, z, N)];
-    const T dy = phi[sidx(x, wrapi(y - 1, N), z, N)] - phi[sidx(x, wrapi(y + 1, N), z, N)];
-    const T dz = phi[sidx(x, y, wrapi(z - 1, N), N)] - phi[sidx(x, y, wrapi(z + 1, N), N)];
+    const T dx = phi[i + b.xm] - phi[i + b.xp];
+    const T dy = phi[i + b.ym] - phi[i + b.yp];
+    const T dz = phi[i + b.zm] - phi[i + b.zp];
     T r = coeff2 * (source[i] - bgmodel);
     r *= (T)1 - (T)2 * p;
     r += (T)0.125 * (dx * dx + dy * dy + dz * dz);
@@ -105,10 +107,12 @@ int gev_prepare_source_tensor(gev_ctx *ctx, const gev_field *phi, const gev_fiel
   const int blocks = grid_for(ctx, V, 256, 16);
   if (ctx->prec == GEV_PREC_FP64)
     k_source_tensor<double><<<blocks, 256, 0, ctx->stream>>>((const double *)phi->d, (const double *)Tij->d,
-                                                             (double *)Sij->d, coeff, ctx->N);
+                                                             (double *)Sij->d, coeff, ctx->N, lg_pow2(ctx->N),
+                                                             make_div32(ctx->N));
   else
     k_source_tensor<float><<<blocks, 256, 0, ctx->stream>>>((const float *)phi->d, (const float *)Tij->d,
-                                                            (float *)Sij->d, (float)coeff, ctx->N);
+                                                            (float *)Sij->d, (float)coeff, ctx->N, lg_pow2(ctx->N),
+                                                            make_div32(ctx->N));
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
@@ -124,11 +128,12 @@ int gev_prepare_source_scalar(gev_ctx *ctx, const gev_field *phi, const gev_fiel
   if (ctx->prec == GEV_PREC_FP64)
     k_source_scalar<double><<<blocks, 256, 0, ctx->stream>>>((const double *)phi->d, (const double *)chi->d,
                                                              (const double *)source->d, bgmodel, (double *)result->d,
-                                                             coeff, coeff2, coeff3, ctx->N);
+                                                             coeff, coeff2, coeff3, ctx->N, lg_pow2(ctx->N),
+                                                             make_div32(ctx->N));
   else
     k_source_scalar<float><<<blocks, 256, 0, ctx->stream>>>(
         (const float *)phi->d, (const float *)chi->d, (const float *)source->d, (float)bgmodel, (float *)result->d,
-        (float)coeff, (float)coeff2, (float)coeff3, ctx->N);
+        (float)coeff, (float)coeff2, (float)coeff3, ctx->N, lg_pow2(ctx->N), make_div32(ctx->N));
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
