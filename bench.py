@@ -193,8 +193,9 @@ def run_ours(args, rank, world, local):
     if not args.no_pk_check and prec == gpu.PREC_MIXED and world == 1:
         pk = spectra_of(gpu, ctx, sim)
 
-    # dominant-kernel roofline: one FFT column pass
-    roof = dominant_kernel_roofline(gpu, ctx, sim, stream, N, args.prec)
+    # roofline of the dominant kernel (the T00 + Tij deposit) and of the FFT column pass
+    roof = deposit_roofline(gpu, ctx, sim, stream, N, args.prec)
+    roof_fft = dominant_kernel_roofline(gpu, ctx, sim, stream, N, args.prec)
 
     # e2e: particle state from pinned host memory in, cycle, particle state out
     e2e = None
@@ -205,7 +206,7 @@ def run_ours(args, rank, world, local):
         del sim, ctx
         fp64 = fp64_form_check(args, gpu, N, box, local, pk, torch)
     return dict(value=value, ms=ms_max / args.steps, launches=launches, clocks=clk, state=st, roofline=roof,
-                e2e=e2e, box=box, fp64=fp64)
+                roofline_fft=roof_fft, e2e=e2e, box=box, fp64=fp64)
 
 
 PK_FIELDS = (("phi", 1), ("chi", 1), ("Bi", 3), ("source", 1))
@@ -264,9 +265,44 @@ def fp64_form_check(args, gpu, N, box, local, pk_mixed, torch):
 COLS_TRAFFIC = {(512, "mixed"): 1.0675e9}
 
 
+# DRAM traffic per launch of the T00 + Tij deposit from an ncu capture of the same
+# kernel on the 256^3 cycle (opbench --grid 256 --only step), scaled by 8 to 512^3:
+# particles and fields both grow as N^3.  (843.0 MB read + 517.4 MB written) x 8
+DEPOSIT_TRAFFIC = {(512, "mixed"): 10.883e9}
+
+
+def deposit_roofline(gpu, ctx, sim, stream, N, prec):
+    """The largest kernel of the cycle in the ncu launch list: the deposit of T00 and
+    Tij in one sweep (projection_init + projection_T00 + projection_Tij).  Its
+    algorithmic bytes per launch: each particle's cell, in-cell offset and momentum
+    read once (4 + 3r + 3r bytes), phi read once and the 7 target components
+    written once per cell (8 r bytes), r the real size of the form."""
+    import torch
+    r = 8 if prec == "fp64" else 4
+    p, src, Sij, phi = sim.particles(), sim.field("source"), sim.field("Sij"), sim.field("phi")
+    a = sim.state()["a"]
+    reps = 4
+    gpu.projection_T00_Tij(p, src, Sij, a, phi)
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        gpu.projection_T00_Tij(p, src, Sij, a, phi)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    n = C = N ** 3
+    alg = n * (4 + 6 * r) + C * 8 * r
+    peak, kind = hbm_peak()
+    achieved = alg / (ms / 1e3) / 1e9
+    return {"kernel": "k_dep_fx<T00+Tij> (the T00 and Tij deposits in one sweep; with its bounds and face passes)",
+            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": DEPOSIT_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
+
+
 def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
-    """The FFT column pass (k_fft_cols_reg, the y / z passes of every transform) is
-    the largest kernel family of the cycle in the ncu launch list.  One launch transforms one
+    """The FFT column pass (k_fft_cols_reg, the y / z passes of every transform; 24
+    launches a cycle, the largest kernel family by count).  One launch transforms one
     spectrum component along y or z in place: its algorithmic bytes are one read
     and one write of the component, 2 * N^2 (N/2+1) * sizeof(complex)."""
     import torch
@@ -386,7 +422,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.prec == "fp64" else "f32+f64pos+i64dep",
             "data": "synthetic (device-generated BBKS Zel'dovich IC)", "config": config,
-            "roofline": res["roofline"], "cpu_baseline": cpu, "e2e": res["e2e"], "gpu_launches": res["launches"],
+            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "cpu_baseline": cpu, "e2e": res["e2e"], "gpu_launches": res["launches"],
             "clocks": res["clocks"], "bytes_per_cycle_alg": cycle_bytes(N, args.prec),
             "final_a": res["state"]["a"]}
     if res.get("fp64"):

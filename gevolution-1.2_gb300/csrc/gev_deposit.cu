@@ -268,6 +268,12 @@ int gev_projection_Tij(gev_ctx *ctx, gev_pcls *p, gev_field *Tij, double a, cons
     return gev_fail(ctx, GEV_EINVAL, "projection_Tij: 6-component target, optional 1-component phi, a > 0");
   return run_deposit<DEP_TIJ>(ctx, p, Tij, a, phi, coeff);
 }
+int gev_projection_T00_Tij(gev_ctx *ctx, gev_pcls *p, gev_field *T00, gev_field *Tij, double a, const gev_field *phi) {
+  if (!ctx || !p || p->ctx != ctx || !ok_field(ctx, T00, 1) || !ok_field(ctx, Tij, 6) ||
+      (phi && !ok_field(ctx, phi, 1)) || a <= 0.)
+    return gev_fail(ctx, GEV_EINVAL, "projection_T00_Tij: 1- and 6-component targets, optional phi, a > 0");
+  return projection_replace_t00_tij(ctx, p, T00, Tij, a, phi);
+}
 int gev_projection_mass(gev_ctx *ctx, gev_pcls *p, gev_field *rho) {
   if (!ctx || !p || p->ctx != ctx || !ok_field(ctx, rho, 1))
     return gev_fail(ctx, GEV_EINVAL, "projection_mass: 1-component target");

@@ -970,6 +970,29 @@ int gev_update_q(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_fie
   return GEV_OK;
 }
 
+int gev_update_q_pos(gev_ctx *ctx, gev_pcls *p, double dtau_kick, double a_kick, int nfield_kick, double dtau_drift,
+                     double a_drift, int nfield_drift, const gev_field *phi, const gev_field *chi, const gev_field *Bi,
+                     double *maxvel) {
+  if (!ctx || !p || p->ctx != ctx || !field_ok(ctx, phi, 1) || !field_ok(ctx, chi, 1) || !field_ok(ctx, Bi, 3) ||
+      a_kick <= 0. || a_drift <= 0. || nfield_kick < 1 || nfield_kick > 3 || nfield_drift < 0 || nfield_drift > 3)
+    return gev_fail(ctx, GEV_EINVAL, "update_q_pos: phi, chi (1 comp) and Bi (3 comps), a > 0, nfield 1..3 / 0..3");
+  int rc = ctx_ensure_red(ctx, 2);
+  if (rc) return rc;
+  unsigned long long *mb = (unsigned long long *)ctx->d_red;
+  rc = pcls_kick_drift_async(ctx, p, dtau_kick, a_kick, nfield_kick, dtau_drift, a_drift, nfield_drift, phi, chi, Bi,
+                             mb);
+  if (rc) return rc;
+  if (maxvel) {
+    unsigned long long bits = 0;
+    GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(&bits, mb, sizeof(bits), cudaMemcpyDeviceToHost, ctx->stream));
+    GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    double m;
+    memcpy(&m, &bits, sizeof(m));
+    *maxvel = sqrt(m);
+  }
+  return GEV_OK;
+}
+
 int gev_update_pos(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
                    const gev_field *Bi, int nfield, double a, double a2N) {
   if (!ctx || !p || p->ctx != ctx || (kind != GEV_GR && kind != GEV_NEWTON) || a <= 0. || nfield < 0 ||

@@ -69,6 +69,8 @@ _SIGS = {
     "gev_project_tensor": [_vp, _vp, _vp],
     "gev_update_q": [_vp, _vp, _i, _d, _vp, _vp, _vp, _i, _d, _d, ctypes.POINTER(_d)],
     "gev_update_pos": [_vp, _vp, _i, _d, _vp, _vp, _vp, _i, _d, _d],
+    "gev_update_q_pos": [_vp, _vp, _d, _d, _i, _d, _d, _i, _vp, _vp, _vp, _vp],
+    "gev_projection_T00_Tij": [_vp, _vp, _vp, _vp, _d, _vp],
     "gev_field_sum": [_vp, _vp, _i, ctypes.POINTER(_d)],
     "gev_cross_spectrum": [_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i, _i, _i],
 }
@@ -327,6 +329,21 @@ def project_vector(SiFT, BiFT, coeff=1.0, modif=0.0):
 
 def project_tensor(SijFT, hijFT):
     _check(lib().gev_project_tensor(SijFT.ctx.handle, SijFT.handle, hijFT.handle), SijFT.ctx, "gev_project_tensor")
+
+
+def projection_T00_Tij(pcls, T00, Tij, a, phi=None):
+    """projection_init + projection_T00 and projection_init + projection_Tij in one sweep."""
+    _check(lib().gev_projection_T00_Tij(pcls.ctx.handle, pcls.handle, T00.handle, Tij.handle, _d(a),
+                                        phi.handle if phi is not None else None), pcls.ctx, "gev_projection_T00_Tij")
+
+
+def update_q_pos(pcls, dtau_kick, a_kick, nfield_kick, dtau_drift, a_drift, nfield_drift, phi, chi, Bi, wait=True):
+    """updateVel(update_q) then moveParticles(update_pos) in one pass (GR); returns maxvel."""
+    out = _d()
+    _check(lib().gev_update_q_pos(pcls.ctx.handle, pcls.handle, _d(dtau_kick), _d(a_kick), nfield_kick,
+                                  _d(dtau_drift), _d(a_drift), nfield_drift, phi.handle, chi.handle, Bi.handle,
+                                  ctypes.byref(out) if wait else None), pcls.ctx, "gev_update_q_pos")
+    return out.value if wait else None
 
 
 def update_q(pcls, kind, dtau, phi, chi, Bi, nfield, a, a2N):

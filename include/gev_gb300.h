@@ -97,6 +97,10 @@ int gev_projection_T0i(gev_ctx *ctx, gev_pcls *p, gev_field *T0i, const gev_fiel
 int gev_projection_Tij(gev_ctx *ctx, gev_pcls *p, gev_field *Tij, double a, const gev_field *phi, double coeff);
 /* scalarProjectionCIC_project + _comm (LATfield2; main.cpp:402, ic_basic.hpp:2180) */
 int gev_projection_mass(gev_ctx *ctx, gev_pcls *p, gev_field *rho);
+/* projection_init + projection_T00_project and projection_init + projection_Tij_project
+ * (+ _comm), coefficient 1, as main.cpp:378-450 calls them: both targets are replaced,
+ * in one sweep over the particles (the mixed form; the FP64 form runs the two deposits) */
+int gev_projection_T00_Tij(gev_ctx *ctx, gev_pcls *p, gev_field *T00, gev_field *Tij, double a, const gev_field *phi);
 
 /* ---- real-space sources ---- */
 /* prepareFTsource (tensor), gevolution.hpp:56-147; Sij may equal Tij */
@@ -134,6 +138,15 @@ int gev_update_q(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_fie
  * relink to the new cells is the on-device counting sort */
 int gev_update_pos(gev_ctx *ctx, gev_pcls *p, int kind, double dtau, const gev_field *phi, const gev_field *chi,
                    const gev_field *Bi, int nfield, double a, double a2N);
+/* updateVel(update_q) then moveParticles(update_pos) with the relink, as main.cpp:775-798
+ * runs them in GR (kick at a_kick, background half step on the host, drift at a_drift), in
+ * one pass over the particles; phi, chi and Bi are all required.  In the mixed form the
+ * relink leaves each cell's particles in atomic order, which changes no result (its
+ * deposits add integers); downloads restore the (cell, ID) order.  *maxvel as gev_update_q,
+ * or NULL to return without waiting. */
+int gev_update_q_pos(gev_ctx *ctx, gev_pcls *p, double dtau_kick, double a_kick, int nfield_kick, double dtau_drift,
+                     double a_drift, int nfield_drift, const gev_field *phi, const gev_field *chi, const gev_field *Bi,
+                     double *maxvel);
 
 /* ---- reductions ---- */
 /* sum of one component over all cells (T00hom, main.cpp:459-463); deterministic order */

@@ -127,3 +127,42 @@ def test_mixed_cycles_track_fp64(gpu, oracle):
     order_a, order_b = np.argsort(a["ID"]), np.argsort(b["ID"])
     d = (a["pos"][order_a] - b["pos"][order_b] + 0.5) % 1.0 - 0.5
     assert np.abs(d).max() * N < 1e-4
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_fused_entry_points_match_separate_calls(gpu, oracle, prec):
+    """gev_projection_T00_Tij equals projection_init + T00 and projection_init + Tij, and
+    gev_update_q_pos equals update_q followed by update_pos (downloaded in (cell, ID)
+    order), bit for bit in both forms."""
+    N = 16
+    rng = np.random.default_rng(23)
+    n = N ** 3
+    p = np.zeros(n, oracle.PART)
+    p["pos"] = rng.random((n, 3))
+    p["vel"] = rng.standard_normal((n, 3)) * 1e-4
+    p["ID"] = rng.permutation(n)
+    fields = [rng.standard_normal((c, N, N, N)) * 1e-5 for c in (1, 1, 3)]
+    out = []
+    for fused in (True, False):
+        c = gpu.Context(N, prec)
+        pc = c.particles(n, 1.0 / n).upload(p)
+        phi, chi, Bi = (c.real(f.shape[0]).upload(f) for f in fields)
+        T00, Tij = c.real(1), c.real(6)
+        T00.upload(np.full((1, N, N, N), 7.0))  # replaced, not accumulated into
+        Tij.upload(np.full((6, N, N, N), 7.0))
+        if fused:
+            gpu.projection_T00_Tij(pc, T00, Tij, 0.03, phi)
+            mv = gpu.update_q_pos(pc, 2e-3, 0.03, 3, 2e-3, 0.031, 3, phi, chi, Bi)
+        else:
+            T00.zero()
+            Tij.zero()
+            gpu.projection_T00(pc, T00, 0.03, phi)
+            gpu.projection_Tij(pc, Tij, 0.03, phi)
+            mv = gpu.update_q(pc, 0, 2e-3, phi, chi, Bi, 3, 0.03, 0.03 * 0.03 * N)
+            gpu.update_pos(pc, 0, 2e-3, phi, chi, Bi, 3, 0.031, 0.031 * 0.031 * N)
+        out.append((T00.download(), Tij.download(), mv, pc.download()))
+    a, b = out
+    assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+    assert a[2] == b[2]
+    assert np.array_equal(a[3]["ID"], b[3]["ID"])
+    assert np.array_equal(a[3]["pos"], b[3]["pos"]) and np.array_equal(a[3]["vel"], b[3]["vel"])
