@@ -28,12 +28,27 @@ void rk4bg(double &a, double fourpiG, const gev_cosmology &c, double dtau) {
   a += dtau * (k1a + 2. * k2a + 2. * k3a + k4a) / 6.;
 }
 
+// Fixed-order sum of a field component.  FP32 fields: 8 values (two 16-byte loads)
+// added in a fixed FP32 tree, then one bit-built FP32 -> FP64 conversion and one
+// FP64 add per 8 values (converting and adding every value in FP64 would issue two
+// FP64-pipe instructions per cell on GB300).
 template <typename T>
 __global__ void k_sum_to(const T *__restrict__ f, size_t n, double *partial) {
   __shared__ double sh[256];
   double s = 0.;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
-    s += (double)f[i];
+  if constexpr (sizeof(T) == 4) {
+    const size_t n8 = n / 8;
+    const float4 *f4 = reinterpret_cast<const float4 *>(f);
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n8; i += (size_t)gridDim.x * blockDim.x) {
+      const float4 a = f4[2 * i], b = f4[2 * i + 1];
+      s += f2d_bits(((a.x + a.y) + (a.z + a.w)) + ((b.x + b.y) + (b.z + b.w)));
+    }
+    if (blockIdx.x == 0)
+      for (size_t i = 8 * n8 + threadIdx.x; i < n; i += blockDim.x) s += f2d_bits((float)f[i]);
+  } else {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+      s += (double)f[i];
+  }
   sh[threadIdx.x] = s;
   __syncthreads();
   for (int w = 128; w > 0; w >>= 1) {
@@ -63,7 +78,7 @@ __global__ void k_sum_fin(const double *partial, int nb, double *out) {
 
 int sum_async(gev_sim *s, const gev_field *f, double *dst_dev) {
   gev_ctx *ctx = s->ctx;
-  const int nb = ctx->sms * 4;
+  const int nb = ctx->sms * 8;
   RC(ctx_ensure_red(ctx, (size_t)nb + 4));
   if (ctx->prec == GEV_PREC_FP64)
     k_sum_to<double><<<nb, 256, 0, ctx->stream>>>((const double *)f->d, f->comp_elems, ctx->d_red);

@@ -96,11 +96,15 @@ class Field {
   Lattice *lat = nullptr;
   gev_field *f = nullptr;
   int ncomp = 0;
+  bool sym = false;  // a symmetric rank-2 tensor (components 00 01 02 11 12 22)
   ~Field() {
     if (f) gev_field_destroy(f);
   }
   void initialize(Lattice &l, int nc = 1) { alloc(l, nc); }
-  void initialize(Lattice &l, int rows, int cols, int sym) { alloc(l, sym == symmetric ? rows * (rows + 1) / 2 : rows * cols); }
+  void initialize(Lattice &l, int rows, int cols, int symm) {
+    sym = symm == symmetric;
+    alloc(l, sym ? rows * (rows + 1) / 2 : rows * cols);
+  }
   Lattice &lattice() { return *lat; }
   int components() const { return ncomp; }
   void updateHalo() {}  // periodic indexing inside every kernel
@@ -247,6 +251,26 @@ void projection_Tij_project(Particles<part, part_info, part_dataType> *pcls, Fie
   check(gev_projection_Tij(Tij->lat->ctx, pcls->p, Tij->f, a, phi ? phi->f : nullptr, coeff), Tij->lat->ctx,
         "projection_Tij_project");
 }
+#ifndef KTYPE_GRID
+#define KTYPE_GRID 0
+#define KTYPE_LINEAR 1
+#endif
+// extractCrossSpectrum (tools.hpp:53-212) on device spectra; the per-bin sums are exact
+// integer sums on the GPU, the averages and scatters formed as the reference forms them
+inline void extractCrossSpectrum(Field<Cplx> &fld1FT, Field<Cplx> &fld2FT, Real *kbin, Real *power, Real *kscatter,
+                                 Real *pscatter, int *occupation, const int numbins, const bool deconvolve = true,
+                                 const int ktype = KTYPE_LINEAR, const int comp1 = -1, const int comp2 = -1) {
+  check(gev_cross_spectrum(fld1FT.lat->ctx, fld1FT.f, fld2FT.f, kbin, power, kscatter, pscatter, occupation, numbins,
+                           deconvolve ? 1 : 0, ktype, fld1FT.sym ? 1 : 0, comp1, comp2),
+        fld1FT.lat->ctx, "extractCrossSpectrum");
+}
+// extractPowerSpectrum (tools.hpp:237-240)
+inline void extractPowerSpectrum(Field<Cplx> &fldFT, Real *kbin, Real *power, Real *kscatter, Real *pscatter,
+                                 int *occupation, const int numbins, const bool deconvolve = true,
+                                 const int ktype = KTYPE_LINEAR) {
+  extractCrossSpectrum(fldFT, fldFT, kbin, power, kscatter, pscatter, occupation, numbins, deconvolve, ktype);
+}
+
 template <typename part, typename part_info, typename part_dataType>
 void scalarProjectionCIC_project(Particles<part, part_info, part_dataType> *pcls, Field<Real> *rho) {
   check(gev_projection_mass(rho->lat->ctx, pcls->p, rho->f), rho->lat->ctx, "scalarProjectionCIC_project");

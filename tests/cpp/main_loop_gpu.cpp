@@ -134,10 +134,18 @@ int main(int argc, char **argv) {
       dtau = steplimit / Hconf(a, fourpiG, cosmo);
   }
   pcls_cdm.download(parts.data());
+  // the power spectrum of B (output.hpp's Pk output path calls extractPowerSpectrum)
+  const int numbins = 8;
+  std::vector<Real> kbin(numbins), power(numbins), kscatter(numbins), pscatter(numbins);
+  std::vector<int> occupation(numbins);
+  extractPowerSpectrum(BiFT, kbin.data(), power.data(), kscatter.data(), pscatter.data(), occupation.data(), numbins,
+                       true, KTYPE_LINEAR);
   FILE *out = std::fopen(argv[3], "wb");
   if (!out) return 2;
   std::fwrite(&a, 8, 1, out);
   std::fwrite(parts.data(), sizeof(gev_part), V, out);
+  std::fwrite(power.data(), sizeof(Real), numbins, out);
+  std::fwrite(occupation.data(), sizeof(int), numbins, out);
   std::fclose(out);
   std::printf("a = %.17g maxvel = %.6g\n", a, maxvel);
   return 0;

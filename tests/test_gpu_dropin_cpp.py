@@ -42,7 +42,10 @@ def test_cpp_main_loop_matches_oracle(gpu, oracle, tmp_path):
     subprocess.run([exe, str(state), str(steps), str(out)], check=True)
     raw = open(out, "rb").read()
     a = np.frombuffer(raw[:8], np.float64)[0]
-    got = np.frombuffer(raw[8:], oracle.PART)
+    npart = N ** 3
+    got = np.frombuffer(raw[8:8 + 56 * npart], oracle.PART)
+    pk = np.frombuffer(raw[8 + 56 * npart:8 + 56 * npart + 8 * 8], np.float64)
+    occ = np.frombuffer(raw[8 + 56 * npart + 8 * 8:], np.int32)
     for _ in range(steps):
         o.step()
     assert abs(a - o.s.a) <= 1e-15 * a
@@ -50,3 +53,9 @@ def test_cpp_main_loop_matches_oracle(gpu, oracle, tmp_path):
     assert (got["ID"] == ref["ID"]).all()
     assert np.abs(got["pos"] - ref["pos"]).max() * N < 1e-9
     assert np.abs(got["vel"] - ref["vel"]).max() <= 1e-10 * np.abs(ref["vel"]).max()
+    # extractPowerSpectrum of BiFT through the drop-in layer vs the oracle's restatement
+    _, opw, _, _, oocc = oracle.power_spectrum(o.spectrum("BiFT"), 8)
+    assert (occ == oocc).all()
+    m = occ > 0
+    # the fields agree to 1e-10 of their maximum, so the power per bin to ~1e-9 of the largest bin
+    assert np.max(np.abs(pk[m] - opw[m])) <= 1e-8 * np.abs(opw[m]).max()
