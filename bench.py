@@ -265,18 +265,22 @@ def fp64_form_check(args, gpu, N, box, local, pk_mixed, torch):
 COLS_TRAFFIC = {(512, "mixed"): 1.0675e9}
 
 
-# DRAM traffic per launch of the T00 + Tij deposit from an ncu capture of the same
-# kernel on the 256^3 cycle (opbench --grid 256 --only step), scaled by 8 to 512^3:
-# particles and fields both grow as N^3.  (843.0 MB read + 517.4 MB written) x 8
-DEPOSIT_TRAFFIC = {(512, "mixed"): 10.883e9}
+# DRAM traffic per call of the T00 + Tij deposit: its prefactor pass (k_fx_prep) and
+# its gather (k_dep_gather), from an ncu capture of the same kernels on the 256^3
+# cycle (opbench --grid 256 --only step), scaled by 8 to 512^3: particles and fields
+# both grow as N^3.  k_fx_prep 201.4 MB read + 544.4 MB written, k_dep_gather
+# 1254.6 MB read + 455.6 MB written; (2455.9 MB) x 8
+DEPOSIT_TRAFFIC = {(512, "mixed"): 19.647e9}
 
 
 def deposit_roofline(gpu, ctx, sim, stream, N, prec):
     """The largest kernel of the cycle in the ncu launch list: the deposit of T00 and
-    Tij in one sweep (projection_init + projection_T00 + projection_Tij).  Its
-    algorithmic bytes per launch: each particle's cell, in-cell offset and momentum
-    read once (4 + 3r + 3r bytes), phi read once and the 7 target components
-    written once per cell (8 r bytes), r the real size of the form."""
+    Tij in one call (projection_init + projection_T00 + projection_Tij), timed with
+    its scale pass and its prefactor pass.  Its algorithmic bytes per call: each
+    particle's cell, in-cell offset and momentum read once (4 + 3r + 3r bytes), phi
+    read once and the 7 target components written once per cell (8 r bytes), r the
+    real size of the form.  The prefactor scratch the gather writes and reads back
+    (36 B a particle) is not algorithmic and shows in the traffic."""
     import torch
     r = 8 if prec == "fp64" else 4
     p, src, Sij, phi = sim.particles(), sim.field("source"), sim.field("Sij"), sim.field("phi")
@@ -295,7 +299,8 @@ def deposit_roofline(gpu, ctx, sim, stream, N, prec):
     alg = n * (4 + 6 * r) + C * 8 * r
     peak, kind = hbm_peak()
     achieved = alg / (ms / 1e3) / 1e9
-    return {"kernel": "k_dep_fx<T00+Tij> (the T00 and Tij deposits in one sweep; with its bounds and face passes)",
+    return {"kernel": "k_fx_prep + k_dep_gather<T00+Tij> (the T00 and Tij deposits in one gather; timed with the "
+                      "scale pass)",
             "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": DEPOSIT_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
 

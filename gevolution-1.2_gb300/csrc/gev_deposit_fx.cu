@@ -1,32 +1,39 @@
-// gev_deposit_fx.cu -- the mixed-precision deposit: per-particle FP32
+// gev_deposit_fx.cu -- the mixed-precision deposits: per-particle FP32
 // contributions accumulated as 64-bit fixed-point integers.
 //
 // Same physics as projection_T00/T0i/Tij_project (gevolution.hpp:926-1297) and
-// scalarProjectionCIC_project.  Layout of the work:
+// scalarProjectionCIC_project.  Every contribution is the product of two integers:
+// the particle's prefactor rounded once to an int32 (scale 2^kq) and the corner's
+// weight factor rounded to 22 bits (scale 2^kg, one FFMA).  The scales come from the
+// data (largest |q|, |phi|, fullest cell) so that no sum can overflow, and integer
+// sums make every result independent of the order of the additions.
+//
+// T00 and Tij (the deposits of every step) are gathers: a prepass writes each
+// particle's integer prefactors, then one thread per grid node sums, in int64
+// registers, the contributions of the particles of its 8 neighbouring cells and
+// writes the node once.  No atomics, barriers or halo buffers; HBM traffic is the
+// particle positions and prefactors (read by 8 nodes each, mostly from L2), phi and
+// one write of the target.
+//
+// T0i and the mass deposit are scatters:
 //   * a block owns a column tile of TX x TY cells and a chunk of TZ cell
 //     layers, and sweeps the chunk in z;
 //   * for each source layer z it walks the particles of the layer's TY rows
 //     (contiguous runs of the cell-ordered store, one thread per particle) and
 //     adds each corner contribution into two shared-memory layers (field z and z + 1) with
-//     64-bit shared atomics.  A contribution is the product of two integers:
-//     the particle's prefactor rounded once to an int32 (scale 2^kq) and the
-//     corner's weight factor rounded to 22 bits (scale 2^kg, one FFMA) -- the
-//     scales come from the data (largest |q|, |phi|, fullest cell) so no sum
-//     can overflow, and integer adds make the result independent of order;
+//     64-bit shared atomics;
 //   * when layer z is complete it is flushed: cells that only this block can
 //     touch are added straight into the FP32 field; cells on a tile face
 //     (shared with a neighbouring block, including the periodic wrap) go into
 //     a compact int64 face buffer with global atomics, which a fix-up pass
 //     then adds to the field and clears.
-// HBM traffic is one read of the particles, one read-modify-write of the
-// target components, and the small face buffer -- no per-cell scratch.
 #include <cmath>
 
 #include "gev_internal.cuh"
 
 namespace {
 
-// kinds; FX_T00TIJ deposits T00 (slot 0) and Tij (slots 1-6) in one sweep
+// kinds; FX_T00TIJ deposits T00 and Tij in one gather
 enum { FX_T00 = 0, FX_T0I = 1, FX_TIJ = 2, FX_MASS = 3, FX_T00TIJ = 4 };
 constexpr int FX_NC[5] = {1, 3, 6, 1, 7};
 constexpr int TX = 32, TY = 16, TZ = 32, FX_THREADS = 256;
@@ -149,63 +156,9 @@ __device__ __forceinline__ void iadd(unsigned long long *a, int Q, int G) {
 }
 __device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
 
-// scale power of output component comp
-template <int KIND>
-__device__ __forceinline__ int comp_shift(int comp, int ks0, int ks1) {
-  return (KIND == FX_T00TIJ && comp > 0) ? ks1 : ks0;
-}
-
-// where component comp of the deposit goes: the first output holds nc0 components
-struct FxOut {
-  float *o0, *o1;
-  int nc0;
-};
-__device__ __forceinline__ float *comp_ptr(const FxOut &o, int comp, long C) {
-  return comp < o.nc0 ? o.o0 + comp * C : o.o1 + (comp - o.nc0) * C;
-}
-
-// per-particle contributions.  A: the accumulator layer of field z = zs, B: of
-// zs + 1, each [slot][SY][SX]; off[k] the cell of corner k = 4 dx + 2 dy + dz.
-// sq = 2^kq, sg = 2^kg of the quantity's group.
-template <int SL>
-__device__ __forceinline__ void add_t00(unsigned long long *A, unsigned long long *B, const int *off,
-                                        const float *w, const float *l, float m, float ee, float r, float sq,
-                                        float sg) {
-  const int Q = fixed32_of(m * ee * sq);  // m w (ee + ff phi) = (m ee) w (1 + r phi), r = ff / ee
-#pragma unroll
-  for (int k = 0; k < 8; ++k) iadd(((k & 1) ? B : A) + off[k], Q, gq(w[k] * (1.f + r * l[k]), sg));
-}
-template <int SL>
-__device__ __forceinline__ void add_tij(unsigned long long *A, unsigned long long *B, const int *off, const float *w,
-                                        const float *l, const float *q, float m, float inv_e, float f, float u0,
-                                        float u1, float u2, float sq, float sg) {
-  const float d0 = 1.f - u0, d1 = 1.f - u1, d2 = 1.f - u2;
-  const int o00 = off[0], o01 = off[2], o10 = off[4];
-  int G[8];  // the diagonal components share the corner factors w_k (1 + f phi_k)
-#pragma unroll
-  for (int k = 0; k < 8; ++k) G[k] = gq(w[k] * (1.f + f * l[k]), sg);
-  const int dslot[3] = {0, 3, 5};
-#pragma unroll
-  for (int i = 0; i < 3; ++i) {
-    const int Q = fixed32_of(m * q[i] * q[i] * inv_e * sq);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) iadd(((k & 1) ? B : A) + dslot[i] * SL + off[k], Q, G[k]);
-  }
-  const float qf = 0.25f * f;
-  int Q = fixed32_of(m * q[0] * q[1] * inv_e * sq);  // 01 on plaquettes: CIC in z only
-  iadd(A + 1 * SL + o00, Q, gq(d2 * (1.f + qf * (l[0] + l[2] + l[4] + l[6])), sg));
-  iadd(B + 1 * SL + o00, Q, gq(u2 * (1.f + qf * (l[1] + l[3] + l[5] + l[7])), sg));
-  Q = fixed32_of(m * q[0] * q[2] * inv_e * sq);  // 02: CIC in y only
-  iadd(A + 2 * SL + o00, Q, gq(d1 * (1.f + qf * (l[0] + l[1] + l[4] + l[5])), sg));
-  iadd(A + 2 * SL + o01, Q, gq(u1 * (1.f + qf * (l[2] + l[3] + l[6] + l[7])), sg));
-  Q = fixed32_of(m * q[1] * q[2] * inv_e * sq);  // 12: CIC in x only
-  iadd(A + 4 * SL + o00, Q, gq(d0 * (1.f + qf * (l[0] + l[1] + l[2] + l[3])), sg));
-  iadd(A + 4 * SL + o10, Q, gq(u0 * (1.f + qf * (l[4] + l[5] + l[6] + l[7])), sg));
-}
-
 template <int KIND>
 __global__ void __launch_bounds__(FX_THREADS, 3) k_dep_fx(PclsArrays P, const uint32_t *__restrict__ start,
-                                                       const float *__restrict__ phi, FxOut out,
+                                                       const float *__restrict__ phi, float *out,
                                                        unsigned long long *face, FxParams p,
                                                        const uint32_t *__restrict__ fxb) {
   constexpr int NC = FX_NC[KIND];
@@ -213,9 +166,8 @@ __global__ void __launch_bounds__(FX_THREADS, 3) k_dep_fx(PclsArrays P, const ui
   constexpr bool USE_PHI = KIND != FX_MASS;
   extern __shared__ __align__(16) unsigned long long lay[];  // [2][NC][SY][SX]
   __shared__ uint32_t rowoff[TY + 1], rowbase[TY];
-  const int ks0 = (int)fxb[2], ks1 = (int)fxb[3];  // accumulator scales 2^(kq + kg) of groups 0, 1
+  const int ks0 = (int)fxb[2];  // accumulator scale 2^(kq + kg)
   const float sq0 = pow2f((int)fxb[5]), sg0 = pow2f((int)fxb[6]);
-  const float sq1 = pow2f((int)fxb[7]), sg1 = pow2f((int)fxb[8]);
   const int N = p.N;
   const long C = (long)N * N * N;
   const long NN = (long)N * N;
@@ -288,12 +240,12 @@ __global__ void __launch_bounds__(FX_THREADS, 3) k_dep_fx(PclsArrays P, const ui
 #pragma unroll
         for (int k = 0; k < 8; ++k) l[k] = 0.f;
       }
-      const float m = p.mass, a = p.a;
+      const float m = p.mass;
       if (KIND == FX_MASS) {
         const int Q = fixed32_of(m * sq0);
 #pragma unroll
         for (int k = 0; k < 8; ++k) iadd(((k & 1) ? B : A) + off[k], Q, gq(w[k], sg0));
-      } else if (KIND == FX_T0I) {
+      } else {  // FX_T0I
         const float q0 = ((const float *)P.vx)[j], q1 = ((const float *)P.vy)[j], q2 = ((const float *)P.vz)[j];
         // x component: CIC in y, z; NGP in x (gevolution.hpp:1107-1144)
         int Q = fixed32_of(m * q0 * sq0);
@@ -311,24 +263,6 @@ __global__ void __launch_bounds__(FX_THREADS, 3) k_dep_fx(PclsArrays P, const ui
         iadd(A + 2 * SL + o10, Q, gq(u0 * d1 * (1.f + l[4] + l[5]), sg0));
         iadd(A + 2 * SL + o01, Q, gq(d0 * u1 * (1.f + l[2] + l[3]), sg0));
         iadd(A + 2 * SL + o11, Q, gq(u0 * u1 * (1.f + l[6] + l[7]), sg0));
-      } else {
-        const float q[3] = {((const float *)P.vx)[j], ((const float *)P.vy)[j], ((const float *)P.vz)[j]};
-        const float f2 = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-        if (KIND == FX_T00 || KIND == FX_T00TIJ) {
-          float ee = a, r = 0.f;
-          if (have_phi) {
-            ee = sqrtf(f2 + a * a);
-            r = (3.f * ee + f2 / ee) / ee;
-          }
-          add_t00<SL>(A, B, off, w, l, m, ee, r, sq0, sg0);
-        }
-        if (KIND == FX_TIJ || KIND == FX_T00TIJ) {
-          constexpr int S0 = KIND == FX_T00TIJ ? 1 : 0;  // first Tij slot
-          const float ee = sqrtf(f2 + a * a), inv_e = 1.f / ee;
-          const float f = 4.f + a * a / (f2 + a * a);
-          add_tij<SL>(A + S0 * SL, B + S0 * SL, off, w, l, q, m, inv_e, f, u0, u1, u2,
-                      KIND == FX_T00TIJ ? sq1 : sq0, KIND == FX_T00TIJ ? sg1 : sg0);
-        }
       }
     }
     __syncthreads();
@@ -350,8 +284,8 @@ __global__ void __launch_bounds__(FX_THREADS, 3) k_dep_fx(PclsArrays P, const ui
         if (onface) {
           if (v != 0ull) atomicAdd(&face[(long)comp * fstride + fi], v);
         } else {
-          const float fv = float_of_fixed((long long)v, comp_shift<KIND>(comp, ks0, ks1));
-          float *o = comp_ptr(out, comp, C) + gi;
+          const float fv = float_of_fixed((long long)v, ks0);
+          float *o = out + comp * C + gi;
           if (p.overwrite)
             *o = fv;
           else if (v != 0ull)
@@ -383,14 +317,147 @@ __global__ void __launch_bounds__(FX_THREADS, 3) k_dep_fx(PclsArrays P, const ui
   }
 }
 
+// ---------------------------------------------------------------- gather --
+// T00 and Tij as a gather: each grid node sums, in int64 registers, the
+// contributions of the particles in its 8 neighbouring cells.
+//
+// Prefactor arrays, 9 words a particle (SoA): [0] Q00 = round(m e 2^kq0), [1] rT =
+// (3e + q^2/e) / e, [2..4] Qd_i = round(m q_i^2 / e 2^kq1), [5..7] Qo = round(m q_i q_j / e
+// 2^kq1) for 01, 02, 12, [8] fT = 4 + a^2 / (q^2 + a^2).  Written by k_fx_prep.
+struct PrepArrays {
+  int *q00;
+  float *rT;
+  int *qd0, *qd1, *qd2, *qo01, *qo02, *qo12;
+  float *fT;
+};
+inline PrepArrays prep_arrays(void *base, long cap) {
+  PrepArrays a;
+  int *w = (int *)base;
+  a.q00 = w;
+  a.rT = (float *)(w + cap);
+  a.qd0 = w + 2 * cap;
+  a.qd1 = w + 3 * cap;
+  a.qd2 = w + 4 * cap;
+  a.qo01 = w + 5 * cap;
+  a.qo02 = w + 6 * cap;
+  a.qo12 = w + 7 * cap;
+  a.fT = (float *)(w + 8 * cap);
+  return a;
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArrays A, FxParams p, int have_phi,
+                                                 const uint32_t *__restrict__ fxb) {
+  const float sq0 = pow2f((int)fxb[5]), sq1 = pow2f((int)fxb[7]);
+  const float sqT = KIND == FX_T00TIJ ? sq1 : pow2f((int)fxb[5]);  // Tij's prefactor scale
+  // every operation is an explicitly rounded intrinsic: no multiply-add is contracted
+  // differently in one instantiation than in another, so each kind and the fused
+  // kind produce the same bits
+  const float m = p.mass, a = p.a, a2 = __fmul_rn(a, a);
+  for (long j = blockIdx.x * (long)blockDim.x + threadIdx.x; j < n; j += (long)gridDim.x * blockDim.x) {
+    const float q0 = ((const float *)P.vx)[j], q1 = ((const float *)P.vy)[j], q2 = ((const float *)P.vz)[j];
+    const float f2 = __fadd_rn(__fadd_rn(__fmul_rn(q0, q0), __fmul_rn(q1, q1)), __fmul_rn(q2, q2));
+    const float ee = __fsqrt_rn(__fadd_rn(f2, a2));
+    if (KIND == FX_T00 || KIND == FX_T00TIJ) {
+      const float e00 = have_phi ? ee : a;
+      const float r = have_phi ? __fdiv_rn(__fadd_rn(__fmul_rn(3.f, ee), __fdiv_rn(f2, ee)), ee) : 0.f;
+      A.q00[j] = fixed32_of(__fmul_rn(__fmul_rn(m, e00), sq0));
+      A.rT[j] = r;
+    }
+    if (KIND == FX_TIJ || KIND == FX_T00TIJ) {
+      const float inv_e = __fdiv_rn(1.f, ee), mi = __fmul_rn(m, inv_e);
+      A.fT[j] = __fadd_rn(4.f, __fdiv_rn(a2, __fadd_rn(f2, a2)));
+      A.qd0[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q0, q0), mi), sqT));
+      A.qd1[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q1, q1), mi), sqT));
+      A.qd2[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q2, q2), mi), sqT));
+      A.qo01[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q0, q1), mi), sqT));
+      A.qo02[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q0, q2), mi), sqT));
+      A.qo12[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q1, q2), mi), sqT));
+    }
+  }
+}
+
+// one thread per node (x, y, z); out: T00 (1 comp) and / or Tij (6 comps, 00 01 02 11 12 22)
+template <int KIND>
+__global__ void __launch_bounds__(256) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
+                                                    const float *__restrict__ phi, float *t00, float *tij, FxParams p,
+                                                    Div32 dN, const uint32_t *__restrict__ fxb) {
+  constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
+  const int ks00 = (int)fxb[2], ksij = KIND == FX_T00TIJ ? (int)fxb[3] : (int)fxb[2];
+  const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
+  const int N = p.N;
+  const unsigned C = (unsigned)N * N * N;
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+    int x, y, z;
+    cell_xyz(i, N, p.lg, dN, x, y, z);
+    const Nb3 b = nb3(i, x, y, z, N);
+    // phi at the node and its +x, +y, +z neighbours: the factors of the node's corner
+    // (T00, diagonal Tij) and the three plaquette sums of the off-diagonal components
+    float pn = 0.f, s01 = 0.f, s02 = 0.f, s12 = 0.f;
+    if (phi != nullptr) {  // indices summed in 32 bits: the offsets wrap modulo 2^32
+      const unsigned i100 = i + b.xp, i010 = i + b.yp, i001 = i + b.zp;
+      const unsigned i110 = i100 + b.yp, i101 = i100 + b.zp, i011 = i010 + b.zp;
+      const float f000 = __ldg(&phi[i]), f100 = __ldg(&phi[i100]), f010 = __ldg(&phi[i010]);
+      const float f110 = __ldg(&phi[i110]), f001 = __ldg(&phi[i001]);
+      const float f101 = __ldg(&phi[i101]), f011 = __ldg(&phi[i011]);
+      pn = f000;
+      s01 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f010), f100), f110);  // l0 + l2 + l4 + l6 of the particles' cells
+      s02 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f100), f101);  // l0 + l1 + l4 + l5
+      s12 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f010), f011);  // l0 + l1 + l2 + l3
+    }
+    long long a00 = 0, ad0 = 0, ad1 = 0, ad2 = 0, ao01 = 0, ao02 = 0, ao12 = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {  // the node is corner (dx, dy, dz) of cell (x - dx, y - dy, z - dz)
+      const int dx = (k >> 2) & 1, dy = (k >> 1) & 1, dz = k & 1;
+      const unsigned c = i + (dx ? b.xm : 0u) + (dy ? b.ym : 0u) + (dz ? b.zm : 0u);
+      const uint32_t j0 = start[c], j1 = start[c + 1];
+      for (uint32_t j = j0; j < j1; ++j) {
+        const float u0 = P.rx[j], u1 = P.ry[j], u2 = P.rz[j];
+        const float w0 = dx ? u0 : __fsub_rn(1.f, u0), w1 = dy ? u1 : __fsub_rn(1.f, u1),
+                    w2 = dz ? u2 : __fsub_rn(1.f, u2);
+        const float w = __fmul_rn(__fmul_rn(w0, w1), w2);
+        if (DO00)
+          a00 += (long long)A.q00[j] * (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(A.rT[j], pn))), sg00);
+        if (DOIJ) {
+          const float f = A.fT[j];
+          const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(f, pn))), sgij);
+          ad0 += (long long)A.qd0[j] * G;
+          ad1 += (long long)A.qd1[j] * G;
+          ad2 += (long long)A.qd2[j] * G;
+          const float qf = __fmul_rn(0.25f, f);
+          if (dx == 0 && dy == 0)
+            ao01 += (long long)A.qo01[j] * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, s01))), sgij);
+          if (dx == 0 && dz == 0)
+            ao02 += (long long)A.qo02[j] * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, s02))), sgij);
+          if (dy == 0 && dz == 0)
+            ao12 += (long long)A.qo12[j] * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, s12))), sgij);
+        }
+      }
+    }
+    if (DO00) {
+      const float v = float_of_fixed(a00, ks00);
+      t00[i] = p.overwrite ? v : t00[i] + v;
+    }
+    if (DOIJ) {
+      const long long acc[6] = {ad0, ao01, ao02, ad1, ao12, ad2};
+#pragma unroll
+      for (int c = 0; c < 6; ++c) {
+        const float v = float_of_fixed(acc[c], ksij);
+        float *o = tij + (size_t)c * C + i;
+        *o = p.overwrite ? v : *o + v;
+      }
+    }
+  }
+}
+
 // add the face accumulators into the field (or, with p.overwrite, store them) and
 // clear them.  A cell on several face planes has one entry, on the first of its
 // x, y, z planes (face_index); in overwrite mode the other planes' entries for it
 // (always zero) are skipped so that they do not overwrite the cell.
-__global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, FxOut out, int ncomp, int fused,
-                                                  FxParams p, const uint32_t *__restrict__ fxb) {
+__global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, float *out, int ncomp, FxParams p,
+                                                  const uint32_t *__restrict__ fxb) {
   const int N = p.N;
-  const int ks0 = (int)fxb[2], ks1 = (int)fxb[3];
+  const int ks = (int)fxb[2];
   const long NN = (long)N * N, C = NN * N;
   const int planes = (int)(p.nPX + p.nPY + p.nPZ);
   const long rows = (long)ncomp * planes * N;  // face entries come in rows of N (face_index)
@@ -399,8 +466,7 @@ __global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, FxOu
     const int rr = (int)(row - (long)comp * planes * N);
     const int pl = rr / N, q = rr - pl * N;
     unsigned long long *f = face + row * N;
-    float *o = comp_ptr(out, comp, C);
-    const int ks = (fused && comp > 0) ? ks1 : ks0;
+    float *o = out + comp * C;
     for (int t = threadIdx.x; t < N; t += blockDim.x) {
       const unsigned long long v = f[t];
       if (v == 0ull && !p.overwrite) continue;
@@ -434,7 +500,7 @@ __global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, FxOu
 }  // namespace
 
 // the fixed-point deposit of the mixed form; kind: 0 T00, 1 T0i, 2 Tij, 3 mass,
-// 4 T00 and Tij in one sweep (out: T00, out2: Tij).  overwrite: every cell of the
+// 4 T00 and Tij in one gather (out: T00, out2: Tij).  overwrite: every cell of the
 // target is written (the sum of this deposit alone), which spares the caller
 // zeroing it first and the kernel reading it back.
 int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass, double a, const gev_field *phi,
@@ -451,8 +517,9 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   fp.nPZ = (N + TZ - 1) / TZ;
   fp.overwrite = overwrite ? 1 : 0;
   const size_t face_elems = (size_t)(fp.nPX + fp.nPY + fp.nPZ) * N * N * NC;
-  // the face buffer lives behind the deposit scratch pointer, kept zeroed between uses
-  if (ctx->cube_bytes < face_elems * 8) {
+  const bool gather = kind == FX_T00 || kind == FX_TIJ || kind == FX_T00TIJ;
+  // the face buffer (scatter kinds) lives behind the deposit scratch pointer, kept zeroed between uses
+  if (!gather && ctx->cube_bytes < face_elems * 8) {
     int rc = ctx_ensure_cube(ctx, face_elems * 8);
     if (rc) return rc;
     GEV_CHECK_CUDA(ctx, cudaMemsetAsync(ctx->d_cube, 0, ctx->cube_bytes, ctx->stream));
@@ -461,10 +528,6 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   const size_t smem = 2 * (size_t)NC * (TX + 1) * (TY + 1) * 8;
   unsigned long long *face = (unsigned long long *)ctx->d_cube;
   const float *fphi = phi ? (const float *)phi->d : nullptr;
-  FxOut fo;
-  fo.o0 = (float *)out->d;
-  fo.o1 = out2 ? (float *)out2->d : nullptr;
-  fo.nc0 = kind == FX_T00TIJ ? 1 : NC;
   const unsigned blocks = (unsigned)(ntx * nty * ntz);
   const long C = (long)N * N * N;
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->bounds, 0, 16 * sizeof(uint32_t), ctx->stream));
@@ -474,30 +537,51 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   GEV_LAUNCH_CHECK(ctx);
   k_fx_scale<<<1, 1, 0, ctx->stream>>>(p->bounds, kind, mass, a);
   GEV_LAUNCH_CHECK(ctx);
+  if (gather) {
+    if (!p->prep) {
+      const size_t bytes = (size_t)(p->cap > 0 ? p->cap : 1) * 9 * 4;
+      if (cudaMalloc(&p->prep, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return gev_fail(ctx, GEV_ENOMEM, "deposit: prefactor scratch allocation failed");
+      }
+      ctx->bytes_in_use += bytes;
+    }
+    const PrepArrays pa = prep_arrays(p->prep, p->cap > 0 ? p->cap : 1);
+    float *t00 = kind == FX_TIJ ? nullptr : (float *)out->d;
+    float *tij = kind == FX_TIJ ? (float *)out->d : (out2 ? (float *)out2->d : nullptr);
+    const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
+    const int gb = grid_for(ctx, (size_t)C, 256, 16);
+    const Div32 dN = make_div32((unsigned)N);
+    if (kind == FX_T00) {
+      k_fx_prep<FX_T00><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
+      GEV_LAUNCH_CHECK(ctx);
+      k_dep_gather<FX_T00><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
+    } else if (kind == FX_TIJ) {
+      k_fx_prep<FX_TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
+      GEV_LAUNCH_CHECK(ctx);
+      k_dep_gather<FX_TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
+    } else {
+      k_fx_prep<FX_T00TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
+      GEV_LAUNCH_CHECK(ctx);
+      k_dep_gather<FX_T00TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
+    }
+    GEV_LAUNCH_CHECK(ctx);
+    return GEV_OK;
+  }
 #define GEV_DEP_LAUNCH(K, PHI)                                                                       \
   cudaFuncSetAttribute(k_dep_fx<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);        \
-  k_dep_fx<K><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, PHI, fo, face, fp, p->bounds)
-  switch (kind) {
-    case FX_T00:
-      GEV_DEP_LAUNCH(FX_T00, fphi);
-      break;
-    case FX_T0I:
-      GEV_DEP_LAUNCH(FX_T0I, fphi);
-      break;
-    case FX_TIJ:
-      GEV_DEP_LAUNCH(FX_TIJ, fphi);
-      break;
-    case FX_T00TIJ:
-      GEV_DEP_LAUNCH(FX_T00TIJ, fphi);
-      break;
-    default:
-      GEV_DEP_LAUNCH(FX_MASS, nullptr);
+  k_dep_fx<K><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, PHI, (float *)out->d, face, fp, \
+                                                         p->bounds)
+  if (kind == FX_T0I) {
+    GEV_DEP_LAUNCH(FX_T0I, fphi);
+  } else {
+    GEV_DEP_LAUNCH(FX_MASS, nullptr);
   }
 #undef GEV_DEP_LAUNCH
   GEV_LAUNCH_CHECK(ctx);
   const long face_rows = (long)NC * (fp.nPX + fp.nPY + fp.nPZ) * N;
   const long ff_blocks = face_rows < (long)ctx->sms * 16 ? face_rows : (long)ctx->sms * 16;
-  k_face_fix<<<(unsigned)ff_blocks, 256, 0, ctx->stream>>>(face, fo, NC, kind == FX_T00TIJ ? 1 : 0, fp, p->bounds);
+  k_face_fix<<<(unsigned)ff_blocks, 256, 0, ctx->stream>>>(face, (float *)out->d, NC, fp, p->bounds);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }

@@ -103,6 +103,9 @@ struct gev_pcls {
   // [1] max particles in a cell, [2], [3] the accumulator scale powers of the last
   // deposit's groups, [5..8] their prefactor and weight-factor powers
   uint32_t *bounds = nullptr;
+  // mixed-form T00 / Tij deposit: per-particle integer prefactors (9 words a particle,
+  // allocated on first use)
+  void *prep = nullptr;
 };
 
 // one simulation (include/gev_sim.h)

@@ -893,6 +893,7 @@ int gev_pcls_destroy(gev_pcls *p) {
   cudaFree(p->perm);
   cudaFree(p->big);
   cudaFree(p->bounds);
+  cudaFree(p->prep);
   cudaFree(p->scan_tmp);
   gev_ctx *ctx = p->ctx;
   delete p;
