@@ -545,6 +545,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
         return gev_fail(ctx, GEV_ENOMEM, "deposit: prefactor scratch allocation failed");
       }
       ctx->bytes_in_use += bytes;
+      p->bytes += bytes;
     }
     const PrepArrays pa = prep_arrays(p->prep, p->cap > 0 ? p->cap : 1);
     float *t00 = kind == FX_TIJ ? nullptr : (float *)out->d;

@@ -106,6 +106,7 @@ struct gev_pcls {
   // mixed-form T00 / Tij deposit: per-particle integer prefactors (9 words a particle,
   // allocated on first use)
   void *prep = nullptr;
+  size_t bytes = 0;  // device bytes this store counts in its context's bytes_in_use
 };
 
 // one simulation (include/gev_sim.h)
@@ -356,6 +357,8 @@ int fft_r2c_rows_reg(gev_ctx *ctx, const void *real, void *spec);
 int fft_c2r_rows_reg(gev_ctx *ctx, const void *spec, void *real);
 int pcls_relink(gev_ctx *ctx, gev_pcls *p);
 int pcls_id_order(gev_ctx *ctx, gev_pcls *p);
+int pcls_unpack_at(gev_ctx *ctx, gev_pcls *p, const gev_part *d, long count, long offset);
+int pcls_pack_range(gev_ctx *ctx, gev_pcls *p, gev_part *d, long i0, long count);
 int ctx_ensure_cube(gev_ctx *ctx, size_t bytes);
 int ctx_ensure_red(gev_ctx *ctx, size_t elems);
 // the deposit of kind 0 T00, 1 T0i, 2 Tij, 3 mass (coefficient 1) replacing the

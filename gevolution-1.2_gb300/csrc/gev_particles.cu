@@ -849,6 +849,57 @@ int pcls_relink(gev_ctx *ctx, gev_pcls *p) {
   return GEV_OK;
 }
 
+// device records d[0, count) into slots [offset, offset + count) of the store's
+// arrays (cell keys and in-cell offsets derived as gev_pcls_upload does); the
+// caller sets p->n and relinks
+int pcls_unpack_at(gev_ctx *ctx, gev_pcls *p, const gev_part *d, long count, long offset) {
+  if (count <= 0) return GEV_OK;
+  if (offset < 0 || offset + count > p->cap) return gev_fail(ctx, GEV_EINVAL, "particles exceed the store's capacity");
+  PclsArrays A = p->cur;
+  const size_t vsz = ctx->prec == GEV_PREC_FP64 ? 8 : 4;
+  A.px += offset;
+  A.py += offset;
+  A.pz += offset;
+  A.vx = (char *)A.vx + offset * vsz;
+  A.vy = (char *)A.vy + offset * vsz;
+  A.vz = (char *)A.vz + offset * vsz;
+  A.id += offset;
+  A.cell += offset;
+  if (A.rx) {
+    A.rx += offset;
+    A.ry += offset;
+    A.rz += offset;
+  }
+  const int b = grid_for(ctx, (size_t)count, 256, 16);
+  if (ctx->prec == GEV_PREC_FP64)
+    k_unpack<double><<<b, 256, 0, ctx->stream>>>(d, count, A, ctx->N);
+  else
+    k_unpack<float><<<b, 256, 0, ctx->stream>>>(d, count, A, ctx->N);
+  GEV_LAUNCH_CHECK(ctx);
+  return GEV_OK;
+}
+
+// records [i0, i0 + count) of the store, in its current order, into d
+int pcls_pack_range(gev_ctx *ctx, gev_pcls *p, gev_part *d, long i0, long count) {
+  if (count <= 0) return GEV_OK;
+  PclsArrays A = p->cur;
+  const size_t vsz = ctx->prec == GEV_PREC_FP64 ? 8 : 4;
+  A.px += i0;
+  A.py += i0;
+  A.pz += i0;
+  A.vx = (char *)A.vx + i0 * vsz;
+  A.vy = (char *)A.vy + i0 * vsz;
+  A.vz = (char *)A.vz + i0 * vsz;
+  A.id += i0;
+  const int b = grid_for(ctx, (size_t)count, 256, 16);
+  if (ctx->prec == GEV_PREC_FP64)
+    k_pack<double><<<b, 256, 0, ctx->stream>>>(d, count, A);
+  else
+    k_pack<float><<<b, 256, 0, ctx->stream>>>(d, count, A);
+  GEV_LAUNCH_CHECK(ctx);
+  return GEV_OK;
+}
+
 extern "C" {
 
 int gev_pcls_create(gev_ctx *ctx, long capacity, double mass, gev_pcls **out) {
@@ -861,6 +912,7 @@ int gev_pcls_create(gev_ctx *ctx, long capacity, double mass, gev_pcls **out) {
   const size_t vsz = ctx->prec == GEV_PREC_FP64 ? 8 : 4;
   const long C = (long)ctx->N * ctx->N * ctx->N;
   const long cap = capacity > 0 ? capacity : 1;
+  const size_t bytes0 = ctx->bytes_in_use;
   int rc = alloc_arrays(ctx, p->cur, cap, vsz);
   if (!rc) rc = alloc_arrays(ctx, p->alt, cap, vsz);
   if (!rc) {
@@ -873,6 +925,7 @@ int gev_pcls_create(gev_ctx *ctx, long capacity, double mass, gev_pcls **out) {
     else
       ctx->bytes_in_use += (size_t)C * 12 + (size_t)cap * 8 + p->scan_tmp_elems * 4;
   }
+  p->bytes = ctx->bytes_in_use - bytes0;
   if (rc) {
     gev_pcls_destroy(p);
     cudaGetLastError();
@@ -896,6 +949,7 @@ int gev_pcls_destroy(gev_pcls *p) {
   cudaFree(p->prep);
   cudaFree(p->scan_tmp);
   gev_ctx *ctx = p->ctx;
+  if (ctx) ctx->bytes_in_use -= p->bytes;
   delete p;
   if (ctx) ctx_release(ctx);
   return GEV_OK;

@@ -507,3 +507,114 @@ def sim_ic_generate(sim, **params):
 
 
 Sim.ic_generate = sim_ic_generate
+
+
+# ------------------------------------------------ snapshots and restarts --
+class Gadget2Header(ctypes.Structure):
+    """gadget2_header (metadata.hpp:152-171), 256 bytes."""
+    _fields_ = [("npart", ctypes.c_uint32 * 6), ("mass", _d * 6), ("time", _d), ("redshift", _d),
+                ("flag_sfr", ctypes.c_int32), ("flag_feedback", ctypes.c_int32),
+                ("npartTotal", ctypes.c_uint32 * 6), ("flag_cooling", ctypes.c_int32),
+                ("num_files", ctypes.c_int32), ("BoxSize", _d), ("Omega0", _d), ("OmegaLambda", _d),
+                ("HubbleParam", _d), ("flag_age", ctypes.c_int32), ("flag_metals", ctypes.c_int32),
+                ("npartTotalHW", ctypes.c_uint32 * 6), ("fill", ctypes.c_char * 64)]
+
+
+assert ctypes.sizeof(Gadget2Header) == 256
+
+GADGET_LENGTH_CONVERSION = 0.001
+GADGET_MASS_CONVERSION = 1.0e10
+GADGET_VELOCITY_CONVERSION = 3.335640952e-6
+CKPT_FROM_B = 1
+
+
+class CheckpointInfo(ctypes.Structure):
+    _fields_ = [("a", _d), ("tau", _d), ("dtau", _d), ("cycle", _i), ("has_state", _i), ("state", SimState),
+                ("numpcl", _l), ("N", _i), ("prec", _i)]
+
+
+_IO_SIGS = {
+    "gev_gadget2_save": [_vp, _vp, ctypes.c_char_p, ctypes.POINTER(Gadget2Header), _i, _d, _d, _vp, _i, _i],
+    "gev_gadget2_load": [_vp, _vp, ctypes.c_char_p, ctypes.POINTER(Gadget2Header), _i],
+    "gev_checkpoint_save": [_vp, ctypes.c_char_p, _vp, _vp, _vp, _vp, _vp, _d, _d, _d, _i, ctypes.POINTER(SimState)],
+    "gev_checkpoint_load": [_vp, ctypes.c_char_p, _vp, _vp, _vp, _vp, _vp, _i, ctypes.POINTER(CheckpointInfo)],
+    "gev_checkpoint_info_read": [ctypes.c_char_p, ctypes.POINTER(CheckpointInfo)],
+    "gev_sim_hibernate": [_vp, ctypes.c_char_p],
+    "gev_sim_restart": [_vp, ctypes.c_char_p, _i],
+}
+
+
+def _io_lib():
+    L = _sim_lib()
+    if not getattr(L, "_io_ready", False):
+        for name, args in _IO_SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L._io_ready = True
+    return L
+
+
+def gadget2_header(npart, time, boxsize_mpc_h, mass=0.0, Omega0=0.32, OmegaLambda=0.68, h=0.67, redshift=None):
+    """A header filled as writeSnapshots does (output.hpp:362-403) for one CDM species."""
+    hdr = Gadget2Header()
+    hdr.num_files = 1
+    hdr.Omega0, hdr.OmegaLambda, hdr.HubbleParam = Omega0, OmegaLambda, h
+    hdr.BoxSize = boxsize_mpc_h / GADGET_LENGTH_CONVERSION
+    hdr.time = time
+    hdr.redshift = (1.0 / time) - 1.0 if redshift is None else redshift
+    hdr.npart[1] = npart % (1 << 32)
+    hdr.npartTotal[1] = hdr.npart[1]
+    hdr.npartTotalHW[1] = npart >> 32
+    hdr.mass[1] = mass
+    return hdr
+
+
+def gadget2_save(pcls, filename, hdr, tracer_factor=1, dtau_pos=0.0, dtau_vel=0.0, phi=None, exact_output=False,
+                 id_bytes=8):
+    _check(_io_lib().gev_gadget2_save(pcls.ctx.handle, pcls.handle, os.fsencode(filename), ctypes.byref(hdr),
+                                      tracer_factor, dtau_pos, dtau_vel, _h(phi) if phi is not None else None,
+                                      1 if exact_output else 0, id_bytes), pcls.ctx, "gev_gadget2_save")
+
+
+def gadget2_load(pcls, filename, id_bytes=8):
+    hdr = Gadget2Header()
+    _check(_io_lib().gev_gadget2_load(pcls.ctx.handle, pcls.handle, os.fsencode(filename), ctypes.byref(hdr),
+                                      id_bytes), pcls.ctx, "gev_gadget2_load")
+    return hdr
+
+
+def checkpoint_save(ctx, path, pcls, phi, chi, Bi, BiFT, a, tau, dtau, cycle):
+    _check(_io_lib().gev_checkpoint_save(ctx.handle, os.fsencode(path), pcls.handle, _h(phi), _h(chi),
+                                         _h(Bi) if Bi is not None else None,
+                                         _h(BiFT) if BiFT is not None else None, a, tau, dtau, cycle, None),
+           ctx, "gev_checkpoint_save")
+
+
+def checkpoint_load(ctx, path, pcls=None, phi=None, chi=None, Bi=None, BiFT=None, flags=0):
+    info = CheckpointInfo()
+    hv = [_h(x) for x in (pcls, phi, chi, Bi, BiFT)]
+    _check(_io_lib().gev_checkpoint_load(ctx.handle, os.fsencode(path), *hv, flags, ctypes.byref(info)), ctx,
+           "gev_checkpoint_load")
+    return info
+
+
+def checkpoint_info(path):
+    info = CheckpointInfo()
+    rc = _io_lib().gev_checkpoint_info_read(os.fsencode(path), ctypes.byref(info))
+    if rc != OK:
+        raise GevError("gev_checkpoint_info_read: not a readable hibernation file")
+    return info
+
+
+def _sim_hibernate(sim, path):
+    _check(_io_lib().gev_sim_hibernate(sim.handle, os.fsencode(path)), sim.ctx, "gev_sim_hibernate")
+
+
+def _sim_restart(sim, path, flags=0):
+    _check(_io_lib().gev_sim_restart(sim.handle, os.fsencode(path), flags), sim.ctx, "gev_sim_restart")
+    return sim
+
+
+Sim.hibernate = _sim_hibernate
+Sim.restart = _sim_restart

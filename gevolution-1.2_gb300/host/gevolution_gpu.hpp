@@ -33,6 +33,7 @@
 #include <vector>
 
 #include "../../include/gev_gb300.h"
+#include "../../include/gev_io.h"
 
 #ifndef FFT_FORWARD
 #define FFT_FORWARD 1
@@ -167,6 +168,21 @@ inline void update_pos(double, double, part_simple *, double *, part_simple_info
 inline void update_pos_Newton(double, double, part_simple *, double *, part_simple_info, Field<Real> **, void *, int,
                               double *, double *, int) {}
 
+// Gadget-2 snapshots (metadata.hpp:111-171)
+typedef gev_gadget2_header gadget2_header;
+#ifndef GADGET_LENGTH_CONVERSION
+#define GADGET_LENGTH_CONVERSION GEV_GADGET_LENGTH_CONVERSION
+#endif
+#ifndef GADGET_MASS_CONVERSION
+#define GADGET_MASS_CONVERSION GEV_GADGET_MASS_CONVERSION
+#endif
+#ifndef GADGET_VELOCITY_CONVERSION
+#define GADGET_VELOCITY_CONVERSION GEV_GADGET_VELOCITY_CONVERSION
+#endif
+#ifndef GADGET_ID_BYTES
+#define GADGET_ID_BYTES 8
+#endif
+
 template <class part = part_simple, class part_info = part_simple_info, class part_dataType = part_simple_dataType>
 class Particles {
  public:
@@ -194,6 +210,23 @@ class Particles {
                        nfield > 2 ? fields[2]->f : nullptr, nfield, params[0], kind == GEV_GR ? params[1] : 1., &maxvel),
           lat->ctx, "updateVel");
     return maxvel;
+  }
+  // Particles_gevolution::saveGadget2 (Particles_gevolution.hpp:30-251); built with
+  // EXACT_OUTPUT_REDSHIFTS, the drift by dtau_pos and kick by dtau_vel with phi apply
+  void saveGadget2(std::string filename, gadget2_header &hdr, const int tracer_factor = 1, double dtau_pos = 0.,
+                   double dtau_vel = 0., Field<Real> *phi = NULL) {
+#ifdef EXACT_OUTPUT_REDSHIFTS
+    const int exact = 1;
+#else
+    const int exact = 0;
+#endif
+    check(gev_gadget2_save(lat->ctx, p, filename.c_str(), &hdr, tracer_factor, dtau_pos, dtau_vel,
+                           (exact && phi) ? phi->f : nullptr, exact, GADGET_ID_BYTES),
+          lat->ctx, "saveGadget2");
+  }
+  // Particles_gevolution::loadGadget2 (Particles_gevolution.hpp:574-665): adds the file's particles
+  void loadGadget2(std::string filename, gadget2_header &hdr) {
+    check(gev_gadget2_load(lat->ctx, p, filename.c_str(), &hdr, GADGET_ID_BYTES), lat->ctx, "loadGadget2");
   }
   // Particles::moveParticles (main.cpp:798): drift, periodic wrap, relink
   void moveParticles(pos_cb fn, double dtau, Field<Real> **fields, int nfield, double *params) {
@@ -274,6 +307,34 @@ inline void extractPowerSpectrum(Field<Cplx> &fldFT, Real *kbin, Real *power, Re
 template <typename part, typename part_info, typename part_dataType>
 void scalarProjectionCIC_project(Particles<part, part_info, part_dataType> *pcls, Field<Real> *rho) {
   check(gev_projection_mass(rho->lat->ctx, pcls->p, rho->f), rho->lat->ctx, "scalarProjectionCIC_project");
+}
+
+// hibernate (hibernation.hpp:513-611): one binary file at path in place of the
+// reference's HDF5 set -- the particles, phi, chi, B / (a^2 N) and, when given,
+// the spectrum BiFT, which makes a restart exact
+template <typename part, typename part_info, typename part_dataType>
+void hibernate(const std::string &path, Particles<part, part_info, part_dataType> *pcls_cdm, Field<Real> &phi,
+               Field<Real> &chi, Field<Real> &Bi, const double a, const double tau, const double dtau, const int cycle,
+               Field<Cplx> *BiFT = NULL) {
+  check(gev_checkpoint_save(phi.lat->ctx, path.c_str(), pcls_cdm->p, phi.f, chi.f, Bi.f, BiFT ? BiFT->f : nullptr, a,
+                            tau, dtau, cycle, nullptr),
+        phi.lat->ctx, "hibernate");
+}
+// the restart branch of readIC (ic_read.hpp:58-716): particles, phi, chi, B * a^2 / N^2
+// and BiFT (the stored spectrum, or the forward transform of B as readIC makes it);
+// a, tau, dtau_old = the hibernated dtau, cycle = the hibernated cycle + 1
+template <typename part, typename part_info, typename part_dataType>
+void readIC_restart(const std::string &path, Particles<part, part_info, part_dataType> *pcls_cdm, Field<Real> *phi,
+                    Field<Real> *chi, Field<Real> *Bi, Field<Cplx> *BiFT, double &a, double &tau, double &dtau_old,
+                    int &cycle) {
+  gev_checkpoint_info info;
+  check(gev_checkpoint_load(phi->lat->ctx, path.c_str(), pcls_cdm->p, phi->f, chi->f, Bi ? Bi->f : nullptr,
+                            BiFT ? BiFT->f : nullptr, 0, &info),
+        phi->lat->ctx, "readIC");
+  a = info.a;
+  tau = info.tau;
+  dtau_old = info.dtau;
+  cycle = info.cycle + 1;
 }
 
 }  // namespace gevgpu

@@ -141,6 +141,38 @@ void gevo_power_spectrum(int N, const double *FT, int ncomp, int symmetric, int 
                          int deconvolve, double *kbin, double *power, double *kscatter,
                          double *pscatter, int *occupation);
 
+/* ---- Gadget-2 snapshots (Particles_gevolution.hpp:30-251, 574-665) ----
+ * the 256-byte header (metadata.hpp:152-171) */
+typedef struct {
+  uint32_t npart[6];
+  double mass[6];
+  double time;
+  double redshift;
+  int32_t flag_sfr;
+  int32_t flag_feedback;
+  uint32_t npartTotal[6];
+  int32_t flag_cooling;
+  int32_t num_files;
+  double BoxSize;
+  double Omega0;
+  double OmegaLambda;
+  double HubbleParam;
+  int32_t flag_age;
+  int32_t flag_metals;
+  uint32_t npartTotalHW[6];
+  char fill[64];
+} gevo_gadget2_header;
+/* saveGadget2 of one rank: particles in any order (written in (cell, ID)
+ * order); exact = the EXACT_OUTPUT_REDSHIFTS build (needs phi, N^3 values x
+ * fastest); id_bytes = GADGET_ID_BYTES.  Returns 0, or -1 on a bad header, a
+ * tracer count that differs from npart[1], or an I/O error. */
+int gevo_gadget2_save(const char *fname, int N, long np, const gevo_part *p, const double *phi,
+                      const void *hdr256, int tracer_factor, double dtau_pos, double dtau_vel, int exact,
+                      int id_bytes);
+/* loadGadget2: the particles in (cell, ID) order (at most cap), the header;
+ * returns their number or -1 */
+long gevo_gadget2_load(const char *fname, int N, gevo_part *dst, long cap, void *hdr256, int id_bytes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -46,8 +46,7 @@ class SimStruct(ctypes.Structure):
 
 def build(force=False):
     so = os.path.join(HERE, "libgevoracle.so")
-    if force or not os.path.exists(so):
-        subprocess.run(["make", "-s", "-C", HERE, "libgevoracle.so"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "libgevoracle.so"] + (["-B"] if force else []), check=True)
     return so
 
 
@@ -393,3 +392,78 @@ class Sim:
     def cosmo(self):
         c = self.s.cosmo
         return {k: getattr(c, k) for k, _ in Cosmo._fields_}
+
+
+# ------------------------------------------------------ Gadget-2 snapshots --
+_GADGET_REF = None
+
+
+def _gadget_ref():
+    """The reference's own Gadget-2 writer and reader (oracle/_ref/libgevref_gadget.so)."""
+    global _GADGET_REF
+    if _GADGET_REF is None:
+        path = os.path.join(HERE, "_ref", "libgevref_gadget.so")
+        if not os.path.exists(path):
+            if build_ref() is None:
+                return None
+        R = _load(path)
+        for tag in ("plain", "exact", "id4"):
+            f = getattr(R, "gevref_gadget2_save_" + tag)
+            f.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_long, _vp, _vp, _vp, ctypes.c_int, ctypes.c_double,
+                          ctypes.c_double]
+            f = getattr(R, "gevref_gadget2_load_" + tag)
+            f.argtypes = [ctypes.c_char_p, ctypes.c_int, _vp, ctypes.c_long, _vp]
+            f.restype = ctypes.c_long
+        _GADGET_REF = R
+    return _GADGET_REF
+
+
+def _gadget_tag(exact, id_bytes):
+    if exact and id_bytes == 8:
+        return "exact"
+    if not exact and id_bytes == 8:
+        return "plain"
+    if not exact and id_bytes == 4:
+        return "id4"
+    raise ValueError("the reference is built in three variants: default, EXACT_OUTPUT_REDSHIFTS, GADGET_ID_BYTES=4")
+
+
+def gadget2_save(fname, N, parts, hdr, tracer_factor=1, dtau_pos=0.0, dtau_vel=0.0, phi=None, exact=False, id_bytes=8,
+                 impl=None):
+    """saveGadget2 of one rank into fname.  hdr: 256 header bytes.  impl='ref' runs
+    the reference's own code (oracle/_ref)."""
+    p = np.ascontiguousarray(parts, dtype=PART)
+    hb = np.frombuffer(bytes(hdr), np.uint8).copy()
+    assert hb.size == 256
+    ph = None if phi is None else np.ascontiguousarray(phi, np.float64).reshape(-1)
+    fn = os.fsencode(fname)
+    if impl == "ref":
+        R = _gadget_ref()
+        rc = getattr(R, "gevref_gadget2_save_" + _gadget_tag(exact, id_bytes))(
+            fn, N, len(p), _p(p), None if ph is None else _p(ph), _p(hb), tracer_factor, dtau_pos, dtau_vel)
+    else:
+        L = lib()
+        L.gevo_gadget2_save.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.c_long, _vp, _vp, _vp, ctypes.c_int,
+                                        ctypes.c_double, ctypes.c_double, ctypes.c_int, ctypes.c_int]
+        rc = L.gevo_gadget2_save(fn, N, len(p), _p(p), None if ph is None else _p(ph), _p(hb), tracer_factor, dtau_pos,
+                                 dtau_vel, 1 if exact else 0, id_bytes)
+    if rc != 0:
+        raise RuntimeError("gadget2_save failed")
+
+
+def gadget2_load(fname, N, cap, id_bytes=8, impl=None):
+    """loadGadget2 of one file: (particles in (cell, ID) order, 256 header bytes)."""
+    out = np.zeros(max(cap, 1), PART)
+    hb = np.zeros(256, np.uint8)
+    fn = os.fsencode(fname)
+    if impl == "ref":
+        R = _gadget_ref()
+        n = getattr(R, "gevref_gadget2_load_" + _gadget_tag(False, id_bytes))(fn, N, _p(out), cap, _p(hb))
+    else:
+        L = lib()
+        L.gevo_gadget2_load.argtypes = [ctypes.c_char_p, ctypes.c_int, _vp, ctypes.c_long, _vp, ctypes.c_int]
+        L.gevo_gadget2_load.restype = ctypes.c_long
+        n = L.gevo_gadget2_load(fn, N, _p(out), cap, _p(hb), id_bytes)
+    if n < 0 or n > cap:
+        raise RuntimeError("gadget2_load failed")
+    return out[:n], hb.tobytes()

@@ -281,11 +281,18 @@ class Particles {
   double res_;
   part_info info_;
   CellField<part> field_;
+  // the member names Particles_gevolution.hpp reads (its Gadget-2 writer and reader)
+  Lattice lat_part_;
+  double lat_resolution_;
+  CellField<part> &field_part_;
 
+  Particles() : lat_(0), res_(0.), lat_resolution_(0.), field_part_(field_) {}
   void initialize(part_info info, part_dataType, Lattice *lat, Real *) {
     info_ = info;
     lat_ = lat;
     res_ = 1.0 / (double)lat->size_[0];
+    lat_part_ = *lat;
+    lat_resolution_ = res_;
     field_.lat_ = lat;
     field_.cells_.assign((size_t)lat->size_[0] * lat->size_[1] * lat->size_[2], CellList<part>());
   }

@@ -3,15 +3,18 @@
 // the reference's own call sequence and names, so that the drop-in surface is
 // exercised from C++ exactly as main.cpp would call it.
 //
-//   main_loop_gpu <state.bin> <steps> <out.bin>
+//   main_loop_gpu <state.bin> <steps> <out.bin> [<snapshot> <hibernation> <boxsize>]
 //
 // state.bin: int32 N, int32 pad, then doubles a, tau, dtau, dtau_old, fourpiG,
 // Cf, steplimit, z_relax, mass, Omega_cdm, Omega_b, Omega_Lambda, Omega_rad,
 // then N^3 gev_part records, phi (N^3), chi (N^3), Bi (3 N^3) and BiFT
-// (3 N^2 (N/2+1) complex).  out.bin: a, then the N^3 particle records.
+// (3 N^2 (N/2+1) complex).  out.bin: a, then the N^3 particle records.  With
+// the optional arguments the run ends as an output cycle would: a Gadget-2
+// snapshot (header filled as output.hpp:362-403 fills it) and a hibernation point.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "../../gevolution-1.2_gb300/host/gevolution_gpu.hpp"
@@ -35,8 +38,8 @@ static void rungekutta4bg(double &a, double fourpiG, const Cosmo &c, double dtau
 }
 
 int main(int argc, char **argv) {
-  if (argc != 4) {
-    std::fprintf(stderr, "usage: %s state.bin steps out.bin\n", argv[0]);
+  if (argc != 4 && argc != 7) {
+    std::fprintf(stderr, "usage: %s state.bin steps out.bin [snapshot hibernation boxsize]\n", argv[0]);
     return 2;
   }
   FILE *in = std::fopen(argv[1], "rb");
@@ -92,7 +95,8 @@ int main(int argc, char **argv) {
   const double dx = 1.0 / (double)N;
   double maxvel = 0.;
 
-  for (int cycle = 0; cycle < steps; ++cycle) {
+  int cycle = 0;
+  for (; cycle < steps; ++cycle) {
     projection_init(&source);
     projection_T00_project(&pcls_cdm, &source, a, &phi);
     projection_T00_comm(&source);
@@ -132,6 +136,25 @@ int main(int argc, char **argv) {
       dtau = Cf * dx;
     else
       dtau = steplimit / Hconf(a, fourpiG, cosmo);
+  }
+  if (argc == 7) {
+    const double boxsize = std::atof(argv[6]);
+    gadget2_header hdr;
+    std::memset(&hdr, 0, sizeof(hdr));
+    hdr.num_files = 1;
+    hdr.Omega0 = cosmo.Omega_cdm + cosmo.Omega_b;
+    hdr.OmegaLambda = cosmo.Omega_Lambda;
+    hdr.HubbleParam = 0.67;
+    hdr.BoxSize = boxsize / GADGET_LENGTH_CONVERSION;
+    hdr.time = a;
+    hdr.redshift = (1. / a) - 1.;
+    hdr.npart[1] = (uint32_t)V;
+    hdr.npartTotal[1] = hdr.npart[1];
+    hdr.mass[1] = 2.77459457e11 * (cosmo.Omega_cdm + cosmo.Omega_b) * boxsize * boxsize * boxsize / V /
+                  GADGET_MASS_CONVERSION;
+    pcls_cdm.saveGadget2(argv[4], hdr, 1);
+    // main.cpp:845: hibernate(..., a, tau, dtau, cycle) with the step just taken
+    hibernate(argv[5], &pcls_cdm, phi, chi, Bi, a, tau, dtau_old, cycle, &BiFT);
   }
   pcls_cdm.download(parts.data());
   // the power spectrum of B (output.hpp's Pk output path calls extractPowerSpectrum)

@@ -5,11 +5,16 @@ sources are present).
 
     python tests/golden/make_golden.py
 
+    python tests/golden/make_golden.py gadget     # only the Gadget-2 files
+
 Every hot-path function is run on seeded random inputs at N = 8 and N = 12
 (a radix-3 size), and a full initial condition plus three cycles of the main
-loop are run at N = 8.  Inputs and the reference's outputs are stored in
-golden_N{8,12}.npz and golden_run_N8.npz; tests/test_oracle_golden.py checks
-the CPU restatement against them and the GPU tests check the CUDA path.
+loop are run at N = 8.  Gadget-2 snapshots are written and read back by the
+reference's own Particles_gevolution.hpp (oracle/_ref/libgevref_gadget.so) in
+three of its build variants.  Inputs and the reference's outputs are stored in
+golden_N{8,12}.npz, golden_run_N8.npz and golden_gadget2_N8.npz;
+tests/test_oracle_golden.py checks the CPU restatement against them and the GPU
+tests check the CUDA path.
 """
 import os
 import sys
@@ -95,12 +100,54 @@ def run(N=8, steps=3):
     np.savez_compressed(os.path.join(HERE, "golden_run_N%d.npz" % N), **d)
 
 
+GADGET_VARIANTS = (("plain", False, 8), ("exact", True, 8), ("id4", False, 4))
+
+
+def gadget_header(npart, time, boxsize):
+    """The 256 header bytes of one CDM snapshot, filled as output.hpp:362-403 does."""
+    import struct
+    u6 = [0, npart, 0, 0, 0, 0]
+    mass = [0.0, 1.5e-3, 0.0, 0.0, 0.0, 0.0]
+    b = struct.pack("<6I6d2d2i6I2i4d2i6I", *u6, *mass, time, 1.0 / time - 1.0, 0, 0, *u6, 0, 1,
+                    boxsize / 0.001, 0.32, 0.68, 0.67, 0, 0, 0, 0, 0, 0, 0, 0)
+    return b + bytes(256 - len(b))
+
+
+def gadget(N=8, seed=103):
+    """Gadget-2 files written and read back by the reference's own
+    Particles_gevolution.hpp (three build variants, tracer factors 1 and 3)."""
+    import tempfile
+    rng = np.random.default_rng(seed)
+    n = 700
+    p = particles(rng, N, n)
+    p["ID"] = rng.permutation(n) + 5
+    phi = rng.standard_normal(N ** 3) * 1e-5
+    time, box, dtau_pos, dtau_vel = 0.02, 320.0, 0.01, 0.015
+    d = {"parts": p, "phi": phi, "params": np.array([time, box, dtau_pos, dtau_vel])}
+    with tempfile.TemporaryDirectory() as tmp:
+        for tf in (1, 3):
+            S = int((p["ID"] % tf == 0).sum())
+            hdr = gadget_header(S, time, box)
+            d["hdr_tf%d" % tf] = np.frombuffer(hdr, np.uint8).copy()
+            for tag, exact, idb in GADGET_VARIANTS:
+                f = os.path.join(tmp, "snap")
+                G.gadget2_save(f, N, p, hdr, tf, dtau_pos, dtau_vel, phi if exact else None, exact, idb, impl="ref")
+                d["file_%s_tf%d" % (tag, tf)] = np.frombuffer(open(f, "rb").read(), np.uint8).copy()
+                parts, _ = G.gadget2_load(f, N, n, idb, impl="ref")
+                d["load_%s_tf%d" % (tag, tf)] = parts
+    np.savez_compressed(os.path.join(HERE, "golden_gadget2_N%d.npz" % N), **d)
+
+
 if __name__ == "__main__":
     if G.ref() is None:
         sys.exit("the reference sources are not available here; golden vectors cannot be regenerated")
-    one(8, 101)
-    one(12, 102)
-    run(8, 3)
+    which = sys.argv[1:] or ["hotpath", "gadget"]
+    if "hotpath" in which:
+        one(8, 101)
+        one(12, 102)
+        run(8, 3)
+    if "gadget" in which:
+        gadget(8, 103)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

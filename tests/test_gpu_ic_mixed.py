@@ -166,3 +166,36 @@ def test_fused_entry_points_match_separate_calls(gpu, oracle, prec):
     assert a[2] == b[2]
     assert np.array_equal(a[3]["ID"], b[3]["ID"])
     assert np.array_equal(a[3]["pos"], b[3]["pos"]) and np.array_equal(a[3]["vel"], b[3]["vel"])
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_particle_store_returns_its_bytes(gpu, oracle, prec):
+    """A particle store gives back every device byte it counted, including the
+    deposit's prefactor scratch that it allocates on first use.  The context's own
+    deposit scratch stays (it is sized by the grid), so the count is compared after
+    a first store has come and gone."""
+    import gc
+    N = 16
+    c = gpu.Context(N, prec)
+    phi = c.real(1).zero()
+    T00, Tij = c.real(1), c.real(6)
+    rng = np.random.default_rng(3)
+    p = np.zeros(N ** 3, oracle.PART)
+    p["pos"] = rng.random((N ** 3, 3))
+    p["vel"] = rng.standard_normal((N ** 3, 3)) * 1e-3
+    p["ID"] = np.arange(N ** 3)
+
+    def one_store():
+        pc = c.particles(N ** 3, 1.0 / N ** 3).upload(p)
+        gpu.projection_T00_Tij(pc, T00, Tij, 0.02, phi)
+        c.sync()
+        held = c.bytes_in_use()
+        del pc
+        gc.collect()
+        return held
+
+    one_store()
+    base = c.bytes_in_use()
+    held = one_store()
+    assert held >= base + N ** 3 * 56
+    assert c.bytes_in_use() == base
