@@ -182,14 +182,15 @@ int gev_sim_get_state(gev_sim *s, gev_sim_state *st) {
   return GEV_OK;
 }
 
-int gev_sim_step(gev_sim *s) {
+// the first part of a cycle, main.cpp:372-598: stress-energy, phi, chi and B
+int gev_sim_step_fields(gev_sim *s) {
   if (!s) return GEV_EINVAL;
   gev_ctx *ctx = s->ctx;
   gev_sim_state &st = s->st;
   const int N = ctx->N;
   const double dx = 1.0 / (double)N;
   const double fourpiG = st.fourpiG;
-  double a = st.a;
+  const double a = st.a;
   const gev_cosmology &cm = st.cosmo;
 
   // stress-energy (main.cpp:378-450)
@@ -228,6 +229,22 @@ int gev_sim_step(gev_sim *s) {
     RC(gev_evolve_vector(ctx, s->SijFT, s->BiFT, a * a * st.dtau_old));
   }
   RC(gev_fft_c2r(ctx, s->BiFT, s->Bi));
+  return GEV_OK;
+}
+
+// the rest of the cycle, main.cpp:743-872: kick, background half step, drift,
+// background half step, next dtau.  Reads phi, chi and Bi only: the outputs the
+// reference writes between the two parts (spectra, snapshots) may use every
+// other field as scratch.
+int gev_sim_step_particles(gev_sim *s) {
+  if (!s) return GEV_EINVAL;
+  gev_ctx *ctx = s->ctx;
+  gev_sim_state &st = s->st;
+  const int N = ctx->N;
+  const double dx = 1.0 / (double)N;
+  const double fourpiG = st.fourpiG;
+  double a = st.a;
+  const gev_cosmology &cm = st.cosmo;
 
   // particles (main.cpp:764-822): the kick at a, the background half step, the
   // drift at the new a -- the host runs the RK4 first so that one fused pass
@@ -250,6 +267,11 @@ int gev_sim_step(gev_sim *s) {
   st.dtau = (st.Cf * dx < st.steplimit / H) ? st.Cf * dx : st.steplimit / H;  // main.cpp:869-872
   st.cycle++;
   return GEV_OK;
+}
+
+int gev_sim_step(gev_sim *s) {
+  const int rc = gev_sim_step_fields(s);
+  return rc ? rc : gev_sim_step_particles(s);
 }
 
 }  // extern "C"

@@ -618,3 +618,64 @@ def _sim_restart(sim, path, flags=0):
 
 Sim.hibernate = _sim_hibernate
 Sim.restart = _sim_restart
+
+
+# ------------------------------------------------------- spectrum outputs --
+MASK_PHI, MASK_CHI, MASK_POT, MASK_B, MASK_T00, MASK_RBARE, MASK_HIJ, MASK_DELTA, MASK_DBARE = (
+    1, 2, 4, 8, 16, 64, 128, 4096, 8192)
+
+
+class PkSettings(ctypes.Structure):
+    _fields_ = [("out_pk", _i), ("numbins", _i), ("boxsize", _d), ("z_target", _d), ("exact_output", _i),
+                ("output_path", ctypes.c_char_p), ("basename_pk", ctypes.c_char_p)]
+
+
+_PK_SIGS = {
+    "gev_write_power_spectrum": [_vp, _vp, _vp, _vp, _vp, _i, _d, _d, ctypes.c_char_p, ctypes.c_char_p, _d, _d, _i],
+    "gev_sim_write_spectra": [_vp, ctypes.POINTER(PkSettings), _i],
+    "gev_sim_step_fields": [_vp],
+    "gev_sim_step_particles": [_vp],
+}
+
+
+def _pk_lib():
+    L = _io_lib()
+    if not getattr(L, "_pk_ready", False):
+        for name, args in _PK_SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L._pk_ready = True
+    return L
+
+
+def write_power_spectrum(kbin, power, kscatter, pscatter, occupation, rescalek, rescalep, filename, description, a,
+                         z_target=-1.0, exact_output=False):
+    """writePowerSpectrum (tools.hpp:268-345): host code, no GPU needed."""
+    arrs = [np.ascontiguousarray(x, np.float64) for x in (kbin, power, kscatter, pscatter)]
+    occ = np.ascontiguousarray(occupation, np.int32)
+    rc = _pk_lib().gev_write_power_spectrum(*[x.ctypes.data for x in arrs], occ.ctypes.data, len(occ), rescalek,
+                                            rescalep, os.fsencode(filename), description.encode(), a, z_target,
+                                            1 if exact_output else 0)
+    if rc != OK:
+        raise GevError("gev_write_power_spectrum failed (%d)" % rc)
+
+
+def _sim_write_spectra(sim, out_pk, numbins, boxsize, pkcount, output_path="", basename_pk="pk_", z_target=-1.0,
+                       exact_output=False):
+    cfg = PkSettings(out_pk, numbins, boxsize, z_target, 1 if exact_output else 0, os.fsencode(output_path),
+                     os.fsencode(basename_pk))
+    _check(_pk_lib().gev_sim_write_spectra(sim.handle, ctypes.byref(cfg), pkcount), sim.ctx, "gev_sim_write_spectra")
+
+
+def _sim_step_fields(sim):
+    _check(_pk_lib().gev_sim_step_fields(sim.handle), sim.ctx, "gev_sim_step_fields")
+
+
+def _sim_step_particles(sim):
+    _check(_pk_lib().gev_sim_step_particles(sim.handle), sim.ctx, "gev_sim_step_particles")
+
+
+Sim.write_spectra = _sim_write_spectra
+Sim.step_fields = _sim_step_fields
+Sim.step_particles = _sim_step_particles

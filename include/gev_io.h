@@ -60,8 +60,9 @@ typedef struct {
  * exact_output = 0: positions * BoxSize, velocities * rescale / time (the
  * default build).  exact_output = 1: the EXACT_OUTPUT_REDSHIFTS build -- each
  * particle drifts by dtau_pos with its CIC-interpolated phi and kicks by
- * dtau_vel with the CIC gradient of phi (phi may be NULL: no correction
- * terms, the drift still applies).  id_bytes: GADGET_ID_BYTES, 8 or 4. */
+ * dtau_vel with the CIC gradient of phi; phi is required (main.cpp always
+ * passes it; without it the reference's correction carries the previous
+ * particle's integer part as phi).  id_bytes: GADGET_ID_BYTES, 8 or 4. */
 int gev_gadget2_save(gev_ctx *ctx, gev_pcls *p, const char *filename, const gev_gadget2_header *hdr,
                      int tracer_factor, double dtau_pos, double dtau_vel, const gev_field *phi, int exact_output,
                      int id_bytes);
@@ -104,6 +105,46 @@ int gev_checkpoint_info_read(const char *path, gev_checkpoint_info *info);
 /* the whole simulation of gev_sim.h */
 int gev_sim_hibernate(gev_sim *s, const char *path);
 int gev_sim_restart(gev_sim *s, const char *path, int flags);
+
+/* power-spectrum outputs.
+ * writePowerSpectrum (tools.hpp:268-345): the ASCII table of one spectrum (k,
+ * P(k), sigma(k), sigma(P), count per occupied bin, k / rescalek and
+ * P / rescalep).  exact_output = the EXACT_OUTPUT_REDSHIFTS build: when
+ * 1/a < z_target + 1 and the file already holds the spectrum written one cycle
+ * earlier, the table is interpolated linearly in redshift to z_target. */
+int gev_write_power_spectrum(const double *kbin, const double *power, const double *kscatter, const double *pscatter,
+                             const int *occupation, int numbins, double rescalek, double rescalep,
+                             const char *filename, const char *description, double a, double z_target,
+                             int exact_output);
+
+/* the output masks of metadata.hpp:56-71 that a CDM-only GR run writes */
+#define GEV_MASK_PHI 1
+#define GEV_MASK_CHI 2
+#define GEV_MASK_POT 4
+#define GEV_MASK_B 8
+#define GEV_MASK_T00 16
+#define GEV_MASK_RBARE 64
+#define GEV_MASK_HIJ 128
+#define GEV_MASK_DELTA 4096
+#define GEV_MASK_DBARE 8192
+
+typedef struct {
+  int out_pk;              /* sim.out_pk: an OR of GEV_MASK_* */
+  int numbins;             /* sim.numbins */
+  double boxsize;          /* sim.boxsize [Mpc/h] */
+  double z_target;         /* sim.z_pk[pkcount] (read by exact_output) */
+  int exact_output;        /* the EXACT_OUTPUT_REDSHIFTS build */
+  const char *output_path; /* sim.output_path */
+  const char *basename_pk; /* sim.basename_pk */
+} gev_pk_settings;
+
+/* writeSpectra (output.hpp:1762-2204) for the CDM particles of a GR simulation,
+ * called between gev_sim_step_fields and gev_sim_step_particles as main.cpp
+ * calls it: the spectra are binned on the GPU (gev_cross_spectrum) and written
+ * as <output_path><basename_pk><pkcount %03d>_<name>.dat with the reference's
+ * descriptions and normalisations.  Uses source, Sij, scalarFT and SijFT as
+ * scratch, as the reference does. */
+int gev_sim_write_spectra(gev_sim *s, const gev_pk_settings *cfg, int pkcount);
 
 #ifdef __cplusplus
 }

@@ -50,6 +50,13 @@ int gev_sim_field(gev_sim *s, int which, gev_field **out);
 int gev_sim_particles(gev_sim *s, gev_pcls **out);
 /* one cycle: deposits, phi / chi / B solves, kick, drift, background, next dtau */
 int gev_sim_step(gev_sim *s);
+/* the same cycle in its two parts, for a loop that writes outputs where
+ * main.cpp writes them (between the field solves and the particle update):
+ * gev_sim_step_fields = main.cpp:372-598 (stress-energy, phi, chi, B);
+ * gev_sim_step_particles = main.cpp:743-872 (kick, drift, background, dtau).
+ * Between the two, source, Sij, scalarFT and SijFT are free scratch. */
+int gev_sim_step_fields(gev_sim *s);
+int gev_sim_step_particles(gev_sim *s);
 
 /* Zel'dovich initial conditions at z_in generated on the device, following the
  * power-spectrum branch of generateIC_basic (ic_basic.hpp:1626-2259): sc1

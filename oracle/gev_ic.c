@@ -322,6 +322,7 @@ int gevo_ic_generate(gevo_sim *s, const gevo_icparams *ic) {
 void gevo_power_spectrum(int N, const double *FTd, int ncomp, int symmetric, int numbins, int deconvolve,
                          double *kbin, double *power, double *kscatter, double *pscatter, int *occupation) {
   const int NH = N / 2 + 1;
+  if (N < 2) return;
   const size_t NK = (size_t)N * N * NH;
   double *typek2 = (double *)malloc(sizeof(double) * N), *sinc = (double *)malloc(sizeof(double) * N);
   int i;

@@ -175,3 +175,46 @@ long gevo_gadget2_load(const char *fname, int N, gevo_part *dst, long cap, void 
   gevo_sort(N, (long)S, dst, NULL);
   return (long)S;
 }
+
+/* writePowerSpectrum (tools.hpp:268-345) on one rank; exact = the
+ * EXACT_OUTPUT_REDSHIFTS build, which interpolates with the spectrum that an
+ * earlier call left in the same file when 1/a < z_target + 1 */
+int gevo_write_power_spectrum(const double *kbin, const double *power, const double *kscatter, const double *pscatter,
+                              const int *occupation, int numbins, double rescalek, double rescalep,
+                              const char *filename, const char *description, double a, double z_target, int exact) {
+  double *power2 = (double *)malloc(sizeof(double) * (size_t)(numbins > 0 ? numbins : 1));
+  for (int i = 0; i < numbins; i++) power2[i] = power[i] / rescalep;
+  if (exact && 1. / a < z_target + 1.) {
+    FILE *in = fopen(filename, "r");
+    if (in) {
+      double w = 1.;
+      if (fscanf(in, "%*[^\n]\n") < 0) w = 1.;
+      if (fscanf(in, "# redshift z=%lf\n", &w) != 1) {
+        w = 1.;
+      } else {
+        w = (w - z_target) / (1. + w - 1. / a);
+        if (fscanf(in, "%*[^\n]\n") < 0) w = w;
+        for (int i = 0; i < numbins; i++)
+          if (occupation[i] > 0 && fscanf(in, " %*e %le %*e %*e %*d \n", power2 + i) != 1) break;
+      }
+      fclose(in);
+      for (int i = 0; i < numbins; i++) power2[i] = (1. - w) * power2[i] + w * power[i] / rescalep;
+      a = 1. / (z_target + 1.);
+    }
+  }
+  FILE *out = fopen(filename, "w");
+  if (!out) {
+    free(power2);
+    return -1;
+  }
+  fprintf(out, "# %s\n", description);
+  fprintf(out, "# redshift z=%f\n", (1. / a) - 1.);
+  fprintf(out, "# k              Pk             sigma(k)       sigma(Pk)      count\n");
+  for (int i = 0; i < numbins; i++)
+    if (occupation[i] > 0)
+      fprintf(out, "  %e   %e   %e   %e   %d\n", kbin[i] / rescalek, exact ? power2[i] : power[i] / rescalep,
+              kscatter[i] / rescalek, pscatter[i] / rescalep / sqrt(occupation[i]), occupation[i]);
+  fclose(out);
+  free(power2);
+  return 0;
+}

@@ -173,6 +173,11 @@ int gevo_gadget2_save(const char *fname, int N, long np, const gevo_part *p, con
  * returns their number or -1 */
 long gevo_gadget2_load(const char *fname, int N, gevo_part *dst, long cap, void *hdr256, int id_bytes);
 
+/* writePowerSpectrum (tools.hpp:268-345); exact = the EXACT_OUTPUT_REDSHIFTS build */
+int gevo_write_power_spectrum(const double *kbin, const double *power, const double *kscatter, const double *pscatter,
+                              const int *occupation, int numbins, double rescalek, double rescalep,
+                              const char *filename, const char *description, double a, double z_target, int exact);
+
 #ifdef __cplusplus
 }
 #endif

@@ -467,3 +467,56 @@ def gadget2_load(fname, N, cap, id_bytes=8, impl=None):
     if n < 0 or n > cap:
         raise RuntimeError("gadget2_load failed")
     return out[:n], hb.tobytes()
+
+
+# ------------------------------------------------------- spectrum tables --
+_TOOLS_REF = None
+
+
+def _tools_ref():
+    """The reference's own tools.hpp spectra and writer (oracle/_ref/libgevref_tools.so)."""
+    global _TOOLS_REF
+    if _TOOLS_REF is None:
+        path = os.path.join(HERE, "_ref", "libgevref_tools.so")
+        if not os.path.exists(path):
+            if build_ref() is None:
+                return None
+        R = _load(path)
+        R.gevref_cross_spectrum.argtypes = [ctypes.c_int, _vp, _vp] + [ctypes.c_int] * 6 + [_vp] * 5
+        for tag in ("plain", "exact"):
+            getattr(R, "gevref_write_power_spectrum_" + tag).argtypes = [_vp] * 5 + [
+                ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_double,
+                ctypes.c_double]
+        _TOOLS_REF = R
+    return _TOOLS_REF
+
+
+def cross_spectrum_ref(F1, F2, numbins, deconvolve=True, ktype=1, comp1=-1, comp2=-1):
+    """extractCrossSpectrum of the reference itself (spectra (ncomp, N, N, N/2+1))."""
+    F1 = _c(F1, np.complex128)
+    F2 = _c(F2, np.complex128)
+    if F1.ndim == 3:
+        F1, F2 = F1[None], F2[None]
+    N = F1.shape[-2]
+    out = [np.zeros(numbins) for _ in range(4)] + [np.zeros(numbins, np.int32)]
+    _tools_ref().gevref_cross_spectrum(N, _p(F1), _p(F2), F1.shape[0], numbins, int(deconvolve), ktype, comp1, comp2,
+                                       *[_p(o) for o in out])
+    return tuple(out)
+
+
+def write_power_spectrum(kbin, power, kscatter, pscatter, occupation, rescalek, rescalep, filename, description, a,
+                         z_target=-1.0, exact=False, impl=None):
+    """writePowerSpectrum: the restatement, or (impl='ref') the reference's own."""
+    arrs = [np.ascontiguousarray(x, np.float64) for x in (kbin, power, kscatter, pscatter)]
+    occ = np.ascontiguousarray(occupation, np.int32)
+    args = [_p(x) for x in arrs] + [_p(occ), len(occ), rescalek, rescalep, os.fsencode(filename), description.encode(),
+                                      a, z_target]
+    if impl == "ref":
+        getattr(_tools_ref(), "gevref_write_power_spectrum_" + ("exact" if exact else "plain"))(*args)
+    else:
+        L = lib()
+        L.gevo_write_power_spectrum.argtypes = [_vp] * 5 + [ctypes.c_int, ctypes.c_double, ctypes.c_double,
+                                                           ctypes.c_char_p, ctypes.c_char_p, ctypes.c_double,
+                                                           ctypes.c_double, ctypes.c_int]
+        if L.gevo_write_power_spectrum(*args, 1 if exact else 0) != 0:
+            raise RuntimeError("write_power_spectrum failed")

@@ -1,6 +1,7 @@
 // mpi_io_shim.hpp -- single-rank stand-ins for the MPI-IO calls and the
 // LATfield2 `parallel` object that Particles_gevolution.hpp's Gadget-2 writer
-// and reader use (Particles_gevolution.hpp:30-251, 574-665).  Files are plain
+// and reader (Particles_gevolution.hpp:30-251, 574-665) and tools.hpp's spectra
+// use.  Files are plain
 // stdio; one rank owns the whole grid, so the rank-to-rank particle counts are a
 // mailbox that a rank reads back from itself.
 //
@@ -33,6 +34,13 @@ typedef GevShimFile *MPI_File;
 #define MPI_BYTE 1
 #define MPI_FLOAT 4
 #define MPI_SEEK_SET 0
+
+// one rank: a reduction onto rank 0 in place leaves the buffer as it is
+#define MPI_IN_PLACE ((void *)1)
+#define MPI_DOUBLE 8
+#define MPI_INT 4
+#define MPI_SUM 0
+inline int MPI_Reduce(const void *, void *, int, MPI_Datatype, int, int, MPI_Comm) { return 0; }
 
 inline int MPI_File_open(MPI_Comm, const char *name, int mode, MPI_Info, MPI_File *fh) {
   FILE *f = 0;
@@ -103,6 +111,13 @@ struct GevShimParallel {
   void broadcast_dim0(T &, int) {}
   template <class T>
   void broadcast(T &, int) {}
+  // one rank: reductions leave their operands as they are
+  template <class T>
+  void max(T &) {}
+  template <class T>
+  void sum(T &) {}
+  template <class T>
+  void sum(T *, int) {}
 };
 static GevShimParallel parallel;
 

@@ -6,13 +6,16 @@ sources are present).
     python tests/golden/make_golden.py
 
     python tests/golden/make_golden.py gadget     # only the Gadget-2 files
+    python tests/golden/make_golden.py spectra    # only the power spectra
 
 Every hot-path function is run on seeded random inputs at N = 8 and N = 12
 (a radix-3 size), and a full initial condition plus three cycles of the main
 loop are run at N = 8.  Gadget-2 snapshots are written and read back by the
 reference's own Particles_gevolution.hpp (oracle/_ref/libgevref_gadget.so) in
-three of its build variants.  Inputs and the reference's outputs are stored in
-golden_N{8,12}.npz, golden_run_N8.npz and golden_gadget2_N8.npz;
+three of its build variants, and tools.hpp's spectra and table writer are run
+on random spectra.  Inputs and the reference's outputs are stored in
+golden_N{8,12}.npz, golden_run_N8.npz, golden_gadget2_N8.npz and
+golden_spectra_N12.npz;
 tests/test_oracle_golden.py checks the CPU restatement against them and the GPU
 tests check the CUDA path.
 """
@@ -138,16 +141,58 @@ def gadget(N=8, seed=103):
     np.savez_compressed(os.path.join(HERE, "golden_gadget2_N%d.npz" % N), **d)
 
 
+SPECTRA_CASES = (  # (name, field, field2 or None, deconvolve, comp1, comp2)
+    ("auto1_dec", "F1", None, 1, -1, -1), ("auto1", "F1", None, 0, -1, -1), ("auto3", "F3", None, 0, -1, -1),
+    ("auto6", "F6", None, 0, -1, -1), ("auto6_dec", "F6", None, 1, -1, -1), ("cross1", "F1", "G1", 1, -1, -1),
+    ("comps6", "F6", None, 1, 0, 3))
+
+
+def spectra(N=12, seed=104, numbins=10):
+    """extractCrossSpectrum and writePowerSpectrum of the reference's own tools.hpp."""
+    import tempfile
+    rng = np.random.default_rng(seed)
+    NH = N // 2 + 1
+    d = {}
+    for name, nc in (("F1", 1), ("G1", 1), ("F3", 3), ("F6", 6)):
+        d[name] = rng.standard_normal((nc, N, N, NH)) + 1j * rng.standard_normal((nc, N, N, NH))
+    for name, f1, f2, dec, c1, c2 in SPECTRA_CASES:
+        out = G.cross_spectrum_ref(d[f1], d[f2 or f1], numbins, bool(dec), 1, c1, c2)
+        for k, v in zip(("kbin", "power", "kscatter", "pscatter", "occupation"), out):
+            d["%s_%s" % (name, k)] = v
+    # the table writer: default build; EXACT_OUTPUT_REDSHIFTS before and after z_target = 2
+    kb, pw, ks, ps, occ = (d["auto1_dec_" + k] for k in ("kbin", "power", "kscatter", "pscatter", "occupation"))
+    occ = occ.copy()
+    occ[3] = 0  # an empty bin: no row, skipped by the interpolation's reader
+    d["table_occupation"] = occ
+    pw2 = pw * 1.37
+    d["table_power2"] = pw2
+    with tempfile.TemporaryDirectory() as tmp:
+        f = os.path.join(tmp, "pk.dat")
+        G.write_power_spectrum(kb, pw, ks, ps, occ, 320.0, 7.5e5, f, "power spectrum of phi", 0.3, 2.0, impl="ref")
+        d["table_plain"] = np.frombuffer(open(f, "rb").read(), np.uint8).copy()
+        os.remove(f)
+        # one cycle before z = 2 (1/a - 1 = 2.1 > 2), then one after (1.9 < 2)
+        G.write_power_spectrum(kb, pw, ks, ps, occ, 320.0, 7.5e5, f, "power spectrum of phi", 1 / 3.1, 2.0, True,
+                               impl="ref")
+        d["table_exact_before"] = np.frombuffer(open(f, "rb").read(), np.uint8).copy()
+        G.write_power_spectrum(kb, pw2, ks, ps, occ, 320.0, 7.5e5, f, "power spectrum of phi", 1 / 2.9, 2.0, True,
+                               impl="ref")
+        d["table_exact_after"] = np.frombuffer(open(f, "rb").read(), np.uint8).copy()
+    np.savez_compressed(os.path.join(HERE, "golden_spectra_N%d.npz" % N), **d)
+
+
 if __name__ == "__main__":
     if G.ref() is None:
         sys.exit("the reference sources are not available here; golden vectors cannot be regenerated")
-    which = sys.argv[1:] or ["hotpath", "gadget"]
+    which = sys.argv[1:] or ["hotpath", "gadget", "spectra"]
     if "hotpath" in which:
         one(8, 101)
         one(12, 102)
         run(8, 3)
     if "gadget" in which:
         gadget(8, 103)
+    if "spectra" in which:
+        spectra(12, 104)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

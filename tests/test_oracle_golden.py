@@ -2,6 +2,8 @@
 reference's own gevolution.hpp (tests/golden/make_golden.py).  With the same
 compile flags the two agree bit for bit; the assertions allow one rounding of
 slack so that a different compiler or CPU (the Arm GPU hosts) still passes."""
+import os
+
 import numpy as np
 import pytest
 
@@ -197,3 +199,55 @@ def test_gadget2_against_live_reference(oracle, tmp_path):
         pa, _ = oracle.gadget2_load(a, N, n, idb)
         pb, _ = oracle.gadget2_load(b, N, n, idb, impl="ref")
         assert pa.tobytes() == pb.tobytes(), tag
+
+
+SPECTRA_AUTO = (("auto1_dec", "F1", True), ("auto1", "F1", False), ("auto3", "F3", False), ("auto6", "F6", False),
+                ("auto6_dec", "F6", True))
+
+
+@pytest.mark.parametrize("name,field,dec", SPECTRA_AUTO)
+def test_power_spectrum_matches_reference(oracle, name, field, dec):
+    """extractPowerSpectrum (tools.hpp:53-240) restated: bit-identical to the
+    reference's own on scalar, vector and symmetric-tensor spectra."""
+    g = golden("golden_spectra_N12.npz")
+    F = g[field]
+    got = oracle.power_spectrum(F, 10, symmetric=F.shape[0] == 6, deconvolve=dec)
+    for k, v in zip(("kbin", "power", "kscatter", "pscatter", "occupation"), got):
+        assert v.tobytes() == g["%s_%s" % (name, k)].tobytes(), k
+
+
+def _table_inputs(g):
+    return (g["auto1_dec_kbin"], g["auto1_dec_power"], g["auto1_dec_kscatter"], g["auto1_dec_pscatter"],
+            g["table_occupation"])
+
+
+def _write_tables(write, tmp_path):
+    """The golden sequence: a default-build table, then an EXACT_OUTPUT_REDSHIFTS
+    table one cycle before z = 2 and its interpolated successor one cycle after."""
+    g = golden("golden_spectra_N12.npz")
+    kb, pw, ks, ps, occ = _table_inputs(g)
+    f = str(tmp_path / "pk.dat")
+    write(kb, pw, ks, ps, occ, 320.0, 7.5e5, f, "power spectrum of phi", 0.3, 2.0, False)
+    plain = open(f, "rb").read()
+    os.remove(f)
+    write(kb, pw, ks, ps, occ, 320.0, 7.5e5, f, "power spectrum of phi", 1 / 3.1, 2.0, True)
+    before = open(f, "rb").read()
+    write(kb, g["table_power2"], ks, ps, occ, 320.0, 7.5e5, f, "power spectrum of phi", 1 / 2.9, 2.0, True)
+    after = open(f, "rb").read()
+    assert plain == g["table_plain"].tobytes()
+    assert before == g["table_exact_before"].tobytes()
+    assert after == g["table_exact_after"].tobytes()
+
+
+def test_power_spectrum_table_matches_reference(oracle, tmp_path):
+    """writePowerSpectrum (tools.hpp:268-345) restated, with its
+    EXACT_OUTPUT_REDSHIFTS interpolation: byte-identical tables."""
+    _write_tables(lambda *a: oracle.write_power_spectrum(*a[:11], exact=a[11]), tmp_path)
+
+
+def test_library_table_writer_matches_reference(tmp_path):
+    """The library's own table writer (host code of the C-ABI, no GPU involved)."""
+    import build
+    build.build()
+    import gev_gb300
+    _write_tables(lambda *a: gev_gb300.write_power_spectrum(*a[:11], exact_output=a[11]), tmp_path)
