@@ -406,32 +406,48 @@ __global__ void __launch_bounds__(256) k_dep_gather(PclsArrays P, const uint32_t
       s12 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f010), f011);  // l0 + l1 + l2 + l3
     }
     long long a00 = 0, ad0 = 0, ad1 = 0, ad2 = 0, ao01 = 0, ao02 = 0, ao12 = 0;
+    // the contributions of particle j to this node, the node being corner (dx, dy, dz)
+    // of the particle's cell
+    auto add = [&](uint32_t j, int dx, int dy, int dz) {
+      const float u0 = P.rx[j], u1 = P.ry[j], u2 = P.rz[j];
+      const float w0 = dx ? u0 : __fsub_rn(1.f, u0), w1 = dy ? u1 : __fsub_rn(1.f, u1),
+                  w2 = dz ? u2 : __fsub_rn(1.f, u2);
+      const float w = __fmul_rn(__fmul_rn(w0, w1), w2);
+      if (DO00) a00 += (long long)A.q00[j] * (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(A.rT[j], pn))), sg00);
+      if (DOIJ) {
+        const float f = A.fT[j];
+        const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(f, pn))), sgij);
+        ad0 += (long long)A.qd0[j] * G;
+        ad1 += (long long)A.qd1[j] * G;
+        ad2 += (long long)A.qd2[j] * G;
+        const float qf = __fmul_rn(0.25f, f);
+        if (dx == 0 && dy == 0)
+          ao01 += (long long)A.qo01[j] * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, s01))), sgij);
+        if (dx == 0 && dz == 0)
+          ao02 += (long long)A.qo02[j] * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, s02))), sgij);
+        if (dy == 0 && dz == 0)
+          ao12 += (long long)A.qo12[j] * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, s12))), sgij);
+      }
+    };
+    // the 4 cell pairs (x - 1, x) of rows (y - dy, z - dz): all their bounds first;
+    // for x > 0 the two cells' particles are one contiguous run of the store
+    const unsigned cb[4] = {i, i + b.zm, i + b.ym, i + b.ym + b.zm};
+    uint32_t s0[4], s1[4], s2[4];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {  // the node is corner (dx, dy, dz) of cell (x - dx, y - dy, z - dz)
-      const int dx = (k >> 2) & 1, dy = (k >> 1) & 1, dz = k & 1;
-      const unsigned c = i + (dx ? b.xm : 0u) + (dy ? b.ym : 0u) + (dz ? b.zm : 0u);
-      const uint32_t j0 = start[c], j1 = start[c + 1];
-      for (uint32_t j = j0; j < j1; ++j) {
-        const float u0 = P.rx[j], u1 = P.ry[j], u2 = P.rz[j];
-        const float w0 = dx ? u0 : __fsub_rn(1.f, u0), w1 = dy ? u1 : __fsub_rn(1.f, u1),
-                    w2 = dz ? u2 : __fsub_rn(1.f, u2);
-        const float w = __fmul_rn(__fmul_rn(w0, w1), w2);
-        if (DO00)
-          a00 += (long long)A.q00[j] * (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(A.rT[j], pn))), sg00);
-        if (DOIJ) {
-          const float f = A.fT[j];
-          const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(f, pn))), sgij);
-          ad0 += (long long)A.qd0[j] * G;
-          ad1 += (long long)A.qd1[j] * G;
-          ad2 += (long long)A.qd2[j] * G;
-          const float qf = __fmul_rn(0.25f, f);
-          if (dx == 0 && dy == 0)
-            ao01 += (long long)A.qo01[j] * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, s01))), sgij);
-          if (dx == 0 && dz == 0)
-            ao02 += (long long)A.qo02[j] * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, s02))), sgij);
-          if (dy == 0 && dz == 0)
-            ao12 += (long long)A.qo12[j] * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, s12))), sgij);
-        }
+    for (int q = 0; q < 4; ++q) {
+      s0[q] = start[cb[q] + b.xm];
+      s1[q] = start[cb[q]];
+      s2[q] = start[cb[q] + 1];
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int dy = q >> 1, dz = q & 1;
+      if (x > 0) {
+        for (uint32_t j = s0[q]; j < s2[q]; ++j) add(j, j < s1[q] ? 1 : 0, dy, dz);
+      } else {
+        for (uint32_t j = s1[q]; j < s2[q]; ++j) add(j, 0, dy, dz);
+        const uint32_t t1 = start[cb[q] + b.xm + 1];
+        for (uint32_t j = s0[q]; j < t1; ++j) add(j, 1, dy, dz);
       }
     }
     if (DO00) {
