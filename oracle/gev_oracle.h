@@ -120,21 +120,30 @@ int gevo_sim_step(gevo_sim *s);
 double gevo_next_dtau(const gevo_sim *s);
 
 /* ---- initial conditions (restating the mPk path of ic_basic.hpp) ----
- * gaussian potential: unit-variance complex modes from a counter-based hash,
- * scaled by sqrt(P(k)) of a BBKS spectrum; see gev_ic.c */
+ * the displacement potential from the sitmo stream, the CIC kernel and the
+ * spline of a tabulated BBKS spectrum; see gev_ic.c */
 typedef struct {
   double h, Omega_cdm, Omega_b, n_s, sigma8, z_in, boxsize, Cf, steplimit;
-  uint64_t seed;
+  uint64_t seed;     /* the sitmo seed is its low 32 bits, (unsigned int) ic.seed */
   int ksphere;
+  int correct_displacement; /* ICFLAG_CORRECT_DISPLACEMENT: the template's CIC kernel */
 } gevo_icparams;
 /* BBKS linear P(k) [(Mpc/h)^3] at z_in for k [h/Mpc], sigma8-normalised */
 double gevo_ic_pk(const gevo_icparams *ic, double k);
 /* amplitude factor A*D(z_in)^2/D(0)^2 so that P = amp * k^n_s T(k)^2 */
 double gevo_ic_pk_amplitude(const gevo_icparams *ic);
 double gevo_bbks_T(double k, double Gamma);
-uint64_t gevo_hash64(uint64_t seed, uint64_t counter);
 void gevo_ic_potential_k(int N, const gevo_icparams *ic, double *potFT);
 int gevo_ic_generate(gevo_sim *s, const gevo_icparams *ic);
+
+/* the sitmo stream (prng_engine.hpp) and generateDisplacementField's layout of it */
+void gevo_sitmo_block(uint32_t seed, uint64_t block, uint64_t out[4]);
+uint32_t gevo_sitmo_draw(uint32_t seed, uint64_t d);
+void gevo_spline_init(int n, const double *x, const double *y, double *c);
+double gevo_spline_eval(int n, const double *x, const double *y, const double *c, double v);
+void gevo_displacement_field(int N, double *F, double coeff, int n, const double *x, const double *y, uint32_t seed,
+                             int ksphere);
+void gevo_cic_kernel(int N, long numpcl, const float *pcldata, int numtile, double K[27]);
 
 /* ---- power spectrum (tools.hpp:53-212, extractPowerSpectrum) ---- */
 void gevo_power_spectrum(int N, const double *FT, int ncomp, int symmetric, int numbins,

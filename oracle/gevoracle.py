@@ -33,7 +33,7 @@ class Cosmo(ctypes.Structure):
 class ICParams(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in
                 ("h", "Omega_cdm", "Omega_b", "n_s", "sigma8", "z_in", "boxsize", "Cf", "steplimit")] + [
-                    ("seed", ctypes.c_uint64), ("ksphere", ctypes.c_int)]
+                    ("seed", ctypes.c_uint64), ("ksphere", ctypes.c_int), ("correct_displacement", ctypes.c_int)]
 
 
 class SimStruct(ctypes.Structure):
@@ -79,8 +79,6 @@ def lib():
         L.gevo_ic_pk.restype = ctypes.c_double
         L.gevo_ic_pk_amplitude.restype = ctypes.c_double
         L.gevo_bbks_T.restype = ctypes.c_double
-        L.gevo_hash64.restype = ctypes.c_uint64
-        L.gevo_hash64.argtypes = [ctypes.c_uint64, ctypes.c_uint64]
         for f in ("gevo_poisson", "gevo_project_vector"):
             getattr(L, f).argtypes = [ctypes.c_int, _vp, _vp, ctypes.c_double, ctypes.c_double]
         L.gevo_evolve_vector.argtypes = [ctypes.c_int, _vp, _vp, ctypes.c_double]
@@ -322,9 +320,9 @@ def power_spectrum(F, numbins, symmetric=False, deconvolve=True):
 
 # ------------------------------------------------------------ simulation ----
 def default_icparams(N, boxsize, seed=1, z_in=100.0, Cf=48.0, steplimit=0.04, Omega_cdm=0.27, Omega_b=0.05,
-                     sigma8=0.81, n_s=0.96, h=0.67, ksphere=1):
+                     sigma8=0.81, n_s=0.96, h=0.67, ksphere=1, correct_displacement=1):
     return dict(h=h, Omega_cdm=Omega_cdm, Omega_b=Omega_b, n_s=n_s, sigma8=sigma8, z_in=z_in, boxsize=boxsize, Cf=Cf,
-                steplimit=steplimit, seed=seed, ksphere=ksphere)
+                steplimit=steplimit, seed=seed, ksphere=ksphere, correct_displacement=correct_displacement)
 
 
 class Sim:
@@ -520,3 +518,94 @@ def write_power_spectrum(kbin, power, kscatter, pscatter, occupation, rescalek, 
                                                            ctypes.c_double, ctypes.c_int]
         if L.gevo_write_power_spectrum(*args, 1 if exact else 0) != 0:
             raise RuntimeError("write_power_spectrum failed")
+
+
+# ------------------------------------------------------ initial conditions --
+_IC_REF = None
+
+
+def _ic_ref():
+    """The reference's sitmo engine, generateCICKernel and generateDisplacementField
+    (oracle/_ref/libgevref_ic.so)."""
+    global _IC_REF
+    if _IC_REF is None:
+        path = os.path.join(HERE, "_ref", "libgevref_ic.so")
+        if not os.path.exists(path):
+            if build_ref() is None:
+                return None
+        R = _load(path)
+        R.gevref_sitmo_draws.argtypes = [ctypes.c_uint, ctypes.c_ulonglong, ctypes.c_long, _vp]
+        R.gevref_displacement_field.argtypes = [ctypes.c_int, _vp, ctypes.c_double, ctypes.c_int, _vp, _vp,
+                                                ctypes.c_uint, ctypes.c_int]
+        R.gevref_cic_kernel.argtypes = [ctypes.c_int, ctypes.c_long, _vp, ctypes.c_int, _vp]
+        _IC_REF = R
+    return _IC_REF
+
+
+def sitmo_draws(seed, d0, n, impl=None):
+    """Draws [d0, d0 + n) of sitmo::prng_engine seeded with seed."""
+    out = np.zeros(n, np.uint32)
+    if impl == "ref":
+        _ic_ref().gevref_sitmo_draws(seed, d0, n, _p(out))
+    else:
+        L = lib()
+        L.gevo_sitmo_draw.argtypes = [ctypes.c_uint32, ctypes.c_uint64]
+        L.gevo_sitmo_draw.restype = ctypes.c_uint32
+        for i in range(n):
+            out[i] = L.gevo_sitmo_draw(seed, d0 + i)
+    return out
+
+
+def displacement_field(K, coeff, x, y, seed, ksphere, impl=None):
+    """generateDisplacementField<0> on the kernel spectrum K (N, N, N/2+1)."""
+    F = np.ascontiguousarray(K, np.complex128).copy()
+    N = F.shape[0]
+    x = np.ascontiguousarray(x, np.float64)
+    y = np.ascontiguousarray(y, np.float64)
+    if impl == "ref":
+        _ic_ref().gevref_displacement_field(N, _p(F), coeff, len(x), _p(x), _p(y), seed, ksphere)
+    else:
+        L = lib()
+        L.gevo_displacement_field.argtypes = [ctypes.c_int, _vp, ctypes.c_double, ctypes.c_int, _vp, _vp,
+                                              ctypes.c_uint32, ctypes.c_int]
+        L.gevo_displacement_field(N, _p(F), coeff, len(x), _p(x), _p(y), seed, ksphere)
+    return F
+
+
+def cic_kernel(N, pcldata=None, numtile=1, impl=None):
+    """generateCICKernel as an N^3 field (pcldata None: the standard kernel)."""
+    pc = None if pcldata is None else np.ascontiguousarray(pcldata, np.float32).reshape(-1)
+    npcl = 0 if pc is None else len(pc) // 3
+    if impl == "ref":
+        out = np.zeros(N ** 3)
+        _ic_ref().gevref_cic_kernel(N, npcl, None if pc is None else _p(pc), numtile, _p(out))
+        return out.reshape(N, N, N)
+    L = lib()
+    L.gevo_cic_kernel.argtypes = [ctypes.c_int, ctypes.c_long, _vp, ctypes.c_int, _vp]
+    K = np.zeros(27)
+    L.gevo_cic_kernel(N, npcl, None if pc is None else _p(pc), numtile, _p(K))
+    out = np.zeros((N, N, N))
+    for dz in (-1, 0, 1):
+        for dy in (-1, 0, 1):
+            for dx in (-1, 0, 1):
+                out[dz % N, dy % N, dx % N] += K[(dx + 1) + 3 * (dy + 1) + 9 * (dz + 1)]
+    return out
+
+
+SC1_DIGITS = [0, 16, 20, 4, 5, 21, 17, 1, 32, 48, 52, 36, 37, 53, 49, 33, 40, 56, 60, 44, 45, 61, 57, 41, 8, 24, 28,
+              12, 13, 29, 25, 9, 10, 26, 30, 14, 15, 31, 27, 11, 42, 58, 62, 46, 47, 63, 59, 43, 34, 50, 54, 38, 39,
+              55, 51, 35, 2, 18, 22, 6, 7, 23, 19, 3]
+
+
+def sc1_pcldata():
+    """The sc1 template (64 particles of a 4^3 cell-centred lattice) in file order."""
+    return np.array([[0.125 + 0.25 * ((d >> (2 * c)) & 3) for c in range(3)] for d in SC1_DIGITS], np.float32)
+
+
+def ic_spline_knots(N, **params):
+    icp = ICParams(**params)
+    x, y = np.zeros(512), np.zeros(512)
+    L = lib()
+    L.gevo_ic_spline_knots.argtypes = [ctypes.c_int, ctypes.POINTER(ICParams), _vp, _vp]
+    L.gevo_ic_spline_knots(N, ctypes.byref(icp), _p(x), _p(y))
+    return x, y

@@ -32,12 +32,15 @@
 typedef double Real;
 
 #define COUT std::cout
+
 #define FFT_FORWARD 1
 #define FFT_BACKWARD -1
 
 namespace LATfield2 {
 
 enum { symmetric = 1, unsymmetric = 0 };
+// the reduction kinds moveParticles / updateVel accept for their outputs
+enum { SUM = 1, MAX = 2, MIN = 4 };
 
 class Imag {
  public:
@@ -55,6 +58,11 @@ class Imag {
   Imag operator*(const Imag &b) const { return Imag(re_ * b.re_ - im_ * b.im_, re_ * b.im_ + im_ * b.re_); }
   Imag operator*(double d) const { return Imag(re_ * d, im_ * d); }
   Imag operator/(double d) const { return Imag(re_ / d, im_ / d); }
+  // complex quotient (a + bi)(c - di) / (c^2 + d^2): a convention of this shim
+  Imag operator/(const Imag &b) const {
+    const double n = b.re_ * b.re_ + b.im_ * b.im_;
+    return Imag((re_ * b.re_ + im_ * b.im_) / n, (im_ * b.re_ - re_ * b.im_) / n);
+  }
   Imag &operator+=(const Imag &b) { re_ += b.re_; im_ += b.im_; return *this; }
   Imag &operator-=(const Imag &b) { re_ -= b.re_; im_ -= b.im_; return *this; }
   Imag &operator*=(double d) { re_ *= d; im_ *= d; return *this; }
@@ -89,6 +97,9 @@ class Lattice {
   int halo() const { return halo_; }
   int *coordSkip() { return skip_; }
   long ext(int i) const { return size_[i] + 2 * halo_; }
+  // one rank owns every site: the first and last site, x fastest
+  long siteFirst() const { return 0; }
+  long siteLast() const { return (long)size_[0] * size_[1] * size_[2] - 1; }
   long sitesGross() const { return ext(0) * ext(1) * ext(2); }
 };
 
@@ -99,6 +110,12 @@ class Site {
   Site() : lat_(0) { c_[0] = c_[1] = c_[2] = 0; }
   Site(const Lattice &lat) : lat_(&lat) { c_[0] = c_[1] = c_[2] = 0; }
   void initialize(const Lattice &lat) { lat_ = &lat; c_[0] = c_[1] = c_[2] = 0; }
+  void initialize(const Lattice &lat, long index) {
+    lat_ = &lat;
+    c_[0] = (int)(index % lat.size_[0]);
+    c_[1] = (int)((index / lat.size_[0]) % lat.size_[1]);
+    c_[2] = (int)(index / ((long)lat.size_[0] * lat.size_[1]));
+  }
   void first() { c_[0] = c_[1] = c_[2] = 0; }
   bool test() const { return c_[2] < lat_->size_[2]; }
   void next() {
@@ -378,6 +395,35 @@ class Particles {
     relink();
   }
 };
+
+/* scalarProjectionCIC_project (LATfield2): the CIC mass deposit m/dx^3 w of the
+ * oracle (gevo_deposit_mass, which folds its own halo), added to the field */
+template <class part, class part_info, class part_dataType>
+void scalarProjectionCIC_project(Particles<part, part_info, part_dataType> *pcls, Field<Real> *rho) {
+  const int N = pcls->lat_->size_[0];
+  const size_t V = (size_t)N * N * N;
+  std::vector<gevo_part> flat;
+  std::vector<long> cs(V + 1, 0);
+  for (size_t c = 0; c < V; c++) {
+    cs[c] = (long)flat.size();
+    for (typename std::list<part>::iterator it = pcls->field_.cells_[c].parts.begin();
+         it != pcls->field_.cells_[c].parts.end(); ++it) {
+      gevo_part q;
+      for (int l = 0; l < 3; l++) {
+        q.pos[l] = it->pos[l];
+        q.vel[l] = it->vel[l];
+      }
+      q.ID = it->ID;
+      flat.push_back(q);
+    }
+  }
+  cs[V] = (long)flat.size();
+  std::vector<double> out(V, 0.);
+  gevo_deposit_mass(N, (long)flat.size(), flat.data(), cs.data(), pcls->info_.mass, out.data());
+  Site x(rho->lattice());
+  for (x.first(); x.test(); x.next())
+    (*rho)(x) += out[x.coord(0) + (size_t)N * (x.coord(1) + (size_t)N * x.coord(2))];
+}
 
 }  // namespace LATfield2
 

@@ -15,6 +15,7 @@
 #include <unistd.h>
 
 #include <cstdio>
+#include <cstdlib>
 
 typedef long long MPI_Offset;
 typedef int MPI_Status;
@@ -111,6 +112,12 @@ struct GevShimParallel {
   void broadcast_dim0(T &, int) {}
   template <class T>
   void broadcast(T &, int) {}
+  template <class T>
+  void broadcast_dim0(T *, long, int) {}
+  template <class T>
+  void broadcast(T *, long, int) {}
+  void abortForce() { std::abort(); }
+  void barrier() {}
   // one rank: reductions leave their operands as they are
   template <class T>
   void max(T &) {}

@@ -7,6 +7,8 @@ sources are present).
 
     python tests/golden/make_golden.py gadget     # only the Gadget-2 files
     python tests/golden/make_golden.py spectra    # only the power spectra
+    python tests/golden/make_golden.py run        # only the initial conditions and cycles
+    python tests/golden/make_golden.py ic         # only the random stream, kernel, displacement field
 
 Every hot-path function is run on seeded random inputs at N = 8 and N = 12
 (a radix-3 size), and a full initial condition plus three cycles of the main
@@ -14,8 +16,9 @@ loop are run at N = 8.  Gadget-2 snapshots are written and read back by the
 reference's own Particles_gevolution.hpp (oracle/_ref/libgevref_gadget.so) in
 three of its build variants, and tools.hpp's spectra and table writer are run
 on random spectra.  Inputs and the reference's outputs are stored in
-golden_N{8,12}.npz, golden_run_N8.npz, golden_gadget2_N8.npz and
-golden_spectra_N12.npz;
+golden_N{8,12}.npz, golden_run_N8.npz, golden_gadget2_N8.npz,
+golden_spectra_N12.npz and golden_ic.npz (the sitmo stream, generateCICKernel and
+generateDisplacementField of ic_basic.hpp, oracle/_ref/libgevref_ic.so);
 tests/test_oracle_golden.py checks the CPU restatement against them and the GPU
 tests check the CUDA path.
 """
@@ -181,18 +184,40 @@ def spectra(N=12, seed=104, numbins=10):
     np.savez_compressed(os.path.join(HERE, "golden_spectra_N%d.npz" % N), **d)
 
 
+def ic(seed=105):
+    """The reference's sitmo stream, CIC kernel and displacement field."""
+    d = {}
+    for s, d0 in ((7, 0), (7, 1000003), (4294967295, 3 * 65536 ** 3 + 65536 * 17 + 5)):
+        d["draws_%d_%d" % (s, d0)] = G.sitmo_draws(s, d0, 40, impl="ref")
+    for N, nt in ((8, 2), (12, 3), (16, 4)):
+        d["kernel_sc1_N%d" % N] = G.cic_kernel(N, G.sc1_pcldata(), nt, impl="ref")
+    d["kernel_std_N16"] = G.cic_kernel(16, None, 1, impl="ref")
+    rng = np.random.default_rng(seed)
+    for N in (8, 12, 16):
+        K = np.fft.rfftn(d["kernel_sc1_N%d" % N] if N != 16 else d["kernel_sc1_N16"])
+        x, y = G.ic_spline_knots(N, **G.default_icparams(N, 5.0 * N))
+        d["dfield_in_N%d" % N] = K
+        d["dfield_x_N%d" % N], d["dfield_y_N%d" % N] = x, y
+        for ks in (0, 1):
+            d["dfield_out_N%d_ks%d" % (N, ks)] = G.displacement_field(K, 0.37, x, y, 777 + N, ks, impl="ref")
+    np.savez_compressed(os.path.join(HERE, "golden_ic.npz"), **d)
+
+
 if __name__ == "__main__":
     if G.ref() is None:
         sys.exit("the reference sources are not available here; golden vectors cannot be regenerated")
-    which = sys.argv[1:] or ["hotpath", "gadget", "spectra"]
+    which = sys.argv[1:] or ["hotpath", "gadget", "spectra", "ic"]
     if "hotpath" in which:
         one(8, 101)
         one(12, 102)
+    if "hotpath" in which or "run" in which:
         run(8, 3)
     if "gadget" in which:
         gadget(8, 103)
     if "spectra" in which:
         spectra(12, 104)
+    if "ic" in which:
+        ic(105)
     for f in sorted(os.listdir(HERE)):
         if f.endswith(".npz"):
             print(f, os.path.getsize(os.path.join(HERE, f)))

@@ -251,3 +251,36 @@ def test_library_table_writer_matches_reference(tmp_path):
     build.build()
     import gev_gb300
     _write_tables(lambda *a: gev_gb300.write_power_spectrum(*a[:11], exact_output=a[11]), tmp_path)
+
+
+def test_sitmo_stream_matches_reference(oracle):
+    """sitmo::prng_engine (prng_engine.hpp) restated: the reference's own draws,
+    at the start of a stream, past a block boundary and deep in the fourth
+    quadrant's lines of generateDisplacementField."""
+    g = golden("golden_ic.npz")
+    for key in g.files:
+        if key.startswith("draws_"):
+            _, seed, d0 = key.split("_")
+            assert (oracle.sitmo_draws(int(seed), int(d0), 40) == g[key]).all(), key
+
+
+@pytest.mark.parametrize("N,nt", [(8, 2), (12, 3), (16, 4)])
+def test_cic_kernel_matches_reference(oracle, N, nt):
+    """generateCICKernel (ic_basic.hpp:737-1052) of the sc1 template tiled nt
+    times, and the standard kernel: bit-identical."""
+    g = golden("golden_ic.npz")
+    assert oracle.cic_kernel(N, oracle.sc1_pcldata(), nt).tobytes() == g["kernel_sc1_N%d" % N].tobytes()
+    if N == 16:
+        assert oracle.cic_kernel(16).tobytes() == g["kernel_std_N16"].tobytes()
+
+
+@pytest.mark.parametrize("N", [8, 12, 16])
+@pytest.mark.parametrize("ks", [0, 1])
+def test_displacement_field_matches_reference(oracle, N, ks):
+    """generateDisplacementField (ic_basic.hpp:1089-1379): the sitmo stream laid
+    over the four k-space quadrants, the reused and conjugated kx = 0 lines, the
+    zeroed modes, the spline of the spectrum -- bit-identical."""
+    g = golden("golden_ic.npz")
+    F = oracle.displacement_field(g["dfield_in_N%d" % N], 0.37, g["dfield_x_N%d" % N], g["dfield_y_N%d" % N],
+                                  777 + N, ks)
+    assert F.tobytes() == g["dfield_out_N%d_ks%d" % (N, ks)].tobytes()
