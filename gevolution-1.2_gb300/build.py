@@ -21,7 +21,11 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgev_gb300.so")
 CUDA_LIB = os.path.join(os.path.dirname(os.path.dirname(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")), "lib64")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+# host code rounds every expression as written (no contraction into FMAs, which the
+# Arm host compiler would otherwise do): the initial conditions' setup follows the
+# reference's float / double arithmetic term by term
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "-Xcompiler",
+              "-ffp-contract=off",
               "--expt-relaxed-constexpr", "-I", os.path.join(ROOT, "include")]
 
 

@@ -485,14 +485,16 @@ class _BorrowedParticles(Particles):
 
 class ICParams(ctypes.Structure):
     _fields_ = [(n, _d) for n in ("h", "Omega_cdm", "Omega_b", "n_s", "sigma8", "z_in", "boxsize", "Cf",
-                                  "steplimit")] + [("seed", ctypes.c_uint64), ("ksphere", _i)]
+                                  "steplimit")] + [("seed", ctypes.c_uint64), ("ksphere", _i),
+                                                   ("correct_displacement", _i)]
 
 
 def ic_params(boxsize, seed=1, z_in=100.0, Cf=48.0, steplimit=0.04, Omega_cdm=0.27, Omega_b=0.05, sigma8=0.81,
-              n_s=0.96, h=0.67, ksphere=1):
-    """The initial-condition settings of the benchmark configurations (BBKS, z_in = 100)."""
+              n_s=0.96, h=0.67, ksphere=1, correct_displacement=1):
+    """The initial-condition settings of the benchmark configurations (BBKS, z_in = 100,
+    k-domain = sphere, correct displacement = yes)."""
     return dict(h=h, Omega_cdm=Omega_cdm, Omega_b=Omega_b, n_s=n_s, sigma8=sigma8, z_in=z_in, boxsize=boxsize, Cf=Cf,
-                steplimit=steplimit, seed=seed, ksphere=ksphere)
+                steplimit=steplimit, seed=seed, ksphere=ksphere, correct_displacement=correct_displacement)
 
 
 def sim_ic_generate(sim, **params):

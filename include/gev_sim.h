@@ -60,13 +60,15 @@ int gev_sim_step_particles(gev_sim *s);
 
 /* Zel'dovich initial conditions at z_in generated on the device, following the
  * power-spectrum branch of generateIC_basic (ic_basic.hpp:1626-2259): sc1
- * template tiled N/4 times, BBKS spectrum normalised to sigma8, baryons folded
- * into CDM, no radiation.  Requires N % 4 == 0 and capacity >= N^3.  Sets the
+ * template tiled N/4 times, a tabulated BBKS spectrum normalised to sigma8 and
+ * read through the mPk spline, the reference's sitmo stream laid over k-space as
+ * generateDisplacementField lays it, baryons folded into CDM, no radiation.  Requires N % 4 == 0 and capacity >= N^3.  Sets the
  * whole state (a, tau, dtau, dtau_old = 0, fourpiG, cosmology, particle mass). */
 typedef struct {
   double h, Omega_cdm, Omega_b, n_s, sigma8, z_in, boxsize, Cf, steplimit;
-  uint64_t seed;
-  int ksphere; /* 1: k-domain = sphere */
+  uint64_t seed;              /* the sitmo stream is seeded with its low 32 bits, (unsigned int) ic.seed */
+  int ksphere;                /* 1: k-domain = sphere */
+  int correct_displacement;   /* 1: correct displacement = yes, the template's CIC kernel (ICFLAG_CORRECT_DISPLACEMENT) */
 } gev_ic_params;
 int gev_sim_ic_generate(gev_sim *s, const gev_ic_params *ic);
 

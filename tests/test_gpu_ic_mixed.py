@@ -11,8 +11,20 @@ def rel(a, b):
     return float(np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300))
 
 
+# The modes take the reference's float logarithm of the uniform draw r1 (log of a
+# float is <cmath>'s float overload).  The device rounds the FP64 log to float, the
+# C library computes logf: on rare draws the two differ by one unit in the last
+# place, 3e-8 of that mode's amplitude, and the kernel spectrum comes from two
+# different FFTs (1e-16).  Positions then agree to ~1e-11 cell, fields to ~1e-10;
+# B, the transverse remainder of the momentum deposit, cancels most of it and
+# magnifies the difference a hundredfold.
+TOL_IC_POS, TOL_IC_REL, TOL_IC_B = 1e-10, 1e-9, 1e-8
+
+
 @pytest.mark.parametrize("N", [16, 32])
 def test_device_ic_matches_oracle(gpu, oracle, N):
+    """The device IC against the oracle's (whose displacement field, CIC kernel and
+    random stream are bit-identical to the reference's own, tests/test_oracle_golden.py)."""
     L = 5.0 * N
     o = oracle.Sim(N).ic(**oracle.default_icparams(N, L, seed=21))
     ctx = gpu.Context(N)
@@ -25,11 +37,12 @@ def test_device_ic_matches_oracle(gpu, oracle, N):
     got = s.particles().download()
     ref = o.particles
     assert (got["ID"] == ref["ID"]).all()
-    assert np.abs(got["pos"] - ref["pos"]).max() * N < 1e-12
-    assert rel(got["vel"], ref["vel"]) < 1e-11
-    for name in ("phi", "chi", "Bi"):
-        assert rel(s.field(name).download(), o.field(name)) < 1e-11, name
-    assert rel(s.field("BiFT").download(), o.spectrum("BiFT")) < 1e-11
+    assert np.abs(got["pos"] - ref["pos"]).max() * N < TOL_IC_POS
+    assert rel(got["vel"], ref["vel"]) < TOL_IC_REL
+    for name in ("phi", "chi"):
+        assert rel(s.field(name).download(), o.field(name)) < TOL_IC_REL, name
+    assert rel(s.field("Bi").download(), o.field("Bi")) < TOL_IC_B
+    assert rel(s.field("BiFT").download(), o.spectrum("BiFT")) < TOL_IC_B
 
 
 @pytest.mark.parametrize("N", [16, 32, 48])
