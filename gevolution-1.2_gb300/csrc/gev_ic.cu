@@ -95,6 +95,11 @@ struct GdfParams {
   double coeff, two_pi, four_pi2;
   const double *x, *y, *c;  // spline knots, values, half second derivatives
   const float *sinc;
+  // the mixed form: the kernel spectrum as the DFT of its 27 values, in FP64 (an FP32
+  // transform of the stencil, whose entries are O(N^2) while its spectrum near k = 0
+  // is O(k^2), would lose the large scales); the FP64 form transforms the kernel field
+  int dft;
+  Stencil27 K;
 };
 
 __device__ inline double spline_eval(const GdfParams &p, double v) {
@@ -152,6 +157,15 @@ __global__ void __launch_bounds__(128) k_ic_modes(typename CT<T>::C *F, GdfParam
   SitmoCursor cur;
   cur.seed = p.seed;
   cur.blk = ~0ull;
+  // the line's factors e^{-2 pi i k d / N} for d = -1, 0, 1 along y and z (mixed form)
+  double eyr[3] = {1., 1., 1.}, eyi[3] = {0., 0., 0.}, ezr[3] = {1., 1., 1.}, ezi[3] = {0., 0., 0.};
+  if (p.dft) {
+    double sy_, cy_, sz_, cz_;
+    sincos(__ddiv_rn(__dmul_rn(p.two_pi, (double)ky), (double)N), &sy_, &cy_);
+    sincos(__ddiv_rn(__dmul_rn(p.two_pi, (double)kz), (double)N), &sz_, &cz_);
+    eyr[0] = cy_, eyi[0] = sy_, eyr[2] = cy_, eyi[2] = -sy_;
+    ezr[0] = cz_, ezi[0] = sz_, ezr[2] = cz_, ezi[2] = -sz_;
+  }
   auto walk = [&](uint64_t line, int kx0, int kx1, bool conj) {
     cur.d = line * H;
     for (int kx = kx0; kx <= kx1; ++kx) {
@@ -174,7 +188,23 @@ __global__ void __launch_bounds__(128) k_ic_modes(typename CT<T>::C *F, GdfParam
       const double arg = __dmul_rn(p.two_pi, (double)r2);
       const double cr = cos(arg), sn = sin(arg);
       const double tr = __dmul_rn(cr, d1), ti = __dmul_rn(conj ? -sn : sn, d1);
-      const double Kr = (double)f->x, Ki = (double)f->y;
+      double Kr = (double)f->x, Ki = (double)f->y;
+      if (p.dft) {  // sum over the stencil of K_d e^{-2 pi i k . d / N}
+        double sx_, cx_;
+        sincos(__ddiv_rn(__dmul_rn(p.two_pi, (double)kx), (double)N), &sx_, &cx_);
+        const double exr[3] = {cx_, 1., cx_}, exi[3] = {sx_, 0., -sx_};
+        Kr = 0.;
+        Ki = 0.;
+        for (int q = 0; q < 27; ++q) {
+          const int a = q % 3, b = (q / 3) % 3, c = q / 9;
+          const double yzr = __dsub_rn(__dmul_rn(eyr[b], ezr[c]), __dmul_rn(eyi[b], ezi[c]));
+          const double yzi = __dadd_rn(__dmul_rn(eyr[b], ezi[c]), __dmul_rn(eyi[b], ezr[c]));
+          const double er = __dsub_rn(__dmul_rn(exr[a], yzr), __dmul_rn(exi[a], yzi));
+          const double ei = __dadd_rn(__dmul_rn(exr[a], yzi), __dmul_rn(exi[a], yzr));
+          Kr = __dadd_rn(Kr, __dmul_rn(p.K.v[q], er));
+          Ki = __dadd_rn(Ki, __dmul_rn(p.K.v[q], ei));
+        }
+      }
       const double nn = __dadd_rn(__dmul_rn(Kr, Kr), __dmul_rn(Ki, Ki));
       double qr = __ddiv_rn(__dadd_rn(__dmul_rn(tr, Kr), __dmul_rn(ti, Ki)), nn);
       double qi = __ddiv_rn(__dsub_rn(__dmul_rn(ti, Kr), __dmul_rn(tr, Ki)), nn);
@@ -551,6 +581,8 @@ int ic_t(gev_sim *s, const gev_ic_params &ic) {
   gp.y = gp.x + NPK;
   gp.c = gp.x + 2 * NPK;
   gp.sinc = (const float *)((const char *)dtab + tab.size() * 8);
+  gp.dft = sizeof(T) == 4;
+  gp.K = K;
   k_ic_modes<T><<<(unsigned)(((long)N * N + 127) / 128), 128, 0, ctx->stream>>>((C *)s->scalarFT->d, gp);
   GEV_LAUNCH_CHECK(ctx);
   GEV_CHECK_CUDA(ctx, cudaFreeAsync(dtab, ctx->stream));
