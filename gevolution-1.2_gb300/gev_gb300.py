@@ -681,3 +681,114 @@ def _sim_step_particles(sim):
 Sim.write_spectra = _sim_write_spectra
 Sim.step_fields = _sim_step_fields
 Sim.step_particles = _sim_step_particles
+
+
+# ------------------------------------------------------------------ serving --
+SERVE_MAX_BINS = 64
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("N", _i), ("prec", _i), ("boxsize", _d), ("Omega_cdm", _d), ("Omega_b", _d), ("sigma8", _d),
+                ("n_s", _d), ("h", _d), ("z_in", _d), ("z_target", _d), ("seed", ctypes.c_uint64), ("numbins", _i)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("id", _l), ("N", _i), ("prec", _i), ("cycles", _i), ("status", _i), ("a", _d), ("tau", _d),
+                ("t_submit", _d), ("t_admit", _d), ("t_done", _d), ("kbin", _d * SERVE_MAX_BINS),
+                ("power", _d * SERVE_MAX_BINS), ("occupation", _i * SERVE_MAX_BINS), ("numbins", _i)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [(n, _l) for n in ("submitted", "admitted", "completed", "failed", "active", "pending",
+                                  "max_active_seen")] + [("particle_steps", _d), ("busy_seconds", _d)] + [
+        (n, ctypes.c_size_t) for n in ("bytes_budget", "bytes_in_use", "bytes_peak")]
+
+
+_SERVE_SIGS = {
+    "gev_server_create": [_i, ctypes.c_size_t, _i, _i, ctypes.POINTER(_vp)],
+    "gev_server_submit": [_vp, ctypes.POINTER(Request), ctypes.POINTER(_l)],
+    "gev_server_poll": [_vp, ctypes.POINTER(Result), _i, ctypes.POINTER(_i)],
+    "gev_server_drain": [_vp, _d],
+    "gev_server_stats_get": [_vp, ctypes.POINTER(ServerStats)],
+    "gev_server_footprint": [_i, _i, _i, ctypes.POINTER(ctypes.c_size_t)],
+    "gev_server_destroy": [_vp],
+}
+
+
+def _serve_lib():
+    L = _pk_lib()
+    if not getattr(L, "_serve_ready", False):
+        for name, args in _SERVE_SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L._serve_ready = True
+    return L
+
+
+def request(N, seed, z_target=0.0, prec=PREC_MIXED, boxsize=None, Omega_cdm=0.27, Omega_b=0.05, sigma8=0.81,
+            n_s=0.96, h=0.67, z_in=100.0, numbins=32):
+    """A simulation request: grid N (= particles per side), cosmology, seed, target redshift."""
+    return Request(N, prec, 2.5 * N if boxsize is None else boxsize, Omega_cdm, Omega_b, sigma8, n_s, h, z_in, z_target,
+                   seed, numbins)
+
+
+def result_dict(r):
+    nb = r.numbins
+    return {"id": r.id, "N": r.N, "prec": r.prec, "cycles": r.cycles, "status": r.status, "a": r.a, "tau": r.tau,
+            "t_submit": r.t_submit, "t_admit": r.t_admit, "t_done": r.t_done,
+            "kbin": np.array(r.kbin[:nb]), "power": np.array(r.power[:nb]), "occupation": np.array(r.occupation[:nb])}
+
+
+class Server:
+    """Continuous batching of simulations on one GPU (include/gev_serve.h)."""
+
+    def __init__(self, device=0, bytes_budget=0, max_active=0, inflight=0):
+        self.handle = None
+        h = _vp()
+        rc = _serve_lib().gev_server_create(device, bytes_budget, max_active, inflight, ctypes.byref(h))
+        if rc != OK:
+            raise GevError("gev_server_create failed (%d)" % rc)
+        self.handle = h.value
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _serve_lib().gev_server_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+    def close(self):
+        self.__del__()
+
+    def submit(self, req):
+        i = _l()
+        rc = _serve_lib().gev_server_submit(self.handle, ctypes.byref(req), ctypes.byref(i))
+        if rc != OK:
+            raise GevError("gev_server_submit failed (%d)" % rc)
+        return i.value
+
+    def poll(self, max_results=256):
+        buf = (Result * max_results)()
+        n = _i()
+        _serve_lib().gev_server_poll(self.handle, buf, max_results, ctypes.byref(n))
+        return [result_dict(buf[k]) for k in range(n.value)]
+
+    def drain(self, timeout=0.0):
+        rc = _serve_lib().gev_server_drain(self.handle, timeout)
+        if rc != OK:
+            raise GevError("gev_server_drain: %d" % rc)
+
+    def stats(self):
+        st = ServerStats()
+        _serve_lib().gev_server_stats_get(self.handle, ctypes.byref(st))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+
+def footprint(N, prec=PREC_MIXED, device=0):
+    b = ctypes.c_size_t()
+    rc = _serve_lib().gev_server_footprint(device, N, prec, ctypes.byref(b))
+    if rc != OK:
+        raise GevError("gev_server_footprint failed (%d)" % rc)
+    return b.value
