@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-pk-check", action="store_true", help="skip the FP64-form run and spectrum comparison")
+    ap.add_argument("--serve-seconds", type=float, default=20.0,
+                    help="length of the serving run's Poisson arrivals (0: no serving measurement)")
+    ap.add_argument("--serve-rate", type=float, default=2.0, help="serving requests per second")
+    ap.add_argument("--serve-burst", type=int, default=24, help="requests submitted at once for the capacity run")
     return ap.parse_args()
 
 
@@ -205,8 +209,11 @@ def run_ours(args, rank, world, local):
     if pk is not None:
         del sim, ctx
         fp64 = fp64_form_check(args, gpu, N, box, local, pk, torch)
+    serve = None
+    if args.serve_seconds > 0 and world == 1:
+        serve = run_serve(args, gpu)
     return dict(value=value, ms=ms_max / args.steps, launches=launches, clocks=clk, state=st, roofline=roof,
-                roofline_fft=roof_fft, e2e=e2e, box=box, fp64=fp64)
+                roofline_fft=roof_fft, e2e=e2e, box=box, fp64=fp64, serve=serve)
 
 
 PK_FIELDS = (("phi", 1), ("chi", 1), ("Bi", 3), ("source", 1))
@@ -331,6 +338,129 @@ def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
             "traffic": COLS_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
 
 
+# ------------------------------------------------------------ serving --------
+SERVE_SIZES = (64, 96, 128, 192, 256)
+SERVE_Z = (1.0, 0.5, 0.0)
+
+
+def serve_requests(gpu, rng, n, first_seed):
+    """Requests of the serving workload: grid drawn from SERVE_SIZES, box 2.5 N Mpc/h,
+    Omega_cdm U[0.25, 0.35], sigma8 U[0.75, 0.87], n_s U[0.94, 0.98], target
+    redshift from SERVE_Z, BBKS Zel'dovich IC at z = 100, distinct seeds."""
+    out = []
+    for k in range(n):
+        N = int(rng.choice(SERVE_SIZES))
+        out.append(gpu.request(N, seed=first_seed + k, z_target=float(rng.choice(SERVE_Z)),
+                               Omega_cdm=float(rng.uniform(0.25, 0.35)), sigma8=float(rng.uniform(0.75, 0.87)),
+                               n_s=float(rng.uniform(0.94, 0.98)), prec=gpu.PREC_MIXED))
+    return out
+
+
+def fp64_sequential_seconds(gpu, sizes):
+    """Per grid size, the wall time of a plain FP64 run on this GPU: the initial
+    conditions, and one cycle (the median of 3 after one warm-up)."""
+    out = {}
+    for N in sizes:
+        c = gpu.Context(N, gpu.PREC_FP64)
+        s = gpu.Sim(c, N ** 3)
+        t0 = time.perf_counter()
+        s.ic_generate(**gpu.ic_params(2.5 * N, seed=7))
+        c.sync()
+        t_ic = time.perf_counter() - t0
+        s.step()
+        c.sync()
+        ts = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            s.step()
+            c.sync()
+            ts.append(time.perf_counter() - t0)
+        out[N] = (t_ic, sorted(ts)[1])
+        del s, c
+    return out
+
+
+def run_serve(args, gpu):
+    """The serving loop under load: Poisson arrivals at --serve-rate for
+    --serve-seconds (time to result p50 / p99, sustained sims/hour), then a burst of
+    --serve-burst requests at once (capacity), against sequential plain FP64 runs of
+    the same requests on the same GPU (their IC and cycle times measured per size)."""
+    import numpy as np
+    rng = np.random.default_rng(args.seed + 77)
+    n_poisson = max(1, int(args.serve_seconds * args.serve_rate * 1.5) + 8)
+    reqs = serve_requests(gpu, rng, n_poisson, 100000)
+    srv = gpu.Server()
+    t_start = time.perf_counter()
+    t_next, sent = 0.0, 0
+    while True:
+        t_next += float(rng.exponential(1.0 / args.serve_rate))
+        if t_next > args.serve_seconds or sent == len(reqs):
+            break
+        dt = t_start + t_next - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        srv.submit(reqs[sent])
+        sent += 1
+    srv.drain(900.0)
+    res = [r for r in srv.poll(100000) if r["status"] == 0]
+    st = srv.stats()
+    srv.close()
+    lat = sorted(r["t_done"] - r["t_submit"] for r in res)
+    span = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
+    # capacity: a burst of requests at once
+    burst = serve_requests(gpu, rng, args.serve_burst, 200000)
+    srv = gpu.Server()
+    for r in burst:
+        srv.submit(r)
+    srv.drain(900.0)
+    bres = [r for r in srv.poll(100000) if r["status"] == 0]
+    bst = srv.stats()
+    srv.close()
+    b_span = max(r["t_done"] for r in bres) - min(r["t_submit"] for r in bres)
+    seq = fp64_sequential_seconds(gpu, sorted({r["N"] for r in res} | {r["N"] for r in bres} | {64, 96, 128}))
+
+    def seq_seconds(rs):
+        return sum(seq[r["N"]][0] + r["cycles"] * seq[r["N"]][1] for r in rs)
+
+    cap = len(bres) / b_span * 3600.0
+    seq_rate = len(bres) / seq_seconds(bres) * 3600.0
+    # the batched ensemble: 16 simulations each at 64^3, 96^3 and 128^3, box 2.5 N,
+    # cosmologies and seeds as above, all to z = 0, admitted at once
+    ens = []
+    for k, N in enumerate([64] * 16 + [96] * 16 + [128] * 16):
+        ens.append(gpu.request(N, seed=300000 + k, z_target=0.0, Omega_cdm=float(rng.uniform(0.25, 0.35)),
+                               sigma8=float(rng.uniform(0.75, 0.87)), n_s=float(rng.uniform(0.94, 0.98)),
+                               prec=gpu.PREC_MIXED))
+    srv = gpu.Server()
+    for r in ens:
+        srv.submit(r)
+    srv.drain(900.0)
+    eres = [r for r in srv.poll(100000) if r["status"] == 0]
+    est = srv.stats()
+    srv.close()
+    e_span = max(r["t_done"] for r in eres) - min(r["t_submit"] for r in eres)
+    e_steps = sum(float(r["N"]) ** 3 * r["cycles"] for r in eres)
+    pct = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]  # noqa: E731
+    return {
+        "precision": "mixed", "arrivals": "Poisson %.3g/s for %.3g s" % (args.serve_rate, args.serve_seconds),
+        "sizes": list(SERVE_SIZES), "z_target": list(SERVE_Z), "completed": len(res), "failed": st["failed"],
+        "p50_s": pct(0.50), "p99_s": pct(0.99), "max_s": lat[-1],
+        "sims_per_hour_offered_load": len(res) / span * 3600.0,
+        "max_active_seen": st["max_active_seen"],
+        "burst": {"requests": len(bres), "makespan_s": b_span, "sims_per_hour": cap,
+                  "max_active_seen": bst["max_active_seen"]},
+        "sequential_fp64": {"sims_per_hour": seq_rate,
+                            "per_size_s": {str(N): {"ic": v[0], "cycle": v[1]} for N, v in seq.items()},
+                            "note": "the burst's requests run one after another in the plain FP64 form: IC time plus "
+                                    "their cycles times the measured FP64 cycle time of their size"},
+        "capacity_vs_sequential_fp64": cap / seq_rate,
+        "ensemble": {"simulations": len(eres), "sizes": "16 x 64^3, 16 x 96^3, 16 x 128^3, z = 100 -> 0",
+                     "makespan_s": e_span, "particle_steps_per_s": e_steps / e_span,
+                     "max_active_seen": est["max_active_seen"],
+                     "sequential_fp64_s": seq_seconds(eres) if all(r["N"] in seq for r in eres) else None},
+    }
+
+
 def run_e2e(gpu, ctx, sim, stream, N, steps, torch):
     import numpy as np
     pcls = sim.particles()
@@ -432,6 +562,8 @@ def main():
             "final_a": res["state"]["a"]}
     if res.get("fp64"):
         line.update(res["fp64"])
+    if res.get("serve"):
+        line["serve"] = res["serve"]
     print(json.dumps(line))
 
 
