@@ -62,6 +62,23 @@ def parse():
     return ap.parse_args()
 
 
+def reduce_max_ms(ms, world, device):
+    """The slowest rank's time: every rank's timed region ends at a barrier and the
+    maximum over ranks is what the aggregate is measured against."""
+    import torch
+    t = torch.tensor([ms], dtype=torch.float64, device=device)
+    if world > 1:
+        torch.distributed.barrier()
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def aggregate_value(N, steps, world, ms_max):
+    """Whole-job particle-steps/s: every rank advances its own N^3 replica (replicas
+    only, weak scaling) for `steps` cycles within the slowest rank's time."""
+    return float(N) ** 3 * steps * world / (ms_max / 1e3)
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -186,12 +203,8 @@ def run_ours(args, rank, world, local):
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     torch.cuda.synchronize()
-    t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-    if world > 1:
-        torch.distributed.barrier()
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-    ms_max = float(t.item())
-    value = N ** 3 * args.steps * world / (ms_max / 1e3)
+    ms_max = reduce_max_ms(ms, world, "cuda")
+    value = aggregate_value(N, args.steps, world, ms_max)
     st = sim.state()
     pk = None
     if not args.no_pk_check and prec == gpu.PREC_MIXED and world == 1:
