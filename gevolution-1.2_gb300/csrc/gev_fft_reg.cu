@@ -30,12 +30,19 @@ constexpr int ilog2c(int v) { return v <= 1 ? 0 : 1 + ilog2c(v >> 1); }
 
 // lines per tile: 8 for FP32, 4 for FP64 (64 bytes of every column-tile row)
 template <typename T>
-constexpr int tile_lg() {
+__host__ __device__ constexpr int tile_lg() {
   return sizeof(T) == 4 ? 3 : 2;
 }
+// The column passes take 2^LGB lines per tile.  The z pass of an FP32 spectrum,
+// whose rows lie a plane apart, reads 16 lines (a whole 128-byte line per row)
+// up to L = 512 (1024 threads): fewer, longer DRAM bursts than 8 lines.  The y
+// pass, whose rows are consecutive in a plane, is faster with the default 8.
 template <typename T, int L>
 constexpr int reg_threads() {
   return (L / 8) << tile_lg<T>();
+}
+constexpr int col_min_blocks(int esize, int threads) {
+  return (esize == 4 ? 1024 : 512) / threads > 0 ? (esize == 4 ? 1024 : 512) / threads : 1;
 }
 // resident blocks asked of the compiler: 1024 threads per SM for FP32 (64
 // registers), 512 for FP64, whose own pipe bounds it anyway
@@ -122,16 +129,16 @@ __device__ __forceinline__ void stage_tw(C *tw, const C *__restrict__ g, int L) 
 }
 
 // y / z pass over B columns (consecutive kx) of one plane per tile; in may equal out
-template <typename T, int SIGN, int L>
-__global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k_fft_cols_reg(const typename CT<T>::C *in, typename CT<T>::C *out,
-                                                       const typename CT<T>::C *__restrict__ twg, int NH, long ES,
-                                                       long PS, int lgB, int ntiles) {
+template <typename T, int SIGN, int L, int LGB>
+__global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L / 8) << LGB))
+    k_fft_cols_reg(const typename CT<T>::C *in, typename CT<T>::C *out, const typename CT<T>::C *__restrict__ twg,
+                   int NH, long ES, long PS, int ntiles) {
   typedef RegFft<T, SIGN, L> R;
   typedef typename CT<T>::C C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
   C *X = tw + L;
-  const int B = 1 << lgB;
+  constexpr int lgB = LGB, B = 1 << LGB;
   stage_tw(tw, twg, L);
   const int c = threadIdx.x & (B - 1), m = threadIdx.x >> lgB;
   const unsigned nchunks = (unsigned)(NH + B - 1) >> lgB;
@@ -160,13 +167,13 @@ template <typename T, int L>
 __global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k_fft_r2c_rows_reg(const T *__restrict__ in, typename CT<T>::C *__restrict__ out,
                                                            const typename CT<T>::C *__restrict__ twHg,
                                                            const typename CT<T>::C *__restrict__ twN, int NH,
-                                                           long nrows, int lgB, int ntiles) {
+                                                           long nrows, int ntiles) {
   typedef RegFft<T, -1, L> R;
   typedef typename CT<T>::C C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
   C *X = tw + L;
-  const int B = 1 << lgB;
+  constexpr int lgB = tile_lg<T>(), B = 1 << lgB;
   stage_tw(tw, twHg, L);
   const int c = threadIdx.x & (B - 1), m = threadIdx.x >> lgB;
   const int kb = R::freq(m << 3);
@@ -204,13 +211,13 @@ template <typename T, int L>
 __global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k_fft_c2r_rows_reg(const typename CT<T>::C *__restrict__ in, T *__restrict__ out,
                                                            const typename CT<T>::C *__restrict__ twHg,
                                                            const typename CT<T>::C *__restrict__ twN, int NH,
-                                                           long nrows, int lgB, int ntiles) {
+                                                           long nrows, int ntiles) {
   typedef RegFft<T, +1, L> R;
   typedef typename CT<T>::C C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
   C *X = tw + L;  // (L + 1) * B
-  const int B = 1 << lgB;
+  constexpr int lgB = tile_lg<T>(), B = 1 << lgB;
   stage_tw(tw, twHg, L);
   const int c = threadIdx.x & (B - 1), m = threadIdx.x >> lgB;
   const int kb = R::freq(m << 3);
@@ -272,21 +279,30 @@ int launch_cfg(gev_ctx *ctx, K kern, int threads, size_t smem, long ntiles, int 
   return GEV_OK;
 }
 
-template <typename T, int SIGN, int L>
-int cols_L(gev_ctx *ctx, const void *in, void *out, long ES, long PS) {
+template <typename T, int SIGN, int L, int LGB>
+int cols_LB(gev_ctx *ctx, const void *in, void *out, long ES, long PS) {
   typedef typename CT<T>::C C;
   static int per_sm = 0;
-  const int NH = ctx->N / 2 + 1, lgB = tile_lg<T>(), B = 1 << lgB;
-  const int threads = (L / 8) * B;
+  constexpr int B = 1 << LGB, threads = (L / 8) * B;
+  const int NH = ctx->N / 2 + 1;
   const long ntiles = (long)ctx->N * ((NH + B - 1) / B);
   const size_t smem = ((size_t)L + (size_t)L * B) * sizeof(C);
   int grid = 0;
-  int rc = launch_cfg(ctx, k_fft_cols_reg<T, SIGN, L>, threads, smem, ntiles, per_sm, grid);
+  int rc = launch_cfg(ctx, k_fft_cols_reg<T, SIGN, L, LGB>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
-  k_fft_cols_reg<T, SIGN, L><<<grid, threads, smem, ctx->stream>>>((const C *)in, (C *)out, (const C *)ctx->d_twN, NH,
-                                                                   ES, PS, lgB, (int)ntiles);
+  k_fft_cols_reg<T, SIGN, L, LGB><<<grid, threads, smem, ctx->stream>>>((const C *)in, (C *)out,
+                                                                        (const C *)ctx->d_twN, NH, ES, PS, (int)ntiles);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
+}
+
+// the wide tile for a pass whose rows are further apart than its tiles (ES > PS)
+template <typename T, int SIGN, int L>
+int cols_L(gev_ctx *ctx, const void *in, void *out, long ES, long PS) {
+  if constexpr (sizeof(T) == 4 && L <= 512) {
+    if (ES > PS) return cols_LB<T, SIGN, L, 4>(ctx, in, out, ES, PS);
+  }
+  return cols_LB<T, SIGN, L, tile_lg<T>()>(ctx, in, out, ES, PS);
 }
 
 template <typename T, int L>
@@ -301,7 +317,7 @@ int r2c_L(gev_ctx *ctx, const void *real, void *spec) {
   int rc = launch_cfg(ctx, k_fft_r2c_rows_reg<T, L>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
   k_fft_r2c_rows_reg<T, L><<<grid, threads, smem, ctx->stream>>>((const T *)real, (C *)spec, (const C *)ctx->d_twH,
-                                                                 (const C *)ctx->d_twN, NH, nrows, lgB, (int)ntiles);
+                                                                 (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
@@ -318,7 +334,7 @@ int c2r_L(gev_ctx *ctx, const void *spec, void *real) {
   int rc = launch_cfg(ctx, k_fft_c2r_rows_reg<T, L>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
   k_fft_c2r_rows_reg<T, L><<<grid, threads, smem, ctx->stream>>>((const C *)spec, (T *)real, (const C *)ctx->d_twH,
-                                                                 (const C *)ctx->d_twN, NH, nrows, lgB, (int)ntiles);
+                                                                 (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
