@@ -407,24 +407,97 @@ __device__ __forceinline__ T at(const T *__restrict__ f, const CellNb &b) {
   return __ldg(f + i);
 }
 
+// The field values a particle update reads around its cell, as
+// v<F, DX, DY, DZ>() with F = 0 phi, 1 chi, 2..4 the components of B.
+// MemStencil loads each value where it is used.  RegStencil gathers every value
+// the kick and the drift read (phi and chi on the cell's 8 corners, B^i on the 12
+// nodes of the corners extended by one along axis i) into registers at once: one
+// load per value for both updates, all of them in flight together.
+template <typename T>
+struct MemStencil {
+  const T *phi, *chi, *B0, *B1, *B2;
+  CellNb nb;
+  bool has_chi, has_B;
+  template <int F, int DX, int DY, int DZ>
+  __device__ __forceinline__ T v() const {
+    const T *f = F == 0 ? phi : F == 1 ? chi : F == 2 ? B0 : F == 3 ? B1 : B2;
+    return at<DX, DY, DZ>(f, nb);
+  }
+};
+template <typename T>
+__device__ __forceinline__ MemStencil<T> mem_stencil(const T *phi, const T *chi, const T *Bi, size_t NV,
+                                                     const CellNb &nb) {
+  MemStencil<T> m;
+  m.phi = phi;
+  m.chi = chi;
+  m.B0 = Bi;
+  m.B1 = Bi ? Bi + NV : nullptr;
+  m.B2 = Bi ? Bi + 2 * NV : nullptr;
+  m.nb = nb;
+  m.has_chi = chi != nullptr;
+  m.has_B = Bi != nullptr;
+  return m;
+}
+template <typename T>
+struct RegStencil {
+  T p[8], c[8], b0[12], b1[12], b2[12];
+  bool has_chi, has_B;
+  template <int F, int DX, int DY, int DZ>
+  __device__ __forceinline__ T v() const {
+    if constexpr (F == 0) return p[DX + 2 * DY + 4 * DZ];
+    if constexpr (F == 1) return c[DX + 2 * DY + 4 * DZ];
+    if constexpr (F == 2) return b0[(DX + 1) + 3 * (DY + 2 * DZ)];
+    if constexpr (F == 3) return b1[DX + 2 * ((DY + 1) + 3 * DZ)];
+    return b2[DX + 2 * DY + 4 * (DZ + 1)];
+  }
+};
+template <int D>
+__device__ __forceinline__ uint32_t nb_off(uint32_t m, uint32_t p) {
+  return D < 0 ? m : (D > 0 ? p : 0u);
+}
+template <typename T>
+__device__ __forceinline__ RegStencil<T> reg_stencil(const MemStencil<T> &m, bool chi_on, bool B_on) {
+  RegStencil<T> r;
+  const CellNb &b = m.nb;
+  r.has_chi = m.has_chi;
+  r.has_B = m.has_B;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const uint32_t i = b.base + ((k & 1) ? b.xp : 0u) + ((k & 2) ? b.yp : 0u) + ((k & 4) ? b.zp : 0u);
+    r.p[k] = __ldg(m.phi + i);
+    r.c[k] = chi_on ? __ldg(m.chi + i) : (T)0;
+  }
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    // b0: x in {-1, 0, 1}, (y, z) in {0, 1}^2; b1: y in {-1, 0, 1}; b2: z in {-1, 0, 1}
+    const int e0 = k % 3 - 1, u0 = (k / 3) & 1, w0 = k / 6;
+    const int x1 = k & 1, e1 = (k >> 1) % 3 - 1, w1 = k / 6;
+    const int x2 = k & 1, y2 = (k >> 1) & 1, e2 = (k >> 2) - 1;
+    const uint32_t i0 = b.base + (e0 < 0 ? b.xm : e0 > 0 ? b.xp : 0u) + (u0 ? b.yp : 0u) + (w0 ? b.zp : 0u);
+    const uint32_t i1 = b.base + (x1 ? b.xp : 0u) + (e1 < 0 ? b.ym : e1 > 0 ? b.yp : 0u) + (w1 ? b.zp : 0u);
+    const uint32_t i2 = b.base + (x2 ? b.xp : 0u) + (y2 ? b.yp : 0u) + (e2 < 0 ? b.zm : e2 > 0 ? b.zp : 0u);
+    r.b0[k] = B_on ? __ldg(m.B0 + i0) : (T)0;
+    r.b1[k] = B_on ? __ldg(m.B1 + i1) : (T)0;
+    r.b2[k] = B_on ? __ldg(m.B2 + i2) : (T)0;
+  }
+  return r;
+}
+
 // The per-particle physics of update_q (gevolution.hpp:570-678, GRADIENT_ORDER 1)
 // and update_pos (810-871), on the particle's linked cell (its neighbours nb) and its
 // in-cell offset r = pos*N - cell (ref_dist of the reference).  Field values are
 // gathered with periodic wrap.
 
 // q -> q - dtau e grad / dx (GR) or q - dtau a grad / dx (Newton)
-template <typename T, int KIND>
-__device__ __forceinline__ void kick_one(const T *__restrict__ phi, const T *__restrict__ chi,
-                                         const T *__restrict__ Bi, const Params &pr, const CellNb &nb, T r0, T r1,
-                                         T r2, T &q0, T &q1, T &q2) {
+template <typename T, int KIND, typename S>
+__device__ __forceinline__ void kick_one(const S &st, const Params &pr, T r0, T r1, T r2, T &q0, T &q1, T &q2) {
   const int N = pr.N;
-  const size_t NV = (size_t)N * N * N;
   const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
   T g0, g1, g2;
   {
-    const T f000 = at<0, 0, 0>(phi, nb), f100 = at<1, 0, 0>(phi, nb), f010 = at<0, 1, 0>(phi, nb),
-            f110 = at<1, 1, 0>(phi, nb), f001 = at<0, 0, 1>(phi, nb), f101 = at<1, 0, 1>(phi, nb),
-            f011 = at<0, 1, 1>(phi, nb), f111 = at<1, 1, 1>(phi, nb);
+    const T f000 = st.template v<0, 0, 0, 0>(), f100 = st.template v<0, 1, 0, 0>(), f010 = st.template v<0, 0, 1, 0>(),
+            f110 = st.template v<0, 1, 1, 0>(), f001 = st.template v<0, 0, 0, 1>(), f101 = st.template v<0, 1, 0, 1>(),
+            f011 = st.template v<0, 0, 1, 1>(), f111 = st.template v<0, 1, 1, 1>();
     g0 = s1 * s2 * (f100 - f000) + r1 * s2 * (f110 - f010) + s1 * r2 * (f101 - f001) + r1 * r2 * (f111 - f011);
     g1 = s0 * s2 * (f010 - f000) + r0 * s2 * (f110 - f100) + s0 * r2 * (f011 - f001) + r0 * r2 * (f111 - f101);
     g2 = s0 * s1 * (f001 - f000) + r0 * s1 * (f101 - f100) + s0 * r1 * (f011 - f010) + r0 * r1 * (f111 - f110);
@@ -441,42 +514,41 @@ __device__ __forceinline__ void kick_one(const T *__restrict__ phi, const T *__r
     e = tsqrt<T>(e2);
     inv_e = (T)1 / e;
   }
-  if (pr.nfield >= 2 && chi != nullptr) {
-    const T f000 = at<0, 0, 0>(chi, nb), f100 = at<1, 0, 0>(chi, nb), f010 = at<0, 1, 0>(chi, nb),
-            f110 = at<1, 1, 0>(chi, nb), f001 = at<0, 0, 1>(chi, nb), f101 = at<1, 0, 1>(chi, nb),
-            f011 = at<0, 1, 1>(chi, nb), f111 = at<1, 1, 1>(chi, nb);
+  if (pr.nfield >= 2 && st.has_chi) {
+    const T f000 = st.template v<1, 0, 0, 0>(), f100 = st.template v<1, 1, 0, 0>(), f010 = st.template v<1, 0, 1, 0>(),
+            f110 = st.template v<1, 1, 1, 0>(), f001 = st.template v<1, 0, 0, 1>(), f101 = st.template v<1, 1, 0, 1>(),
+            f011 = st.template v<1, 0, 1, 1>(), f111 = st.template v<1, 1, 1, 1>();
     g0 -= s1 * s2 * (f100 - f000) + r1 * s2 * (f110 - f010) + s1 * r2 * (f101 - f001) + r1 * r2 * (f111 - f011);
     g1 -= s0 * s2 * (f010 - f000) + r0 * s2 * (f110 - f100) + s0 * r2 * (f011 - f001) + r0 * r2 * (f111 - f101);
     g2 -= s0 * s1 * (f001 - f000) + r0 * s1 * (f101 - f100) + s0 * r1 * (f011 - f010) + r0 * r1 * (f111 - f110);
   }
-  if (KIND == GEV_GR && pr.nfield >= 3 && Bi != nullptr) {
-    const T *B0 = Bi, *B1 = Bi + NV, *B2 = Bi + 2 * NV;
+  if (KIND == GEV_GR && pr.nfield >= 3 && st.has_B) {
     const T t0 = (T)2 * r0, t1 = (T)2 * r1, t2 = (T)2 * r2;
     T p0, p1, p2;
-    p0 = (s2 * (at<1, 0, 0>(B1, nb) - at<0, 0, 0>(B1, nb)) +
-          r2 * (at<1, 0, 1>(B1, nb) - at<0, 0, 1>(B1, nb))) * q1;
-    p0 += (s1 * (at<1, 0, 0>(B2, nb) - at<0, 0, 0>(B2, nb)) +
-           r1 * (at<1, 1, 0>(B2, nb) - at<0, 1, 0>(B2, nb))) * q2;
-    p0 += (s1 * s2 * ((r0 - (T)1) * at<-1, 0, 0>(B0, nb) + ((T)1 - t0) * at<0, 0, 0>(B0, nb) + r0 * at<1, 0, 0>(B0, nb)) +
-           r1 * s2 * ((r0 - (T)1) * at<-1, 1, 0>(B0, nb) + ((T)1 - t0) * at<0, 1, 0>(B0, nb) + r0 * at<1, 1, 0>(B0, nb)) +
-           s1 * r2 * ((r0 - (T)1) * at<-1, 0, 1>(B0, nb) + ((T)1 - t0) * at<0, 0, 1>(B0, nb) + r0 * at<1, 0, 1>(B0, nb)) +
-           r1 * r2 * ((r0 - (T)1) * at<-1, 1, 1>(B0, nb) + ((T)1 - t0) * at<0, 1, 1>(B0, nb) + r0 * at<1, 1, 1>(B0, nb))) * q0;
-    p1 = (s0 * (at<0, 1, 0>(B2, nb) - at<0, 0, 0>(B2, nb)) +
-          r0 * (at<1, 1, 0>(B2, nb) - at<1, 0, 0>(B2, nb))) * q2;
-    p1 += (s2 * (at<0, 1, 0>(B0, nb) - at<0, 0, 0>(B0, nb)) +
-           r2 * (at<0, 1, 1>(B0, nb) - at<0, 0, 1>(B0, nb))) * q0;
-    p1 += (s0 * s2 * ((r1 - (T)1) * at<0, -1, 0>(B1, nb) + ((T)1 - t1) * at<0, 0, 0>(B1, nb) + r1 * at<0, 1, 0>(B1, nb)) +
-           r0 * s2 * ((r1 - (T)1) * at<1, -1, 0>(B1, nb) + ((T)1 - t1) * at<1, 0, 0>(B1, nb) + r1 * at<1, 1, 0>(B1, nb)) +
-           s0 * r2 * ((r1 - (T)1) * at<0, -1, 1>(B1, nb) + ((T)1 - t1) * at<0, 0, 1>(B1, nb) + r1 * at<0, 1, 1>(B1, nb)) +
-           r0 * r2 * ((r1 - (T)1) * at<1, -1, 1>(B1, nb) + ((T)1 - t1) * at<1, 0, 1>(B1, nb) + r1 * at<1, 1, 1>(B1, nb))) * q1;
-    p2 = (s1 * (at<0, 0, 1>(B0, nb) - at<0, 0, 0>(B0, nb)) +
-          r1 * (at<0, 1, 1>(B0, nb) - at<0, 1, 0>(B0, nb))) * q0;
-    p2 += (s0 * (at<0, 0, 1>(B1, nb) - at<0, 0, 0>(B1, nb)) +
-           r0 * (at<1, 0, 1>(B1, nb) - at<1, 0, 0>(B1, nb))) * q1;
-    p2 += (s0 * s1 * ((r2 - (T)1) * at<0, 0, -1>(B2, nb) + ((T)1 - t2) * at<0, 0, 0>(B2, nb) + r2 * at<0, 0, 1>(B2, nb)) +
-           r0 * s1 * ((r2 - (T)1) * at<1, 0, -1>(B2, nb) + ((T)1 - t2) * at<1, 0, 0>(B2, nb) + r2 * at<1, 0, 1>(B2, nb)) +
-           s0 * r1 * ((r2 - (T)1) * at<0, 1, -1>(B2, nb) + ((T)1 - t2) * at<0, 1, 0>(B2, nb) + r2 * at<0, 1, 1>(B2, nb)) +
-           r0 * r1 * ((r2 - (T)1) * at<1, 1, -1>(B2, nb) + ((T)1 - t2) * at<1, 1, 0>(B2, nb) + r2 * at<1, 1, 1>(B2, nb))) * q2;
+    p0 = (s2 * (st.template v<3, 1, 0, 0>() - st.template v<3, 0, 0, 0>()) +
+          r2 * (st.template v<3, 1, 0, 1>() - st.template v<3, 0, 0, 1>())) * q1;
+    p0 += (s1 * (st.template v<4, 1, 0, 0>() - st.template v<4, 0, 0, 0>()) +
+           r1 * (st.template v<4, 1, 1, 0>() - st.template v<4, 0, 1, 0>())) * q2;
+    p0 += (s1 * s2 * ((r0 - (T)1) * st.template v<2, -1, 0, 0>() + ((T)1 - t0) * st.template v<2, 0, 0, 0>() + r0 * st.template v<2, 1, 0, 0>()) +
+           r1 * s2 * ((r0 - (T)1) * st.template v<2, -1, 1, 0>() + ((T)1 - t0) * st.template v<2, 0, 1, 0>() + r0 * st.template v<2, 1, 1, 0>()) +
+           s1 * r2 * ((r0 - (T)1) * st.template v<2, -1, 0, 1>() + ((T)1 - t0) * st.template v<2, 0, 0, 1>() + r0 * st.template v<2, 1, 0, 1>()) +
+           r1 * r2 * ((r0 - (T)1) * st.template v<2, -1, 1, 1>() + ((T)1 - t0) * st.template v<2, 0, 1, 1>() + r0 * st.template v<2, 1, 1, 1>())) * q0;
+    p1 = (s0 * (st.template v<4, 0, 1, 0>() - st.template v<4, 0, 0, 0>()) +
+          r0 * (st.template v<4, 1, 1, 0>() - st.template v<4, 1, 0, 0>())) * q2;
+    p1 += (s2 * (st.template v<2, 0, 1, 0>() - st.template v<2, 0, 0, 0>()) +
+           r2 * (st.template v<2, 0, 1, 1>() - st.template v<2, 0, 0, 1>())) * q0;
+    p1 += (s0 * s2 * ((r1 - (T)1) * st.template v<3, 0, -1, 0>() + ((T)1 - t1) * st.template v<3, 0, 0, 0>() + r1 * st.template v<3, 0, 1, 0>()) +
+           r0 * s2 * ((r1 - (T)1) * st.template v<3, 1, -1, 0>() + ((T)1 - t1) * st.template v<3, 1, 0, 0>() + r1 * st.template v<3, 1, 1, 0>()) +
+           s0 * r2 * ((r1 - (T)1) * st.template v<3, 0, -1, 1>() + ((T)1 - t1) * st.template v<3, 0, 0, 1>() + r1 * st.template v<3, 0, 1, 1>()) +
+           r0 * r2 * ((r1 - (T)1) * st.template v<3, 1, -1, 1>() + ((T)1 - t1) * st.template v<3, 1, 0, 1>() + r1 * st.template v<3, 1, 1, 1>())) * q1;
+    p2 = (s1 * (st.template v<2, 0, 0, 1>() - st.template v<2, 0, 0, 0>()) +
+          r1 * (st.template v<2, 0, 1, 1>() - st.template v<2, 0, 1, 0>())) * q0;
+    p2 += (s0 * (st.template v<3, 0, 0, 1>() - st.template v<3, 0, 0, 0>()) +
+           r0 * (st.template v<3, 1, 0, 1>() - st.template v<3, 1, 0, 0>())) * q1;
+    p2 += (s0 * s1 * ((r2 - (T)1) * st.template v<4, 0, 0, -1>() + ((T)1 - t2) * st.template v<4, 0, 0, 0>() + r2 * st.template v<4, 0, 0, 1>()) +
+           r0 * s1 * ((r2 - (T)1) * st.template v<4, 1, 0, -1>() + ((T)1 - t2) * st.template v<4, 1, 0, 0>() + r2 * st.template v<4, 1, 0, 1>()) +
+           s0 * r1 * ((r2 - (T)1) * st.template v<4, 0, 1, -1>() + ((T)1 - t2) * st.template v<4, 0, 1, 0>() + r2 * st.template v<4, 0, 1, 1>()) +
+           r0 * r1 * ((r2 - (T)1) * st.template v<4, 1, 1, -1>() + ((T)1 - t2) * st.template v<4, 1, 1, 0>() + r2 * st.template v<4, 1, 1, 1>())) * q2;
     const T k = pv<T>(pr.inv_a2N, pr.inv_a2N_f) * inv_e;
     g0 += p0 * k;
     g1 += p1 * k;
@@ -489,12 +561,9 @@ __device__ __forceinline__ void kick_one(const T *__restrict__ phi, const T *__r
 }
 
 // the coordinate velocity of update_pos (GR): q (1 + (3 - q^2/e^2) phi - chi) / e + b / (a^2 N)
-template <typename T>
-__device__ __forceinline__ void drift_vel(const T *__restrict__ phi, const T *__restrict__ chi,
-                                          const T *__restrict__ Bi, const Params &pr, const CellNb &nb, T r0,
-                                          T r1, T r2, T q0, T q1, T q2, T &v0, T &v1, T &v2) {
-  const int N = pr.N;
-  const size_t NV = (size_t)N * N * N;
+template <typename T, typename S>
+__device__ __forceinline__ void drift_vel(const S &st, const Params &pr, T r0, T r1, T r2, T q0, T q1, T q2, T &v0,
+                                          T &v1, T &v2) {
   const T s0 = (T)1 - r0, s1 = (T)1 - r1, s2 = (T)1 - r2;
   const T a = pv<T>(pr.a, pr.a_f);
   const T qq = q0 * q0 + q1 * q1 + q2 * q2;
@@ -503,26 +572,25 @@ __device__ __forceinline__ void drift_vel(const T *__restrict__ phi, const T *__
   const T w000 = s0 * s1 * s2, w100 = r0 * s1 * s2, w010 = s0 * r1 * s2, w110 = r0 * r1 * s2;
   const T w001 = s0 * s1 * r2, w101 = r0 * s1 * r2, w011 = s0 * r1 * r2, w111 = r0 * r1 * r2;
   if (pr.nfield >= 1)
-    ph = at<0, 0, 0>(phi, nb) * w000 + at<1, 0, 0>(phi, nb) * w100 + at<0, 1, 0>(phi, nb) * w010 +
-         at<1, 1, 0>(phi, nb) * w110 + at<0, 0, 1>(phi, nb) * w001 + at<1, 0, 1>(phi, nb) * w101 +
-         at<0, 1, 1>(phi, nb) * w011 + at<1, 1, 1>(phi, nb) * w111;
+    ph = st.template v<0, 0, 0, 0>() * w000 + st.template v<0, 1, 0, 0>() * w100 + st.template v<0, 0, 1, 0>() * w010 +
+         st.template v<0, 1, 1, 0>() * w110 + st.template v<0, 0, 0, 1>() * w001 + st.template v<0, 1, 0, 1>() * w101 +
+         st.template v<0, 0, 1, 1>() * w011 + st.template v<0, 1, 1, 1>() * w111;
   if (pr.nfield >= 2)
-    ch = at<0, 0, 0>(chi, nb) * w000 + at<1, 0, 0>(chi, nb) * w100 + at<0, 1, 0>(chi, nb) * w010 +
-         at<1, 1, 0>(chi, nb) * w110 + at<0, 0, 1>(chi, nb) * w001 + at<1, 0, 1>(chi, nb) * w101 +
-         at<0, 1, 1>(chi, nb) * w011 + at<1, 1, 1>(chi, nb) * w111;
+    ch = st.template v<1, 0, 0, 0>() * w000 + st.template v<1, 1, 0, 0>() * w100 + st.template v<1, 0, 1, 0>() * w010 +
+         st.template v<1, 1, 1, 0>() * w110 + st.template v<1, 0, 0, 1>() * w001 + st.template v<1, 1, 0, 1>() * w101 +
+         st.template v<1, 0, 1, 1>() * w011 + st.template v<1, 1, 1, 1>() * w111;
   const T inv_e2 = (T)1 / e2;
   const T fac = ((T)1 + ((T)3 - qq * inv_e2) * ph - ch) * tsqrt<T>(inv_e2);
   v0 = q0 * fac;
   v1 = q1 * fac;
   v2 = q2 * fac;
   if (pr.nfield >= 3) {
-    const T *B0 = Bi, *B1 = Bi + NV, *B2 = Bi + 2 * NV;
-    const T b0 = at<0, 0, 0>(B0, nb) * s1 * s2 + at<0, 1, 0>(B0, nb) * r1 * s2 + at<0, 0, 1>(B0, nb) * s1 * r2 +
-                 at<0, 1, 1>(B0, nb) * r1 * r2;
-    const T b1 = at<0, 0, 0>(B1, nb) * s0 * s2 + at<1, 0, 0>(B1, nb) * r0 * s2 + at<0, 0, 1>(B1, nb) * s0 * r2 +
-                 at<1, 0, 1>(B1, nb) * r0 * r2;
-    const T b2 = at<0, 0, 0>(B2, nb) * s0 * s1 + at<1, 0, 0>(B2, nb) * r0 * s1 + at<0, 1, 0>(B2, nb) * s0 * r1 +
-                 at<1, 1, 0>(B2, nb) * r0 * r1;
+    const T b0 = st.template v<2, 0, 0, 0>() * s1 * s2 + st.template v<2, 0, 1, 0>() * r1 * s2 + st.template v<2, 0, 0, 1>() * s1 * r2 +
+                 st.template v<2, 0, 1, 1>() * r1 * r2;
+    const T b1 = st.template v<3, 0, 0, 0>() * s0 * s2 + st.template v<3, 1, 0, 0>() * r0 * s2 + st.template v<3, 0, 0, 1>() * s0 * r2 +
+                 st.template v<3, 1, 0, 1>() * r0 * r2;
+    const T b2 = st.template v<4, 0, 0, 0>() * s0 * s1 + st.template v<4, 1, 0, 0>() * r0 * s1 + st.template v<4, 0, 1, 0>() * s0 * r1 +
+                 st.template v<4, 1, 1, 0>() * r0 * r1;
     const T ib = pv<T>(pr.inv_a2N, pr.inv_a2N_f);
     v0 += b0 * ib;
     v1 += b1 * ib;
@@ -530,29 +598,68 @@ __device__ __forceinline__ void drift_vel(const T *__restrict__ phi, const T *__
   }
 }
 
-// the particle's linked cell and in-cell offset (the FP32 copy in the mixed form)
-template <typename T>
-__device__ __forceinline__ CellNb load_cell(const PclsArrays &P, long i, int N, int lg, T &r0, T &r1, T &r2) {
-  int cx, cy, cz;
-  const CellNb nb = cell_nb(P.cell[i], N, lg, cx, cy, cz);
+// One particle's payload, read with independent loads before any field gather
+// or store, so that all of it is in flight at once.
+template <typename T, typename V>
+struct Pcl {
+  uint32_t cell;
+  double x, y, z;
+  T q0, q1, q2;
+  float rx, ry, rz;  // the FP32 in-cell offset (mixed form)
+};
+template <typename T, typename V>
+__device__ __forceinline__ Pcl<T, V> load_pcl(const PclsArrays &P, long i, bool pos) {
+  Pcl<T, V> c;
+  c.cell = P.cell[i];
+  if (pos || sizeof(T) == 8) {
+    c.x = P.px[i];
+    c.y = P.py[i];
+    c.z = P.pz[i];
+  }
+  c.q0 = (T)((const V *)P.vx)[i];
+  c.q1 = (T)((const V *)P.vy)[i];
+  c.q2 = (T)((const V *)P.vz)[i];
   if constexpr (sizeof(T) == 4) {
-    r0 = P.rx[i];
-    r1 = P.ry[i];
-    r2 = P.rz[i];
+    c.rx = P.rx[i];
+    c.ry = P.ry[i];
+    c.rz = P.rz[i];
+  }
+  return c;
+}
+// the particle's linked cell and in-cell offset (the FP32 copy in the mixed form)
+template <typename T, typename V>
+__device__ __forceinline__ CellNb cell_of(const Pcl<T, V> &c, int N, int lg, T &r0, T &r1, T &r2) {
+  int cx, cy, cz;
+  const CellNb nb = cell_nb(c.cell, N, lg, cx, cy, cz);
+  if constexpr (sizeof(T) == 4) {
+    r0 = c.rx;
+    r1 = c.ry;
+    r2 = c.rz;
   } else {
-    r0 = (T)(P.px[i] * (double)N - cx);
-    r1 = (T)(P.py[i] * (double)N - cy);
-    r2 = (T)(P.pz[i] * (double)N - cz);
+    r0 = (T)(c.x * (double)N - cx);
+    r1 = (T)(c.y * (double)N - cy);
+    r2 = (T)(c.z * (double)N - cz);
   }
   return nb;
+}
+// the stencil a kernel reads: in registers for FP32, from memory for FP64 (whose
+// 52 doubles would not fit beside the rest)
+template <typename T>
+__device__ __forceinline__ auto stencil(const T *phi, const T *chi, const T *Bi, int N, const CellNb &nb, bool chi_on,
+                                        bool B_on) {
+  const MemStencil<T> m = mem_stencil<T>(phi, chi_on ? chi : nullptr, B_on ? Bi : nullptr, (size_t)N * N * N, nb);
+  if constexpr (sizeof(T) == 4)
+    return reg_stencil<T>(m, m.has_chi, m.has_B);
+  else
+    return m;
 }
 
 // pos += dtau v, periodic wrap into [0, 1), new cell key (and offset) for the relink
 template <typename T>
-__device__ __forceinline__ uint32_t move_store(PclsArrays &P, long i, const Params &pr, T v0, T v1, T v2) {
+__device__ __forceinline__ uint32_t move_store(PclsArrays &P, long i, const Params &pr, T v0, T v1, T v2, double x,
+                                               double y, double z) {
   const int N = pr.N, lg = pr.lg;
   const double dtau = pr.dtau;
-  double x = P.px[i], y = P.py[i], z = P.pz[i];
   uint32_t key;
   if constexpr (sizeof(T) == 4) {
     const float dt = pr.dtau_f;
@@ -606,11 +713,14 @@ __global__ void __launch_bounds__(256) k_update_q(PclsArrays P, long n, const T 
                                                   const T *__restrict__ chi, const T *__restrict__ Bi, Params pr,
                                                   unsigned long long *maxbits) {
   T vmax = (T)0;
+  const bool chi_on = pr.nfield >= 2 && chi, B_on = KIND == GEV_GR && pr.nfield >= 3 && Bi;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const Pcl<T, V> c = load_pcl<T, V>(P, i, false);
     T r0, r1, r2;
-    const CellNb nb = load_cell<T>(P, i, pr.N, pr.lg, r0, r1, r2);
-    T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
-    kick_one<T, KIND>(phi, chi, Bi, pr, nb, r0, r1, r2, q0, q1, q2);
+    const CellNb nb = cell_of<T, V>(c, pr.N, pr.lg, r0, r1, r2);
+    T q0 = c.q0, q1 = c.q1, q2 = c.q2;
+    const auto st = stencil<T>(phi, chi, Bi, pr.N, nb, chi_on, B_on);
+    kick_one<T, KIND>(st, pr, r0, r1, r2, q0, q1, q2);
     ((V *)P.vx)[i] = (V)q0;
     ((V *)P.vy)[i] = (V)q1;
     ((V *)P.vz)[i] = (V)q2;
@@ -624,8 +734,10 @@ __global__ void __launch_bounds__(256) k_update_q(PclsArrays P, long n, const T 
 template <typename T, typename V, int KIND>
 __global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const T *__restrict__ phi,
                                                     const T *__restrict__ chi, const T *__restrict__ Bi, Params pr) {
+  const bool chi_on = pr.nfield >= 2 && chi, B_on = pr.nfield >= 3 && Bi;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
+    const Pcl<T, V> c = load_pcl<T, V>(P, i, true);
+    const T q0 = c.q0, q1 = c.q1, q2 = c.q2;
     T v0, v1, v2;
     if (KIND == GEV_NEWTON) {  // update_pos_Newton: dtau q / a
       const T ia = pv<T>(1.0 / pr.a, pr.inv_a_f);
@@ -634,10 +746,11 @@ __global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const 
       v2 = q2 * ia;
     } else {
       T r0, r1, r2;
-      const CellNb nb = load_cell<T>(P, i, pr.N, pr.lg, r0, r1, r2);
-      drift_vel<T>(phi, chi, Bi, pr, nb, r0, r1, r2, q0, q1, q2, v0, v1, v2);
+      const CellNb nb = cell_of<T, V>(c, pr.N, pr.lg, r0, r1, r2);
+      const auto st = stencil<T>(phi, chi, Bi, pr.N, nb, chi_on, B_on);
+      drift_vel<T>(st, pr, r0, r1, r2, q0, q1, q2, v0, v1, v2);
     }
-    move_store<T>(P, i, pr, v0, v1, v2);
+    move_store<T>(P, i, pr, v0, v1, v2, c.x, c.y, c.z);
   }
 }
 
@@ -650,19 +763,23 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_kick_drift(Pcls
                                                     Params pd, unsigned long long *maxbits, uint32_t *count,
                                                     uint32_t *rank) {
   T vmax = (T)0;
+  const int nf = pk.nfield > pd.nfield ? pk.nfield : pd.nfield;
+  const bool chi_on = nf >= 2 && chi, B_on = nf >= 3 && Bi;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+    const Pcl<T, V> c = load_pcl<T, V>(P, i, true);
     T r0, r1, r2;
-    const CellNb nb = load_cell<T>(P, i, pk.N, pk.lg, r0, r1, r2);
-    T q0 = (T)((const V *)P.vx)[i], q1 = (T)((const V *)P.vy)[i], q2 = (T)((const V *)P.vz)[i];
-    kick_one<T, GEV_GR>(phi, chi, Bi, pk, nb, r0, r1, r2, q0, q1, q2);
+    const CellNb nb = cell_of<T, V>(c, pk.N, pk.lg, r0, r1, r2);
+    T q0 = c.q0, q1 = c.q1, q2 = c.q2;
+    const auto st = stencil<T>(phi, chi, Bi, pk.N, nb, chi_on, B_on);
+    kick_one<T, GEV_GR>(st, pk, r0, r1, r2, q0, q1, q2);
     ((V *)P.vx)[i] = (V)q0;
     ((V *)P.vy)[i] = (V)q1;
     ((V *)P.vz)[i] = (V)q2;
     const T vv = (q0 * q0 + q1 * q1 + q2 * q2) * pv<T>(pk.inv_a2, pk.inv_a2_f);
     vmax = vv > vmax ? vv : vmax;
     T v0, v1, v2;
-    drift_vel<T>(phi, chi, Bi, pd, nb, r0, r1, r2, q0, q1, q2, v0, v1, v2);
-    const uint32_t key = move_store<T>(P, i, pd, v0, v1, v2);
+    drift_vel<T>(st, pd, r0, r1, r2, q0, q1, q2, v0, v1, v2);
+    const uint32_t key = move_store<T>(P, i, pd, v0, v1, v2, c.x, c.y, c.z);
     if (count) rank[i] = atomicAdd(&count[key], 1u);  // the histogram of the relink, fused
   }
   block_max_to<T>(vmax, maxbits);
