@@ -256,64 +256,61 @@ __global__ void k_gather(PclsArrays src, PclsArrays dst, const uint32_t *__restr
 // inside a cell then follows atomic timing, which changes no result of the mixed
 // form (its deposits add integers, the updates are per particle); downloads
 // restore the (cell, ID) order first.
-// Mixed form (FP32 momenta and offsets).  Four consecutive particles per thread,
-// read with 16-byte vector loads (cudaMalloc'd arrays, index a multiple of 4), so
-// that each thread has its whole payload in flight before the scattered stores.
+// Mixed form (FP32 momenta and offsets).  A warp moves 128 consecutive particles
+// per round, lane l the particles l, l + 32, l + 64 and l + 96, all four payloads
+// loaded before any store: every load and every store instruction of the warp
+// covers 32 consecutive particles, and the destinations of consecutive particles
+// (one cell's, or neighbouring cells') are consecutive too, so the scattered
+// stores still fill whole lines.
 __global__ void __launch_bounds__(256) k_move(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ start,
                                               const uint32_t *__restrict__ rank, long n) {
-  const long n4 = n >> 2;
   const float *svx = (const float *)src.vx, *svy = (const float *)src.vy, *svz = (const float *)src.vz;
   float *dvx = (float *)dst.vx, *dvy = (float *)dst.vy, *dvz = (float *)dst.vz;
-  for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < n4; q += (long)gridDim.x * blockDim.x) {
-    const long i = q << 2;
-    const uint4 c = *reinterpret_cast<const uint4 *>(src.cell + i);
-    const uint4 rk = *reinterpret_cast<const uint4 *>(rank + i);
-    const double2 x01 = *reinterpret_cast<const double2 *>(src.px + i), x23 = *reinterpret_cast<const double2 *>(src.px + i + 2);
-    const double2 y01 = *reinterpret_cast<const double2 *>(src.py + i), y23 = *reinterpret_cast<const double2 *>(src.py + i + 2);
-    const double2 z01 = *reinterpret_cast<const double2 *>(src.pz + i), z23 = *reinterpret_cast<const double2 *>(src.pz + i + 2);
-    const longlong2 d01 = *reinterpret_cast<const longlong2 *>(src.id + i), d23 = *reinterpret_cast<const longlong2 *>(src.id + i + 2);
-    const float4 vx = *reinterpret_cast<const float4 *>(svx + i), vy = *reinterpret_cast<const float4 *>(svy + i),
-                 vz = *reinterpret_cast<const float4 *>(svz + i);
-    const float4 rx = *reinterpret_cast<const float4 *>(src.rx + i), ry = *reinterpret_cast<const float4 *>(src.ry + i),
-                 rz = *reinterpret_cast<const float4 *>(src.rz + i);
-    const uint32_t j[4] = {start[c.x] + rk.x, start[c.y] + rk.y, start[c.z] + rk.z, start[c.w] + rk.w};
-    const uint32_t cc[4] = {c.x, c.y, c.z, c.w};
-    const double X[4] = {x01.x, x01.y, x23.x, x23.y}, Y[4] = {y01.x, y01.y, y23.x, y23.y},
-                 Z[4] = {z01.x, z01.y, z23.x, z23.y};
-    const long long D[4] = {d01.x, d01.y, d23.x, d23.y};
-    const float VX[4] = {vx.x, vx.y, vx.z, vx.w}, VY[4] = {vy.x, vy.y, vy.z, vy.w}, VZ[4] = {vz.x, vz.y, vz.z, vz.w};
-    const float RX[4] = {rx.x, rx.y, rx.z, rx.w}, RY[4] = {ry.x, ry.y, ry.z, ry.w}, RZ[4] = {rz.x, rz.y, rz.z, rz.w};
+  const int lane = threadIdx.x & 31;
+  const long nw = (n + 127) >> 7, nwarps = ((long)gridDim.x * blockDim.x) >> 5;
+  for (long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5; w < nw; w += nwarps) {
+    const long i0 = (w << 7) + lane;
+    uint32_t c[4], t[4];
+    double X[4], Y[4], Z[4];
+    long long D[4];
+    float VX[4], VY[4], VZ[4], RX[4], RY[4], RZ[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
-      const uint32_t t = j[k];
-      dst.px[t] = X[k];
-      dst.py[t] = Y[k];
-      dst.pz[t] = Z[k];
-      dvx[t] = VX[k];
-      dvy[t] = VY[k];
-      dvz[t] = VZ[k];
-      dst.id[t] = D[k];
-      dst.cell[t] = cc[k];
-      dst.rx[t] = RX[k];
-      dst.ry[t] = RY[k];
-      dst.rz[t] = RZ[k];
+      const long i = i0 + 32 * k;
+      if (i < n) {
+        c[k] = src.cell[i];
+        t[k] = rank[i];
+        X[k] = src.px[i];
+        Y[k] = src.py[i];
+        Z[k] = src.pz[i];
+        D[k] = src.id[i];
+        VX[k] = svx[i];
+        VY[k] = svy[i];
+        VZ[k] = svz[i];
+        RX[k] = src.rx[i];
+        RY[k] = src.ry[i];
+        RZ[k] = src.rz[i];
+      }
     }
-  }
-  // the last n % 4 particles
-  for (long i = (n4 << 2) + blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const uint32_t c = src.cell[i];
-    const uint32_t t = start[c] + rank[i];
-    dst.px[t] = src.px[i];
-    dst.py[t] = src.py[i];
-    dst.pz[t] = src.pz[i];
-    dvx[t] = svx[i];
-    dvy[t] = svy[i];
-    dvz[t] = svz[i];
-    dst.id[t] = src.id[i];
-    dst.cell[t] = c;
-    dst.rx[t] = src.rx[i];
-    dst.ry[t] = src.ry[i];
-    dst.rz[t] = src.rz[i];
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (i0 + 32 * k < n) t[k] += start[c[k]];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      if (i0 + 32 * k >= n) continue;
+      const uint32_t j = t[k];
+      dst.px[j] = X[k];
+      dst.py[j] = Y[k];
+      dst.pz[j] = Z[k];
+      dvx[j] = VX[k];
+      dvy[j] = VY[k];
+      dvz[j] = VZ[k];
+      dst.id[j] = D[k];
+      dst.cell[j] = c[k];
+      dst.rx[j] = RX[k];
+      dst.ry[j] = RY[k];
+      dst.rz[j] = RZ[k];
+    }
   }
 }
 
@@ -758,7 +755,7 @@ __global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const 
 // in one pass: both read the same cell and the same phi / chi / B values.  The
 // drift's scale factor (after the background half step) comes in pd.
 template <typename T, typename V>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_kick_drift(PclsArrays P, long n, const T *__restrict__ phi,
+__global__ void __launch_bounds__(256, 2) k_kick_drift(PclsArrays P, long n, const T *__restrict__ phi,
                                                     const T *__restrict__ chi, const T *__restrict__ Bi, Params pk,
                                                     Params pd, unsigned long long *maxbits, uint32_t *count,
                                                     uint32_t *rank) {

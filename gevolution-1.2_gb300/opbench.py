@@ -81,6 +81,8 @@ def main():
         ("fft_axis_z", lambda: gpu.fft_axis(sFT, 2, -1)),
         ("kick", lambda: gpu.update_q(p, 0, 1e-9, phi, chi, Bi, 3, a, a * a * N)),
         ("drift_relink", lambda: gpu.update_pos(p, 0, 1e-9, phi, chi, Bi, 3, a, a * a * N)),
+        # the cycle's own particle path: kick, drift and histogram in one pass, scan, move
+        ("kick_drift_move", lambda: gpu.update_q_pos(p, 1e-9, a, 3, 1e-9, a, 3, phi, chi, Bi, wait=False)),
     ]
     names = [n for n, _ in ops]
     if args.only and args.only not in names:
