@@ -321,27 +321,22 @@ __global__ void __launch_bounds__(FX_THREADS, 3) k_dep_fx(PclsArrays P, const ui
 // T00 and Tij as a gather: each grid node sums, in int64 registers, the
 // contributions of the particles in its 8 neighbouring cells.
 //
-// Prefactor arrays, 9 words a particle (SoA): [0] Q00 = round(m e 2^kq0), [1] rT =
-// (3e + q^2/e) / e, [2..4] Qd_i = round(m q_i^2 / e 2^kq1), [5..7] Qo = round(m q_i q_j / e
-// 2^kq1) for 01, 02, 12, [8] fT = 4 + a^2 / (q^2 + a^2).  Written by k_fx_prep.
+// Prefactor records, one per particle in store order, 12 words (three 16-byte
+// vectors) written by k_fx_prep, so that a particle visit of the gather is three
+// vector loads from one address:
+//   [0..2] the in-cell offset (rx, ry, rz)      [3] Q00 = round(m e 2^kq0)
+//   [4] rT = (3e + q^2/e) / e                    [5] fT = 4 + a^2 / (q^2 + a^2)
+//   [6], [7], [8] Qd_i = round(m q_i^2 / e 2^kq1)
+//   [9], [10], [11] Qo = round(m q_i q_j / e 2^kq1) for 01, 02, 12
+// Words a kind does not deposit are zero.  T00 alone keeps a record of two
+// words, (Q00, rT), and reads the offsets from the particle store.
+constexpr int PREP_WORDS = 12;
 struct PrepArrays {
-  int *q00;
-  float *rT;
-  int *qd0, *qd1, *qd2, *qo01, *qo02, *qo12;
-  float *fT;
+  uint4 *rec;  // 3 vectors per particle
 };
-inline PrepArrays prep_arrays(void *base, long cap) {
+inline PrepArrays prep_arrays(void *base, long) {
   PrepArrays a;
-  int *w = (int *)base;
-  a.q00 = w;
-  a.rT = (float *)(w + cap);
-  a.qd0 = w + 2 * cap;
-  a.qd1 = w + 3 * cap;
-  a.qd2 = w + 4 * cap;
-  a.qo01 = w + 5 * cap;
-  a.qo02 = w + 6 * cap;
-  a.qo12 = w + 7 * cap;
-  a.fT = (float *)(w + 8 * cap);
+  a.rec = (uint4 *)base;
   return a;
 }
 
@@ -358,28 +353,41 @@ __global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArray
     const float q0 = ((const float *)P.vx)[j], q1 = ((const float *)P.vy)[j], q2 = ((const float *)P.vz)[j];
     const float f2 = __fadd_rn(__fadd_rn(__fmul_rn(q0, q0), __fmul_rn(q1, q1)), __fmul_rn(q2, q2));
     const float ee = __fsqrt_rn(__fadd_rn(f2, a2));
+    uint4 v0 = make_uint4(0u, 0u, 0u, 0u);
+    if (KIND != FX_T00) v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), 0u);
+    uint4 v1 = make_uint4(0u, 0u, 0u, 0u), v2 = make_uint4(0u, 0u, 0u, 0u);
     if (KIND == FX_T00 || KIND == FX_T00TIJ) {
       const float e00 = have_phi ? ee : a;
       const float r = have_phi ? __fdiv_rn(__fadd_rn(__fmul_rn(3.f, ee), __fdiv_rn(f2, ee)), ee) : 0.f;
-      A.q00[j] = fixed32_of(__fmul_rn(__fmul_rn(m, e00), sq0));
-      A.rT[j] = r;
+      v0.w = (unsigned)fixed32_of(__fmul_rn(__fmul_rn(m, e00), sq0));
+      v1.x = __float_as_uint(r);
     }
     if (KIND == FX_TIJ || KIND == FX_T00TIJ) {
       const float inv_e = __fdiv_rn(1.f, ee), mi = __fmul_rn(m, inv_e);
-      A.fT[j] = __fadd_rn(4.f, __fdiv_rn(a2, __fadd_rn(f2, a2)));
-      A.qd0[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q0, q0), mi), sqT));
-      A.qd1[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q1, q1), mi), sqT));
-      A.qd2[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q2, q2), mi), sqT));
-      A.qo01[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q0, q1), mi), sqT));
-      A.qo02[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q0, q2), mi), sqT));
-      A.qo12[j] = fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q1, q2), mi), sqT));
+      v1.y = __float_as_uint(__fadd_rn(4.f, __fdiv_rn(a2, __fadd_rn(f2, a2))));
+      v1.z = (unsigned)fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q0, q0), mi), sqT));
+      v1.w = (unsigned)fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q1, q1), mi), sqT));
+      v2.x = (unsigned)fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q2, q2), mi), sqT));
+      v2.y = (unsigned)fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q0, q1), mi), sqT));
+      v2.z = (unsigned)fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q0, q2), mi), sqT));
+      v2.w = (unsigned)fixed32_of(__fmul_rn(__fmul_rn(__fmul_rn(q1, q2), mi), sqT));
+    }
+    if (KIND == FX_T00) {
+      reinterpret_cast<uint2 *>(A.rec)[j] = make_uint2(v0.w, v1.x);
+    } else {
+      uint4 *o = A.rec + 3 * j;
+      o[0] = v0;
+      o[1] = v1;
+      o[2] = v2;
     }
   }
 }
 
-// one thread per node (x, y, z); out: T00 (1 comp) and / or Tij (6 comps, 00 01 02 11 12 22)
+// one thread per node (x, y, z); out: T00 (1 comp) and / or Tij (6 comps, 00 01 02 11 12 22).
+// At most 64 registers (four resident blocks per SM; 40 and six blocks for T00
+// alone): the loop is latency-bound.
 template <int KIND>
-__global__ void __launch_bounds__(256) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
+__global__ void __launch_bounds__(256, KIND == FX_T00 ? 6 : 4) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
                                                     const float *__restrict__ phi, float *t00, float *tij, FxParams p,
                                                     Div32 dN, const uint32_t *__restrict__ fxb) {
   constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
@@ -409,24 +417,37 @@ __global__ void __launch_bounds__(256) k_dep_gather(PclsArrays P, const uint32_t
     // the contributions of particle j to this node, the node being corner (dx, dy, dz)
     // of the particle's cell
     auto add = [&](uint32_t j, int dx, int dy, int dz) {
-      const float u0 = P.rx[j], u1 = P.ry[j], u2 = P.rz[j];
+      uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
+      if constexpr (KIND == FX_T00) {
+        const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
+        v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), q.x);
+        v1 = make_uint4(q.y, 0u, 0u, 0u);
+      } else {
+        const uint4 *rec = A.rec + 3 * (size_t)j;
+        v0 = __ldg(rec);
+        v1 = __ldg(rec + 1);
+        v2 = __ldg(rec + 2);
+      }
+      const float u0 = __uint_as_float(v0.x), u1 = __uint_as_float(v0.y), u2 = __uint_as_float(v0.z);
       const float w0 = dx ? u0 : __fsub_rn(1.f, u0), w1 = dy ? u1 : __fsub_rn(1.f, u1),
                   w2 = dz ? u2 : __fsub_rn(1.f, u2);
       const float w = __fmul_rn(__fmul_rn(w0, w1), w2);
-      if (DO00) a00 += (long long)A.q00[j] * (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(A.rT[j], pn))), sg00);
+      if (DO00)
+        a00 += (long long)(int)v0.w *
+               (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), pn))), sg00);
       if (DOIJ) {
-        const float f = A.fT[j];
+        const float f = __uint_as_float(v1.y);
         const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(f, pn))), sgij);
-        ad0 += (long long)A.qd0[j] * G;
-        ad1 += (long long)A.qd1[j] * G;
-        ad2 += (long long)A.qd2[j] * G;
+        ad0 += (long long)(int)v1.z * G;
+        ad1 += (long long)(int)v1.w * G;
+        ad2 += (long long)(int)v2.x * G;
         const float qf = __fmul_rn(0.25f, f);
         if (dx == 0 && dy == 0)
-          ao01 += (long long)A.qo01[j] * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, s01))), sgij);
+          ao01 += (long long)(int)v2.y * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, s01))), sgij);
         if (dx == 0 && dz == 0)
-          ao02 += (long long)A.qo02[j] * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, s02))), sgij);
+          ao02 += (long long)(int)v2.z * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, s02))), sgij);
         if (dy == 0 && dz == 0)
-          ao12 += (long long)A.qo12[j] * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, s12))), sgij);
+          ao12 += (long long)(int)v2.w * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, s12))), sgij);
       }
     };
     // the 4 cell pairs (x - 1, x) of rows (y - dy, z - dz): all their bounds first;
@@ -555,7 +576,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   GEV_LAUNCH_CHECK(ctx);
   if (gather) {
     if (!p->prep) {
-      const size_t bytes = (size_t)(p->cap > 0 ? p->cap : 1) * 9 * 4;
+      const size_t bytes = (size_t)(p->cap > 0 ? p->cap : 1) * PREP_WORDS * 4;
       if (cudaMalloc(&p->prep, bytes) != cudaSuccess) {
         cudaGetLastError();
         return gev_fail(ctx, GEV_ENOMEM, "deposit: prefactor scratch allocation failed");
