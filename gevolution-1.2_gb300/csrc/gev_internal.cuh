@@ -101,9 +101,10 @@ struct gev_pcls {
   bool id_order = true;
   // mixed-form deposit scales (16 words): [0] max |q|^2 and [4] max |phi| (FP32 bits),
   // [1] max particles in a cell, [2], [3] the accumulator scale powers of the last
-  // deposit's groups, [5..8] their prefactor and weight-factor powers
+  // deposit's groups, [5..8] their prefactor and weight-factor powers; [15] set by an
+  // upload whose particles are not in (cell, ID) order
   uint32_t *bounds = nullptr;
-  // mixed-form T00 / Tij deposit: per-particle integer prefactors (9 words a particle,
+  // mixed-form T00 / Tij deposit: per-particle prefactor records (12 words a particle,
   // allocated on first use)
   void *prep = nullptr;
   size_t bytes = 0;  // device bytes this store counts in its context's bytes_in_use

@@ -40,9 +40,7 @@ __device__ __forceinline__ double wrap01(double p) {
 
 // ------------------------------------------------------------ upload ----
 template <typename V>
-__global__ void k_unpack(const gev_part *__restrict__ in, long n, PclsArrays P, int N) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    const gev_part q = in[i];
+__device__ __forceinline__ void unpack_one(const gev_part &q, long i, PclsArrays &P, int N) {
     P.px[i] = q.pos[0];
     P.py[i] = q.pos[1];
     P.pz[i] = q.pos[2];
@@ -59,20 +57,80 @@ __global__ void k_unpack(const gev_part *__restrict__ in, long n, PclsArrays P, 
       pos_split(q.pos[2], N, lg, cz, P.rz[i]);
       P.cell[i] = (uint32_t)cx + (uint32_t)N * ((uint32_t)cy + (uint32_t)N * (uint32_t)cz);
     }
-  }
+}
+template <typename V>
+__global__ void k_unpack(const gev_part *__restrict__ in, long n, PclsArrays P, int N) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    unpack_one<V>(in[i], i, P, N);
+}
+template <typename V>
+__device__ __forceinline__ gev_part pack_one(const PclsArrays &P, long i) {
+  gev_part q;
+  q.pos[0] = P.px[i];
+  q.pos[1] = P.py[i];
+  q.pos[2] = P.pz[i];
+  q.vel[0] = (double)((const V *)P.vx)[i];
+  q.vel[1] = (double)((const V *)P.vy)[i];
+  q.vel[2] = (double)((const V *)P.vz)[i];
+  q.ID = P.id[i];
+  return q;
 }
 template <typename V>
 __global__ void k_pack(gev_part *__restrict__ out, long n, PclsArrays P) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
-    gev_part q;
-    q.pos[0] = P.px[i];
-    q.pos[1] = P.py[i];
-    q.pos[2] = P.pz[i];
-    q.vel[0] = (double)((const V *)P.vx)[i];
-    q.vel[1] = (double)((const V *)P.vy)[i];
-    q.vel[2] = (double)((const V *)P.vz)[i];
-    q.ID = P.id[i];
-    out[i] = q;
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+    out[i] = pack_one<V>(P, i);
+}
+
+// Records read from / written to the caller's host buffer directly, when it is
+// pinned or registered memory (the GPU reaches it over NVLink-C2C): no device
+// staging copy.  A block moves 256 records (14336 bytes, 896 16-byte vectors)
+// through shared memory, so that every host access of a warp is one contiguous
+// run of 16-byte vectors; an odd record count leaves a last 8-byte half vector.
+constexpr int HREC = 256, HVEC = HREC * 56 / 16;
+template <typename V>
+__global__ void __launch_bounds__(256) k_unpack_host(const gev_part *in, long n, PclsArrays P, int N) {
+  __shared__ uint4 s[HVEC];
+  const long ntile = (n + HREC - 1) / HREC;
+  for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
+    const long r0 = t * HREC;
+    const int cnt = (int)(n - r0 < HREC ? n - r0 : HREC);
+    const int nv = (cnt * 56) >> 4;
+    const uint4 *src = reinterpret_cast<const uint4 *>(in + r0);  // r0 even: 16-byte aligned
+    __syncthreads();
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) s[k] = src[k];
+    if ((cnt & 1) && threadIdx.x == 0)
+      reinterpret_cast<uint2 *>(s)[2 * nv] = reinterpret_cast<const uint2 *>(src)[2 * nv];
+    __syncthreads();
+    if ((int)threadIdx.x < cnt)
+      unpack_one<V>(*reinterpret_cast<const gev_part *>(reinterpret_cast<const char *>(s) + threadIdx.x * 56),
+                    r0 + threadIdx.x, P, N);
+  }
+}
+template <typename V>
+__global__ void __launch_bounds__(256) k_pack_host(gev_part *out, long n, PclsArrays P) {
+  __shared__ uint4 s[HVEC];
+  const long ntile = (n + HREC - 1) / HREC;
+  for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
+    const long r0 = t * HREC;
+    const int cnt = (int)(n - r0 < HREC ? n - r0 : HREC);
+    const int nv = (cnt * 56) >> 4;
+    __syncthreads();
+    if ((int)threadIdx.x < cnt)
+      *reinterpret_cast<gev_part *>(reinterpret_cast<char *>(s) + threadIdx.x * 56) = pack_one<V>(P, r0 + threadIdx.x);
+    __syncthreads();
+    uint4 *dst = reinterpret_cast<uint4 *>(out + r0);
+    for (int k = threadIdx.x; k < nv; k += blockDim.x) dst[k] = s[k];
+    if ((cnt & 1) && threadIdx.x == 0)
+      reinterpret_cast<uint2 *>(dst)[2 * nv] = reinterpret_cast<const uint2 *>(s)[2 * nv];
+  }
+}
+
+// flag[0] = 1 if the particles are not in strictly increasing (cell, ID) order
+__global__ void k_unordered(const uint32_t *__restrict__ cell, const int64_t *__restrict__ id, long n,
+                            uint32_t *flag) {
+  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i + 1 < n; i += (long)gridDim.x * blockDim.x) {
+    const uint32_t c0 = cell[i], c1 = cell[i + 1];
+    if (c0 > c1 || (c0 == c1 && id[i] >= id[i + 1])) *flag = 1u;
   }
 }
 
@@ -461,7 +519,7 @@ __device__ __forceinline__ RegStencil<T> reg_stencil(const MemStencil<T> &m, boo
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     const uint32_t i = b.base + ((k & 1) ? b.xp : 0u) + ((k & 2) ? b.yp : 0u) + ((k & 4) ? b.zp : 0u);
-    r.p[k] = __ldg(m.phi + i);
+    r.p[k] = m.phi ? __ldg(m.phi + i) : (T)0;  // no phi: a drift with nfield = 0
     r.c[k] = chi_on ? __ldg(m.chi + i) : (T)0;
   }
 #pragma unroll
@@ -913,6 +971,45 @@ int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, 
 }
 
 // restore the (cell, ID) order after moves that skipped it
+// The device address of a host buffer that kernels may access directly (pinned
+// or registered memory, 16-byte aligned), or nullptr: pageable memory goes
+// through a device staging copy instead.
+static const void *host_alias(const void *h) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, h) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || a.devicePointer == nullptr || ((uintptr_t)a.devicePointer & 15u) != 0u)
+    return nullptr;
+  return a.devicePointer;
+}
+
+int pcls_relink(gev_ctx *ctx, gev_pcls *p);
+
+// relink of uploaded particles: a store already in (cell, ID) order -- as
+// gev_pcls_download writes it -- needs only its cell counts and starts (one read
+// of the cell keys and IDs decides, and the host waits for that answer)
+static int relink_uploaded(gev_ctx *ctx, gev_pcls *p) {
+  if (p->n < 2) return pcls_relink(ctx, p);
+  const long C = (long)ctx->N * ctx->N * ctx->N;
+  const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->bounds + 15, 0, sizeof(uint32_t), ctx->stream));
+  k_unordered<<<pb, 256, 0, ctx->stream>>>(p->cur.cell, p->cur.id, p->n, p->bounds + 15);
+  GEV_LAUNCH_CHECK(ctx);
+  uint32_t unordered = 1u;
+  GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(&unordered, p->bounds + 15, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  if (unordered) return pcls_relink(ctx, p);
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->count, 0, C * sizeof(uint32_t), ctx->stream));
+  k_count<<<pb, 256, 0, ctx->stream>>>(p->cur.cell, p->n, p->count, p->rank);
+  GEV_LAUNCH_CHECK(ctx);
+  int rc = scan_cells(ctx, p);
+  if (rc) return rc;
+  p->id_order = true;
+  return GEV_OK;
+}
+
 int pcls_id_order(gev_ctx *ctx, gev_pcls *p) {
   if (p->id_order || p->n == 0) return GEV_OK;
   const long C = (long)ctx->N * ctx->N * ctx->N;
@@ -1074,6 +1171,15 @@ int gev_pcls_upload(gev_pcls *p, const gev_part *host, long n) {
   gev_ctx *ctx = p->ctx;
   p->n = n;
   if (n > 0) {
+    if (const gev_part *h = (const gev_part *)host_alias(host)) {
+      const int hb = grid_for(ctx, (size_t)((n + HREC - 1) / HREC), 1, 8);
+      if (ctx->prec == GEV_PREC_FP64)
+        k_unpack_host<double><<<hb, 256, 0, ctx->stream>>>(h, n, p->cur, ctx->N);
+      else
+        k_unpack_host<float><<<hb, 256, 0, ctx->stream>>>(h, n, p->cur, ctx->N);
+      GEV_LAUNCH_CHECK(ctx);
+      return relink_uploaded(ctx, p);
+    }
     gev_part *d = nullptr;
     GEV_CHECK_CUDA(ctx, cudaMallocAsync(&d, n * sizeof(gev_part), ctx->stream));
     GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(d, host, n * sizeof(gev_part), cudaMemcpyHostToDevice, ctx->stream));
@@ -1085,7 +1191,7 @@ int gev_pcls_upload(gev_pcls *p, const gev_part *host, long n) {
     GEV_LAUNCH_CHECK(ctx);
     GEV_CHECK_CUDA(ctx, cudaFreeAsync(d, ctx->stream));
   }
-  return pcls_relink(ctx, p);
+  return relink_uploaded(ctx, p);
 }
 
 int gev_pcls_download(gev_pcls *p, gev_part *host, long *n) {
@@ -1094,7 +1200,15 @@ int gev_pcls_download(gev_pcls *p, gev_part *host, long *n) {
   if (n) *n = p->n;
   int rc = pcls_id_order(ctx, p);
   if (rc) return rc;
-  if (p->n > 0) {
+  if (p->n > 0 && host_alias(host)) {
+    gev_part *h = (gev_part *)host_alias(host);
+    const int hb = grid_for(ctx, (size_t)((p->n + HREC - 1) / HREC), 1, 8);
+    if (ctx->prec == GEV_PREC_FP64)
+      k_pack_host<double><<<hb, 256, 0, ctx->stream>>>(h, p->n, p->cur);
+    else
+      k_pack_host<float><<<hb, 256, 0, ctx->stream>>>(h, p->n, p->cur);
+    GEV_LAUNCH_CHECK(ctx);
+  } else if (p->n > 0) {
     gev_part *d = nullptr;
     GEV_CHECK_CUDA(ctx, cudaMallocAsync(&d, p->n * sizeof(gev_part), ctx->stream));
     const int b = grid_for(ctx, (size_t)p->n, 256, 16);

@@ -246,3 +246,66 @@ def test_damaged_hibernation_files_are_refused(gpu, tmp_path):
         gpu.Sim(gpu.Context(16, gpu.PREC_FP64), 16 ** 3).restart(path)
     s2.restart(path)  # the intact file still loads
     assert os.path.getsize(path) == len(raw)
+
+
+def pinned(gpu, n):
+    """A pinned host buffer of n particle records (the direct host-access path of
+    upload and download) and its numpy view."""
+    torch = pytest.importorskip("torch")
+    buf = torch.empty(max(n, 1) * gpu.PART.itemsize, dtype=torch.uint8, pin_memory=True)
+    return buf, buf.numpy().view(gpu.PART)[:n]
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("n", [1, 255, 257, 4097])
+def test_pinned_upload_download_match_pageable(gpu, prec, n):
+    """Upload and download through pinned memory (the kernels read and write the host
+    buffer directly) give the same bits as through pageable memory (a device staging
+    copy); odd counts exercise the last half vector of a block's tile.  An upload
+    already in (cell, ID) order -- a download -- takes the order-preserving relink, and
+    the next cycle is the same bits either way."""
+    N = 16
+    rng = np.random.default_rng(n)
+    parts = np.zeros(n, gpu.PART)
+    parts["pos"] = rng.random((n, 3))
+    parts["vel"] = rng.standard_normal((n, 3)) * 1e-3
+    parts["ID"] = rng.permutation(4 * n)[:n]
+    ctx = gpu.Context(N, prec)
+    a = gpu.Particles(ctx, n, 1.0).upload(parts)
+    ref = a.download()
+    _keep, hp = pinned(gpu, n)
+    hp[:] = parts
+    b = gpu.Particles(ctx, n, 1.0).upload(hp)
+    _keep2, out = pinned(gpu, n)
+    b.download(out=out)
+    assert np.array_equal(out.view(np.uint8), ref.view(np.uint8))
+    # ordered upload from pinned memory, then one update of both stores
+    c = gpu.Particles(ctx, n, 1.0).upload(out)
+    phi = ctx.real(1).upload(rng.standard_normal((N, N, N)) * 1e-5)
+    for p in (a, c):
+        gpu.update_pos(p, 0, 0.3, phi, None, None, 1, 1.0, float(N))
+    _keep3, o2 = pinned(gpu, n)
+    c.download(out=o2)
+    assert np.array_equal(o2.view(np.uint8), a.download().view(np.uint8))
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_drift_without_fields(gpu, prec):
+    """moveParticles(update_pos) in GR with nfield = 0: no field is read, each particle
+    moves by dtau q / sqrt(q^2 + a^2) (wrapped into the box)."""
+    N, n, dtau, a = 16, 1000, 0.5, 0.8
+    rng = np.random.default_rng(5)
+    parts = np.zeros(n, gpu.PART)
+    parts["pos"] = rng.random((n, 3))
+    parts["vel"] = rng.standard_normal((n, 3)) * 1e-2
+    parts["ID"] = np.arange(n)
+    ctx = gpu.Context(N, prec)
+    p = gpu.Particles(ctx, n, 1.0).upload(parts)
+    gpu.update_pos(p, 0, dtau, None, None, None, 0, a, a * a * N)
+    got = p.download()
+    got = got[np.argsort(got["ID"])]
+    q = parts["vel"]
+    want = (parts["pos"] + dtau * q / np.sqrt((q * q).sum(1) + a * a)[:, None]) % 1.0
+    d = np.abs(got["pos"] - want)
+    d = np.minimum(d, 1.0 - d)
+    assert d.max() < (1e-12 if prec == 0 else 1e-6)
