@@ -288,9 +288,9 @@ COLS_TRAFFIC = {(512, "mixed"): 1.0675e9}
 # DRAM traffic per call of the T00 + Tij deposit: its prefactor pass (k_fx_prep) and
 # its gather (k_dep_gather), from an ncu capture of the same kernels on the 256^3
 # cycle (opbench --grid 256 --only step), scaled by 8 to 512^3: particles and fields
-# both grow as N^3.  k_fx_prep 201.4 MB read + 544.4 MB written, k_dep_gather
-# 1254.6 MB read + 455.6 MB written; (2455.9 MB) x 8
-DEPOSIT_TRAFFIC = {(512, "mixed"): 19.647e9}
+# both grow as N^3.  k_fx_prep 404.0 MB read + 746.4 MB written, k_dep_gather
+# 1499.8 MB read + 458.8 MB written; (3109.0 MB) x 8
+DEPOSIT_TRAFFIC = {(512, "mixed"): 24.872e9}
 
 
 def deposit_roofline(gpu, ctx, sim, stream, N, prec):
@@ -299,8 +299,8 @@ def deposit_roofline(gpu, ctx, sim, stream, N, prec):
     its scale pass and its prefactor pass.  Its algorithmic bytes per call: each
     particle's cell, in-cell offset and momentum read once (4 + 3r + 3r bytes), phi
     read once and the 7 target components written once per cell (8 r bytes), r the
-    real size of the form.  The prefactor scratch the gather writes and reads back
-    (36 B a particle) is not algorithmic and shows in the traffic."""
+    real size of the form.  The prefactor records the gather writes and reads back
+    (48 B a particle) are not algorithmic and show in the traffic."""
     import torch
     r = 8 if prec == "fp64" else 4
     p, src, Sij, phi = sim.particles(), sim.field("source"), sim.field("Sij"), sim.field("phi")
