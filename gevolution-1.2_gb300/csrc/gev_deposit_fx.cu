@@ -384,10 +384,10 @@ __global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArray
 }
 
 // one thread per node (x, y, z); out: T00 (1 comp) and / or Tij (6 comps, 00 01 02 11 12 22).
-// At most 64 registers (four resident blocks per SM; 51 and five blocks for T00
-// alone): the loop is latency-bound.
+// Six resident blocks per SM (40 registers; 48 and five blocks for T00 alone): the
+// loop is latency-bound, and the warps hide more than the few spilled words cost.
 template <int KIND>
-__global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 4) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
+__global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
                                                     const float *__restrict__ phi, float *t00, float *tij, FxParams p,
                                                     Div32 dN, const uint32_t *__restrict__ fxb) {
   constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;

@@ -122,6 +122,11 @@ struct RegFft {
   }
 };
 
+// row of natural-order element k in the tile the row kernels write after the last
+// stage: bit 0 flipped by bit 4, so that the four thread groups of a warp, whose
+// outputs lie 16 elements apart, fall on both halves of the banks
+__device__ __forceinline__ int nat(int k) { return k ^ ((k >> 4) & 1); }
+
 template <typename C>
 __device__ __forceinline__ void stage_tw(C *tw, const C *__restrict__ g, int L) {
   for (int i = threadIdx.x; i < L; i += blockDim.x) tw[i] = __ldg(&g[i]);
@@ -187,7 +192,7 @@ __global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k
     R::template run_from<0>(v, X, B, c, m, tw);
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 8; ++q) X[(kb | R::freq(q)) * B + c] = v[q];  // Z[k], natural order
+    for (int q = 0; q < 8; ++q) X[nat(kb | R::freq(q)) * B + c] = v[q];  // Z[k], natural order
     __syncthreads();
     if (on) {
       C *dst = out + row * NH;
@@ -195,8 +200,8 @@ __global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k
       for (int r = 0; r <= 8; ++r) {
         if (r == 8 && m != 0) break;
         const int k = r < 8 ? m + r * R::TPL : L;
-        const C zk = X[(k & (L - 1)) * B + c];
-        const C zc = cconj(X[((L - k) & (L - 1)) * B + c]);
+        const C zk = X[nat(k & (L - 1)) * B + c];
+        const C zc = cconj(X[nat((L - k) & (L - 1)) * B + c]);
         const C E = cscale((T)0.5, cadd(zk, zc));
         const C d = csub(zk, zc);
         const C O = cmk<C>((T)0.5 * d.y, (T)-0.5 * d.x);  // -i/2 (zk - zc)
@@ -250,14 +255,14 @@ __global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k
     R::template run_from<0>(v, X, B, c, m, tw);
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 8; ++q) X[(kb | R::freq(q)) * B + c] = v[q];
+    for (int q = 0; q < 8; ++q) X[nat(kb | R::freq(q)) * B + c] = v[q];
     __syncthreads();
     if (on) {
       C *dst = reinterpret_cast<C *>(out) + row * L;
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
         const int k = m + r * R::TPL;
-        dst[k] = X[k * B + c];
+        dst[k] = X[nat(k) * B + c];
       }
     }
   }

@@ -33,6 +33,27 @@ def main():
 
     N = args.grid
     ctx = gpu.Context(N, gpu.PREC_MIXED if args.prec == "mixed" else gpu.PREC_FP64)
+    if args.only in ("r2c_alone", "c2r_alone"):
+        # one real component and its spectrum and nothing else: the row and column kernels
+        # of one 3-D transform, small enough for a full profiler capture at 512^3
+        import numpy as np
+        rng = np.random.default_rng(1)
+        real, spec = ctx.real(1), ctx.spectrum(1)
+        real.upload(rng.standard_normal(real.shape))
+        gpu.fft_r2c(real, spec)
+        fn = (lambda: gpu.fft_r2c(real, spec)) if args.only == "r2c_alone" else (lambda: gpu.fft_c2r(spec, real))
+        st = torch.cuda.ExternalStream(ctx.stream())
+        fn()
+        ctx.sync()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(args.reps):
+            fn()
+        e1.record(st)
+        e1.synchronize()
+        print("grid %d^3, %s form, one component; %s %.3f ms per call (CUDA events), %d calls"
+              % (N, args.prec, args.only, e0.elapsed_time(e1) / args.reps, args.reps))
+        return
     if args.only in ("fft_axis_y", "fft_axis_z"):
         # one spectrum component of random values and nothing else (small enough for a
         # full profiler capture at 512^3): the same kernel as inside the cycle
