@@ -106,8 +106,11 @@ __global__ void __launch_bounds__(256) k_unpack_host(const gev_part *in, long n,
                     r0 + threadIdx.x, P, N);
   }
 }
+// perm: when given, record i is particle perm[i] of the store (the store's own order
+// is left as it is)
 template <typename V>
-__global__ void __launch_bounds__(256) k_pack_host(gev_part *out, long n, PclsArrays P) {
+__global__ void __launch_bounds__(256) k_pack_host(gev_part *out, long n, PclsArrays P,
+                                                   const uint32_t *__restrict__ perm) {
   __shared__ uint4 s[HVEC];
   const long ntile = (n + HREC - 1) / HREC;
   for (long t = blockIdx.x; t < ntile; t += gridDim.x) {
@@ -115,8 +118,11 @@ __global__ void __launch_bounds__(256) k_pack_host(gev_part *out, long n, PclsAr
     const int cnt = (int)(n - r0 < HREC ? n - r0 : HREC);
     const int nv = (cnt * 56) >> 4;
     __syncthreads();
-    if ((int)threadIdx.x < cnt)
-      *reinterpret_cast<gev_part *>(reinterpret_cast<char *>(s) + threadIdx.x * 56) = pack_one<V>(P, r0 + threadIdx.x);
+    if ((int)threadIdx.x < cnt) {
+      const long i = r0 + threadIdx.x;
+      *reinterpret_cast<gev_part *>(reinterpret_cast<char *>(s) + threadIdx.x * 56) =
+          pack_one<V>(P, perm ? (long)perm[i] : i);
+    }
     __syncthreads();
     uint4 *dst = reinterpret_cast<uint4 *>(out + r0);
     for (int k = threadIdx.x; k < nv; k += blockDim.x) dst[k] = s[k];
@@ -201,31 +207,34 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(uint32_t *bsum, long nb) {
 __global__ void __launch_bounds__(SCAN_T) k_scan_down(const uint32_t *__restrict__ in, long n,
                                                       const uint32_t *__restrict__ bsum, uint32_t *out,
                                                       uint32_t total_n) {
-  __shared__ uint32_t tile[SCAN_TILE];
+  // one word of padding per 32: the thread-major accesses (tid * SCAN_PER + k) then
+  // fall on 32 distinct banks instead of 2
+  __shared__ uint32_t tile[SCAN_TILE + SCAN_TILE / 32];
   __shared__ uint32_t sh[64];
+  auto pad = [](int i) { return i + (i >> 5); };
   const long base = (long)blockIdx.x * SCAN_TILE;
   for (int k = 0; k < SCAN_PER; ++k) {
     const long i = base + (long)k * SCAN_T + threadIdx.x;
-    tile[k * SCAN_T + threadIdx.x] = i < n ? in[i] : 0u;
+    tile[pad(k * SCAN_T + threadIdx.x)] = i < n ? in[i] : 0u;
   }
   __syncthreads();
   uint32_t loc[SCAN_PER], s = 0;
 #pragma unroll
   for (int k = 0; k < SCAN_PER; ++k) {
-    loc[k] = tile[threadIdx.x * SCAN_PER + k];
+    loc[k] = tile[pad(threadIdx.x * SCAN_PER + k)];
     s += loc[k];
   }
   uint32_t total;
   uint32_t off = block_exclusive_scan(s, sh, total) + bsum[blockIdx.x];
 #pragma unroll
   for (int k = 0; k < SCAN_PER; ++k) {
-    tile[threadIdx.x * SCAN_PER + k] = off;
+    tile[pad(threadIdx.x * SCAN_PER + k)] = off;
     off += loc[k];
   }
   __syncthreads();
   for (int k = 0; k < SCAN_PER; ++k) {
     const long i = base + (long)k * SCAN_T + threadIdx.x;
-    if (i < n) out[i] = tile[k * SCAN_T + threadIdx.x];
+    if (i < n) out[i] = tile[pad(k * SCAN_T + threadIdx.x)];
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = total_n;
 }
@@ -1010,8 +1019,8 @@ static int relink_uploaded(gev_ctx *ctx, gev_pcls *p) {
   return GEV_OK;
 }
 
-int pcls_id_order(gev_ctx *ctx, gev_pcls *p) {
-  if (p->id_order || p->n == 0) return GEV_OK;
+// perm = the store's particles in (cell, ID) order (each cell's run sorted by ID)
+static int id_permutation(gev_ctx *ctx, gev_pcls *p) {
   const long C = (long)ctx->N * ctx->N * ctx->N;
   const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->big, 0, sizeof(uint32_t), ctx->stream));
@@ -1021,6 +1030,14 @@ int pcls_id_order(gev_ctx *ctx, gev_pcls *p) {
   GEV_LAUNCH_CHECK(ctx);
   k_canon_big<<<ctx->sms * 2, 256, 0, ctx->stream>>>(p->start, p->cur.id, p->perm, p->rank, p->big);
   GEV_LAUNCH_CHECK(ctx);
+  return GEV_OK;
+}
+
+int pcls_id_order(gev_ctx *ctx, gev_pcls *p) {
+  if (p->id_order || p->n == 0) return GEV_OK;
+  const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
+  int rc = id_permutation(ctx, p);
+  if (rc) return rc;
   if (ctx->prec == GEV_PREC_FP64)
     k_gather<double><<<pb, 256, 0, ctx->stream>>>(p->cur, p->alt, p->perm, p->n);
   else
@@ -1198,17 +1215,28 @@ int gev_pcls_download(gev_pcls *p, gev_part *host, long *n) {
   if (!p || (!host && p->n > 0)) return gev_fail(p ? p->ctx : nullptr, GEV_EINVAL, "pcls_download: null buffer");
   gev_ctx *ctx = p->ctx;
   if (n) *n = p->n;
-  int rc = pcls_id_order(ctx, p);
-  if (rc) return rc;
-  if (p->n > 0 && host_alias(host)) {
-    gev_part *h = (gev_part *)host_alias(host);
+  gev_part *h = p->n > 0 ? (gev_part *)host_alias(host) : nullptr;
+  if (h) {
+    // the pack runs at the host link's rate, so it reads the particles through the
+    // (cell, ID) permutation rather than moving the store into that order first
+    const uint32_t *perm = nullptr;
+    if (!p->id_order) {
+      int rc = id_permutation(ctx, p);
+      if (rc) return rc;
+      perm = p->perm;
+    }
     const int hb = grid_for(ctx, (size_t)((p->n + HREC - 1) / HREC), 1, 8);
     if (ctx->prec == GEV_PREC_FP64)
-      k_pack_host<double><<<hb, 256, 0, ctx->stream>>>(h, p->n, p->cur);
+      k_pack_host<double><<<hb, 256, 0, ctx->stream>>>(h, p->n, p->cur, perm);
     else
-      k_pack_host<float><<<hb, 256, 0, ctx->stream>>>(h, p->n, p->cur);
+      k_pack_host<float><<<hb, 256, 0, ctx->stream>>>(h, p->n, p->cur, perm);
     GEV_LAUNCH_CHECK(ctx);
-  } else if (p->n > 0) {
+    GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    return GEV_OK;
+  }
+  int rc = pcls_id_order(ctx, p);
+  if (rc) return rc;
+  if (p->n > 0) {
     gev_part *d = nullptr;
     GEV_CHECK_CUDA(ctx, cudaMallocAsync(&d, p->n * sizeof(gev_part), ctx->stream));
     const int b = grid_for(ctx, (size_t)p->n, 256, 16);

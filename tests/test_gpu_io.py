@@ -287,6 +287,18 @@ def test_pinned_upload_download_match_pageable(gpu, prec, n):
     _keep3, o2 = pinned(gpu, n)
     c.download(out=o2)
     assert np.array_equal(o2.view(np.uint8), a.download().view(np.uint8))
+    # the cycle's fused kick + drift (mixed form: each cell's run left in atomic order);
+    # a pinned download packs through the (cell, ID) permutation, a pageable one reorders
+    # the store first: the same records
+    chi = ctx.real(1).upload(rng.standard_normal((N, N, N)) * 1e-6)
+    Bi = ctx.real(3).upload(rng.standard_normal((3, N, N, N)) * 1e-7)
+    for p in (a, c):
+        gpu.update_q_pos(p, 0.2, 1.0, 3, 0.3, 1.0, 3, phi, chi, Bi)
+    _keep4, o3 = pinned(gpu, n)
+    c.download(out=o3)
+    assert np.array_equal(o3.view(np.uint8), a.download().view(np.uint8))
+    c.download(out=o3)  # twice: the pinned download leaves the store usable
+    assert np.array_equal(o3.view(np.uint8), a.download().view(np.uint8))
 
 
 @pytest.mark.parametrize("prec", [0, 1])
