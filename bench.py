@@ -213,6 +213,7 @@ def run_ours(args, rank, world, local):
     # roofline of the dominant kernel (the T00 + Tij deposit) and of the FFT column pass
     roof = deposit_roofline(gpu, ctx, sim, stream, N, args.prec)
     roof_fft = dominant_kernel_roofline(gpu, ctx, sim, stream, N, args.prec)
+    cufft = fft_vs_cufft(gpu, ctx, stream, N, args.prec, torch) if world == 1 else None
 
     # e2e: particle state from pinned host memory in, cycle, particle state out
     e2e = None
@@ -226,7 +227,7 @@ def run_ours(args, rank, world, local):
     if args.serve_seconds > 0 and world == 1:
         serve = run_serve(args, gpu)
     return dict(value=value, ms=ms_max / args.steps, launches=launches, clocks=clk, state=st, roofline=roof,
-                roofline_fft=roof_fft, e2e=e2e, box=box, fp64=fp64, serve=serve)
+                roofline_fft=roof_fft, cufft=cufft, e2e=e2e, box=box, fp64=fp64, serve=serve)
 
 
 PK_FIELDS = (("phi", 1), ("chi", 1), ("Bi", 3), ("source", 1))
@@ -349,6 +350,43 @@ def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
     return {"kernel": "k_fft_cols_reg (one y or z pass of the 3-D FFT over one spectrum component)", "bound": "hbm",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": COLS_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
+
+
+def fft_vs_cufft(gpu, ctx, stream, N, prec, torch, reps=5):
+    """One component's 3-D r2c and c2r, the library's own FFT against NVIDIA's cuFFT
+    (through torch.fft) on the same grid and precision.  CUDA events on each one's
+    stream, after a warm-up call (plan creation), mean of reps.  cuFFT's inverse runs
+    unnormalised (norm="forward"), as the library's c2r does; its c2r may overwrite
+    its input, so torch works on a copy, where the library's keeps its input."""
+    import numpy as np
+    rng = np.random.default_rng(3)
+    real, spec = ctx.real(1), ctx.spectrum(1)
+    real.upload(rng.standard_normal(real.shape))
+
+    def timed(fn, st):
+        fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            fn()
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    ours_r2c = timed(lambda: gpu.fft_r2c(real, spec), stream)
+    ours_c2r = timed(lambda: gpu.fft_c2r(spec, real), stream)
+    del real, spec
+    dt = torch.float64 if prec == "fp64" else torch.float32
+    x = torch.randn((N, N, N), dtype=dt, device="cuda")
+    cur = torch.cuda.current_stream()
+    cu_r2c = timed(lambda: torch.fft.rfftn(x), cur)
+    y = torch.fft.rfftn(x)
+    cu_c2r = timed(lambda: torch.fft.irfftn(y, s=(N, N, N), norm="forward"), cur)
+    del x, y
+    torch.cuda.empty_cache()
+    return {"grid": N, "precision": prec, "ours_r2c_ms": ours_r2c, "cufft_r2c_ms": cu_r2c, "ours_c2r_ms": ours_c2r,
+            "cufft_c2r_ms": cu_c2r, "library": "cuFFT via torch.fft (torch %s)" % torch.__version__}
 
 
 # ------------------------------------------------------------ serving --------
@@ -570,7 +608,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.prec == "fp64" else "f32+f64pos+i64dep",
             "data": "synthetic (device-generated BBKS Zel'dovich IC)", "config": config,
-            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "cpu_baseline": cpu, "e2e": res["e2e"], "gpu_launches": res["launches"],
+            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "fft_vs_cufft": res["cufft"], "cpu_baseline": cpu, "e2e": res["e2e"], "gpu_launches": res["launches"],
             "clocks": res["clocks"], "bytes_per_cycle_alg": cycle_bytes(N, args.prec),
             "final_a": res["state"]["a"]}
     if res.get("fp64"):

@@ -4,10 +4,10 @@
 // its shared-memory staged kernels otherwise (lengths with a factor 3).
 //
 // Work layout.  A line of L elements is held by L/8 threads, 8 elements
-// (registers) each.  A tile is B consecutive lines (B = 8 for FP32, 4 for FP64,
-// so every row of a column tile is 64 contiguous bytes and every row segment of
-// a row tile one 32-byte sector or more); thread (m, c) = (tid / B, tid % B)
-// holds elements of line c.
+// (registers) each.  A tile is B consecutive lines: column tiles take 8 lines for
+// FP32 and 4 for FP64 (every row of a tile 64 contiguous bytes; 16 lines in the
+// FP32 z pass), row tiles 4 lines; thread (m, c) = (tid / B, tid % B) holds
+// elements of line c.
 //
 // Transform.  Decimation in frequency, in place: stages s = 0 .. N8-1 are
 // radix 8 (span L / 8^s); when log2 L is not a multiple of 3 a last radix-4 or
@@ -37,9 +37,12 @@ __host__ __device__ constexpr int tile_lg() {
 // whose rows lie a plane apart, reads 16 lines (a whole 128-byte line per row)
 // up to L = 512 (1024 threads): fewer, longer DRAM bursts than 8 lines.  The y
 // pass, whose rows are consecutive in a plane, is faster with the default 8.
+// the x-pass (row) kernels take 4 rows a tile in both precisions: smaller blocks,
+// more of them resident, measured faster than 8 or 16 (and than 2) for FP32
+constexpr int row_tile_lg() { return 2; }
 template <typename T, int L>
 constexpr int reg_threads() {
-  return (L / 8) << tile_lg<T>();
+  return (L / 8) << row_tile_lg();
 }
 constexpr int col_min_blocks(int esize, int threads) {
   return (esize == 4 ? 1024 : 512) / threads > 0 ? (esize == 4 ? 1024 : 512) / threads : 1;
@@ -123,9 +126,9 @@ struct RegFft {
 };
 
 // row of natural-order element k in the tile the row kernels write after the last
-// stage: bit 0 flipped by bit 4, so that the four thread groups of a warp, whose
-// outputs lie 16 elements apart, fall on both halves of the banks
-__device__ __forceinline__ int nat(int k) { return k ^ ((k >> 4) & 1); }
+// stage: bits 0-1 flipped by bits 4-5, so that the thread groups of a warp, whose
+// outputs lie 16 elements apart, fall on all four quarters of the banks
+__device__ __forceinline__ int nat(int k) { return k ^ ((k >> 4) & 3); }
 
 template <typename C>
 __device__ __forceinline__ void stage_tw(C *tw, const C *__restrict__ g, int L) {
@@ -178,7 +181,7 @@ __global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
   C *X = tw + L;
-  constexpr int lgB = tile_lg<T>(), B = 1 << lgB;
+  constexpr int lgB = row_tile_lg(), B = 1 << lgB;
   stage_tw(tw, twHg, L);
   const int c = threadIdx.x & (B - 1), m = threadIdx.x >> lgB;
   const int kb = R::freq(m << 3);
@@ -222,7 +225,7 @@ __global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
   C *X = tw + L;  // (L + 1) * B
-  constexpr int lgB = tile_lg<T>(), B = 1 << lgB;
+  constexpr int lgB = row_tile_lg(), B = 1 << lgB;
   stage_tw(tw, twHg, L);
   const int c = threadIdx.x & (B - 1), m = threadIdx.x >> lgB;
   const int kb = R::freq(m << 3);
@@ -314,7 +317,7 @@ template <typename T, int L>
 int r2c_L(gev_ctx *ctx, const void *real, void *spec) {
   typedef typename CT<T>::C C;
   static int per_sm = 0;
-  const int N = ctx->N, NH = N / 2 + 1, lgB = tile_lg<T>(), B = 1 << lgB;
+  const int N = ctx->N, NH = N / 2 + 1, lgB = row_tile_lg(), B = 1 << lgB;
   const int threads = (L / 8) * B;
   const long nrows = (long)N * N, ntiles = (nrows + B - 1) / B;
   const size_t smem = ((size_t)L + (size_t)L * B) * sizeof(C);
@@ -331,7 +334,7 @@ template <typename T, int L>
 int c2r_L(gev_ctx *ctx, const void *spec, void *real) {
   typedef typename CT<T>::C C;
   static int per_sm = 0;
-  const int N = ctx->N, NH = N / 2 + 1, lgB = tile_lg<T>(), B = 1 << lgB;
+  const int N = ctx->N, NH = N / 2 + 1, lgB = row_tile_lg(), B = 1 << lgB;
   const int threads = (L / 8) * B;
   const long nrows = (long)N * N, ntiles = (nrows + B - 1) / B;
   const size_t smem = ((size_t)L + (size_t)(L + 1) * B) * sizeof(C);
