@@ -571,12 +571,23 @@ __device__ __forceinline__ void kick_one(const S &st, const Params &pr, T r0, T 
   if (KIND == GEV_GR) {
     const T v2 = q0 * q0 + q1 * q1 + q2 * q2;
     const T e2 = v2 + a * a;
-    const T fac = (v2 + e2) / e2;
+    T fac;
+    if constexpr (sizeof(T) == 4) {
+      // FP32: one reciprocal square root for e, 1/e and (v^2 + e^2) / e^2 = 1 + v^2 / e^2
+      // (within 2 ulp, the rounding level of the form) instead of two IEEE divisions
+      // and a square root
+      const T r = rsqrtf(e2);
+      inv_e = r;
+      e = e2 * r;
+      fac = (T)1 + v2 * (r * r);
+    } else {
+      fac = (v2 + e2) / e2;
+      e = tsqrt<T>(e2);
+      inv_e = (T)1 / e;
+    }
     g0 *= fac;
     g1 *= fac;
     g2 *= fac;
-    e = tsqrt<T>(e2);
-    inv_e = (T)1 / e;
   }
   if (pr.nfield >= 2 && st.has_chi) {
     const T f000 = st.template v<1, 0, 0, 0>(), f100 = st.template v<1, 1, 0, 0>(), f010 = st.template v<1, 0, 1, 0>(),
@@ -643,8 +654,14 @@ __device__ __forceinline__ void drift_vel(const S &st, const Params &pr, T r0, T
     ch = st.template v<1, 0, 0, 0>() * w000 + st.template v<1, 1, 0, 0>() * w100 + st.template v<1, 0, 1, 0>() * w010 +
          st.template v<1, 1, 1, 0>() * w110 + st.template v<1, 0, 0, 1>() * w001 + st.template v<1, 1, 0, 1>() * w101 +
          st.template v<1, 0, 1, 1>() * w011 + st.template v<1, 1, 1, 1>() * w111;
-  const T inv_e2 = (T)1 / e2;
-  const T fac = ((T)1 + ((T)3 - qq * inv_e2) * ph - ch) * tsqrt<T>(inv_e2);
+  T fac;
+  if constexpr (sizeof(T) == 4) {  // FP32: 1/e^2 and 1/e from one reciprocal square root
+    const T r = rsqrtf(e2);
+    fac = ((T)1 + ((T)3 - qq * (r * r)) * ph - ch) * r;
+  } else {
+    const T inv_e2 = (T)1 / e2;
+    fac = ((T)1 + ((T)3 - qq * inv_e2) * ph - ch) * tsqrt<T>(inv_e2);
+  }
   v0 = q0 * fac;
   v1 = q1 * fac;
   v2 = q2 * fac;
