@@ -353,10 +353,12 @@ int fft_init_kernels(int prec) {
 }
 
 int fft_r2c_comp(gev_ctx *ctx, const void *real, void *spec) {
+  fft_autotune(ctx);
   return ctx->prec == GEV_PREC_FP64 ? r2c_comp<double>(ctx, real, spec) : r2c_comp<float>(ctx, real, spec);
 }
 
 int fft_c2r_comp(gev_ctx *ctx, const void *spec, void *real, void *scratch) {
+  fft_autotune(ctx);  // before the scratch holds this transform's z pass
   return ctx->prec == GEV_PREC_FP64 ? c2r_comp<double>(ctx, spec, real, scratch)
                                     : c2r_comp<float>(ctx, spec, real, scratch);
 }
@@ -367,6 +369,7 @@ extern "C" int gev_fft_axis(gev_ctx *ctx, gev_field *spec, int axis, int sign) {
     return gev_fail(ctx, GEV_EINVAL, "fft_axis: spectrum, axis 1 (y) or 2 (z), sign -1 or +1");
   const int N = ctx->N, NH = N / 2 + 1;
   const long ls = axis == 1 ? NH : (long)N * NH, ps = axis == 1 ? (long)N * NH : NH;
+  fft_autotune(ctx);
   for (int c = 0; c < spec->ncomp; ++c) {
     void *d = (char *)spec->d + c * spec->comp_elems * spec->elem_bytes;
     int rc;

@@ -37,22 +37,19 @@ __host__ __device__ constexpr int tile_lg() {
 // whose rows lie a plane apart, reads 16 lines (a whole 128-byte line per row)
 // up to L = 512 (1024 threads): fewer, longer DRAM bursts than 8 lines.  The y
 // pass, whose rows are consecutive in a plane, is faster with the default 8.
-// the x-pass (row) kernels take 4 rows a tile in both precisions: smaller blocks,
-// more of them resident, measured faster than 8 or 16 (and than 2) for FP32
-constexpr int row_tile_lg() { return 2; }
-template <typename T, int L>
-constexpr int reg_threads() {
-  return (L / 8) << row_tile_lg();
-}
-constexpr int col_min_blocks(int esize, int threads) {
-  return (esize == 4 ? 1024 : 512) / threads > 0 ? (esize == 4 ? 1024 : 512) / threads : 1;
+// Tile widths (log2 of the lines a tile) are compile-time constants of each kernel
+// instance.  The FP32 widths of a context's row, y and z passes are chosen by
+// timing the candidates once on the context's scratch spectrum (fft_autotune); the
+// defaults below hold until then and for FP64.  Every width gives the same bits.
+constexpr int ROW_LG_DEFAULT = 2;
+template <int L, int LG>
+constexpr bool fits() {
+  return ((L / 8) << LG) <= 1024;
 }
 // resident blocks asked of the compiler: 1024 threads per SM for FP32 (64
 // registers), 512 for FP64, whose own pipe bounds it anyway
-template <typename T, int L>
-constexpr int reg_min_blocks() {
-  return (sizeof(T) == 4 ? 1024 : 512) / reg_threads<T, L>() > 0 ? (sizeof(T) == 4 ? 1024 : 512) / reg_threads<T, L>()
-                                                                 : 1;
+constexpr int col_min_blocks(int esize, int threads) {
+  return (esize == 4 ? 1024 : 512) / threads > 0 ? (esize == 4 ? 1024 : 512) / threads : 1;
 }
 
 template <typename T, int SIGN, int L>
@@ -171,8 +168,8 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
 
 // x pass, forward: rows of N = 2L reals, each an L-point complex FFT followed by
 // the real-to-complex split into N/2+1 outputs (row stride NH)
-template <typename T, int L>
-__global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k_fft_r2c_rows_reg(const T *__restrict__ in, typename CT<T>::C *__restrict__ out,
+template <typename T, int L, int LGB>
+__global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L / 8) << LGB)) k_fft_r2c_rows_reg(const T *__restrict__ in, typename CT<T>::C *__restrict__ out,
                                                            const typename CT<T>::C *__restrict__ twHg,
                                                            const typename CT<T>::C *__restrict__ twN, int NH,
                                                            long nrows, int ntiles) {
@@ -181,7 +178,7 @@ __global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
   C *X = tw + L;
-  constexpr int lgB = row_tile_lg(), B = 1 << lgB;
+  constexpr int lgB = LGB, B = 1 << lgB;
   stage_tw(tw, twHg, L);
   const int c = threadIdx.x & (B - 1), m = threadIdx.x >> lgB;
   const int kb = R::freq(m << 3);
@@ -215,8 +212,8 @@ __global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k
 }
 
 // x pass, backward: rows of N/2+1 complex -> N = 2L reals
-template <typename T, int L>
-__global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k_fft_c2r_rows_reg(const typename CT<T>::C *__restrict__ in, T *__restrict__ out,
+template <typename T, int L, int LGB>
+__global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L / 8) << LGB)) k_fft_c2r_rows_reg(const typename CT<T>::C *__restrict__ in, T *__restrict__ out,
                                                            const typename CT<T>::C *__restrict__ twHg,
                                                            const typename CT<T>::C *__restrict__ twN, int NH,
                                                            long nrows, int ntiles) {
@@ -225,7 +222,7 @@ __global__ void __launch_bounds__(reg_threads<T, L>(), reg_min_blocks<T, L>()) k
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
   C *X = tw + L;  // (L + 1) * B
-  constexpr int lgB = row_tile_lg(), B = 1 << lgB;
+  constexpr int lgB = LGB, B = 1 << lgB;
   stage_tw(tw, twHg, L);
   const int c = threadIdx.x & (B - 1), m = threadIdx.x >> lgB;
   const int kb = R::freq(m << 3);
@@ -289,6 +286,7 @@ int launch_cfg(gev_ctx *ctx, K kern, int threads, size_t smem, long ntiles, int 
 
 template <typename T, int SIGN, int L, int LGB>
 int cols_LB(gev_ctx *ctx, const void *in, void *out, long ES, long PS) {
+  static_assert(fits<L, LGB>(), "column tile too wide");
   typedef typename CT<T>::C C;
   static int per_sm = 0;
   constexpr int B = 1 << LGB, threads = (L / 8) * B;
@@ -304,47 +302,172 @@ int cols_LB(gev_ctx *ctx, const void *in, void *out, long ES, long PS) {
   return GEV_OK;
 }
 
-// the wide tile for a pass whose rows are further apart than its tiles (ES > PS)
+// the width of a pass: tuned (FP32), else 16 lines for the FP32 z pass up to L = 512
+// (rows a plane apart: ES > PS) and tile_lg otherwise
+template <typename T, int L>
+int col_lg(const gev_ctx *ctx, bool zpass) {
+  if (sizeof(T) == 4 && ctx->fft_lg[zpass ? 2 : 1] >= 0) return ctx->fft_lg[zpass ? 2 : 1];
+  return (sizeof(T) == 4 && L <= 512 && zpass) ? 4 : tile_lg<T>();
+}
 template <typename T, int SIGN, int L>
 int cols_L(gev_ctx *ctx, const void *in, void *out, long ES, long PS) {
-  if constexpr (sizeof(T) == 4 && L <= 512) {
-    if (ES > PS) return cols_LB<T, SIGN, L, 4>(ctx, in, out, ES, PS);
+  if constexpr (sizeof(T) == 8) {
+    return cols_LB<T, SIGN, L, tile_lg<T>()>(ctx, in, out, ES, PS);
+  } else {
+    switch (col_lg<T, L>(ctx, ES > PS)) {
+      case 2: return cols_LB<T, SIGN, L, 2>(ctx, in, out, ES, PS);
+      case 3:
+        if constexpr (fits<L, 3>()) return cols_LB<T, SIGN, L, 3>(ctx, in, out, ES, PS);
+        break;
+      case 4:
+        if constexpr (fits<L, 4>()) return cols_LB<T, SIGN, L, 4>(ctx, in, out, ES, PS);
+        break;
+    }
+    return gev_fail(ctx, GEV_EINVAL, "fft: column tile width");
   }
-  return cols_LB<T, SIGN, L, tile_lg<T>()>(ctx, in, out, ES, PS);
 }
 
-template <typename T, int L>
-int r2c_L(gev_ctx *ctx, const void *real, void *spec) {
+// nrows: rows of the transform (N^2; fewer only while tuning)
+template <typename T, int L, int LGB>
+int r2c_LB(gev_ctx *ctx, const void *real, void *spec, long nrows) {
+  static_assert(fits<L, LGB>(), "row tile too wide");
   typedef typename CT<T>::C C;
   static int per_sm = 0;
-  const int N = ctx->N, NH = N / 2 + 1, lgB = row_tile_lg(), B = 1 << lgB;
-  const int threads = (L / 8) * B;
-  const long nrows = (long)N * N, ntiles = (nrows + B - 1) / B;
+  constexpr int B = 1 << LGB, threads = (L / 8) * B;
+  const int NH = ctx->N / 2 + 1;
+  const long ntiles = (nrows + B - 1) / B;
   const size_t smem = ((size_t)L + (size_t)L * B) * sizeof(C);
   int grid = 0;
-  int rc = launch_cfg(ctx, k_fft_r2c_rows_reg<T, L>, threads, smem, ntiles, per_sm, grid);
+  int rc = launch_cfg(ctx, k_fft_r2c_rows_reg<T, L, LGB>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
-  k_fft_r2c_rows_reg<T, L><<<grid, threads, smem, ctx->stream>>>((const T *)real, (C *)spec, (const C *)ctx->d_twH,
-                                                                 (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
+  k_fft_r2c_rows_reg<T, L, LGB><<<grid, threads, smem, ctx->stream>>>(
+      (const T *)real, (C *)spec, (const C *)ctx->d_twH, (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
+  GEV_LAUNCH_CHECK(ctx);
+  return GEV_OK;
+}
+
+template <typename T, int L, int LGB>
+int c2r_LB(gev_ctx *ctx, const void *spec, void *real, long nrows) {
+  static_assert(fits<L, LGB>(), "row tile too wide");
+  typedef typename CT<T>::C C;
+  static int per_sm = 0;
+  constexpr int B = 1 << LGB, threads = (L / 8) * B;
+  const int NH = ctx->N / 2 + 1;
+  const long ntiles = (nrows + B - 1) / B;
+  const size_t smem = ((size_t)L + (size_t)(L + 1) * B) * sizeof(C);
+  int grid = 0;
+  int rc = launch_cfg(ctx, k_fft_c2r_rows_reg<T, L, LGB>, threads, smem, ntiles, per_sm, grid);
+  if (rc) return rc;
+  k_fft_c2r_rows_reg<T, L, LGB><<<grid, threads, smem, ctx->stream>>>(
+      (const C *)spec, (T *)real, (const C *)ctx->d_twH, (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
 
 template <typename T, int L>
+int row_lg(const gev_ctx *ctx, bool c2r) {
+  if (sizeof(T) == 4 && ctx->fft_lg[c2r ? 3 : 0] >= 0) return ctx->fft_lg[c2r ? 3 : 0];
+  return ROW_LG_DEFAULT;
+}
+template <typename T, int L>
+int rows_L(gev_ctx *ctx, const void *in, void *out, bool c2r, long nrows, int lg) {
+  if constexpr (sizeof(T) == 8) {
+    return c2r ? c2r_LB<T, L, ROW_LG_DEFAULT>(ctx, in, out, nrows) : r2c_LB<T, L, ROW_LG_DEFAULT>(ctx, in, out, nrows);
+  } else {
+    switch (lg) {
+      case 1: return c2r ? c2r_LB<T, L, 1>(ctx, in, out, nrows) : r2c_LB<T, L, 1>(ctx, in, out, nrows);
+      case 2:
+        if constexpr (fits<L, 2>())
+          return c2r ? c2r_LB<T, L, 2>(ctx, in, out, nrows) : r2c_LB<T, L, 2>(ctx, in, out, nrows);
+        break;
+      case 3:
+        if constexpr (fits<L, 3>())
+          return c2r ? c2r_LB<T, L, 3>(ctx, in, out, nrows) : r2c_LB<T, L, 3>(ctx, in, out, nrows);
+        break;
+    }
+    return gev_fail(ctx, GEV_EINVAL, "fft: row tile width");
+  }
+}
+template <typename T, int L>
+int r2c_L(gev_ctx *ctx, const void *real, void *spec) {
+  return rows_L<T, L>(ctx, real, spec, false, (long)ctx->N * ctx->N, row_lg<T, L>(ctx, false));
+}
+template <typename T, int L>
 int c2r_L(gev_ctx *ctx, const void *spec, void *real) {
-  typedef typename CT<T>::C C;
-  static int per_sm = 0;
-  const int N = ctx->N, NH = N / 2 + 1, lgB = row_tile_lg(), B = 1 << lgB;
-  const int threads = (L / 8) * B;
-  const long nrows = (long)N * N, ntiles = (nrows + B - 1) / B;
-  const size_t smem = ((size_t)L + (size_t)(L + 1) * B) * sizeof(C);
-  int grid = 0;
-  int rc = launch_cfg(ctx, k_fft_c2r_rows_reg<T, L>, threads, smem, ntiles, per_sm, grid);
-  if (rc) return rc;
-  k_fft_c2r_rows_reg<T, L><<<grid, threads, smem, ctx->stream>>>((const C *)spec, (T *)real, (const C *)ctx->d_twH,
-                                                                 (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
-  GEV_LAUNCH_CHECK(ctx);
-  return GEV_OK;
+  return rows_L<T, L>(ctx, spec, real, true, (long)ctx->N * ctx->N, row_lg<T, L>(ctx, true));
+}
+
+// ---------------------------------------------------------------- tuning --
+// mean ms of 3 launches of fn after one warm-up launch, on the context's stream;
+// a candidate that fails to launch gets +inf
+template <typename F>
+float time_ms(gev_ctx *ctx, F &&fn) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  float ms = 3.4e38f;
+  if (cudaEventCreate(&a) != cudaSuccess || cudaEventCreate(&b) != cudaSuccess) {
+    cudaGetLastError();
+  } else if (fn() == GEV_OK) {
+    cudaEventRecord(a, ctx->stream);
+    int rc = GEV_OK;
+    for (int k = 0; k < 3 && rc == GEV_OK; ++k) rc = fn();
+    cudaEventRecord(b, ctx->stream);
+    if (rc == GEV_OK && cudaEventSynchronize(b) == cudaSuccess && cudaEventElapsedTime(&ms, a, b) == cudaSuccess)
+      ms /= 3.f;
+    else
+      ms = 3.4e38f;
+  }
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  return ms;
+}
+
+// The candidates run on the context's scratch spectrum (zeroed first): the column
+// passes in place over the whole component, the row passes over half the rows,
+// reading one half of the scratch and writing the other.
+template <int L>
+void tune_cols(gev_ctx *ctx) {
+  float2 *S = (float2 *)ctx->d_fft_scratch;
+  const long N = ctx->N, NH = N / 2 + 1;
+  for (int z = 0; z < 2; ++z) {
+    const long ES = z ? N * NH : NH, PS = z ? NH : N * NH;
+    int best = -1;
+    float bt = 3.4e38f;
+    for (int lg = 2; lg <= 4; ++lg) {
+      float t = 3.4e38f;
+      if (lg == 2) t = time_ms(ctx, [&] { return cols_LB<float, -1, L, 2>(ctx, S, S, ES, PS); });
+      if constexpr (fits<L, 3>())
+        if (lg == 3) t = time_ms(ctx, [&] { return cols_LB<float, -1, L, 3>(ctx, S, S, ES, PS); });
+      if constexpr (fits<L, 4>())
+        if (lg == 4) t = time_ms(ctx, [&] { return cols_LB<float, -1, L, 4>(ctx, S, S, ES, PS); });
+      if (t < bt) {
+        bt = t;
+        best = lg;
+      }
+    }
+    ctx->fft_lg[z ? 2 : 1] = best;
+  }
+}
+template <int L>
+void tune_rows(gev_ctx *ctx) {
+  float2 *S = (float2 *)ctx->d_fft_scratch;
+  const long N = ctx->N, NH = N / 2 + 1, half = N * N / 2;
+  // r2c: half * N reals at S[0, half * L), half * NH complex after them; c2r: half * NH
+  // complex at S[0, half * NH), half * N reals after them (both within N^2 NH complex)
+  for (int c2r = 0; c2r < 2; ++c2r) {
+    const void *in = S;
+    void *out = c2r ? (void *)(S + half * NH) : (void *)(S + half * L);
+    int best = -1;
+    float bt = 3.4e38f;
+    for (int lg = 1; lg <= 3; ++lg) {
+      if (((L / 8) << lg) > 1024) continue;
+      const float t = time_ms(ctx, [&] { return rows_L<float, L>(ctx, in, out, c2r != 0, half, lg); });
+      if (t < bt) {
+        bt = t;
+        best = lg;
+      }
+    }
+    ctx->fft_lg[c2r ? 3 : 0] = best;
+  }
 }
 
 #define GEV_REG_SWITCH(L, CALL) \
@@ -363,6 +486,62 @@ int c2r_L(gev_ctx *ctx, const void *spec, void *real) {
 }  // namespace
 
 bool fft_reg_ok(int L) { return L >= 8 && L <= 1024 && (L & (L - 1)) == 0; }
+
+extern "C" int gev_ctx_fft_tiles(gev_ctx *ctx, int *lg) {
+  if (!ctx || !lg) return gev_fail(ctx, GEV_EINVAL, "ctx_fft_tiles: null argument");
+  const bool f32 = ctx->prec != GEV_PREC_FP64;
+  const int N = ctx->N;
+  const int defaults[4] = {ROW_LG_DEFAULT, f32 ? 3 : 2, (f32 && N <= 512) ? 4 : (f32 ? 3 : 2), ROW_LG_DEFAULT};
+  for (int p = 0; p < 4; ++p) lg[p] = (f32 && ctx->fft_lg[p] >= 0) ? ctx->fft_lg[p] : defaults[p];
+  return GEV_OK;
+}
+
+extern "C" int gev_ctx_set_fft_tiles(gev_ctx *ctx, const int *lg) {
+  if (!ctx || !lg) return gev_fail(ctx, GEV_EINVAL, "ctx_set_fft_tiles: null argument");
+  const int N = ctx->N;
+  if (ctx->prec == GEV_PREC_FP64 || !fft_reg_ok(N))
+    return gev_fail(ctx, GEV_EINVAL, "ctx_set_fft_tiles: the FP64 form and non-power-of-two grids keep fixed tiles");
+  const bool rows_ok = fft_reg_ok(N / 2);
+  for (int p = 0; p < 4; ++p) {
+    const bool row = p == 0 || p == 3;
+    const int L = row ? N / 2 : N, lo = row ? 1 : 2, hi = row ? 3 : 4;
+    if ((row && !rows_ok) ? lg[p] != ROW_LG_DEFAULT : (lg[p] < lo || lg[p] > hi || ((L / 8) << lg[p]) > 1024))
+      return gev_fail(ctx, GEV_EINVAL, "ctx_set_fft_tiles: rows 1..3, columns 2..4, at most 1024 threads a tile");
+  }
+  for (int p = 0; p < 4; ++p) ctx->fft_lg[p] = lg[p];
+  ctx->fft_tuned = true;
+  return GEV_OK;
+}
+
+void fft_autotune(gev_ctx *ctx) {
+  if (ctx->fft_tuned) return;
+  ctx->fft_tuned = true;
+  const int N = ctx->N;
+  if (ctx->prec == GEV_PREC_FP64 || !ctx->d_fft_scratch || !fft_reg_ok(N)) return;
+  if (cudaMemsetAsync(ctx->d_fft_scratch, 0, ctx->fft_scratch_bytes, ctx->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  switch (N) {
+#define TUNE(l)         \
+  case l:               \
+    tune_cols<l>(ctx);  \
+    break;
+    TUNE(8) TUNE(16) TUNE(32) TUNE(64) TUNE(128) TUNE(256) TUNE(512) TUNE(1024)
+#undef TUNE
+    default: break;
+  }
+  if (!fft_reg_ok(N / 2)) return;
+  switch (N / 2) {
+#define TUNE(l)         \
+  case l:               \
+    tune_rows<l>(ctx);  \
+    break;
+    TUNE(8) TUNE(16) TUNE(32) TUNE(64) TUNE(128) TUNE(256) TUNE(512) TUNE(1024)
+#undef TUNE
+    default: break;
+  }
+}
 
 int fft_cols_reg(gev_ctx *ctx, const void *in, void *out, long ES, long PS, int sign) {
   const int L = ctx->N;

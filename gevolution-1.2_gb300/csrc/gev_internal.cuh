@@ -51,6 +51,10 @@ struct gev_ctx {
   size_t cube_bytes = 0;
   double *d_red = nullptr;  // partial sums / max
   size_t red_elems = 0;
+  // FP32 FFT tile widths (log2 lines a tile) of the r2c rows, y, z and c2r rows
+  // passes, chosen by timing on the first transform (-1: the default)
+  int fft_lg[4] = {-1, -1, -1, -1};
+  bool fft_tuned = false;
   long long launches = 0;
   size_t bytes_in_use = 0;
   std::string err;
@@ -356,6 +360,9 @@ bool fft_reg_ok(int L);
 int fft_cols_reg(gev_ctx *ctx, const void *in, void *out, long ES, long PS, int sign);
 int fft_r2c_rows_reg(gev_ctx *ctx, const void *real, void *spec);
 int fft_c2r_rows_reg(gev_ctx *ctx, const void *spec, void *real);
+// times the FP32 tile-width candidates of each pass once per context (a no-op after
+// the first call and for FP64)
+void fft_autotune(gev_ctx *ctx);
 int pcls_relink(gev_ctx *ctx, gev_pcls *p);
 int pcls_id_order(gev_ctx *ctx, gev_pcls *p);
 int pcls_unpack_at(gev_ctx *ctx, gev_pcls *p, const gev_part *d, long count, long offset);

@@ -42,6 +42,8 @@ _SIGS = {
     "gev_ctx_stream": [_vp, ctypes.POINTER(_vp)],
     "gev_ctx_info": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_size_t)],
     "gev_ctx_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "gev_ctx_fft_tiles": [_vp, ctypes.POINTER(_i)],
+    "gev_ctx_set_fft_tiles": [_vp, ctypes.POINTER(_i)],
     "gev_field_create": [_vp, _i, _i, ctypes.POINTER(_vp)],
     "gev_field_destroy": [_vp],
     "gev_field_upload": [_vp, _vp],
@@ -144,6 +146,17 @@ class Context:
         n = ctypes.c_longlong()
         _check(lib().gev_ctx_launch_count(self.handle, ctypes.byref(n)), self, "gev_ctx_launch_count")
         return n.value
+
+    def fft_tiles(self):
+        """log2 of the lines a tile of the r2c rows, y, z and c2r rows FFT passes."""
+        lg = (_i * 4)()
+        _check(lib().gev_ctx_fft_tiles(self.handle, lg), self, "gev_ctx_fft_tiles")
+        return {"r2c_rows": lg[0], "y": lg[1], "z": lg[2], "c2r_rows": lg[3]}
+
+    def set_fft_tiles(self, r2c_rows, y, z, c2r_rows):
+        """Pins the mixed form's FFT tile widths instead of timing them."""
+        lg = (_i * 4)(r2c_rows, y, z, c2r_rows)
+        _check(lib().gev_ctx_set_fft_tiles(self.handle, lg), self, "gev_ctx_set_fft_tiles")
 
     def bytes_in_use(self):
         b = ctypes.c_size_t()

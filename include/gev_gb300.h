@@ -67,6 +67,13 @@ const char *gev_ctx_last_error(gev_ctx *ctx);
 const char *gev_strerror(int status);
 /* count of kernels this library launched on the context since creation */
 int gev_ctx_launch_count(gev_ctx *ctx, long long *count);
+/* the FFT tile widths in use, log2 of the lines a tile, for the r2c rows, y, z and
+ * c2r rows passes: in the mixed form each is chosen by timing its candidates once,
+ * on the context's first transform; every width gives the same bits */
+int gev_ctx_fft_tiles(gev_ctx *ctx, int lg[4]);
+/* pins the mixed form's FFT tile widths (rows 1..3, columns 2..4, at most 1024
+ * threads a tile) instead of timing them; GEV_EINVAL for the FP64 form */
+int gev_ctx_set_fft_tiles(gev_ctx *ctx, const int lg[4]);
 
 /* ---- fields (Field<Real> / Field<Cplx>::initialize, main.cpp:226-237) ---- */
 int gev_field_create(gev_ctx *ctx, int kind, int ncomp, gev_field **out);

@@ -47,3 +47,33 @@ def test_mixed_fft_against_numpy(gpu, N):
     gpu.fft_c2r(s, out)
     want = np.fft.irfftn(herm, s=(N, N, N), axes=AXES) * float(N) ** 3
     assert rel(out.download().reshape(N, N, N), want) < TOL_F32
+
+
+@pytest.mark.parametrize("N", [32, 256])
+def test_tile_widths_give_the_same_bits(gpu, N):
+    """The mixed form's FFT tile widths are chosen by timing (once per context); every
+    width computes the same butterflies on the same values, so each combination gives
+    the same bits, and the timed choice is one of them."""
+    rng = np.random.default_rng(N)
+    x = rng.standard_normal((N, N, N)).astype(np.float32)
+    ref = None
+    # one pass's width varied at a time around (rows 2, y 3, z 4)
+    combos = sorted({(r, 3, 4) for r in (1, 2, 3)} | {(2, y, 4) for y in (2, 3, 4)} | {(2, 3, z) for z in (2, 3, 4)})
+    for r, y, z in combos:
+        ctx = gpu.Context(N, gpu.PREC_MIXED)
+        ctx.set_fft_tiles(r, y, z, r)
+        real, spec, back = ctx.real(1).upload(x), ctx.spectrum(1), ctx.real(1)
+        gpu.fft_r2c(real, spec)
+        gpu.fft_c2r(spec, back)
+        got = (spec.download(), back.download())
+        if ref is None:
+            ref = got
+        assert np.array_equal(got[0], ref[0]) and np.array_equal(got[1], ref[1]), (r, y, z)
+    ctx = gpu.Context(N, gpu.PREC_MIXED)
+    real, spec = ctx.real(1).upload(x), ctx.spectrum(1)
+    gpu.fft_r2c(real, spec)
+    tiles = ctx.fft_tiles()
+    assert 1 <= tiles["r2c_rows"] <= 3 and 2 <= tiles["y"] <= 4 and 2 <= tiles["z"] <= 4, tiles
+    assert np.array_equal(spec.download(), ref[0])
+    with pytest.raises(RuntimeError):
+        gpu.Context(N, gpu.PREC_FP64).set_fft_tiles(2, 2, 2, 2)
