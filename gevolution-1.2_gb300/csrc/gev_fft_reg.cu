@@ -229,20 +229,15 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {
     const long row = ((long)t << lgB) + c;
     const bool on = row < nrows;
-    const C *src = in + row * NH;
-    __syncthreads();
-#pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      const int k = m + r * R::TPL;
-      X[k * B + c] = on ? src[k] : cmk<C>(0, 0);
-    }
-    if (m == 0) X[L * B + c] = on ? src[L] : cmk<C>(0, 0);
-    __syncthreads();
+    // element k and its mirror L - k straight from the row (a warp's mirrored reads
+    // are consecutive too, and the second read of each element hits L1); the first
+    // exchange of run_from starts with the barrier that protects X
+    const C *src = in + (on ? row : 0) * NH;
     C v[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) {
       const int k = m + r * R::TPL;
-      C A = X[k * B + c], Bv = X[(L - k) * B + c];
+      C A = on ? src[k] : cmk<C>(0, 0), Bv = on ? src[L - k] : cmk<C>(0, 0);
       if (k == 0) {  // the imaginary parts of the kx = 0 and N/2 modes do not enter a real transform
         A.y = (T)0;
         Bv.y = (T)0;
