@@ -393,7 +393,7 @@ int c2r_L(gev_ctx *ctx, const void *spec, void *real) {
 }
 
 // ---------------------------------------------------------------- tuning --
-// mean ms of 3 launches of fn after one warm-up launch, on the context's stream;
+// mean ms of 5 launches of fn after one warm-up launch, on the context's stream;
 // a candidate that fails to launch gets +inf
 template <typename F>
 float time_ms(gev_ctx *ctx, F &&fn) {
@@ -404,10 +404,10 @@ float time_ms(gev_ctx *ctx, F &&fn) {
   } else if (fn() == GEV_OK) {
     cudaEventRecord(a, ctx->stream);
     int rc = GEV_OK;
-    for (int k = 0; k < 3 && rc == GEV_OK; ++k) rc = fn();
+    for (int k = 0; k < 5 && rc == GEV_OK; ++k) rc = fn();
     cudaEventRecord(b, ctx->stream);
     if (rc == GEV_OK && cudaEventSynchronize(b) == cudaSuccess && cudaEventElapsedTime(&ms, a, b) == cudaSuccess)
-      ms /= 3.f;
+      ms /= 5.f;
     else
       ms = 3.4e38f;
   }
@@ -418,27 +418,26 @@ float time_ms(gev_ctx *ctx, F &&fn) {
 
 // The candidates run on the context's scratch spectrum (zeroed first): the column
 // passes in place over the whole component, the row passes over half the rows,
-// reading one half of the scratch and writing the other.
+// reading one half of the scratch and writing the other.  Two rounds over the
+// candidates, each keeping its best time: the first rounds of a process may run
+// before the clocks have settled.
 template <int L>
 void tune_cols(gev_ctx *ctx) {
   float2 *S = (float2 *)ctx->d_fft_scratch;
   const long N = ctx->N, NH = N / 2 + 1;
   for (int z = 0; z < 2; ++z) {
     const long ES = z ? N * NH : NH, PS = z ? NH : N * NH;
-    int best = -1;
-    float bt = 3.4e38f;
-    for (int lg = 2; lg <= 4; ++lg) {
-      float t = 3.4e38f;
-      if (lg == 2) t = time_ms(ctx, [&] { return cols_LB<float, -1, L, 2>(ctx, S, S, ES, PS); });
+    float t[5] = {3.4e38f, 3.4e38f, 3.4e38f, 3.4e38f, 3.4e38f};
+    for (int round = 0; round < 2; ++round) {
+      t[2] = fminf(t[2], time_ms(ctx, [&] { return cols_LB<float, -1, L, 2>(ctx, S, S, ES, PS); }));
       if constexpr (fits<L, 3>())
-        if (lg == 3) t = time_ms(ctx, [&] { return cols_LB<float, -1, L, 3>(ctx, S, S, ES, PS); });
+        t[3] = fminf(t[3], time_ms(ctx, [&] { return cols_LB<float, -1, L, 3>(ctx, S, S, ES, PS); }));
       if constexpr (fits<L, 4>())
-        if (lg == 4) t = time_ms(ctx, [&] { return cols_LB<float, -1, L, 4>(ctx, S, S, ES, PS); });
-      if (t < bt) {
-        bt = t;
-        best = lg;
-      }
+        t[4] = fminf(t[4], time_ms(ctx, [&] { return cols_LB<float, -1, L, 4>(ctx, S, S, ES, PS); }));
     }
+    int best = 2;
+    for (int lg = 3; lg <= 4; ++lg)
+      if (t[lg] < t[best]) best = lg;
     ctx->fft_lg[z ? 2 : 1] = best;
   }
 }
@@ -451,16 +450,14 @@ void tune_rows(gev_ctx *ctx) {
   for (int c2r = 0; c2r < 2; ++c2r) {
     const void *in = S;
     void *out = c2r ? (void *)(S + half * NH) : (void *)(S + half * L);
-    int best = -1;
-    float bt = 3.4e38f;
-    for (int lg = 1; lg <= 3; ++lg) {
-      if (((L / 8) << lg) > 1024) continue;
-      const float t = time_ms(ctx, [&] { return rows_L<float, L>(ctx, in, out, c2r != 0, half, lg); });
-      if (t < bt) {
-        bt = t;
-        best = lg;
-      }
-    }
+    float t[4] = {3.4e38f, 3.4e38f, 3.4e38f, 3.4e38f};
+    for (int round = 0; round < 2; ++round)
+      for (int lg = 1; lg <= 3; ++lg)
+        if (((L / 8) << lg) <= 1024)
+          t[lg] = fminf(t[lg], time_ms(ctx, [&] { return rows_L<float, L>(ctx, in, out, c2r != 0, half, lg); }));
+    int best = 1;
+    for (int lg = 2; lg <= 3; ++lg)
+      if (t[lg] < t[best]) best = lg;
     ctx->fft_lg[c2r ? 3 : 0] = best;
   }
 }
