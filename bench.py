@@ -289,9 +289,9 @@ COLS_TRAFFIC = {(512, "mixed"): 1.0675e9}
 # DRAM traffic per call of the T00 + Tij deposit: its prefactor pass (k_fx_prep) and
 # its gather (k_dep_gather), from an ncu capture of the same kernels on the 256^3
 # cycle (opbench --grid 256 --only step), scaled by 8 to 512^3: particles and fields
-# both grow as N^3.  k_fx_prep 404.0 MB read + 746.4 MB written, k_dep_gather
-# 1499.8 MB read + 458.8 MB written; (3109.0 MB) x 8
-DEPOSIT_TRAFFIC = {(512, "mixed"): 24.872e9}
+# both grow as N^3.  k_fx_prep 403.9 MB read + 746.9 MB written, k_dep_gather
+# 1410.0 MB read + 502.4 MB written; (3063.2 MB) x 8
+DEPOSIT_TRAFFIC = {(512, "mixed"): 24.506e9}
 
 
 def deposit_roofline(gpu, ctx, sim, stream, N, prec):
