@@ -213,6 +213,7 @@ def run_ours(args, rank, world, local):
     # roofline of the dominant kernel (the T00 + Tij deposit) and of the FFT column pass
     roof = deposit_roofline(gpu, ctx, sim, stream, N, args.prec)
     roof_fft = dominant_kernel_roofline(gpu, ctx, sim, stream, N, args.prec)
+    roof_pcl = particle_update_roofline(gpu, ctx, sim, stream, N, args.prec)
     cufft = fft_vs_cufft(gpu, ctx, stream, N, args.prec, torch) if world == 1 else None
 
     # e2e: particle state from pinned host memory in, cycle, particle state out
@@ -227,7 +228,7 @@ def run_ours(args, rank, world, local):
     if args.serve_seconds > 0 and world == 1:
         serve = run_serve(args, gpu)
     return dict(value=value, ms=ms_max / args.steps, launches=launches, clocks=clk, state=st, roofline=roof,
-                roofline_fft=roof_fft, cufft=cufft, e2e=e2e, box=box, fp64=fp64, serve=serve)
+                roofline_fft=roof_fft, roofline_pcl=roof_pcl, cufft=cufft, e2e=e2e, box=box, fp64=fp64, serve=serve)
 
 
 PK_FIELDS = (("phi", 1), ("chi", 1), ("Bi", 3), ("source", 1))
@@ -350,6 +351,39 @@ def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
     return {"kernel": "k_fft_cols_reg (one y or z pass of the 3-D FFT over one spectrum component)", "bound": "hbm",
             "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "traffic": COLS_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
+
+
+def particle_update_roofline(gpu, ctx, sim, stream, N, prec):
+    """The cycle's particle update, whose kick+drift kernel is the largest single kernel
+    of the launch list: gev_update_q_pos (updateVel + moveParticles with the relink),
+    kick+drift+histogram, scan and move in one call, timed with CUDA events.  Its
+    algorithmic bytes per call: kick+drift reads each particle's cell, offset, momentum
+    and position and writes them back with its rank (52 + 56 B in the mixed form), and
+    reads phi, chi and B once per cell (20 B); the scan reads the counts and writes the
+    starts (8 B a cell); the move reads and writes the payload with its rank and start
+    (128 B a particle).  The particles move by about 1e-9 of a cell per call here."""
+    import torch
+    r = 8 if prec == "fp64" else 4
+    p, phi, chi, Bi = sim.particles(), sim.field("phi"), sim.field("chi"), sim.field("Bi")
+    a = sim.state()["a"]
+    reps = 4
+    gpu.update_q_pos(p, 1e-9, a, 3, 1e-9, a, 3, phi, chi, Bi, wait=False)
+    ctx.sync()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        gpu.update_q_pos(p, 1e-9, a, 3, 1e-9, a, 3, phi, chi, Bi, wait=False)
+    e1.record(stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / reps
+    n = C = N ** 3
+    payload = 3 * 8 + 3 * r + 4 + (3 * 4 if r == 4 else 0)  # pos, q, cell, FP32 offset
+    alg = n * (2 * payload + 4) + C * 5 * r + C * 8 + n * (2 * (payload + 8) + 4)
+    peak, kind = hbm_peak()
+    achieved = alg / (ms / 1e3) / 1e9
+    return {"kernel": "k_kick_drift + k_scan_* + k_move (gev_update_q_pos: kick, drift, relink)", "bound": "hbm",
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+            "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
 
 
 def fft_vs_cufft(gpu, ctx, stream, N, prec, torch, reps=5):
@@ -608,7 +642,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.prec == "fp64" else "f32+f64pos+i64dep",
             "data": "synthetic (device-generated BBKS Zel'dovich IC)", "config": config,
-            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "fft_vs_cufft": res["cufft"], "cpu_baseline": cpu, "e2e": res["e2e"], "gpu_launches": res["launches"],
+            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "roofline_particle_update": res["roofline_pcl"], "fft_vs_cufft": res["cufft"], "cpu_baseline": cpu, "e2e": res["e2e"], "gpu_launches": res["launches"],
             "clocks": res["clocks"], "bytes_per_cycle_alg": cycle_bytes(N, args.prec),
             "final_a": res["state"]["a"]}
     if res.get("fp64"):
