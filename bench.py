@@ -224,11 +224,15 @@ def run_ours(args, rank, world, local):
     if pk is not None:
         del sim, ctx
         fp64 = fp64_form_check(args, gpu, N, box, local, pk, torch)
+    e2e2 = None
+    if not args.no_e2e and world == 1:
+        e2e2 = run_e2e_two_sims(gpu, N, args.steps, box, local, torch)
     serve = None
     if args.serve_seconds > 0 and world == 1:
         serve = run_serve(args, gpu)
     return dict(value=value, ms=ms_max / args.steps, launches=launches, clocks=clk, state=st, roofline=roof,
-                roofline_fft=roof_fft, roofline_pcl=roof_pcl, cufft=cufft, e2e=e2e, box=box, fp64=fp64, serve=serve)
+                roofline_fft=roof_fft, roofline_pcl=roof_pcl, cufft=cufft, e2e=e2e, e2e2=e2e2, box=box, fp64=fp64,
+                serve=serve)
 
 
 PK_FIELDS = (("phi", 1), ("chi", 1), ("Bi", 3), ("source", 1))
@@ -566,6 +570,56 @@ def run_e2e(gpu, ctx, sim, stream, N, steps, torch):
             "d2h_bytes_per_step": n * 56}
 
 
+def run_e2e_two_sims(gpu, N, steps, box, device, torch):
+    """The e2e loop of two independent simulations at once, each driven by its own host
+    thread through the same calls (upload from pinned memory, cycle, download into pinned
+    memory): one simulation's transfers over the host link overlap the other's cycle, and
+    its uploads the other's downloads.  Value: both simulations' particle-steps over the
+    wall time."""
+    import threading
+    n = N ** 3
+    sims = []
+    for k in range(2):
+        ctx = gpu.Context(N, gpu.PREC_MIXED, device=device)
+        sim = gpu.Sim(ctx, n)
+        sim.ic_generate(**gpu.ic_params(box, seed=7 + k))
+        sim.step()
+        host = torch.empty(n * 56, dtype=torch.uint8, pin_memory=True)
+        back = torch.empty(n * 56, dtype=torch.uint8, pin_memory=True)
+        arr, barr = host.numpy().view(gpu.PART), back.numpy().view(gpu.PART)
+        sim.particles().download(out=arr)
+        ctx.sync()
+        sims.append((ctx, sim, host, back, arr, barr))
+    start = threading.Barrier(3)
+    errors = []
+
+    def loop(ctx, sim, host, back, arr, barr):
+        try:
+            pcls = sim.particles()
+            start.wait()
+            for _ in range(steps):
+                pcls.upload(arr)
+                sim.step()
+                pcls.download(out=barr)
+        except Exception as e:  # reported after the join
+            errors.append(e)
+
+    threads = [threading.Thread(target=loop, args=s) for s in sims]
+    for t in threads:
+        t.start()
+    start.wait()
+    t0 = time.perf_counter()
+    for t in threads:
+        t.join()
+    dt = time.perf_counter() - t0
+    if errors:
+        raise errors[0]
+    del sims
+    torch.cuda.empty_cache()
+    return {"value": 2 * n * steps / dt, "unit": "particle-steps/s", "simulations": 2,
+            "h2d_bytes_per_step": n * 56, "d2h_bytes_per_step": n * 56}
+
+
 # ---------------------------------------------------------- CPU side --------
 def _cpu_worker(args):
     N, steps, seed = args
@@ -642,7 +696,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.prec == "fp64" else "f32+f64pos+i64dep",
             "data": "synthetic (device-generated BBKS Zel'dovich IC)", "config": config,
-            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "roofline_particle_update": res["roofline_pcl"], "fft_vs_cufft": res["cufft"], "cpu_baseline": cpu, "e2e": res["e2e"], "gpu_launches": res["launches"],
+            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "roofline_particle_update": res["roofline_pcl"], "fft_vs_cufft": res["cufft"], "cpu_baseline": cpu, "e2e": res["e2e"], "e2e_two_sims": res["e2e2"], "gpu_launches": res["launches"],
             "clocks": res["clocks"], "bytes_per_cycle_alg": cycle_bytes(N, args.prec),
             "final_a": res["state"]["a"]}
     if res.get("fp64"):

@@ -86,6 +86,8 @@ __global__ void k_pack(gev_part *__restrict__ out, long n, PclsArrays P) {
 // staging copy.  A block moves 256 records (14336 bytes, 896 16-byte vectors)
 // through shared memory, so that every host access of a warp is one contiguous
 // run of 16-byte vectors; an odd record count leaves a last 8-byte half vector.
+// Two blocks per SM keep several MB in flight, more than the host link needs, and
+// leave the SMs to other streams' kernels.
 constexpr int HREC = 256, HVEC = HREC * 56 / 16;
 template <typename V>
 __global__ void __launch_bounds__(256) k_unpack_host(const gev_part *in, long n, PclsArrays P, int N) {
@@ -1206,7 +1208,7 @@ int gev_pcls_upload(gev_pcls *p, const gev_part *host, long n) {
   p->n = n;
   if (n > 0) {
     if (const gev_part *h = (const gev_part *)host_alias(host)) {
-      const int hb = grid_for(ctx, (size_t)((n + HREC - 1) / HREC), 1, 8);
+      const int hb = grid_for(ctx, (size_t)((n + HREC - 1) / HREC), 1, 2);
       if (ctx->prec == GEV_PREC_FP64)
         k_unpack_host<double><<<hb, 256, 0, ctx->stream>>>(h, n, p->cur, ctx->N);
       else
@@ -1242,7 +1244,7 @@ int gev_pcls_download(gev_pcls *p, gev_part *host, long *n) {
       if (rc) return rc;
       perm = p->perm;
     }
-    const int hb = grid_for(ctx, (size_t)((p->n + HREC - 1) / HREC), 1, 8);
+    const int hb = grid_for(ctx, (size_t)((p->n + HREC - 1) / HREC), 1, 2);
     if (ctx->prec == GEV_PREC_FP64)
       k_pack_host<double><<<hb, 256, 0, ctx->stream>>>(h, p->n, p->cur, perm);
     else
