@@ -22,24 +22,136 @@ __global__ void k_source_tensor(const T *__restrict__ phi, const T *Tij, T *Sij,
     const T pzp = phi[i + b.zp], pzm = phi[i + b.zm];
     const T pxy = phi[i + b.xp + b.yp], pxz = phi[i + b.xp + b.zp], pyz = phi[i + b.yp + b.zp];
     const T h = (T)0.5;
-    const T t00 = Tij[i], t01 = Tij[V + i], t02 = Tij[2 * V + i], t11 = Tij[3 * V + i], t12 = Tij[4 * V + i],
-            t22 = Tij[5 * V + i];
+    const size_t Vs = V;  // component offsets past 2^32 elements at N = 1024
+    const T t00 = Tij[i], t01 = Tij[Vs + i], t02 = Tij[2 * Vs + i], t11 = Tij[3 * Vs + i], t12 = Tij[4 * Vs + i],
+            t22 = Tij[5 * Vs + i];
     Sij[i] = coeff * t00 + h * (pxp - pxm) * (pxp - pxm);
-    Sij[3 * V + i] = coeff * t11 + h * (pyp - pym) * (pyp - pym);
-    Sij[5 * V + i] = coeff * t22 + h * (pzp - pzm) * (pzp - pzm);
+    Sij[3 * Vs + i] = coeff * t11 + h * (pyp - pym) * (pyp - pym);
+    Sij[5 * Vs + i] = coeff * t22 + h * (pzp - pzm) * (pzp - pzm);
     if constexpr (sizeof(T) == 8) {  // the reference's expression, term by term
-      Sij[V + i] = coeff * t01 + (pxp * pyp - p * pxy) + h * p * p - h * pxp * pxp - h * pyp * pyp + h * pxy * pxy;
-      Sij[2 * V + i] = coeff * t02 + (pxp * pzp - p * pxz) + h * p * p - h * pxp * pxp - h * pzp * pzp + h * pxz * pxz;
-      Sij[4 * V + i] = coeff * t12 + (pyp * pzp - p * pyz) + h * p * p - h * pyp * pyp - h * pzp * pzp + h * pyz * pyz;
+      Sij[Vs + i] = coeff * t01 + (pxp * pyp - p * pxy) + h * p * p - h * pxp * pxp - h * pyp * pyp + h * pxy * pxy;
+      Sij[2 * Vs + i] = coeff * t02 + (pxp * pzp - p * pxz) + h * p * p - h * pxp * pxp - h * pzp * pzp + h * pxz * pxz;
+      Sij[4 * Vs + i] = coeff * t12 + (pyp * pzp - p * pyz) + h * p * p - h * pyp * pyp - h * pzp * pzp + h * pyz * pyz;
     } else {
       // FP32: with a = phi(x), b = phi(x+i), c = phi(x+j), d = phi(x+i+j) the sum
       // bc - ad + a^2/2 - b^2/2 - c^2/2 + d^2/2 equals ((a-d) - (b-c)) ((a-d) + (b-c)) / 2,
       // which never forms the O(phi^2) terms that cancel down to O((grad phi)^2)
       const T dxy = p - pxy, exy = pxp - pyp, dxz = p - pxz, exz = pxp - pzp, dyz = p - pyz, eyz = pyp - pzp;
-      Sij[V + i] = coeff * t01 + h * (dxy - exy) * (dxy + exy);
-      Sij[2 * V + i] = coeff * t02 + h * (dxz - exz) * (dxz + exz);
-      Sij[4 * V + i] = coeff * t12 + h * (dyz - eyz) * (dyz + eyz);
+      Sij[Vs + i] = coeff * t01 + h * (dxy - exy) * (dxy + exy);
+      Sij[2 * Vs + i] = coeff * t02 + h * (dxz - exz) * (dxz + exz);
+      Sij[4 * Vs + i] = coeff * t12 + h * (dyz - eyz) * (dyz + eyz);
     }
+  }
+}
+
+// FP32 with N % 4 == 0: four consecutive x cells a thread (cell i, i % 4 == 0).  The
+// rows at (y, z), (y +- 1, z), (y, z +- 1) and the streamed arrays are read as 16-byte
+// vectors (every row offset is a multiple of 4 elements); the x neighbours outside
+// the vector, phi(x0 - 1) and phi(x0 + 4), are scalar loads with the periodic wrap.
+// Each cell's expression is the scalar kernel's, term for term.
+__device__ __forceinline__ float4 ld4(const float *p) { return *reinterpret_cast<const float4 *>(p); }
+__device__ __forceinline__ void st4(float *p, const float4 &v) { *reinterpret_cast<float4 *>(p) = v; }
+__device__ __forceinline__ void unpack4(const float4 &v, float (&a)[4]) {
+  a[0] = v.x;
+  a[1] = v.y;
+  a[2] = v.z;
+  a[3] = v.w;
+}
+// the element 4 past the first of a vector at row offset `off`, wrapped when x0 + 4 == N
+__device__ __forceinline__ unsigned next4(unsigned i, int x, int N) {
+  return x + 4 == N ? i + 4u - (unsigned)N : i + 4u;
+}
+
+__global__ void k_source_tensor4(const float *__restrict__ phi, const float *Tij, float *Sij, float coeff, int N,
+                                 int lg, Div32 dN) {
+  const unsigned V = (unsigned)N * N * N, V4 = V / 4;
+  const float h = 0.5f;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < V4; q += gridDim.x * blockDim.x) {
+    const unsigned i = q * 4u;
+    int x, y, z;
+    cell_xyz(i, N, lg, dN, x, y, z);
+    const Nb3 b = nb3(i, x, y, z, N);
+    float P[4], YP[4], YM[4], ZP[4], ZM[4], XY[4], XZ[4], YZ[4];
+    // neighbour indices summed in 32 bits, where the periodic offsets wrap, before
+    // they touch a pointer
+    const unsigned iyp = i + b.yp, iym = i + b.ym, izp = i + b.zp, izm = i + b.zm, iyz = i + b.yp + b.zp;
+    unpack4(ld4(phi + i), P);
+    unpack4(ld4(phi + iyp), YP);
+    unpack4(ld4(phi + iym), YM);
+    unpack4(ld4(phi + izp), ZP);
+    unpack4(ld4(phi + izm), ZM);
+    unpack4(ld4(phi + iyz), YZ);
+    const float pl = phi[i + b.xm], pr = phi[next4(i, x, N)];
+    const float pry = phi[next4(iyp, x, N)], prz = phi[next4(izp, x, N)];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      XY[j] = j < 3 ? YP[j + 1] : pry;
+      XZ[j] = j < 3 ? ZP[j + 1] : prz;
+    }
+    const size_t Vs = V;  // component offsets past 2^32 elements at N = 1024
+    float T0[4], T1[4], T2[4], T3[4], T4[4], T5[4];
+    unpack4(ld4(Tij + i), T0);
+    unpack4(ld4(Tij + Vs + i), T1);
+    unpack4(ld4(Tij + 2 * Vs + i), T2);
+    unpack4(ld4(Tij + 3 * Vs + i), T3);
+    unpack4(ld4(Tij + 4 * Vs + i), T4);
+    unpack4(ld4(Tij + 5 * Vs + i), T5);
+    float S0[4], S1[4], S2[4], S3[4], S4[4], S5[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float p = P[j];
+      const float pxp = j < 3 ? P[j + 1] : pr, pxm = j > 0 ? P[j - 1] : pl;
+      const float pyp = YP[j], pym = YM[j], pzp = ZP[j], pzm = ZM[j];
+      const float pxy = XY[j], pxz = XZ[j], pyz = YZ[j];
+      S0[j] = coeff * T0[j] + h * (pxp - pxm) * (pxp - pxm);
+      S3[j] = coeff * T3[j] + h * (pyp - pym) * (pyp - pym);
+      S5[j] = coeff * T5[j] + h * (pzp - pzm) * (pzp - pzm);
+      const float dxy = p - pxy, exy = pxp - pyp, dxz = p - pxz, exz = pxp - pzp, dyz = p - pyz, eyz = pyp - pzp;
+      S1[j] = coeff * T1[j] + h * (dxy - exy) * (dxy + exy);
+      S2[j] = coeff * T2[j] + h * (dxz - exz) * (dxz + exz);
+      S4[j] = coeff * T4[j] + h * (dyz - eyz) * (dyz + eyz);
+    }
+    st4(Sij + i, make_float4(S0[0], S0[1], S0[2], S0[3]));
+    st4(Sij + Vs + i, make_float4(S1[0], S1[1], S1[2], S1[3]));
+    st4(Sij + 2 * Vs + i, make_float4(S2[0], S2[1], S2[2], S2[3]));
+    st4(Sij + 3 * Vs + i, make_float4(S3[0], S3[1], S3[2], S3[3]));
+    st4(Sij + 4 * Vs + i, make_float4(S4[0], S4[1], S4[2], S4[3]));
+    st4(Sij + 5 * Vs + i, make_float4(S5[0], S5[1], S5[2], S5[3]));
+  }
+}
+
+__global__ void k_source_scalar4(const float *__restrict__ phi, const float *__restrict__ chi, const float *source,
+                                 float bgmodel, float *result, float coeff, float coeff2, float coeff3, int N,
+                                 int lg, Div32 dN) {
+  const unsigned V4 = (unsigned)N * N * N / 4;
+  for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < V4; q += gridDim.x * blockDim.x) {
+    const unsigned i = q * 4u;
+    int x, y, z;
+    cell_xyz(i, N, lg, dN, x, y, z);
+    const Nb3 b = nb3(i, x, y, z, N);
+    float P[4], YP[4], YM[4], ZP[4], ZM[4], SRC[4], CHI[4], R[4];
+    const unsigned iyp = i + b.yp, iym = i + b.ym, izp = i + b.zp, izm = i + b.zm;  // wrapped in 32 bits
+    unpack4(ld4(phi + i), P);
+    unpack4(ld4(phi + iyp), YP);
+    unpack4(ld4(phi + iym), YM);
+    unpack4(ld4(phi + izp), ZP);
+    unpack4(ld4(phi + izm), ZM);
+    unpack4(ld4(source + i), SRC);
+    unpack4(ld4(chi + i), CHI);
+    const float pl = phi[i + b.xm], pr = phi[next4(i, x, N)];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const float p = P[j];
+      const float dx = (j > 0 ? P[j - 1] : pl) - (j < 3 ? P[j + 1] : pr);
+      const float dy = YM[j] - YP[j];
+      const float dz = ZM[j] - ZP[j];
+      float r = coeff2 * (SRC[j] - bgmodel);
+      r *= 1.f - 2.f * p;
+      r += 0.125f * (dx * dx + dy * dy + dz * dz);
+      r += (coeff3 - coeff) * p - coeff3 * CHI[j];
+      R[j] = r;
+    }
+    st4(result + i, make_float4(R[0], R[1], R[2], R[3]));
   }
 }
 
@@ -109,6 +221,10 @@ int gev_prepare_source_tensor(gev_ctx *ctx, const gev_field *phi, const gev_fiel
     k_source_tensor<double><<<blocks, 256, 0, ctx->stream>>>((const double *)phi->d, (const double *)Tij->d,
                                                              (double *)Sij->d, coeff, ctx->N, lg_pow2(ctx->N),
                                                              make_div32(ctx->N));
+  else if (ctx->N % 4 == 0)
+    k_source_tensor4<<<grid_for(ctx, V / 4, 256, 16), 256, 0, ctx->stream>>>(
+        (const float *)phi->d, (const float *)Tij->d, (float *)Sij->d, (float)coeff, ctx->N, lg_pow2(ctx->N),
+        make_div32(ctx->N));
   else
     k_source_tensor<float><<<blocks, 256, 0, ctx->stream>>>((const float *)phi->d, (const float *)Tij->d,
                                                             (float *)Sij->d, (float)coeff, ctx->N, lg_pow2(ctx->N),
@@ -130,6 +246,10 @@ int gev_prepare_source_scalar(gev_ctx *ctx, const gev_field *phi, const gev_fiel
                                                              (const double *)source->d, bgmodel, (double *)result->d,
                                                              coeff, coeff2, coeff3, ctx->N, lg_pow2(ctx->N),
                                                              make_div32(ctx->N));
+  else if (ctx->N % 4 == 0)
+    k_source_scalar4<<<grid_for(ctx, V / 4, 256, 16), 256, 0, ctx->stream>>>(
+        (const float *)phi->d, (const float *)chi->d, (const float *)source->d, (float)bgmodel, (float *)result->d,
+        (float)coeff, (float)coeff2, (float)coeff3, ctx->N, lg_pow2(ctx->N), make_div32(ctx->N));
   else
     k_source_scalar<float><<<blocks, 256, 0, ctx->stream>>>(
         (const float *)phi->d, (const float *)chi->d, (const float *)source->d, (float)bgmodel, (float *)result->d,
