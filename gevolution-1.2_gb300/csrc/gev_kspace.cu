@@ -62,6 +62,38 @@ __global__ void k_poisson(const typename CT<T>::C *src, typename CT<T>::C *pot, 
   }
 }
 
+// projectFTscalar, gevolution.hpp:211-265: chi at one k != 0
+template <typename T, typename C>
+__device__ __forceinline__ C chi_at(C S00, C S01, C S02, C S11, C S12, C S22, T g0, T g1, T g2, C k0, C k1, C k2,
+                                    int N) {
+  C t = cscale(g1 + g2 - (T)2 * g0, S00);
+  t = cadd(t, cscale(g0 + g2 - (T)2 * g1, S11));
+  t = cadd(t, cscale(g0 + g1 - (T)2 * g2, S22));
+  t = csub(t, cmul(cscale((T)6, cmul(k0, k1)), S01));
+  t = csub(t, cmul(cscale((T)6, cmul(k0, k2)), S02));
+  t = csub(t, cmul(cscale((T)6, cmul(k1, k2)), S12));
+  const T kk = g0 + g1 + g2;
+  return cscale((T)1 / ((T)2 * kk * kk * (T)N), t);
+}
+// evolveFTvector, gevolution.hpp:284-330: the increments of B_0, B_1, B_2 at one k != 0
+template <typename T, typename C>
+__device__ __forceinline__ void evolve_at(C S00, C S01, C S02, C S11, C S12, C S22, T g0, T g1, T g2, C k0, C k1,
+                                          C k2, T a2dtau, C &d0, C &d1, C &d2) {
+  T k4 = g0 + g1 + g2;
+  k4 *= k4;
+  const T pre = (T)-2 * a2dtau / k4;  // multiplies by i * pre
+  C x, u;
+  x = csub(csub(csub(cscale(g1 + g2, S00), cscale(g1, S11)), cscale(g2, S22)), cmul(cscale((T)2, cmul(k1, k2)), S12));
+  u = cadd(cmul(cconj(k0), x), cscale(g1 + g2 - g0, cadd(cmul(k1, S01), cmul(k2, S02))));
+  d0 = cmk<C>(-pre * u.y, pre * u.x);
+  x = csub(csub(csub(cscale(g0 + g2, S11), cscale(g0, S00)), cscale(g2, S22)), cmul(cscale((T)2, cmul(k0, k2)), S02));
+  u = cadd(cmul(cconj(k1), x), cscale(g0 + g2 - g1, cadd(cmul(k0, S01), cmul(k2, S12))));
+  d1 = cmk<C>(-pre * u.y, pre * u.x);
+  x = csub(csub(csub(cscale(g0 + g1, S22), cscale(g0, S00)), cscale(g1, S11)), cmul(cscale((T)2, cmul(k0, k1)), S01));
+  u = cadd(cmul(cconj(k2), x), cscale(g0 + g1 - g2, cadd(cmul(k0, S02), cmul(k1, S12))));
+  d2 = cmk<C>(-pre * u.y, pre * u.x);
+}
+
 // projectFTscalar, gevolution.hpp:211-265
 template <typename T>
 __global__ void k_project_scalar(const typename CT<T>::C *__restrict__ S, typename CT<T>::C *chi,
@@ -80,14 +112,7 @@ __global__ void k_project_scalar(const typename CT<T>::C *__restrict__ S, typena
     const C k0 = ks[k.kx], k1 = ks[k.ky], k2 = ks[k.kz];
     const C S00 = S[id], S01 = S[n + id], S02 = S[2 * n + id], S11 = S[3 * n + id], S12 = S[4 * n + id],
             S22 = S[5 * n + id];
-    C t = cscale(g1 + g2 - (T)2 * g0, S00);
-    t = cadd(t, cscale(g0 + g2 - (T)2 * g1, S11));
-    t = cadd(t, cscale(g0 + g1 - (T)2 * g2, S22));
-    t = csub(t, cmul(cscale((T)6, cmul(k0, k1)), S01));
-    t = csub(t, cmul(cscale((T)6, cmul(k0, k2)), S02));
-    t = csub(t, cmul(cscale((T)6, cmul(k1, k2)), S12));
-    const T kk = g0 + g1 + g2;
-    t = cscale((T)1 / ((T)2 * kk * kk * (T)N), t);
+    const C t = chi_at<T>(S00, S01, S02, S11, S12, S22, g0, g1, g2, k0, k1, k2, N);
     chi[id] = add ? cadd(chi[id], t) : t;
   }
 }
@@ -110,19 +135,40 @@ __global__ void k_evolve_vector(const typename CT<T>::C *__restrict__ S, typenam
     const C k0 = ks[k.kx], k1 = ks[k.ky], k2 = ks[k.kz];
     const C S00 = S[id], S01 = S[n + id], S02 = S[2 * n + id], S11 = S[3 * n + id], S12 = S[4 * n + id],
             S22 = S[5 * n + id];
-    T k4 = g0 + g1 + g2;
-    k4 *= k4;
-    const T pre = (T)-2 * a2dtau / k4;  // multiplies by i * pre
-    C x, u;
-    x = csub(csub(csub(cscale(g1 + g2, S00), cscale(g1, S11)), cscale(g2, S22)), cmul(cscale((T)2, cmul(k1, k2)), S12));
-    u = cadd(cmul(cconj(k0), x), cscale(g1 + g2 - g0, cadd(cmul(k1, S01), cmul(k2, S02))));
-    B[id] = cadd(B[id], cmk<C>(-pre * u.y, pre * u.x));
-    x = csub(csub(csub(cscale(g0 + g2, S11), cscale(g0, S00)), cscale(g2, S22)), cmul(cscale((T)2, cmul(k0, k2)), S02));
-    u = cadd(cmul(cconj(k1), x), cscale(g0 + g2 - g1, cadd(cmul(k0, S01), cmul(k2, S12))));
-    B[n + id] = cadd(B[n + id], cmk<C>(-pre * u.y, pre * u.x));
-    x = csub(csub(csub(cscale(g0 + g1, S22), cscale(g0, S00)), cscale(g1, S11)), cmul(cscale((T)2, cmul(k0, k1)), S01));
-    u = cadd(cmul(cconj(k2), x), cscale(g0 + g1 - g2, cadd(cmul(k0, S02), cmul(k1, S12))));
-    B[2 * n + id] = cadd(B[2 * n + id], cmk<C>(-pre * u.y, pre * u.x));
+    C d0, d1, d2;
+    evolve_at<T>(S00, S01, S02, S11, S12, S22, g0, g1, g2, k0, k1, k2, a2dtau, d0, d1, d2);
+    B[id] = cadd(B[id], d0);
+    B[n + id] = cadd(B[n + id], d1);
+    B[2 * n + id] = cadd(B[2 * n + id], d2);
+  }
+}
+
+// projectFTscalar (add = 0) and evolveFTvector in one pass: the six SijFT components
+// read once for both, the same arithmetic as the two kernels
+template <typename T>
+__global__ void k_project_evolve(const typename CT<T>::C *__restrict__ S, typename CT<T>::C *chi,
+                                 typename CT<T>::C *B, const T *__restrict__ gk2,
+                                 const typename CT<T>::C *__restrict__ ks, T a2dtau, KDim kd, size_t n) {
+  const int N = kd.N;
+  typedef typename CT<T>::C C;
+  for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < n; id += (size_t)gridDim.x * blockDim.x) {
+    if (id == 0) {
+      chi[0] = cmk<C>(0, 0);
+      B[0] = B[n] = B[2 * n] = cmk<C>(0, 0);
+      continue;
+    }
+    KIdx<T> k;
+    kidx<T>(id, kd, k);
+    const T g0 = gk2[k.kx], g1 = gk2[k.ky], g2 = gk2[k.kz];
+    const C k0 = ks[k.kx], k1 = ks[k.ky], k2 = ks[k.kz];
+    const C S00 = S[id], S01 = S[n + id], S02 = S[2 * n + id], S11 = S[3 * n + id], S12 = S[4 * n + id],
+            S22 = S[5 * n + id];
+    chi[id] = chi_at<T>(S00, S01, S02, S11, S12, S22, g0, g1, g2, k0, k1, k2, N);
+    C d0, d1, d2;
+    evolve_at<T>(S00, S01, S02, S11, S12, S22, g0, g1, g2, k0, k1, k2, a2dtau, d0, d1, d2);
+    B[id] = cadd(B[id], d0);
+    B[n + id] = cadd(B[n + id], d1);
+    B[2 * n + id] = cadd(B[2 * n + id], d2);
   }
 }
 
@@ -265,6 +311,26 @@ int gev_project_scalar(gev_ctx *ctx, const gev_field *SijFT, gev_field *chiFT, i
 }
 int gev_evolve_vector(gev_ctx *ctx, const gev_field *SijFT, gev_field *BiFT, double a2dtau) {
   return kspace(ctx, 2, SijFT, 6, BiFT, 3, a2dtau, 0., 0);
+}
+int gev_project_scalar_evolve_vector(gev_ctx *ctx, const gev_field *SijFT, gev_field *chiFT, gev_field *BiFT,
+                                     double a2dtau) {
+  if (!ctx || !SijFT || !chiFT || !BiFT || SijFT->ctx != ctx || chiFT->ctx != ctx || BiFT->ctx != ctx ||
+      SijFT->kind != GEV_FIELD_SPECTRUM || chiFT->kind != GEV_FIELD_SPECTRUM || BiFT->kind != GEV_FIELD_SPECTRUM ||
+      SijFT->ncomp != 6 || chiFT->ncomp != 1 || BiFT->ncomp != 3 || chiFT == SijFT || BiFT == SijFT)
+    return gev_fail(ctx, GEV_EINVAL, "project_scalar_evolve_vector: SijFT (6), chiFT (1), BiFT (3), distinct spectra");
+  const int N = ctx->N, NH = N / 2 + 1;
+  const size_t n = (size_t)N * N * NH;
+  const int blocks = grid_for(ctx, n, 256, 16);
+  if (ctx->prec == GEV_PREC_FP64)
+    k_project_evolve<double><<<blocks, 256, 0, ctx->stream>>>(
+        (const CT<double>::C *)SijFT->d, (CT<double>::C *)chiFT->d, (CT<double>::C *)BiFT->d,
+        (const double *)ctx->d_gridk2, (const CT<double>::C *)ctx->d_kshift, a2dtau, make_kdim(N), n);
+  else
+    k_project_evolve<float><<<blocks, 256, 0, ctx->stream>>>(
+        (const CT<float>::C *)SijFT->d, (CT<float>::C *)chiFT->d, (CT<float>::C *)BiFT->d,
+        (const float *)ctx->d_gridk2, (const CT<float>::C *)ctx->d_kshift, (float)a2dtau, make_kdim(N), n);
+  GEV_LAUNCH_CHECK(ctx);
+  return GEV_OK;
 }
 int gev_project_vector(gev_ctx *ctx, const gev_field *SiFT, gev_field *BiFT, double coeff, double modif) {
   return kspace(ctx, 3, SiFT, 3, BiFT, 3, coeff, modif, 0);

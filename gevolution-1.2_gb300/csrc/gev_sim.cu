@@ -218,15 +218,17 @@ int gev_sim_step_fields(gev_sim *s) {
   // chi (main.cpp:539-568)
   RC(gev_prepare_source_tensor(ctx, s->phi, s->Sij, s->Sij, 2. * fourpiG * dx * dx / a));
   RC(gev_fft_r2c(ctx, s->Sij, s->SijFT));
-  RC(gev_project_scalar(ctx, s->SijFT, s->scalarFT, 0));
-  RC(gev_fft_c2r(ctx, s->scalarFT, s->chi));
-
-  // B (main.cpp:570-598)
   if (st.vector_elliptic) {
+    RC(gev_project_scalar(ctx, s->SijFT, s->scalarFT, 0));
+    RC(gev_fft_c2r(ctx, s->scalarFT, s->chi));
+    // B (main.cpp:570-598)
     RC(gev_fft_r2c(ctx, s->Bi, s->BiFT));
     RC(gev_project_vector(ctx, s->BiFT, s->BiFT, fourpiG * dx * dx, 0.));
   } else {
-    RC(gev_evolve_vector(ctx, s->SijFT, s->BiFT, a * a * st.dtau_old));
+    // chi's projection and B's evolution (main.cpp:558, 586) share one read of SijFT;
+    // neither c2r reads what the other's k-space step writes
+    RC(gev_project_scalar_evolve_vector(ctx, s->SijFT, s->scalarFT, s->BiFT, a * a * st.dtau_old));
+    RC(gev_fft_c2r(ctx, s->scalarFT, s->chi));
   }
   RC(gev_fft_c2r(ctx, s->BiFT, s->Bi));
   return GEV_OK;

@@ -67,6 +67,7 @@ _SIGS = {
     "gev_solve_poisson": [_vp, _vp, _vp, _d, _d],
     "gev_project_scalar": [_vp, _vp, _vp, _i],
     "gev_evolve_vector": [_vp, _vp, _vp, _d],
+    "gev_project_scalar_evolve_vector": [_vp, _vp, _vp, _vp, _d],
     "gev_project_vector": [_vp, _vp, _vp, _d, _d],
     "gev_project_tensor": [_vp, _vp, _vp],
     "gev_update_q": [_vp, _vp, _i, _d, _vp, _vp, _vp, _i, _d, _d, ctypes.POINTER(_d)],
@@ -333,6 +334,11 @@ def project_scalar(SijFT, chiFT, add=0):
 def evolve_vector(SijFT, BiFT, a2dtau):
     _check(lib().gev_evolve_vector(SijFT.ctx.handle, SijFT.handle, BiFT.handle, a2dtau), SijFT.ctx,
            "gev_evolve_vector")
+
+def project_scalar_evolve_vector(SijFT, chiFT, BiFT, a2dtau):
+    """projectFTscalar(SijFT, chiFT) and evolveFTvector(SijFT, BiFT, a2dtau) in one pass."""
+    _check(lib().gev_project_scalar_evolve_vector(SijFT.ctx.handle, SijFT.handle, chiFT.handle, BiFT.handle,
+                                                  a2dtau), SijFT.ctx, "gev_project_scalar_evolve_vector")
 
 
 def project_vector(SiFT, BiFT, coeff=1.0, modif=0.0):

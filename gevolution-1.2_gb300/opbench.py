@@ -97,6 +97,7 @@ def main():
         ("r2c_x6", lambda: gpu.fft_r2c(Sij, SFT)),
         ("project_scalar", lambda: gpu.project_scalar(SFT, sFT, 0)),
         ("evolve_vector", lambda: gpu.evolve_vector(SFT, BFT, 1e-9)),
+        ("project_evolve", lambda: gpu.project_scalar_evolve_vector(SFT, sFT, BFT, 1e-9)),
         ("c2r_x3", lambda: gpu.fft_c2r(BFT, Bi)),
         ("fft_axis_y", lambda: gpu.fft_axis(sFT, 1, -1)),
         ("fft_axis_z", lambda: gpu.fft_axis(sFT, 2, -1)),

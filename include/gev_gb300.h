@@ -131,6 +131,10 @@ int gev_project_scalar(gev_ctx *ctx, const gev_field *SijFT, gev_field *chiFT,
                        int add); /* projectFTscalar, gevolution.hpp:211 */
 int gev_evolve_vector(gev_ctx *ctx, const gev_field *SijFT, gev_field *BiFT,
                       double a2dtau); /* evolveFTvector, gevolution.hpp:284 */
+/* projectFTscalar(SijFT, chiFT) and evolveFTvector(SijFT, BiFT, a2dtau) as main.cpp:558 and 586
+ * call them in the parabolic vector method, in one pass over SijFT; the same bits as the two */
+int gev_project_scalar_evolve_vector(gev_ctx *ctx, const gev_field *SijFT, gev_field *chiFT, gev_field *BiFT,
+                                     double a2dtau);
 int gev_project_vector(gev_ctx *ctx, const gev_field *SiFT, gev_field *BiFT, double coeff,
                        double modif); /* projectFTvector, gevolution.hpp:350 */
 int gev_project_tensor(gev_ctx *ctx, const gev_field *SijFT,

@@ -191,3 +191,23 @@ def load_sim(gpu, s, o):
     s.set_state(a=sc["a"], tau=sc["tau"], dtau=sc["dtau"], dtau_old=sc["dtau_old"], fourpiG=sc["fourpiG"],
                 Cf=sc["Cf"], steplimit=sc["steplimit"], z_relax=sc["z_relax"], mass=sc["mass"], cycle=sc["cycle"],
                 vector_elliptic=sc["vector_elliptic"], cosmo=o.cosmo)
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_project_scalar_evolve_vector_fused_equals_separate(gpu, prec):
+    """gev_project_scalar_evolve_vector (the cycle's one pass over SijFT) equals
+    projectFTscalar followed by evolveFTvector, bit for bit in both forms, k = 0 included."""
+    N = 16
+    rng = np.random.default_rng(40 + prec)
+    ctx = gpu.Context(N, prec)
+    S = ctx.spectrum(6)
+    shp = S.shape
+    S.upload(rng.standard_normal(shp) + 1j * rng.standard_normal(shp))
+    B0 = rng.standard_normal((3,) + shp[1:]) + 1j * rng.standard_normal((3,) + shp[1:])
+    chi1, B1 = ctx.spectrum(1), ctx.spectrum(3).upload(B0)
+    gpu.project_scalar(S, chi1, 0)
+    gpu.evolve_vector(S, B1, 3.7e-3)
+    chi2, B2 = ctx.spectrum(1), ctx.spectrum(3).upload(B0)
+    gpu.project_scalar_evolve_vector(S, chi2, B2, 3.7e-3)
+    assert np.array_equal(chi1.download(), chi2.download())
+    assert np.array_equal(B1.download(), B2.download())
