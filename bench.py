@@ -357,6 +357,13 @@ def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
             "traffic": COLS_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
 
 
+# DRAM traffic per call of the particle update: k_kick_drift and k_move from an ncu
+# capture of the 256^3 cycle (opbench --grid 256 --only step), scaled by 8 to 512^3.
+# k_kick_drift 1624.8 MB read + 973.8 MB written, k_move 1140.9 MB read + 958.6 MB
+# written; (4698.1 MB) x 8.  The scan's three kernels (about 1 GB at 512^3) are not in it.
+PARTICLE_TRAFFIC = {(512, "mixed"): 37.585e9}
+
+
 def particle_update_roofline(gpu, ctx, sim, stream, N, prec):
     """The cycle's particle update, whose kick+drift kernel is the largest single kernel
     of the launch list: gev_update_q_pos (updateVel + moveParticles with the relink),
@@ -386,8 +393,8 @@ def particle_update_roofline(gpu, ctx, sim, stream, N, prec):
     peak, kind = hbm_peak()
     achieved = alg / (ms / 1e3) / 1e9
     return {"kernel": "k_kick_drift + k_scan_* + k_move (gev_update_q_pos: kick, drift, relink)", "bound": "hbm",
-            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
-            "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
+            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "traffic": PARTICLE_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
 
 
 def fft_vs_cufft(gpu, ctx, stream, N, prec, torch, reps=5):
