@@ -341,4 +341,11 @@ int gev_fft_c2r(gev_ctx *ctx, const gev_field *spec, gev_field *real) {
   return GEV_OK;
 }
 
+int gev_fft_c2r_poisson(gev_ctx *ctx, const gev_field *srcFT, gev_field *real, double coeff, double modif) {
+  if (!ctx || !real || !srcFT || real->ctx != ctx || srcFT->ctx != ctx || real->kind != GEV_FIELD_REAL ||
+      srcFT->kind != GEV_FIELD_SPECTRUM || real->ncomp != 1 || srcFT->ncomp != 1)
+    return gev_fail(ctx, GEV_EINVAL, "fft_c2r_poisson: one spectrum component and one real component");
+  return fft_c2r_poisson_comp(ctx, srcFT->d, real->d, coeff, modif);
+}
+
 }  // extern "C"

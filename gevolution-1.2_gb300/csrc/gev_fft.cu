@@ -286,11 +286,14 @@ int r2c_comp(gev_ctx *ctx, const void *real, void *spec) {
   return run_cols<T, -1>(ctx, spec, spec, (long)N * NH, NH);  // z: lines along kz, planes ky
 }
 
+// pois: the FP32 power-of-two z pass applies solveModifiedPoissonFT's factor (coeff,
+// already divided by -N^3, and modif) to its input as it loads it
 template <typename T>
-int c2r_comp(gev_ctx *ctx, const void *spec, void *real, void *scratch) {
+int c2r_comp(gev_ctx *ctx, const void *spec, void *real, void *scratch, const double *pois = nullptr) {
   typedef typename CT<T>::C C;
   const int N = ctx->N, NH = N / 2 + 1, M = N / 2;
-  int rc = run_cols<T, +1>(ctx, spec, scratch, (long)N * NH, NH);  // z, out of place
+  int rc = pois ? fft_cols_z_poisson(ctx, spec, scratch, pois[0], pois[1])
+                : run_cols<T, +1>(ctx, spec, scratch, (long)N * NH, NH);  // z, out of place
   if (rc) return rc;
   rc = run_cols<T, +1>(ctx, scratch, scratch, NH, (long)N * NH);  // y, in place
   if (rc) return rc;
@@ -355,6 +358,23 @@ int fft_init_kernels(int prec) {
 int fft_r2c_comp(gev_ctx *ctx, const void *real, void *spec) {
   fft_autotune(ctx);
   return ctx->prec == GEV_PREC_FP64 ? r2c_comp<double>(ctx, real, spec) : r2c_comp<float>(ctx, real, spec);
+}
+
+// c2r of the solution of solveModifiedPoissonFT for the spectrum srcFT, which is kept.
+// FP32 on power-of-two grids: the factor is applied in the first (z) pass as it loads
+// its input; otherwise the solve writes the scratch spectrum and the c2r transforms it
+// there in place.  Either way the bits of the two calls in place.
+int fft_c2r_poisson_comp(gev_ctx *ctx, const void *srcFT, void *real, double coeff, double modif) {
+  fft_autotune(ctx);
+  const double N3 = (double)((long)ctx->N * (long)ctx->N * (long)ctx->N);
+  if (ctx->prec != GEV_PREC_FP64 && fft_reg_ok(ctx->N)) {
+    const double pois[2] = {coeff / -N3, modif};
+    return c2r_comp<float>(ctx, srcFT, real, ctx->d_fft_scratch, pois);
+  }
+  int rc = kspace_poisson_raw(ctx, srcFT, ctx->d_fft_scratch, coeff / -N3, modif);
+  if (rc) return rc;
+  return ctx->prec == GEV_PREC_FP64 ? c2r_comp<double>(ctx, ctx->d_fft_scratch, real, ctx->d_fft_scratch)
+                                    : c2r_comp<float>(ctx, ctx->d_fft_scratch, real, ctx->d_fft_scratch);
 }
 
 int fft_c2r_comp(gev_ctx *ctx, const void *spec, void *real, void *scratch) {

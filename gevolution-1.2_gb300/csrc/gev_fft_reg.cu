@@ -133,11 +133,24 @@ __device__ __forceinline__ void stage_tw(C *tw, const C *__restrict__ g, int L) 
   __syncthreads();
 }
 
-// y / z pass over B columns (consecutive kx) of one plane per tile; in may equal out
-template <typename T, int SIGN, int L, int LGB>
+// solveModifiedPoissonFT's factor at (kx, ky, kz), as k_poisson applies it (coeff
+// already divided by -N^3)
+struct PoisArgs {
+  const float *gk2;
+  float coeff, modif;
+};
+__device__ __forceinline__ float poisson_factor(const PoisArgs &p, int kx, int ky, int kz) {
+  if ((kx | ky | kz) == 0) return p.modif == 0.f ? 0.f : p.coeff / p.modif;
+  return p.coeff / (p.gk2[kx] + p.gk2[ky] + p.gk2[kz] + p.modif);
+}
+
+// y / z pass over B columns (consecutive kx) of one plane per tile; in may equal out.
+// POIS (FP32 z pass, lines along kz, planes ky): each element is multiplied by its
+// Poisson factor as it is loaded, the pass that follows the solve folded into it.
+template <typename T, int SIGN, int L, int LGB, bool POIS = false>
 __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L / 8) << LGB))
     k_fft_cols_reg(const typename CT<T>::C *in, typename CT<T>::C *out, const typename CT<T>::C *__restrict__ twg,
-                   int NH, long ES, long PS, int ntiles) {
+                   int NH, long ES, long PS, int ntiles, PoisArgs pois) {
   typedef RegFft<T, SIGN, L> R;
   typedef typename CT<T>::C C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -157,6 +170,11 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
     C v[8];
 #pragma unroll
     for (int r = 0; r < 8; ++r) v[r] = on ? src[r * rstep] : cmk<C>(0, 0);
+    if constexpr (POIS) {
+#pragma unroll
+      for (int r = 0; r < 8; ++r)
+        if (on) v[r] = cscale(poisson_factor(pois, col, (int)plane, m + r * R::TPL), v[r]);
+    }
     R::template run_from<0>(v, X, B, c, m, tw);
     if (on) {
       C *dst = out + (long)plane * PS + col;
@@ -279,8 +297,8 @@ int launch_cfg(gev_ctx *ctx, K kern, int threads, size_t smem, long ntiles, int 
   return GEV_OK;
 }
 
-template <typename T, int SIGN, int L, int LGB>
-int cols_LB(gev_ctx *ctx, const void *in, void *out, long ES, long PS) {
+template <typename T, int SIGN, int L, int LGB, bool POIS = false>
+int cols_LB(gev_ctx *ctx, const void *in, void *out, long ES, long PS, PoisArgs pois = PoisArgs{nullptr, 0.f, 0.f}) {
   static_assert(fits<L, LGB>(), "column tile too wide");
   typedef typename CT<T>::C C;
   static int per_sm = 0;
@@ -289,10 +307,10 @@ int cols_LB(gev_ctx *ctx, const void *in, void *out, long ES, long PS) {
   const long ntiles = (long)ctx->N * ((NH + B - 1) / B);
   const size_t smem = ((size_t)L + (size_t)L * B) * sizeof(C);
   int grid = 0;
-  int rc = launch_cfg(ctx, k_fft_cols_reg<T, SIGN, L, LGB>, threads, smem, ntiles, per_sm, grid);
+  int rc = launch_cfg(ctx, k_fft_cols_reg<T, SIGN, L, LGB, POIS>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
-  k_fft_cols_reg<T, SIGN, L, LGB><<<grid, threads, smem, ctx->stream>>>((const C *)in, (C *)out,
-                                                                        (const C *)ctx->d_twN, NH, ES, PS, (int)ntiles);
+  k_fft_cols_reg<T, SIGN, L, LGB, POIS><<<grid, threads, smem, ctx->stream>>>((const C *)in, (C *)out,
+                                                                        (const C *)ctx->d_twN, NH, ES, PS, (int)ntiles, pois);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
@@ -320,6 +338,22 @@ int cols_L(gev_ctx *ctx, const void *in, void *out, long ES, long PS) {
     }
     return gev_fail(ctx, GEV_EINVAL, "fft: column tile width");
   }
+}
+
+// the FP32 backward z pass (spectrum -> out) with the Poisson factor applied to its input
+template <int L>
+int cols_z_poisson(gev_ctx *ctx, const void *in, void *out, PoisArgs pois) {
+  const long N = ctx->N, NH = N / 2 + 1, ES = N * NH, PS = NH;
+  switch (col_lg<float, L>(ctx, true)) {
+    case 2: return cols_LB<float, 1, L, 2, true>(ctx, in, out, ES, PS, pois);
+    case 3:
+      if constexpr (fits<L, 3>()) return cols_LB<float, 1, L, 3, true>(ctx, in, out, ES, PS, pois);
+      break;
+    case 4:
+      if constexpr (fits<L, 4>()) return cols_LB<float, 1, L, 4, true>(ctx, in, out, ES, PS, pois);
+      break;
+  }
+  return gev_fail(ctx, GEV_EINVAL, "fft: column tile width");
 }
 
 // nrows: rows of the transform (N^2; fewer only while tuning)
@@ -503,6 +537,17 @@ extern "C" int gev_ctx_set_fft_tiles(gev_ctx *ctx, const int *lg) {
   for (int p = 0; p < 4; ++p) ctx->fft_lg[p] = lg[p];
   ctx->fft_tuned = true;
   return GEV_OK;
+}
+
+int fft_cols_z_poisson(gev_ctx *ctx, const void *spec, void *out, double coeff, double modif) {
+  const PoisArgs pois{(const float *)ctx->d_gridk2, (float)coeff, (float)modif};
+  switch (ctx->N) {
+#define CALL(l) \
+  case l: return cols_z_poisson<l>(ctx, spec, out, pois);
+    CALL(8) CALL(16) CALL(32) CALL(64) CALL(128) CALL(256) CALL(512) CALL(1024)
+#undef CALL
+    default: return gev_fail(ctx, GEV_EINVAL, "fft_cols_z_poisson: power-of-two grids of 8 to 1024");
+  }
 }
 
 void fft_autotune(gev_ctx *ctx) {

@@ -363,6 +363,11 @@ int fft_c2r_rows_reg(gev_ctx *ctx, const void *spec, void *real);
 // times the FP32 tile-width candidates of each pass once per context (a no-op after
 // the first call and for FP64)
 void fft_autotune(gev_ctx *ctx);
+// FP32, power-of-two N: the backward z pass of a spectrum into out with
+// solveModifiedPoissonFT's factor (coeff already divided by -N^3) applied on load
+int fft_cols_z_poisson(gev_ctx *ctx, const void *spec, void *out, double coeff, double modif);
+int fft_c2r_poisson_comp(gev_ctx *ctx, const void *srcFT, void *real, double coeff, double modif);
+int kspace_poisson_raw(gev_ctx *ctx, const void *in, void *out, double coeff, double modif);
 int pcls_relink(gev_ctx *ctx, gev_pcls *p);
 int pcls_id_order(gev_ctx *ctx, gev_pcls *p);
 int pcls_unpack_at(gev_ctx *ctx, gev_pcls *p, const gev_part *d, long count, long offset);

@@ -299,6 +299,13 @@ int kspace(gev_ctx *ctx, int op, const gev_field *in, int nin, gev_field *out, i
 
 }  // namespace
 
+// k_poisson over one component's raw device spectra (in may equal out); coeff as the
+// kernel takes it, already divided by -N^3
+int kspace_poisson_raw(gev_ctx *ctx, const void *in, void *out, double coeff, double modif) {
+  return ctx->prec == GEV_PREC_FP64 ? launch_kspace<double>(ctx, 0, in, out, coeff, modif, 0)
+                                    : launch_kspace<float>(ctx, 0, in, out, coeff, modif, 0);
+}
+
 extern "C" {
 
 int gev_solve_poisson(gev_ctx *ctx, const gev_field *srcFT, gev_field *potFT, double coeff, double modif) {

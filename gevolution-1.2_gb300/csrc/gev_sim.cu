@@ -206,8 +206,12 @@ int gev_sim_step_fields(gev_sim *s) {
     RC(gev_prepare_source_scalar(ctx, s->phi, s->chi, s->source, cm.Omega_cdm + cm.Omega_b, s->source,
                                  3. * H * dx * dx / st.dtau_old, fourpiG * dx * dx / a, 3. * H * H * dx * dx));
     RC(gev_fft_r2c(ctx, s->source, s->scalarFT));
-    RC(gev_solve_poisson(ctx, s->scalarFT, s->scalarFT, 1. / (dx * dx), 3. * H / st.dtau_old));
-    RC(gev_fft_c2r(ctx, s->scalarFT, s->phi));
+    if (ctx->prec == GEV_PREC_FP64) {  // scalarFT keeps the potential: phi(k=0) is read from it below
+      RC(gev_solve_poisson(ctx, s->scalarFT, s->scalarFT, 1. / (dx * dx), 3. * H / st.dtau_old));
+      RC(gev_fft_c2r(ctx, s->scalarFT, s->phi));
+    } else {  // the solve folded into the transform's first pass; scalarFT is scratch after it
+      RC(gev_fft_c2r_poisson(ctx, s->scalarFT, s->phi, 1. / (dx * dx), 3. * H / st.dtau_old));
+    }
   }
   // phi(k=0) for the background record (main.cpp:521-533)
   if (ctx->prec == GEV_PREC_FP64) {

@@ -63,6 +63,7 @@ _SIGS = {
     "gev_prepare_source_scalar": [_vp, _vp, _vp, _vp, _d, _vp, _d, _d, _d],
     "gev_fft_r2c": [_vp, _vp, _vp],
     "gev_fft_c2r": [_vp, _vp, _vp],
+    "gev_fft_c2r_poisson": [_vp, _vp, _vp, _d, _d],
     "gev_fft_axis": [_vp, _vp, _i, _i],
     "gev_solve_poisson": [_vp, _vp, _vp, _d, _d],
     "gev_project_scalar": [_vp, _vp, _vp, _i],
@@ -301,6 +302,12 @@ def fft_r2c(real, spec):
 
 def fft_c2r(spec, real):
     _check(lib().gev_fft_c2r(spec.ctx.handle, spec.handle, real.handle), spec.ctx, "gev_fft_c2r")
+
+
+def fft_c2r_poisson(srcFT, real, coeff, modif=0.0):
+    """solveModifiedPoissonFT then c2r, srcFT kept (the potential spectrum is not written)."""
+    _check(lib().gev_fft_c2r_poisson(srcFT.ctx.handle, srcFT.handle, real.handle, coeff, modif), srcFT.ctx,
+           "gev_fft_c2r_poisson")
 
 
 def fft_axis(spec, axis, sign):

@@ -120,6 +120,10 @@ int gev_prepare_source_scalar(gev_ctx *ctx, const gev_field *phi, const gev_fiel
 int gev_fft_r2c(gev_ctx *ctx, const gev_field *real, gev_field *spectrum);
 /* backward transform; never modifies its input spectrum */
 int gev_fft_c2r(gev_ctx *ctx, const gev_field *spectrum, gev_field *real);
+/* solveModifiedPoissonFT(srcFT, potFT, coeff, modif) then the c2r of potFT (main.cpp:483-488)
+ * without writing potFT: srcFT is kept.  The mixed form on power-of-two grids applies the
+ * Poisson factor inside the transform's first pass; the bits are those of the two calls. */
+int gev_fft_c2r_poisson(gev_ctx *ctx, const gev_field *srcFT, gev_field *real, double coeff, double modif);
 /* one unnormalised 1-D transform of a half spectrum along y (axis 1) or z (axis 2), in place,
  * sign -1 forward / +1 backward: one of the passes of the 3-D transforms above */
 int gev_fft_axis(gev_ctx *ctx, gev_field *spectrum, int axis, int sign);
