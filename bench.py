@@ -200,6 +200,7 @@ def run_ours(args, rank, world, local):
     e1.record(stream)
     e1.synchronize()
     launches = ctx.launches() - l0
+    tiles = ctx.fft_tiles()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
     torch.cuda.synchronize()
@@ -230,7 +231,7 @@ def run_ours(args, rank, world, local):
     serve = None
     if args.serve_seconds > 0 and world == 1:
         serve = run_serve(args, gpu)
-    return dict(value=value, ms=ms_max / args.steps, launches=launches, clocks=clk, state=st, roofline=roof,
+    return dict(value=value, ms=ms_max / args.steps, launches=launches, tiles=tiles, clocks=clk, state=st, roofline=roof,
                 roofline_fft=roof_fft, roofline_pcl=roof_pcl, cufft=cufft, e2e=e2e, e2e2=e2e2, box=box, fp64=fp64,
                 serve=serve)
 
@@ -703,7 +704,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.prec == "fp64" else "f32+f64pos+i64dep",
             "data": "synthetic (device-generated BBKS Zel'dovich IC)", "config": config,
-            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "roofline_particle_update": res["roofline_pcl"], "fft_vs_cufft": res["cufft"], "cpu_baseline": cpu, "e2e": res["e2e"], "e2e_two_sims": res["e2e2"], "gpu_launches": res["launches"],
+            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "roofline_particle_update": res["roofline_pcl"], "fft_vs_cufft": res["cufft"], "fft_tiles": res["tiles"], "cpu_baseline": cpu, "e2e": res["e2e"], "e2e_two_sims": res["e2e2"], "gpu_launches": res["launches"],
             "clocks": res["clocks"], "bytes_per_cycle_alg": cycle_bytes(N, args.prec),
             "final_a": res["state"]["a"]}
     if res.get("fp64"):
