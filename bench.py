@@ -54,6 +54,7 @@ def parse():
     ap.add_argument("--seed", type=int, default=1)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-hbm-fit", action="store_true", help="skip the 1024^3 HBM-fit demonstration")
     ap.add_argument("--no-pk-check", action="store_true", help="skip the FP64-form run and spectrum comparison")
     ap.add_argument("--serve-seconds", type=float, default=20.0,
                     help="length of the serving run's Poisson arrivals (0: no serving measurement)")
@@ -221,9 +222,10 @@ def run_ours(args, rank, world, local):
     e2e = None
     if not args.no_e2e:
         e2e = run_e2e(gpu, ctx, sim, stream, N, args.steps, torch)
+    del sim, ctx, stream  # the measurements below make their own simulations
+    torch.cuda.synchronize()
     fp64 = None
     if pk is not None:
-        del sim, ctx
         fp64 = fp64_form_check(args, gpu, N, box, local, pk, torch)
     e2e2 = None
     if not args.no_e2e and world == 1:
@@ -231,9 +233,12 @@ def run_ours(args, rank, world, local):
     serve = None
     if args.serve_seconds > 0 and world == 1:
         serve = run_serve(args, gpu)
+    hbm = None
+    if not args.no_hbm_fit and world == 1 and prec == gpu.PREC_MIXED and N == 512:
+        hbm = run_hbm_fit(gpu, local, torch)
     return dict(value=value, ms=ms_max / args.steps, launches=launches, tiles=tiles, clocks=clk, state=st, roofline=roof,
                 roofline_fft=roof_fft, roofline_pcl=roof_pcl, cufft=cufft, e2e=e2e, e2e2=e2e2, box=box, fp64=fp64,
-                serve=serve)
+                serve=serve, hbm=hbm)
 
 
 PK_FIELDS = (("phi", 1), ("chi", 1), ("Bi", 3), ("source", 1))
@@ -578,6 +583,39 @@ def run_e2e(gpu, ctx, sim, stream, N, steps, torch):
             "d2h_bytes_per_step": n * 56}
 
 
+def run_hbm_fit(gpu, device, torch, N=1024, steps=2):
+    """The 1024^3 HBM-fit demonstration of the precision form: 1024^3 particles on a
+    1024^3 grid in a 2 Gpc/h box, device initial conditions at z = 100, one warm-up
+    cycle and `steps` timed cycles.  Reports the device bytes the simulation holds
+    against the GPU's memory; a simulation that does not fit is reported, not raised."""
+    free0, total = torch.cuda.mem_get_info(device)
+    out = {"grid": N, "particles": N ** 3, "box_mpc_h": 2000.0, "gpu_bytes": total, "free_bytes_before": free0}
+    try:
+        ctx = gpu.Context(N, gpu.PREC_MIXED, device=device)
+        sim = gpu.Sim(ctx, N ** 3)
+        t0 = time.perf_counter()
+        sim.ic_generate(**gpu.ic_params(2000.0, seed=11))
+        ctx.sync()
+        out["ic_s"] = time.perf_counter() - t0
+        sim.step()
+        ctx.sync()
+        stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", device))
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            sim.step()
+        e1.record(stream)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1) / steps
+        out.update({"fits": True, "device_bytes": ctx.bytes_in_use(), "ms_per_step": ms, "steps": steps,
+                    "particle_steps_per_s": N ** 3 / (ms / 1e3), "a": sim.state()["a"]})
+        del sim, ctx
+    except gpu.GevError as e:
+        out.update({"fits": False, "error": str(e)[:200]})
+    torch.cuda.synchronize()
+    return out
+
+
 def run_e2e_two_sims(gpu, N, steps, box, device, torch):
     """The e2e loop of two independent simulations at once, each driven by its own host
     thread through the same calls (upload from pinned memory, cycle, download into pinned
@@ -704,7 +742,7 @@ def main():
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.prec == "fp64" else "f32+f64pos+i64dep",
             "data": "synthetic (device-generated BBKS Zel'dovich IC)", "config": config,
-            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "roofline_particle_update": res["roofline_pcl"], "fft_vs_cufft": res["cufft"], "fft_tiles": res["tiles"], "cpu_baseline": cpu, "e2e": res["e2e"], "e2e_two_sims": res["e2e2"], "gpu_launches": res["launches"],
+            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "roofline_particle_update": res["roofline_pcl"], "fft_vs_cufft": res["cufft"], "fft_tiles": res["tiles"], "cpu_baseline": cpu, "e2e": res["e2e"], "e2e_two_sims": res["e2e2"], "hbm_fit_1024": res["hbm"], "gpu_launches": res["launches"],
             "clocks": res["clocks"], "bytes_per_cycle_alg": cycle_bytes(N, args.prec),
             "final_a": res["state"]["a"]}
     if res.get("fp64"):

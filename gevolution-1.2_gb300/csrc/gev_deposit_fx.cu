@@ -575,16 +575,21 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   k_fx_scale<<<1, 1, 0, ctx->stream>>>(p->bounds, kind, mass, a);
   GEV_LAUNCH_CHECK(ctx);
   if (gather) {
-    if (!p->prep) {
-      const size_t bytes = (size_t)(p->cap > 0 ? p->cap : 1) * PREP_WORDS * 4;
+    // the records live in the alt array set, which only a relink writes (an allocation
+    // of their own only if that block were too small)
+    const size_t rec_bytes = (size_t)(p->cap > 0 ? p->cap : 1) * PREP_WORDS * 4;
+    void *rec = p->alt.block_bytes >= rec_bytes ? p->alt.block : p->prep;
+    if (!rec) {
+      const size_t bytes = rec_bytes;
       if (cudaMalloc(&p->prep, bytes) != cudaSuccess) {
         cudaGetLastError();
         return gev_fail(ctx, GEV_ENOMEM, "deposit: prefactor scratch allocation failed");
       }
       ctx->bytes_in_use += bytes;
       p->bytes += bytes;
+      rec = p->prep;
     }
-    const PrepArrays pa = prep_arrays(p->prep, p->cap > 0 ? p->cap : 1);
+    const PrepArrays pa = prep_arrays(rec, p->cap > 0 ? p->cap : 1);
     float *t00 = kind == FX_TIJ ? nullptr : (float *)out->d;
     float *tij = kind == FX_TIJ ? (float *)out->d : (out2 ? (float *)out2->d : nullptr);
     const int pb = grid_for(ctx, (size_t)p->n, 256, 16);

@@ -87,6 +87,11 @@ struct PclsArrays {
   // offset from it, and the kick and the deposits read only the offset, so they
   // issue no FP64 instructions (GB300 runs FP64 at 1/64 of the FP32 rate).
   float *rx = nullptr, *ry = nullptr, *rz = nullptr;
+  // one allocation holds all the arrays of a set; the store's second set (alt) is
+  // written only by a relink, so between relinks the mixed-form deposit keeps its
+  // per-particle prefactor records there
+  void *block = nullptr;
+  size_t block_bytes = 0;
 };
 
 struct gev_pcls {
@@ -108,8 +113,8 @@ struct gev_pcls {
   // deposit's groups, [5..8] their prefactor and weight-factor powers; [15] set by an
   // upload whose particles are not in (cell, ID) order
   uint32_t *bounds = nullptr;
-  // mixed-form T00 / Tij deposit: per-particle prefactor records (12 words a particle,
-  // allocated on first use)
+  // mixed-form T00 / Tij deposit: per-particle prefactor records (12 words a particle),
+  // kept in the alt array set's block; an allocation of its own only if that is smaller
   void *prep = nullptr;
   size_t bytes = 0;  // device bytes this store counts in its context's bytes_in_use
 };

@@ -873,37 +873,39 @@ size_t vbytes() {
   return sizeof(V);
 }
 
+// the arrays of one set carved from one allocation, each on a 256-byte boundary
 int alloc_arrays(gev_ctx *ctx, PclsArrays &A, long cap, size_t vsz) {
   const size_t n = (size_t)cap;
-  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.px, n * 8));
-  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.py, n * 8));
-  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.pz, n * 8));
-  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.vx, n * vsz));
-  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.vy, n * vsz));
-  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.vz, n * vsz));
-  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.id, n * 8));
-  GEV_CHECK_CUDA(ctx, cudaMalloc(&A.cell, n * 4));
-  ctx->bytes_in_use += n * (8 * 4 + 4 + 3 * vsz);
-  if (vsz == 4) {  // mixed form: FP32 in-cell offsets
-    GEV_CHECK_CUDA(ctx, cudaMalloc(&A.rx, n * 4));
-    GEV_CHECK_CUDA(ctx, cudaMalloc(&A.ry, n * 4));
-    GEV_CHECK_CUDA(ctx, cudaMalloc(&A.rz, n * 4));
-    ctx->bytes_in_use += n * 12;
+  const bool mixed = vsz == 4;  // mixed form: FP32 in-cell offsets too
+  const size_t sizes[11] = {n * 8, n * 8, n * 8, n * vsz, n * vsz, n * vsz, n * 8, n * 4,
+                            mixed ? n * 4 : 0, mixed ? n * 4 : 0, mixed ? n * 4 : 0};
+  size_t off[11], total = 0;
+  for (int k = 0; k < 11; ++k) {
+    off[k] = total;
+    total += (sizes[k] + 255) & ~(size_t)255;
   }
+  char *b = nullptr;
+  GEV_CHECK_CUDA(ctx, cudaMalloc(&b, total));
+  A.block = b;
+  A.block_bytes = total;
+  A.px = (double *)(b + off[0]);
+  A.py = (double *)(b + off[1]);
+  A.pz = (double *)(b + off[2]);
+  A.vx = b + off[3];
+  A.vy = b + off[4];
+  A.vz = b + off[5];
+  A.id = (int64_t *)(b + off[6]);
+  A.cell = (uint32_t *)(b + off[7]);
+  if (mixed) {
+    A.rx = (float *)(b + off[8]);
+    A.ry = (float *)(b + off[9]);
+    A.rz = (float *)(b + off[10]);
+  }
+  ctx->bytes_in_use += total;
   return GEV_OK;
 }
 void free_arrays(PclsArrays &A) {
-  cudaFree(A.px);
-  cudaFree(A.py);
-  cudaFree(A.pz);
-  cudaFree(A.vx);
-  cudaFree(A.vy);
-  cudaFree(A.vz);
-  cudaFree(A.id);
-  cudaFree(A.cell);
-  cudaFree(A.rx);
-  cudaFree(A.ry);
-  cudaFree(A.rz);
+  cudaFree(A.block);
   A = PclsArrays();
 }
 
