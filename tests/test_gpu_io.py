@@ -257,7 +257,7 @@ def pinned(gpu, n):
 
 
 @pytest.mark.parametrize("prec", [0, 1])
-@pytest.mark.parametrize("n", [1, 255, 257, 4097])
+@pytest.mark.parametrize("n", [0, 1, 255, 257, 4097])
 def test_pinned_upload_download_match_pageable(gpu, prec, n):
     """Upload and download through pinned memory (the kernels read and write the host
     buffer directly) give the same bits as through pageable memory (a device staging
