@@ -2,33 +2,50 @@
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--grid 512] [--prec mixed|fp64]
+    python bench.py --op NAME [--grid N] ...      one operation, for profiler captures
 
 Workload (default): the precision form at 512^3 grid and 512^3 particles in a
 1 Gpc/h box (FP32 fields and FFTs, FP64 positions, int64 fixed-point
 deposits), seeded BBKS Zel'dovich initial conditions at z = 100 generated on
 the device, GR mode with phi, chi, B_i and T_ij active (parabolic vector
-method).  A step is one cycle of gevolution's main loop (main.cpp:372-879):
-the three deposits, the phi / chi / B solves with 12 FFTs, the kick, the drift
-with the relink, and the background update.  Metric: particle-steps/s.
+method), run to z = 0 as gevolution's main loop runs it (main.cpp:372-879; the
+loop ends at the first cycle whose a has passed 1, main.cpp:639-692).  A step
+is one cycle: the T00 and Tij deposits, the phi / chi / B solves with 12 FFTs,
+the kick, the drift with the relink and the background update.  Metric:
+particle-steps/s.
 
-value    device-timed throughput with the state resident in HBM (CUDA events on
-         the library's stream, K cycles between two synchronised barriers);
-e2e      the same cycles through the C-ABI with the particle state copied in
-         from pinned host memory and back out every step;
-roofline the dominant kernel's algorithmic bytes per launch over its event-
-         timed duration, against the measured HBM copy bandwidth;
-cpu_baseline  the CPU restatement of the same path (oracle/) timed on this
-         host on a bounded sample (rank 0, N = 1 only).
+value        device-timed throughput with the state resident in HBM: the LAST K
+             cycles before z = 0 (clustered particles), after untimed evolution
+             from z = 100; CUDA events on the library's stream between two
+             synchronised barriers.  full_run gives the mean over every cycle of
+             the run, early_cycles the first K.
+e2e          the same K cycles through the C-ABI with the particle state copied
+             in from pinned host memory and back out every cycle.
+kernels      each kernel's device time in the timed cycles (CUDA events the
+             library records around its launches, gev_ctx_set_timing), its
+             algorithmic bytes and fraction of the measured HBM bandwidth;
+             roofline is the largest of them.
+phases_gpu / cpu_baseline.phases   time per cycle in the layout of main.cpp's
+             BENCHMARK breakdown (main.cpp:907-922).
+pk_check     the precision form against the plain FP64 form from the same seeded
+             IC, z = 100 -> 0: per-bin power deviation of phi, chi, B and delta at
+             every Pk redshift up to k_Nyquist / 2 (criterion 1e-3), the rms
+             difference of the final positions (particles matched by ID), and the
+             FP64 form's throughput over the same cycles.
+cpu_baseline the CPU restatement of the path (oracle/, FP64, OpenMP on all host
+             threads) on a bounded sample of the workload: a 256^3 simulation in
+             a 500 Mpc/h box (the 512^3 run's cell size and particle density).
 
---impl reference runs the CPU implementation of the path (the oracle's port of
-the reference; the reference itself needs LATfield2, FFTW, MPI and HDF5, which
-the GPU hosts do not have) on all host cores, one independent simulation per
-core, and prints the same metric.  With --gpus N > 1 each rank runs its own
+--impl reference runs that CPU implementation of the path alone (the oracle's
+port of the reference; the reference itself needs LATfield2, FFTW, MPI and
+HDF5, which the GPU hosts do not have), one cycle of the 256^3 sample per step,
+and prints the same metric.  With --gpus N > 1 each rank runs its own
 simulation (replicas, no data exchange); the value is the sum over ranks of
 particles x steps divided by the slowest rank's time.
 """
 import argparse
 import json
+import math
 import os
 import subprocess
 import sys
@@ -41,6 +58,9 @@ sys.path.insert(0, os.path.join(ROOT, "oracle"))
 
 PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 FALLBACK_HBM_GBS = 6800.0
+PK_REDSHIFTS = (10.0, 3.0, 1.0, 0.5, 0.0)
+PK_BINS = 64
+CPU_SAMPLE_GRID, CPU_SAMPLE_BOX = 256, 500.0
 
 
 def parse():
@@ -56,10 +76,18 @@ def parse():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-hbm-fit", action="store_true", help="skip the 1024^3 HBM-fit demonstration")
     ap.add_argument("--no-pk-check", action="store_true", help="skip the FP64-form run and spectrum comparison")
-    ap.add_argument("--serve-seconds", type=float, default=20.0,
+    ap.add_argument("--serve-seconds", type=float, default=120.0,
                     help="length of the serving run's Poisson arrivals (0: no serving measurement)")
     ap.add_argument("--serve-rate", type=float, default=2.0, help="serving requests per second")
     ap.add_argument("--serve-burst", type=int, default=24, help="requests submitted at once for the capacity run")
+    ap.add_argument("--op", default=None,
+                    help="one operation instead of the benchmark: prepare, cycle, table, r2c_alone, c2r_alone, "
+                         "fft_axis_y, fft_axis_z")
+    ap.add_argument("--reps", type=int, default=3, help="--op: timed calls")
+    ap.add_argument("--z-op", type=float, default=0.0,
+                    help="--op prepare / table: evolve from z = 100 until this redshift first")
+    ap.add_argument("--state", default=None,
+                    help="--op prepare: hibernation file to write; cycle / table: to restart from")
     return ap.parse_args()
 
 
@@ -85,6 +113,11 @@ def dist_env():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     return rank, world, local
+
+
+def replica_seed(base, rank):
+    """The seed of rank `rank`'s replica: every rank runs an independent simulation."""
+    return base + 1000 * rank
 
 
 # ------------------------------------------------------------ clocks --------
@@ -149,28 +182,93 @@ def hbm_peak():
         return FALLBACK_HBM_GBS, "fallback"
 
 
+# ------------------------------------------------- the cycle schedule --------
+def _hconf(a, fourpiG, c):
+    # background.hpp:137-140 without ncdm and fluid terms, as the library's host code
+    return math.sqrt((2. * fourpiG / 3.) * (((c["Omega_cdm"] + c["Omega_b"]) / a) + (c["Omega_Lambda"] * a * a) +
+                                            (c["Omega_rad"] / a / a)))
+
+
+def _rk4bg(a, fourpiG, c, dtau):
+    # background.hpp:167-177
+    k1 = a * _hconf(a, fourpiG, c)
+    k2 = (a + k1 * dtau / 2.) * _hconf(a + k1 * dtau / 2., fourpiG, c)
+    k3 = (a + k2 * dtau / 2.) * _hconf(a + k2 * dtau / 2., fourpiG, c)
+    k4 = (a + k3 * dtau) * _hconf(a + k3 * dtau, fourpiG, c)
+    return a + dtau * (k1 + 2. * k2 + 2. * k3 + k4) / 6.
+
+
+def full_cycles_to(st, N, z_end=0.0):
+    """Cycles the main loop completes before it ends at z_end: a(tau) and dtau follow
+    from the background alone (main.cpp:792-872), so the count is known up front.
+    The loop ends in the fields part of the first cycle whose a has passed 1/(1+z_end)."""
+    a, dtau = st["a"], st["dtau"]
+    dx = 1.0 / N
+    n = 0
+    while not (1.0 / a < z_end + 1.0):
+        a = _rk4bg(_rk4bg(a, st["fourpiG"], st["cosmo"], 0.5 * dtau), st["fourpiG"], st["cosmo"], 0.5 * dtau)
+        H = _hconf(a, st["fourpiG"], st["cosmo"])
+        dtau = st["Cf"] * dx if st["Cf"] * dx < st["steplimit"] / H else st["steplimit"] / H
+        n += 1
+    return n
+
+
 # ------------------------------------------------- algorithmic bytes --------
 def cycle_bytes(N, prec):
-    """Compulsory HBM bytes of one cycle: every persistent or intermediate array
-    read or written once per use, FFTs at three passes (one read and one write of
-    the array per pass).  Particles: deposit reads pos+vel, kick/drift read pos+vel
-    and write them back."""
+    """Compulsory HBM bytes of one cycle (every persistent or intermediate array read
+    or written once per use, each 3-D FFT at its three-pass minimum), with r the real
+    size of the form and a half-spectrum component of about r bytes a cell:
+      particles: the deposit reads pos + q, the kick+drift reads and writes them
+                 (ID, cell keys and the relink excluded): 3 (3*8 + 3*r) a particle;
+      fields a cell: T00 + 6 Tij written 7r; phi read by the deposit r; scalar solve
+                 3r read, half spectrum r, z pass with the Poisson factor 2r, c2r 2r;
+                 tensor: phi + Sij read 7r, SijFT 6r, the k-space pass reads 6r + 3r
+                 and writes r + 3r, the c2r reads 4r and writes 4r; the kick+drift
+                 reads phi, chi and B 5r.
+    Mixed form (r = 4): 108 B a particle + 220 B a cell = 328 B a particle-step.
+    FP64 form (r = 8): 144 + 440 = 584 (the same terms; the 544 often quoted for it
+    leaves out the kick's field reads)."""
     r = 8 if prec == "fp64" else 4
-    V = N ** 3
-    K = N * N * (N // 2 + 1) * 2 * r  # bytes of one half spectrum component
-    pcl_state = 3 * 8 + 3 * r
-    particles = V * (pcl_state + 2 * pcl_state)
-    fields = 0
-    fields += V * r * (1 + 6)          # T00 and Tij written by the deposits
-    fields += V * r * 1                # phi read by the deposits
-    fields += V * r * 3 + V * r        # prepareFTsource (scalar): phi, chi, source in, source out
-    fields += 12 * 3 * 2 * K           # 12 FFTs x 3 passes x (read + write) of one component
-    fields += K * 2                    # Poisson in place
-    fields += V * r * 7 + V * r * 6    # prepareFTsource (tensor): phi + Sij in, Sij out
-    fields += 6 * K + K                # projectFTscalar
-    fields += 6 * K + 2 * 3 * K        # evolveFTvector (Sij in, B in/out)
-    fields += V * r * (1 + 1 + 3)      # kick/drift gather phi, chi, Bi
-    return particles + fields
+    per_particle = 3 * (3 * 8 + 3 * r)
+    per_cell = r * (7 + 1 + (3 + 1 + 2 + 2) + (7 + 6 + 9 + 4 + 8) + 5)
+    return (per_particle + per_cell) * N ** 3, per_particle, per_cell
+
+
+def kernel_alg_bytes(name, N, prec, n=None):
+    """Algorithmic bytes of one launch of a kernel of the cycle (the terms of
+    cycle_bytes that the kernel covers); None for bookkeeping kernels (the relink,
+    scales, sums), which move no bytes the path itself requires."""
+    r = 8 if prec == "fp64" else 4
+    C = N ** 3
+    n = C if n is None else n
+    K = N * N * (N // 2 + 1) * 2 * r  # one half-spectrum component
+    table = {
+        "k_kick_drift": n * 2 * (3 * 8 + 3 * r) + C * 5 * r,
+        "k_dep_gather": n * (3 * 8 + 3 * r) + C * 8 * r,
+        "k_cube_fp64+k_gather": n * (3 * 8 + 3 * r) + C * 8 * r,
+        "k_fft_cols_reg": 2 * K,
+        "k_fft_cols": 2 * K,
+        "k_fft_r2c_rows_reg": C * r + K,
+        "k_fft_r2c_rows": C * r + K,
+        "k_fft_c2r_rows_reg": C * r + K,
+        "k_fft_c2r_rows": C * r + K,
+        "k_source_tensor": C * 13 * r,
+        "k_source_scalar": C * 4 * r,
+        "k_project_evolve": 13 * K,
+        "k_poisson": 2 * K,
+    }
+    return table.get(name)
+
+
+# DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
+# captures of the kernels at late time (the state near z = 0 restarted from a
+# hibernation file: bench.py --op cycle), keyed by (kernel, grid, precision).
+KERNEL_TRAFFIC = {}
+
+
+# ------------------------------------------------------------ our arm --------
+def _events(torch, n):
+    return [torch.cuda.Event(enable_timing=True) for _ in range(n)]
 
 
 def run_ours(args, rank, world, local):
@@ -181,52 +279,65 @@ def run_ours(args, rank, world, local):
     N = args.grid
     prec = gpu.PREC_FP64 if args.prec == "fp64" else gpu.PREC_MIXED
     box = 1000.0 * N / 512
+    seed = replica_seed(args.seed, rank)
     ctx = gpu.Context(N, prec, device=local)
     sim = gpu.Sim(ctx, N ** 3)
-    sim.ic_generate(**gpu.ic_params(box, seed=args.seed + 1000 * rank))
+    sim.ic_generate(**gpu.ic_params(box, seed=seed))
+    st0 = sim.state()
+    n_full = full_cycles_to(st0, N)
+    K = args.steps
+    n_pre = max(n_full - K, args.warmup)
     stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
-    for _ in range(args.warmup):
+    # untimed evolution from z = 100, one event after every cycle for the full-run mean
+    ev = _events(torch, n_pre + 1)
+    ev[0].record(stream)
+    for c in range(n_pre):
         sim.step()
+        ev[c + 1].record(stream)
     ctx.sync()
+    a_start = sim.state()["a"]
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     clocks = ClockSampler(local)
     clocks.start()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ctx.timing(reset=True)
+    ctx.set_timing(True)
+    e0, e1 = _events(torch, 2)
     l0 = ctx.launches()
     e0.record(stream)
-    for _ in range(args.steps):
+    for _ in range(K):
         sim.step()
     e1.record(stream)
     e1.synchronize()
     launches = ctx.launches() - l0
-    tiles = ctx.fft_tiles()
     ms = e0.elapsed_time(e1)
     clk = clocks.stop()
+    ctx.set_timing(False)
+    kt = ctx.timing(reset=True)
     torch.cuda.synchronize()
     ms_max = reduce_max_ms(ms, world, "cuda")
-    value = aggregate_value(N, args.steps, world, ms_max)
+    value = aggregate_value(N, K, world, ms_max)
     st = sim.state()
-    pk = None
-    if not args.no_pk_check and prec == gpu.PREC_MIXED and world == 1:
-        pk = spectra_of(gpu, ctx, sim)
-
-    # roofline of the dominant kernel (the T00 + Tij deposit) and of the FFT column pass
-    roof = deposit_roofline(gpu, ctx, sim, stream, N, args.prec)
-    roof_fft = dominant_kernel_roofline(gpu, ctx, sim, stream, N, args.prec)
-    roof_pcl = particle_update_roofline(gpu, ctx, sim, stream, N, args.prec)
+    pre_ms = ev[0].elapsed_time(ev[-1])
+    k_early = min(K, n_pre)
+    full = {"cycles": n_pre + K, "ms_per_step": (pre_ms + ms) / (n_pre + K),
+            "value": N ** 3 * (n_pre + K) / ((pre_ms + ms) / 1e3), "z_end": 1.0 / st["a"] - 1.0}
+    early = {"cycles": "0..%d" % (k_early - 1), "ms_per_step": ev[0].elapsed_time(ev[k_early]) / k_early}
+    early["value"] = N ** 3 / (early["ms_per_step"] / 1e3)
+    kernels, phases, roof = kernel_table(kt, K, ms / K, N, args.prec)
+    tiles = ctx.fft_tiles()
+    timed = {"first": n_pre, "last": n_pre + K - 1, "of": n_full, "z_from": 1.0 / a_start - 1.0,
+             "z_to": 1.0 / st["a"] - 1.0}
     cufft = fft_vs_cufft(gpu, ctx, stream, N, args.prec, torch) if world == 1 else None
-
-    # e2e: particle state from pinned host memory in, cycle, particle state out
+    del sim, ctx, stream
+    torch.cuda.synchronize()
     e2e = None
     if not args.no_e2e:
-        e2e = run_e2e(gpu, ctx, sim, stream, N, args.steps, torch)
-    del sim, ctx, stream  # the measurements below make their own simulations
-    torch.cuda.synchronize()
-    fp64 = None
-    if pk is not None:
-        fp64 = fp64_form_check(args, gpu, N, box, local, pk, torch)
+        e2e = run_e2e(gpu, N, prec, box, seed, n_pre, K, local, torch)
+    pk = None
+    if not args.no_pk_check and prec == gpu.PREC_MIXED and world == 1:
+        pk = pk_check_z0(gpu, N, box, args.seed, K, local, torch)
     e2e2 = None
     if not args.no_e2e and world == 1:
         e2e2 = run_e2e_two_sims(gpu, N, args.steps, box, local, torch)
@@ -236,171 +347,47 @@ def run_ours(args, rank, world, local):
     hbm = None
     if not args.no_hbm_fit and world == 1 and prec == gpu.PREC_MIXED and N == 512:
         hbm = run_hbm_fit(gpu, local, torch)
-    return dict(value=value, ms=ms_max / args.steps, launches=launches, tiles=tiles, clocks=clk, state=st, roofline=roof,
-                roofline_fft=roof_fft, roofline_pcl=roof_pcl, cufft=cufft, e2e=e2e, e2e2=e2e2, box=box, fp64=fp64,
-                serve=serve, hbm=hbm)
+    return dict(value=value, ms=ms_max / K, launches=launches, tiles=tiles, clocks=clk, state=st, roofline=roof,
+                kernels=kernels, phases=phases, full=full, early=early, timed=timed, cufft=cufft, e2e=e2e, e2e2=e2e2,
+                box=box, pk=pk, serve=serve, hbm=hbm)
 
 
-PK_FIELDS = (("phi", 1), ("chi", 1), ("Bi", 3), ("source", 1))
-PK_BINS = 64
+PHASE_KEYS = (("projections", "phase:projections"), ("gravity solver", "phase:gravity solver"),
+              ("thereof FFTs", "phase:fft"), ("update momenta + move particles (one fused pass with the relink)",
+                                               "phase:update particles"))
 
 
-def spectra_of(gpu, ctx, sim):
-    """Power spectra (device FFT + gev_cross_spectrum) of phi, chi, B_i and the
-    source field of a simulation."""
-    out = {}
-    for name, nc in PK_FIELDS:
-        sp = ctx.spectrum(nc)
-        gpu.fft_r2c(sim.field(name), sp)
-        out[name] = gpu.cross_spectrum(sp, numbins=PK_BINS)
-        del sp
-    return out
-
-
-def fp64_form_check(args, gpu, N, box, local, pk_mixed, torch):
-    """The plain FP64 form from the same initial conditions for the same cycles:
-    its device-timed throughput, and the largest per-bin relative deviation of the
-    mixed form's power spectra from it up to k_Nyquist / 2 (criterion 1e-3)."""
-    import numpy as np
-    ctx = gpu.Context(N, gpu.PREC_FP64, device=local)
-    sim = gpu.Sim(ctx, N ** 3)
-    sim.ic_generate(**gpu.ic_params(box, seed=args.seed))
-    stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", local))
-    for _ in range(args.warmup):
-        sim.step()
-    ctx.sync()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        sim.step()
-    e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1)
-    pk64 = spectra_of(gpu, ctx, sim)
-    dev = {}
-    for name, _ in PK_FIELDS:
-        kb, p64, _, _, occ = pk64[name]
-        p32 = pk_mixed[name][1]
-        m = (occ > 0) & (kb <= 0.5 * np.pi * N)
-        dev[name] = float(np.max(np.abs(p32[m] - p64[m]) / np.maximum(np.abs(p64[m]), 1e-300)))
-    return {"fp64_form": {"value": N ** 3 * args.steps / (ms / 1e3), "unit": "particle-steps/s",
-                          "ms_per_step": ms / args.steps},
-            "pk_check": {"against": "the FP64 form on the GPU, same initial conditions, %d cycles"
-                         % (args.warmup + args.steps), "numbins": PK_BINS, "k_max": "k_Nyquist/2",
-                         "max_rel_dev": dev, "tolerance": 1e-3, "pass": all(v <= 1e-3 for v in dev.values())}}
-
-
-# DRAM traffic per launch of the column pass (dram__bytes_read.sum +
-# dram__bytes_write.sum) from an ncu capture of the same kernel on one 512^3
-# spectrum component (gevolution-1.2_gb300/opbench.py --only fft_axis_z), keyed by
-# (grid, precision): 556.2 MB read + 511.3 MB written
-COLS_TRAFFIC = {(512, "mixed"): 1.0675e9}
-
-
-# DRAM traffic per call of the T00 + Tij deposit: its prefactor pass (k_fx_prep) and
-# its gather (k_dep_gather), from an ncu capture of the same kernels on the 256^3
-# cycle (opbench --grid 256 --only step), scaled by 8 to 512^3: particles and fields
-# both grow as N^3.  k_fx_prep 403.9 MB read + 746.9 MB written, k_dep_gather
-# 1410.0 MB read + 502.4 MB written; (3063.2 MB) x 8
-DEPOSIT_TRAFFIC = {(512, "mixed"): 24.506e9}
-
-
-def deposit_roofline(gpu, ctx, sim, stream, N, prec):
-    """The largest kernel of the cycle in the ncu launch list: the deposit of T00 and
-    Tij in one call (projection_init + projection_T00 + projection_Tij), timed with
-    its scale pass and its prefactor pass.  Its algorithmic bytes per call: each
-    particle's cell, in-cell offset and momentum read once (4 + 3r + 3r bytes), phi
-    read once and the 7 target components written once per cell (8 r bytes), r the
-    real size of the form.  The prefactor records the gather writes and reads back
-    (48 B a particle) are not algorithmic and show in the traffic."""
-    import torch
-    r = 8 if prec == "fp64" else 4
-    p, src, Sij, phi = sim.particles(), sim.field("source"), sim.field("Sij"), sim.field("phi")
-    a = sim.state()["a"]
-    reps = 4
-    gpu.projection_T00_Tij(p, src, Sij, a, phi)
-    ctx.sync()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(reps):
-        gpu.projection_T00_Tij(p, src, Sij, a, phi)
-    e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    n = C = N ** 3
-    alg = n * (4 + 6 * r) + C * 8 * r
+def kernel_table(kt, cycles, ms_cycle, N, prec):
+    """Per-kernel device time of the timed cycles with its algorithmic bytes and HBM
+    fraction; the per-phase breakdown; the roofline object of the largest kernel."""
     peak, kind = hbm_peak()
-    achieved = alg / (ms / 1e3) / 1e9
-    return {"kernel": "k_fx_prep + k_dep_gather<T00+Tij> (the T00 and Tij deposits in one gather; timed with the "
-                      "scale pass)",
-            "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": DEPOSIT_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
-
-
-def dominant_kernel_roofline(gpu, ctx, sim, stream, N, prec):
-    """The FFT column pass (k_fft_cols_reg, the y / z passes of every transform; 24
-    launches a cycle, the largest kernel family by count).  One launch transforms one
-    spectrum component along y or z in place: its algorithmic bytes are one read
-    and one write of the component, 2 * N^2 (N/2+1) * sizeof(complex)."""
-    import torch
-    csz = 16 if prec == "fp64" else 8
-    spec = sim.field("scalarFT")
-    reps = 6
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    gpu.fft_axis(spec, 1, -1)
-    ctx.sync()
-    e0.record(stream)
-    for i in range(reps):
-        gpu.fft_axis(spec, 1 + (i & 1), -1)
-    e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    alg = 2 * N * N * (N // 2 + 1) * csz
-    peak, kind = hbm_peak()
-    achieved = alg / (ms / 1e3) / 1e9
-    return {"kernel": "k_fft_cols_reg (one y or z pass of the 3-D FFT over one spectrum component)", "bound": "hbm",
-            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": COLS_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
-
-
-# DRAM traffic per call of the particle update: k_kick_drift and k_move from an ncu
-# capture of the 256^3 cycle (opbench --grid 256 --only step), scaled by 8 to 512^3.
-# k_kick_drift 1624.8 MB read + 973.8 MB written, k_move 1140.9 MB read + 958.6 MB
-# written; (4698.1 MB) x 8.  The scan's three kernels (about 1 GB at 512^3) are not in it.
-PARTICLE_TRAFFIC = {(512, "mixed"): 37.585e9}
-
-
-def particle_update_roofline(gpu, ctx, sim, stream, N, prec):
-    """The cycle's particle update, whose kick+drift kernel is the largest single kernel
-    of the launch list: gev_update_q_pos (updateVel + moveParticles with the relink),
-    kick+drift+histogram, scan and move in one call, timed with CUDA events.  Its
-    algorithmic bytes per call: kick+drift reads each particle's cell, offset, momentum
-    and position and writes them back with its rank (52 + 56 B in the mixed form), and
-    reads phi, chi and B once per cell (20 B); the scan reads the counts and writes the
-    starts (8 B a cell); the move reads and writes the payload with its rank and start
-    (128 B a particle).  The particles move by about 1e-9 of a cell per call here."""
-    import torch
-    r = 8 if prec == "fp64" else 4
-    p, phi, chi, Bi = sim.particles(), sim.field("phi"), sim.field("chi"), sim.field("Bi")
-    a = sim.state()["a"]
-    reps = 4
-    gpu.update_q_pos(p, 1e-9, a, 3, 1e-9, a, 3, phi, chi, Bi, wait=False)
-    ctx.sync()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(reps):
-        gpu.update_q_pos(p, 1e-9, a, 3, 1e-9, a, 3, phi, chi, Bi, wait=False)
-    e1.record(stream)
-    e1.synchronize()
-    ms = e0.elapsed_time(e1) / reps
-    n = C = N ** 3
-    payload = 3 * 8 + 3 * r + 4 + (3 * 4 if r == 4 else 0)  # pos, q, cell, FP32 offset
-    alg = n * (2 * payload + 4) + C * 5 * r + C * 8 + n * (2 * (payload + 8) + 4)
-    peak, kind = hbm_peak()
-    achieved = alg / (ms / 1e3) / 1e9
-    return {"kernel": "k_kick_drift + k_scan_* + k_move (gev_update_q_pos: kick, drift, relink)", "bound": "hbm",
-            "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": PARTICLE_TRAFFIC.get((N, prec)), "peak_kind": kind, "ms_per_launch": ms, "alg_bytes": alg}
+    rows = {}
+    for name, (cnt, tot) in kt.items():
+        if name.startswith("phase:"):
+            continue
+        alg = kernel_alg_bytes(name, N, prec)
+        per = tot / cnt
+        row = {"launches_per_step": cnt / cycles, "ms_per_step": tot / cycles, "share": tot / cycles / ms_cycle,
+               "ms_per_launch": per}
+        if alg:
+            row["alg_bytes_per_launch"] = alg
+            row["achieved_gbs"] = alg / (per / 1e3) / 1e9
+            row["frac"] = row["achieved_gbs"] / peak
+        rows[name] = row
+    phases = {label: kt[key][1] / cycles for label, key in PHASE_KEYS if key in kt}
+    top = max(rows, key=lambda k: rows[k]["ms_per_step"]) if rows else None
+    roof = None
+    if top:
+        r = rows[top]
+        alg = kernel_alg_bytes(top, N, prec)
+        achieved = alg / (r["ms_per_launch"] / 1e3) / 1e9 if alg else None
+        traffic = KERNEL_TRAFFIC.get((top, N, prec))
+        roof = {"kernel": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak if achieved else None, "traffic": traffic, "peak_kind": kind,
+                "ms_per_launch": r["ms_per_launch"], "alg_bytes": alg,
+                "share_of_cycle": r["share"],
+                "timing": "CUDA events around each launch on the library's stream, over the timed cycles"}
+    return rows, phases, roof
 
 
 def fft_vs_cufft(gpu, ctx, stream, N, prec, torch, reps=5):
@@ -417,7 +404,7 @@ def fft_vs_cufft(gpu, ctx, stream, N, prec, torch, reps=5):
     def timed(fn, st):
         fn()
         torch.cuda.synchronize()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0, e1 = _events(torch, 2)
         e0.record(st)
         for _ in range(reps):
             fn()
@@ -440,12 +427,152 @@ def fft_vs_cufft(gpu, ctx, stream, N, prec, torch, reps=5):
             "cufft_c2r_ms": cu_c2r, "library": "cuFFT via torch.fft (torch %s)" % torch.__version__}
 
 
+def run_e2e(gpu, N, prec, box, seed, n_pre, K, device, torch):
+    """The timed cycles again through the public C-ABI with host buffers: a fresh
+    simulation from the same IC evolves untimed to the same cycle, then each of the
+    K cycles uploads the particle records from pinned host memory, runs the cycle
+    and downloads the records into pinned host memory (waiting for them)."""
+    ctx = gpu.Context(N, prec, device=device)
+    sim = gpu.Sim(ctx, N ** 3)
+    sim.ic_generate(**gpu.ic_params(box, seed=seed))
+    for _ in range(n_pre):
+        sim.step()
+    pcls = sim.particles()
+    n = N ** 3
+    host = torch.empty(n * 56, dtype=torch.uint8, pin_memory=True)
+    arr = host.numpy().view(gpu.PART)
+    back = torch.empty(n * 56, dtype=torch.uint8, pin_memory=True)
+    barr = back.numpy().view(gpu.PART)
+    pcls.download(out=arr)
+    ctx.sync()
+    t0 = time.perf_counter()
+    for _ in range(K):
+        pcls.upload(arr)
+        sim.step()
+        pcls.download(out=barr)  # into pinned memory; synchronises the stream
+        arr, barr = barr, arr
+    dt = time.perf_counter() - t0
+    del sim, ctx, host, back
+    torch.cuda.synchronize()
+    return {"value": n * K / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 56,
+            "d2h_bytes_per_step": n * 56, "cycles": "the same late cycles as value, host wall clock"}
+
+
+def _spectra(gpu, ctx, sim, nb):
+    """The parity tables of writeSpectra (output.hpp:1762-2204, CDM in GR): phi and chi
+    (r2c, no deconvolution), B (BiFT), delta (projection_T00_project with phi, r2c,
+    CIC deconvolution)."""
+    st = sim.state()
+    out = {}
+    for name in ("phi", "chi"):
+        sp = ctx.spectrum(1)
+        gpu.fft_r2c(sim.field(name), sp)
+        out[name] = gpu.cross_spectrum(sp, numbins=nb, deconvolve=False)
+    out["B"] = gpu.cross_spectrum(sim.field("BiFT"), numbins=nb, deconvolve=False)
+    T = ctx.real(1)
+    gpu.projection_T00(sim.particles(), T, st["a"], sim.field("phi"))
+    sp = ctx.spectrum(1)
+    gpu.fft_r2c(T, sp)
+    out["delta"] = gpu.cross_spectrum(sp, numbins=nb, deconvolve=True)
+    return out
+
+
+def run_to_z0_with_spectra(gpu, ctx, sim, stream, torch, nb=PK_BINS):
+    """gevolution's loop to z = 0 with the spectra where main.cpp takes them
+    (main.cpp:639-692): after the field solves of the first cycle past each Pk
+    redshift; ends after the last.  Returns (records, device ms of each full cycle,
+    spectra excluded)."""
+    out, cyc_ms = [], []
+    k = 0
+    while True:
+        e = _events(torch, 4)
+        e[0].record(stream)
+        sim.step_fields()
+        e[1].record(stream)
+        a = sim.state()["a"]
+        if 1.0 / a < PK_REDSHIFTS[k] + 1.0:
+            rec = {"z": PK_REDSHIFTS[k], "a": a}
+            rec.update(_spectra(gpu, ctx, sim, nb))
+            out.append(rec)
+            k += 1
+            if k == len(PK_REDSHIFTS):
+                return out, cyc_ms
+        e[2].record(stream)
+        sim.step_particles()
+        e[3].record(stream)
+        e[3].synchronize()
+        cyc_ms.append(e[0].elapsed_time(e[1]) + e[2].elapsed_time(e[3]))
+
+
+def _by_id(gpu, sim, n):
+    import numpy as np
+    p = sim.particles().download()
+    pos = np.empty((n, 3))
+    pos[p["ID"]] = p["pos"]
+    return pos
+
+
+def pk_check_z0(gpu, N, box, seed, K, device, torch):
+    """The precision form against the plain FP64 form, both from device IC of the same
+    seed at z = 100, run to z = 0: per-bin power deviations up to k_Nyquist / 2 at every
+    Pk redshift, the rms difference of the final positions (particles matched by ID),
+    and both forms' device-timed throughput over the last K cycles and the whole run."""
+    import numpy as np
+    runs = {}
+    for name, prec in (("mixed", gpu.PREC_MIXED), ("fp64", gpu.PREC_FP64)):
+        ctx = gpu.Context(N, prec, device=device)
+        sim = gpu.Sim(ctx, N ** 3)
+        sim.ic_generate(**gpu.ic_params(box, seed=seed))
+        pos0 = _by_id(gpu, sim, N ** 3) if name == "fp64" else None
+        stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", device))
+        recs, cyc = run_to_z0_with_spectra(gpu, ctx, sim, stream, torch)
+        pos = _by_id(gpu, sim, N ** 3)
+        runs[name] = (recs, cyc, pos, pos0)
+        del sim, ctx, stream
+        torch.cuda.synchronize()
+    (r32, c32, p32, _), (r64, c64, p64, p0) = runs["mixed"], runs["fp64"]
+    kmax = 0.5 * np.pi * N
+    dev, ok = {}, True
+    for a, b in zip(r32, r64):
+        row = {}
+        for name in ("phi", "chi", "B", "delta"):
+            kb, p, occ = b[name][0], b[name][1], b[name][4]
+            m = (occ > 0) & (kb <= kmax)
+            row[name] = float(np.max(np.abs(a[name][1][m] - p[m]) / np.abs(p[m])))
+            ok = ok and row[name] <= 1e-3
+        dev["z=%g" % b["z"]] = row
+    d = p32 - p64
+    d -= np.round(d)
+    d *= N
+    disp = p64 - p0
+    disp -= np.round(disp)
+    disp *= N
+    rms = float(np.sqrt((d ** 2).sum(axis=1).mean()))
+    rms_disp = float(np.sqrt((disp ** 2).sum(axis=1).mean()))
+
+    def form(cyc):
+        last = cyc[-K:]
+        return {"value": N ** 3 * len(last) / (sum(last) / 1e3), "ms_per_step": sum(last) / len(last),
+                "full_run_ms_per_step": sum(cyc) / len(cyc), "cycles": len(cyc)}
+
+    f64, f32 = form(c64), form(c32)
+    return {"fp64_form": dict(f64, unit="particle-steps/s",
+                              note="the same last %d cycles before z = 0, CUDA events around each cycle" % K),
+            "pk_check": {"against": "the FP64 form on the GPU, device IC of the same seed at z = 100, run to z = 0",
+                         "numbins": PK_BINS, "k_max": "k_Nyquist/2", "pk_redshifts": list(PK_REDSHIFTS),
+                         "max_rel_dev": dev, "tolerance": 1e-3, "pass": ok,
+                         "rms_position_difference_cells": rms, "max_position_difference_cells": float(np.abs(d).max()),
+                         "rms_displacement_since_ic_cells": rms_disp,
+                         "mixed_over_fp64_speed": f32["value"] / f64["value"],
+                         "mixed_form_same_loop": f32}}
+
+
 # ------------------------------------------------------------ serving --------
 SERVE_SIZES = (64, 96, 128, 192, 256)
 SERVE_Z = (1.0, 0.5, 0.0)
 
 
-def serve_requests(gpu, rng, n, first_seed):
+def serve_requests(gpu, rng, n, first_seed, prec=None):
     """Requests of the serving workload: grid drawn from SERVE_SIZES, box 2.5 N Mpc/h,
     Omega_cdm U[0.25, 0.35], sigma8 U[0.75, 0.87], n_s U[0.94, 0.98], target
     redshift from SERVE_Z, BBKS Zel'dovich IC at z = 100, distinct seeds."""
@@ -454,39 +581,21 @@ def serve_requests(gpu, rng, n, first_seed):
         N = int(rng.choice(SERVE_SIZES))
         out.append(gpu.request(N, seed=first_seed + k, z_target=float(rng.choice(SERVE_Z)),
                                Omega_cdm=float(rng.uniform(0.25, 0.35)), sigma8=float(rng.uniform(0.75, 0.87)),
-                               n_s=float(rng.uniform(0.94, 0.98)), prec=gpu.PREC_MIXED))
+                               n_s=float(rng.uniform(0.94, 0.98)), prec=gpu.PREC_MIXED if prec is None else prec))
     return out
 
 
-def fp64_sequential_seconds(gpu, sizes):
-    """Per grid size, the wall time of a plain FP64 run on this GPU: the initial
-    conditions, and one cycle (the median of 3 after one warm-up)."""
-    out = {}
-    for N in sizes:
-        c = gpu.Context(N, gpu.PREC_FP64)
-        s = gpu.Sim(c, N ** 3)
-        t0 = time.perf_counter()
-        s.ic_generate(**gpu.ic_params(2.5 * N, seed=7))
-        c.sync()
-        t_ic = time.perf_counter() - t0
-        s.step()
-        c.sync()
-        ts = []
-        for _ in range(3):
-            t0 = time.perf_counter()
-            s.step()
-            c.sync()
-            ts.append(time.perf_counter() - t0)
-        out[N] = (t_ic, sorted(ts)[1])
-        del s, c
-    return out
+def as_fp64(gpu, req):
+    """The same simulation request in the plain FP64 form."""
+    return gpu.Request(req.N, gpu.PREC_FP64, req.boxsize, req.Omega_cdm, req.Omega_b, req.sigma8, req.n_s, req.h,
+                       req.z_in, req.z_target, req.seed, req.numbins)
 
 
 def run_serve(args, gpu):
     """The serving loop under load: Poisson arrivals at --serve-rate for
     --serve-seconds (time to result p50 / p99, sustained sims/hour), then a burst of
-    --serve-burst requests at once (capacity), against sequential plain FP64 runs of
-    the same requests on the same GPU (their IC and cycle times measured per size)."""
+    --serve-burst requests at once (capacity), against the same burst run one request
+    at a time in the plain FP64 form on the same GPU (a server with one slot)."""
     import numpy as np
     rng = np.random.default_rng(args.seed + 77)
     n_poisson = max(1, int(args.serve_seconds * args.serve_rate * 1.5) + 8)
@@ -519,13 +628,17 @@ def run_serve(args, gpu):
     bst = srv.stats()
     srv.close()
     b_span = max(r["t_done"] for r in bres) - min(r["t_submit"] for r in bres)
-    seq = fp64_sequential_seconds(gpu, sorted({r["N"] for r in res} | {r["N"] for r in bres} | {64, 96, 128}))
-
-    def seq_seconds(rs):
-        return sum(seq[r["N"]][0] + r["cycles"] * seq[r["N"]][1] for r in rs)
-
+    # the same burst in the plain FP64 form, one request at a time
+    srv = gpu.Server(max_active=1)
+    t0 = time.perf_counter()
+    for r in burst:
+        srv.submit(as_fp64(gpu, r))
+    srv.drain(1800.0)
+    sres = [r for r in srv.poll(100000) if r["status"] == 0]
+    s_span = time.perf_counter() - t0
+    srv.close()
     cap = len(bres) / b_span * 3600.0
-    seq_rate = len(bres) / seq_seconds(bres) * 3600.0
+    seq_rate = len(sres) / s_span * 3600.0
     # the batched ensemble: 16 simulations each at 64^3, 96^3 and 128^3, box 2.5 N,
     # cosmologies and seeds as above, all to z = 0, admitted at once
     ens = []
@@ -551,36 +664,14 @@ def run_serve(args, gpu):
         "max_active_seen": st["max_active_seen"],
         "burst": {"requests": len(bres), "makespan_s": b_span, "sims_per_hour": cap,
                   "max_active_seen": bst["max_active_seen"]},
-        "sequential_fp64": {"sims_per_hour": seq_rate,
-                            "per_size_s": {str(N): {"ic": v[0], "cycle": v[1]} for N, v in seq.items()},
-                            "note": "the burst's requests run one after another in the plain FP64 form: IC time plus "
-                                    "their cycles times the measured FP64 cycle time of their size"},
+        "sequential_fp64": {"requests": len(sres), "makespan_s": s_span, "sims_per_hour": seq_rate,
+                            "note": "the burst's own requests in the plain FP64 form, run one at a time (a server "
+                                    "with one slot) on the same GPU"},
         "capacity_vs_sequential_fp64": cap / seq_rate,
         "ensemble": {"simulations": len(eres), "sizes": "16 x 64^3, 16 x 96^3, 16 x 128^3, z = 100 -> 0",
                      "makespan_s": e_span, "particle_steps_per_s": e_steps / e_span,
-                     "max_active_seen": est["max_active_seen"],
-                     "sequential_fp64_s": seq_seconds(eres) if all(r["N"] in seq for r in eres) else None},
+                     "max_active_seen": est["max_active_seen"]},
     }
-
-
-def run_e2e(gpu, ctx, sim, stream, N, steps, torch):
-    import numpy as np
-    pcls = sim.particles()
-    n = N ** 3
-    host = torch.empty(n * 56, dtype=torch.uint8, pin_memory=True)
-    arr = host.numpy().view(gpu.PART)
-    back = torch.empty(n * 56, dtype=torch.uint8, pin_memory=True)
-    barr = back.numpy().view(gpu.PART)
-    pcls.download(out=arr)
-    ctx.sync()
-    t0 = time.perf_counter()
-    for _ in range(steps):
-        pcls.upload(arr)
-        sim.step()
-        pcls.download(out=barr)  # into pinned memory; synchronises the stream
-    dt = time.perf_counter() - t0
-    return {"value": n * steps / dt, "unit": "particle-steps/s", "h2d_bytes_per_step": n * 56,
-            "d2h_bytes_per_step": n * 56}
 
 
 def run_hbm_fit(gpu, device, torch, N=1024, steps=2):
@@ -600,7 +691,7 @@ def run_hbm_fit(gpu, device, torch, N=1024, steps=2):
         sim.step()
         ctx.sync()
         stream = torch.cuda.ExternalStream(ctx.stream(), device=torch.device("cuda", device))
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0, e1 = _events(torch, 2)
         e0.record(stream)
         for _ in range(steps):
             sim.step()
@@ -621,8 +712,7 @@ def run_e2e_two_sims(gpu, N, steps, box, device, torch):
     thread through the same calls (upload from pinned memory, cycle, download into pinned
     memory): one simulation's transfers over the host link overlap the other's cycle, and
     its uploads the other's downloads.  Value: both simulations' particle-steps over the
-    wall time."""
-    import threading
+    wall time.  Early cycles (z near 100)."""
     n = N ** 3
     sims = []
     for k in range(2):
@@ -668,85 +758,196 @@ def run_e2e_two_sims(gpu, N, steps, box, device, torch):
 
 # ---------------------------------------------------------- CPU side --------
 def _cpu_worker(args):
-    N, steps, seed = args
+    """The oracle (FP64 CPU restatement, OpenMP over the host's threads) on the CPU
+    sample: IC at z = 100, `warm` untimed cycles, then `steps` timed cycles."""
+    N, box, warm, steps, seed = args
     import gevoracle as G
-    s = G.Sim(N).ic(**G.default_icparams(N, 1000.0 * N / 512, seed=seed))
-    s.step()  # the first cycle skips the phi solve (dtau_old = 0)
-    t0 = time.perf_counter()
-    for _ in range(steps):
+    s = G.Sim(N).ic(**G.default_icparams(N, box, seed=seed))
+    for _ in range(warm):
         s.step()
-    return N ** 3 * steps, time.perf_counter() - t0
+    t0s = s.phase_seconds()
+    per = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        s.step()
+        per.append(time.perf_counter() - t0)
+    t1s = s.phase_seconds()
+    phases = {k: (t1s[k] - t0s[k]) / max(steps, 1) for k in G.PHASES}
+    phases["fft_count_per_cycle"] = (t1s["fft_count"] - t0s["fft_count"]) / max(steps, 1)
+    return per, phases, os.cpu_count()
 
 
-def cpu_sample(N, steps, workers):
-    """particle-steps/s of the oracle on `workers` independent simulations."""
+def cpu_sample(N, box, warm, steps):
+    """Runs the CPU sample in a spawned process (its own OpenMP runtime, no CUDA)."""
     import multiprocessing as mp
     import gevoracle
     gevoracle.build()
-    if workers == 1:
-        n, t = _cpu_worker((N, steps, 1))
-        return n / t
     ctx = mp.get_context("spawn")
-    with ctx.Pool(workers) as pool:
-        res = pool.map(_cpu_worker, [(N, steps, 1 + i) for i in range(workers)])
-    return sum(r[0] for r in res) / max(r[1] for r in res)
+    with ctx.Pool(1) as pool:
+        return pool.apply(_cpu_worker, ((N, box, warm, steps, 1),))
+
+
+def cpu_line(per, phases, threads, what):
+    n = CPU_SAMPLE_GRID ** 3
+    v = n * len(per) / sum(per)
+    return {"value": v, "unit": "particle-steps/s", "cores": threads, "kind": "port",
+            "sample": "%s of a %d^3 simulation in a %g Mpc/h box (the 512^3 workload's cell size and particle "
+                      "density), BBKS Zel'dovich IC at z = 100; FP64 CPU restatement of the path on %d OpenMP threads; "
+                      "its FFT is the oracle's, not FFTW" % (what, CPU_SAMPLE_GRID, CPU_SAMPLE_BOX, threads),
+            "phases_s_per_cycle": phases}
+
+
+def config_of(args):
+    N = args.grid
+    return {"workload": "gevolution GR PM cycle, %d^3 grid, %d^3 CDM particles, box %g Mpc/h, %s form, "
+                        "BBKS Zel'dovich IC at z=100 (sigma8 0.81, h 0.67, Omega_cdm 0.27 + Omega_b 0.05), "
+                        "parabolic B, 12 FFTs per cycle, run to z=0" % (N, N, 1000.0 * N / 512, args.prec),
+            "grid": N, "particles": N ** 3, "precision": args.prec,
+            "l2": "inputs larger than L2 (fields >= %d MB each)" % (N ** 3 * (8 if args.prec == "fp64" else 4) // 2 ** 20)}
+
+
+def main_reference(args, rank):
+    if rank != 0:
+        return
+    t0 = time.perf_counter()
+    per, phases, threads = cpu_sample(CPU_SAMPLE_GRID, CPU_SAMPLE_BOX, args.warmup, args.steps)
+    cb = cpu_line(per, phases, threads, "%d cycles after %d warm-up cycles" % (args.steps, args.warmup))
+    N = args.grid
+    line = {"impl": "reference", "metric": "particle-steps/s %d^3 %s" % (N, args.prec), "value": cb["value"],
+            "unit": "particle-steps/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": sum(per) / len(per) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": config_of(args),
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t0}
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------ single operations --
+def run_op(args):
+    """One operation for profiler captures and per-operation timing (CUDA events on
+    the context's stream, --reps calls after one untimed call):
+      prepare    IC at z = 100, evolve to --z-op, write the hibernation file --state
+      cycle      restart from --state, --reps cycles (the late-time cycle for ncu)
+      table      restart from --state (or a fresh IC), time each operation of a cycle
+      r2c_alone, c2r_alone, fft_axis_y, fft_axis_z   one component of random values"""
+    import numpy as np
+    import torch
+    import gev_gb300 as gpu
+    N = args.grid
+    prec = gpu.PREC_MIXED if args.prec == "mixed" else gpu.PREC_FP64
+    ctx = gpu.Context(N, prec)
+    st = torch.cuda.ExternalStream(ctx.stream())
+
+    def timed(fn):
+        fn()
+        ctx.sync()
+        e0, e1 = _events(torch, 2)
+        e0.record(st)
+        for _ in range(args.reps):
+            fn()
+        e1.record(st)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / args.reps
+
+    rng = np.random.default_rng(1)
+    if args.op in ("r2c_alone", "c2r_alone"):
+        real, spec = ctx.real(1), ctx.spectrum(1)
+        real.upload(rng.standard_normal(real.shape))
+        gpu.fft_r2c(real, spec)
+        fn = (lambda: gpu.fft_r2c(real, spec)) if args.op == "r2c_alone" else (lambda: gpu.fft_c2r(spec, real))
+        print("grid %d^3, %s form, one component; %s %.3f ms per call" % (N, args.prec, args.op, timed(fn)))
+        return
+    if args.op in ("fft_axis_y", "fft_axis_z"):
+        spec = ctx.spectrum(1)
+        spec.upload(rng.standard_normal(spec.shape) + 1j * rng.standard_normal(spec.shape))
+        axis = 1 if args.op == "fft_axis_y" else 2
+        print("grid %d^3, %s form, one spectrum component; %s %.3f ms per call"
+              % (N, args.prec, args.op, timed(lambda: gpu.fft_axis(spec, axis, -1))))
+        return
+    sim = gpu.Sim(ctx, N ** 3)
+    box = 1000.0 * N / 512
+    if args.op == "prepare":
+        sim.ic_generate(**gpu.ic_params(box, seed=args.seed))
+        n = full_cycles_to(sim.state(), N, args.z_op)
+        for _ in range(n):
+            sim.step()
+        sim.hibernate(args.state)
+        s = sim.state()
+        print("grid %d^3, %s form: %d cycles to z = %.4f, hibernation file %s"
+              % (N, args.prec, n, 1.0 / s["a"] - 1.0, args.state))
+        return
+    if args.state:
+        sim.restart(args.state)
+    else:
+        sim.ic_generate(**gpu.ic_params(box, seed=args.seed))
+        sim.step()
+    z = 1.0 / sim.state()["a"] - 1.0
+    if args.op == "cycle":
+        print("grid %d^3, %s form, z = %.4f: cycle %.3f ms" % (N, args.prec, z, timed(sim.step)))
+        return
+    if args.op != "table":
+        raise SystemExit("unknown --op %r" % args.op)
+    p = sim.particles()
+    phi, chi, Bi, src, Sij = (sim.field(k) for k in ("phi", "chi", "Bi", "source", "Sij"))
+    sFT, SFT, BFT = (sim.field(k) for k in ("scalarFT", "SijFT", "BiFT"))
+    a = sim.state()["a"]
+    ops = [
+        ("cycle", sim.step),
+        ("T00+Tij", lambda: gpu.projection_T00_Tij(p, src, Sij, a, phi)),
+        ("source_scalar", lambda: gpu.prepare_source_scalar(phi, chi, src, 0.32, src, 1e-3, 1e-3, 1e-3)),
+        ("r2c_x1", lambda: gpu.fft_r2c(src, sFT)),
+        ("c2r_x1", lambda: gpu.fft_c2r(sFT, phi)),
+        ("source_tensor", lambda: gpu.prepare_source_tensor(phi, Sij, Sij, 1e-3)),
+        ("r2c_x6", lambda: gpu.fft_r2c(Sij, SFT)),
+        ("project_evolve", lambda: gpu.project_scalar_evolve_vector(SFT, sFT, BFT, 1e-9)),
+        ("c2r_x3", lambda: gpu.fft_c2r(BFT, Bi)),
+        ("kick_drift_move", lambda: gpu.update_q_pos(p, 1e-9, a, 3, 1e-9, a, 3, phi, chi, Bi, wait=False)),
+    ]
+    print("grid %d^3, %s form, z = %.4f; ms per call (CUDA events), %d calls" % (N, args.prec, z, args.reps))
+    for name, fn in ops:
+        print("%-16s %9.3f ms" % (name, timed(fn)), flush=True)
 
 
 def main():
     args = parse()
+    if args.op:
+        run_op(args)
+        return
     rank, world, local = dist_env()
     if world > 1:
         import torch
         torch.distributed.init_process_group("nccl" if args.impl == "ours" else "gloo")
-    N = args.grid
-    metric = "particle-steps/s %d^3 %s" % (N, args.prec)
-    config = {"workload": "gevolution GR PM cycle, %d^3 grid, %d^3 CDM particles, box %g Mpc/h, %s form, "
-                          "BBKS Zel'dovich IC at z=100 (sigma8 0.81, h 0.67, Omega_cdm 0.27 + Omega_b 0.05), "
-                          "parabolic B, 12 FFTs per cycle" % (N, N, 1000.0 * N / 512, args.prec),
-              "grid": N, "particles": N ** 3, "precision": args.prec,
-              "l2": "inputs larger than L2 (fields >= %d MB each)" % (N ** 3 * (8 if args.prec == "fp64" else 4) // 2 ** 20)}
     if args.impl == "reference":
-        if rank != 0:
-            return
-        workers = os.cpu_count() or 1
-        sampleN = 64
-        t0 = time.perf_counter()
-        cpu_sample(sampleN, 1, workers)  # warm-up (builds, spawns)
-        vals = []
-        for _ in range(args.steps):
-            vals.append(cpu_sample(sampleN, 1, workers))
-        v = sorted(vals)[len(vals) // 2]
-        line = {"impl": "reference", "metric": metric, "value": v, "unit": "particle-steps/s", "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-                "config": config,
-                "cpu_baseline": {"value": v, "unit": "particle-steps/s", "cores": workers, "kind": "port",
-                                 "sample": "one cycle per worker of an independent %d^3 simulation (same IC recipe "
-                                           "and box per particle), %d workers; the FFT is the oracle's, not FFTW"
-                                           % (sampleN, workers)},
-                "e2e": {"value": v, "unit": "particle-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-                "wall_s": time.perf_counter() - t0}
-        print(json.dumps(line))
+        main_reference(args, rank)
         return
     res = run_ours(args, rank, world, local)
     if rank != 0:
         return
     cpu = None
     if not args.no_cpu_baseline:
-        sampleN = 64
-        v = cpu_sample(sampleN, 3, 1)
-        cpu = {"value": v, "unit": "particle-steps/s", "cores": 1, "kind": "port",
-               "sample": "3 cycles of one %d^3 simulation with the same IC recipe (CPU restatement, FP64, single "
-                         "thread); the FFT is the oracle's, not FFTW" % sampleN}
-    line = {"metric": metric, "value": res["value"], "unit": "particle-steps/s", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"], "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if args.prec == "fp64" else "f32+f64pos+i64dep",
+        per, phases, threads = cpu_sample(CPU_SAMPLE_GRID, CPU_SAMPLE_BOX, 1, 2)
+        cpu = cpu_line(per, phases, threads, "2 cycles after 1 warm-up cycle")
+    N = args.grid
+    alg, per_particle, per_cell = cycle_bytes(N, args.prec)
+    config = config_of(args)
+    config["timed_cycles"] = res["timed"]
+    line = {"metric": "particle-steps/s %d^3 %s" % (N, args.prec), "value": res["value"], "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": res["ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.prec == "fp64" else "f32+f64pos+i64dep",
             "data": "synthetic (device-generated BBKS Zel'dovich IC)", "config": config,
-            "roofline": res["roofline"], "roofline_fft_cols": res["roofline_fft"], "roofline_particle_update": res["roofline_pcl"], "fft_vs_cufft": res["cufft"], "fft_tiles": res["tiles"], "cpu_baseline": cpu, "e2e": res["e2e"], "e2e_two_sims": res["e2e2"], "hbm_fit_1024": res["hbm"], "gpu_launches": res["launches"],
-            "clocks": res["clocks"], "bytes_per_cycle_alg": cycle_bytes(N, args.prec),
+            "roofline": res["roofline"], "kernels": res["kernels"], "phases_gpu_ms_per_cycle": res["phases"],
+            "full_run": res["full"], "early_cycles": res["early"],
+            "fft_vs_cufft": res["cufft"], "fft_tiles": res["tiles"], "cpu_baseline": cpu, "e2e": res["e2e"],
+            "e2e_two_sims": res["e2e2"], "hbm_fit_1024": res["hbm"], "gpu_launches": res["launches"],
+            "clocks": res["clocks"],
+            "bytes_per_cycle_alg": {"bytes": alg, "per_particle": per_particle, "per_cell": per_cell,
+                                    "achieved_gbs": alg / (res["ms"] / 1e3) / 1e9,
+                                    "frac": alg / (res["ms"] / 1e3) / 1e9 / hbm_peak()[0]},
             "final_a": res["state"]["a"]}
-    if res.get("fp64"):
-        line.update(res["fp64"])
+    if res.get("pk"):
+        line.update(res["pk"])
     if res.get("serve"):
         line["serve"] = res["serve"]
     print(json.dumps(line))

@@ -113,6 +113,59 @@ int ctx_ensure_red(gev_ctx *ctx, size_t elems) {
 
 void ctx_retain(gev_ctx *ctx) { ctx->refs++; }
 
+static cudaEvent_t timer_event(gev_ctx *ctx) {
+  if (!ctx->event_pool.empty()) {
+    cudaEvent_t e = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  if (cudaEventCreate(&e) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return e;
+}
+
+GevTimed::GevTimed(gev_ctx *c, const char *name) : ctx(c) {
+  if (!ctx || !ctx->timing) return;
+  gev_ctx::TimedRegion r{name, timer_event(ctx), timer_event(ctx)};
+  if (!r.start || !r.stop) return;
+  cudaEventRecord(r.start, ctx->stream);
+  idx = (long)ctx->timed.size();
+  ctx->timed.push_back(r);
+}
+
+void GevTimed::stop() {
+  if (idx >= 0) cudaEventRecord(ctx->timed[(size_t)idx].stop, ctx->stream);
+  idx = -1;
+}
+
+// waits for the stream and folds the recorded regions into the per-name sums
+static int timer_collect(gev_ctx *ctx) {
+  GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+  for (const auto &r : ctx->timed) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.start, r.stop) != cudaSuccess) {
+      cudaGetLastError();
+      ms = 0.f;
+    }
+    size_t k = 0;
+    while (k < ctx->timed_names.size() && ctx->timed_names[k] != r.name) ++k;
+    if (k == ctx->timed_names.size()) {
+      ctx->timed_names.push_back(r.name);
+      ctx->timed_count.push_back(0);
+      ctx->timed_ms.push_back(0.);
+    }
+    ctx->timed_count[k] += 1;
+    ctx->timed_ms[k] += (double)ms;
+    ctx->event_pool.push_back(r.start);
+    ctx->event_pool.push_back(r.stop);
+  }
+  ctx->timed.clear();
+  return GEV_OK;
+}
+
 void ctx_release(gev_ctx *ctx) {
   if (--ctx->refs > 0) return;
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
@@ -125,6 +178,11 @@ void ctx_release(gev_ctx *ctx) {
   cudaFree(ctx->d_fft_scratch);
   cudaFree(ctx->d_cube);
   cudaFree(ctx->d_red);
+  for (const auto &r : ctx->timed) {
+    cudaEventDestroy(r.start);
+    cudaEventDestroy(r.stop);
+  }
+  for (cudaEvent_t e : ctx->event_pool) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
 }
@@ -231,6 +289,40 @@ int gev_ctx_launch_count(gev_ctx *ctx, long long *count) {
   return GEV_OK;
 }
 
+int gev_ctx_set_timing(gev_ctx *ctx, int on) {
+  if (!ctx) return GEV_EINVAL;
+  if (!on && ctx->timing) {
+    const int rc = timer_collect(ctx);
+    if (rc) return rc;
+  }
+  ctx->timing = on != 0;
+  return GEV_OK;
+}
+
+int gev_ctx_timing_report(gev_ctx *ctx, char *buf, size_t len, int reset) {
+  if (!ctx || (!buf && len)) return GEV_EINVAL;
+  const int rc = timer_collect(ctx);
+  if (rc) return rc;
+  std::string out;
+  char line[256];
+  for (size_t k = 0; k < ctx->timed_names.size(); ++k) {
+    snprintf(line, sizeof line, "%s\t%ld\t%.6f\n", ctx->timed_names[k].c_str(), ctx->timed_count[k],
+             ctx->timed_ms[k]);
+    out += line;
+  }
+  if (len) {
+    const size_t n = out.size() < len - 1 ? out.size() : len - 1;
+    memcpy(buf, out.data(), n);
+    buf[n] = 0;
+  }
+  if (reset) {
+    ctx->timed_names.clear();
+    ctx->timed_count.clear();
+    ctx->timed_ms.clear();
+  }
+  return out.size() < len ? GEV_OK : gev_fail(ctx, GEV_EINVAL, "timing_report: buffer too small");
+}
+
 int gev_field_create(gev_ctx *ctx, int kind, int ncomp, gev_field **out) {
   if (!ctx || !out || ncomp < 1 || ncomp > 16 || (kind != GEV_FIELD_REAL && kind != GEV_FIELD_SPECTRUM))
     return gev_fail(ctx, GEV_EINVAL, "field_create: bad kind or component count");
@@ -321,6 +413,7 @@ int gev_fft_r2c(gev_ctx *ctx, const gev_field *real, gev_field *spec) {
   if (!ctx || !real || !spec || real->ctx != ctx || spec->ctx != ctx || real->kind != GEV_FIELD_REAL ||
       spec->kind != GEV_FIELD_SPECTRUM || real->ncomp != spec->ncomp)
     return gev_fail(ctx, GEV_EINVAL, "fft_r2c: real field and spectrum with equal component counts");
+  GevTimed tm_(ctx, "phase:fft");
   for (int c = 0; c < real->ncomp; ++c) {
     int rc = fft_r2c_comp(ctx, (const char *)real->d + c * real->comp_elems * real->elem_bytes,
                           (char *)spec->d + c * spec->comp_elems * spec->elem_bytes);
@@ -333,6 +426,7 @@ int gev_fft_c2r(gev_ctx *ctx, const gev_field *spec, gev_field *real) {
   if (!ctx || !real || !spec || real->ctx != ctx || spec->ctx != ctx || real->kind != GEV_FIELD_REAL ||
       spec->kind != GEV_FIELD_SPECTRUM || real->ncomp != spec->ncomp)
     return gev_fail(ctx, GEV_EINVAL, "fft_c2r: spectrum and real field with equal component counts");
+  GevTimed tm_(ctx, "phase:fft");
   for (int c = 0; c < real->ncomp; ++c) {
     int rc = fft_c2r_comp(ctx, (const char *)spec->d + c * spec->comp_elems * spec->elem_bytes,
                           (char *)real->d + c * real->comp_elems * real->elem_bytes, ctx->d_fft_scratch);
@@ -345,6 +439,7 @@ int gev_fft_c2r_poisson(gev_ctx *ctx, const gev_field *srcFT, gev_field *real, d
   if (!ctx || !real || !srcFT || real->ctx != ctx || srcFT->ctx != ctx || real->kind != GEV_FIELD_REAL ||
       srcFT->kind != GEV_FIELD_SPECTRUM || real->ncomp != 1 || srcFT->ncomp != 1)
     return gev_fail(ctx, GEV_EINVAL, "fft_c2r_poisson: one spectrum component and one real component");
+  GevTimed tm_(ctx, "phase:fft");
   return fft_c2r_poisson_comp(ctx, srcFT->d, real->d, coeff, modif);
 }
 

@@ -206,6 +206,7 @@ int run_deposit(gev_ctx *ctx, gev_pcls *p, gev_field *out, double a, const gev_f
       rc = gev_field_zero(out);
       if (rc) return rc;
     }
+    GevTimed tm_(ctx, "k_cube_fp64+k_gather");
     k_cube_fp64<KIND><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->start, phi ? (const double *)phi->d : nullptr, dp,
                                                        (double *)ctx->d_cube);
     GEV_LAUNCH_CHECK(ctx);

@@ -83,8 +83,10 @@ __global__ void __launch_bounds__(256) k_fx_bounds(const float *__restrict__ vx,
 
 // per-particle contribution bounds, |phi| <= 1 taken for the (1 + f phi) factors:
 // T00 m (e + (3e + q^2/e)|phi|) <= m (4e + q^2/a); T0i m |q_i| (1 + 2|phi|) <= 3 m |q|;
-// Tij m q_i q_j / e (1 + 5|phi|) <= 6 m q^2 / a; mass m.  Writes the power k of the
-// scale 2^k into bounds[2], kept in [-60, 100] (FP32 scale and float_of_fixed stay exact).
+// Tij m q_i q_j / e (1 + 5|phi|) <= 6 m q^2 / a; mass m.  Writes the power k = kq + kg
+// of the sum's scale 2^k into bounds[2 + group]: kq is kept in [-60, 100] and kg in
+// [-4, 21], so k stays in [-64, 121], where float_of_fixed is exact (its scale 2^-k and
+// its product stay normal for k in [-64, 126]).
 // Each contribution is Q * G: Q = round(p 2^kq) an int32 per particle and quantity
 // (p its prefactor, e.g. m q_i^2 / e), G = round(g 2^kg) an integer below 2^22 per
 // corner (g its weight factor, e.g. w_k (1 + f phi_k)), their product one 32x32->64
@@ -95,7 +97,10 @@ __global__ void __launch_bounds__(256) k_fx_bounds(const float *__restrict__ vx,
 __device__ void fx_group(uint32_t *bounds, int group, double pmax, double gmax, double mc) {
   int eg = 0;
   frexp(gmax, &eg);  // gmax < 2^eg
-  const int kg = 22 - eg;
+  // gmax >= 1 (eg >= 1); kg >= -4 holds for gmax < 2^26, i.e. |phi| below about 1e7,
+  // which any metric perturbation (|phi| << 1) satisfies by many orders of magnitude
+  int kg = 22 - eg;
+  kg = kg < -4 ? -4 : kg;
   // |Q| <= Qlim with 8 mc Qlim 2^22 <= 2^62
   double qlim = ldexp(1.0, 37) / mc;
   if (qlim > 2147483647.0) qlim = 2147483647.0;
@@ -567,6 +572,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   const float *fphi = phi ? (const float *)phi->d : nullptr;
   const unsigned blocks = (unsigned)(ntx * nty * ntz);
   const long C = (long)N * N * N;
+  GevTimed tm_b(ctx, "k_fx_bounds+k_fx_scale");
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->bounds, 0, 16 * sizeof(uint32_t), ctx->stream));
   k_fx_bounds<<<grid_for(ctx, (size_t)(p->n > C ? p->n : C), 256, 8), 256, 0, ctx->stream>>>(
       (const float *)p->cur.vx, (const float *)p->cur.vy, (const float *)p->cur.vz, p->n, p->count,
@@ -574,6 +580,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   GEV_LAUNCH_CHECK(ctx);
   k_fx_scale<<<1, 1, 0, ctx->stream>>>(p->bounds, kind, mass, a);
   GEV_LAUNCH_CHECK(ctx);
+  tm_b.stop();
   if (gather) {
     // the records live in the alt array set, which only a relink writes (an allocation
     // of their own only if that block were too small)
@@ -598,17 +605,24 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     // of a few large blocks cannot (512^3 cycle: 29.7 ms at 96, 30.7 at 16, 31.8 at 12)
     const int gb = grid_for(ctx, (size_t)C, 256, 96);
     const Div32 dN = make_div32((unsigned)N);
+    GevTimed tm_p(ctx, "k_fx_prep");
     if (kind == FX_T00) {
       k_fx_prep<FX_T00><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
+      tm_p.stop();
+      GevTimed tm_g(ctx, "k_dep_gather");
       k_dep_gather<FX_T00><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
     } else if (kind == FX_TIJ) {
       k_fx_prep<FX_TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
+      tm_p.stop();
+      GevTimed tm_g(ctx, "k_dep_gather");
       k_dep_gather<FX_TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
     } else {
       k_fx_prep<FX_T00TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
+      tm_p.stop();
+      GevTimed tm_g(ctx, "k_dep_gather");
       k_dep_gather<FX_T00TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
     }
     GEV_LAUNCH_CHECK(ctx);
@@ -618,6 +632,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   cudaFuncSetAttribute(k_dep_fx<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);        \
   k_dep_fx<K><<<blocks, FX_THREADS, smem, ctx->stream>>>(p->cur, p->start, PHI, (float *)out->d, face, fp, \
                                                          p->bounds)
+  GevTimed tm_s(ctx, "k_dep_fx+k_face_fix");
   if (kind == FX_T0I) {
     GEV_DEP_LAUNCH(FX_T0I, fphi);
   } else {

@@ -256,6 +256,7 @@ int run_cols(gev_ctx *ctx, const void *in, void *out, long line_stride, long pla
   const long nchunks = (NH + B - 1) / B;
   const long blocks = (long)N * nchunks;
   const size_t smem = ((size_t)N + (size_t)N * B) * sizeof(C) + (size_t)N * 2;
+  GevTimed tm_(ctx, "k_fft_cols");
   k_fft_cols<T, SIGN><<<(unsigned)blocks, 256, smem, ctx->stream>>>(
       (const C *)in, (C *)out, ctx->planN, (const C *)ctx->d_twN, (const unsigned short *)ctx->d_permN, NH,
       line_stride, plane_stride, lgB);
@@ -277,6 +278,7 @@ int r2c_comp(gev_ctx *ctx, const void *real, void *spec) {
   }
   const int lgB = batch_lg(M, sizeof(C), 1, 64, 32768), B = 1 << lgB;
   const size_t smem = ((size_t)M + (size_t)M * (B + 1)) * sizeof(C) + (size_t)M * 2;
+  GevTimed tm_(ctx, "k_fft_r2c_rows");
   k_fft_r2c_rows<T><<<(unsigned)((nrows + B - 1) / B), 256, smem, ctx->stream>>>(
       (const T *)real, (C *)spec, ctx->planH, (const C *)ctx->d_twH, (const unsigned short *)ctx->d_permH,
       (const C *)ctx->d_twN, NH, nrows, lgB, make_div(M), make_div(M + 1));
@@ -301,6 +303,7 @@ int c2r_comp(gev_ctx *ctx, const void *spec, void *real, void *scratch, const do
   const long nrows = (long)N * N;
   const int lgB = batch_lg(M, sizeof(C), 1, 64, 32768), B = 1 << lgB;
   const size_t smem = ((size_t)M + (size_t)M * (B + 1) + (size_t)B * (M + 1)) * sizeof(C) + (size_t)M * 2;
+  GevTimed tm_(ctx, "k_fft_c2r_rows");
   k_fft_c2r_rows<T><<<(unsigned)((nrows + B - 1) / B), 256, smem, ctx->stream>>>(
       (const C *)scratch, (T *)real, ctx->planH, (const C *)ctx->d_twH, (const unsigned short *)ctx->d_permH,
       (const C *)ctx->d_twN, NH, nrows, lgB, make_div(M), make_div(M + 1));

@@ -309,6 +309,7 @@ int cols_LB(gev_ctx *ctx, const void *in, void *out, long ES, long PS, PoisArgs 
   int grid = 0;
   int rc = launch_cfg(ctx, k_fft_cols_reg<T, SIGN, L, LGB, POIS>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
+  GevTimed tm_(ctx, "k_fft_cols_reg");
   k_fft_cols_reg<T, SIGN, L, LGB, POIS><<<grid, threads, smem, ctx->stream>>>((const C *)in, (C *)out,
                                                                         (const C *)ctx->d_twN, NH, ES, PS, (int)ntiles, pois);
   GEV_LAUNCH_CHECK(ctx);
@@ -369,6 +370,7 @@ int r2c_LB(gev_ctx *ctx, const void *real, void *spec, long nrows) {
   int grid = 0;
   int rc = launch_cfg(ctx, k_fft_r2c_rows_reg<T, L, LGB>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
+  GevTimed tm_(ctx, "k_fft_r2c_rows_reg");
   k_fft_r2c_rows_reg<T, L, LGB><<<grid, threads, smem, ctx->stream>>>(
       (const T *)real, (C *)spec, (const C *)ctx->d_twH, (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
   GEV_LAUNCH_CHECK(ctx);
@@ -387,6 +389,7 @@ int c2r_LB(gev_ctx *ctx, const void *spec, void *real, long nrows) {
   int grid = 0;
   int rc = launch_cfg(ctx, k_fft_c2r_rows_reg<T, L, LGB>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
+  GevTimed tm_(ctx, "k_fft_c2r_rows_reg");
   k_fft_c2r_rows_reg<T, L, LGB><<<grid, threads, smem, ctx->stream>>>(
       (const C *)spec, (T *)real, (const C *)ctx->d_twH, (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
   GEV_LAUNCH_CHECK(ctx);

@@ -56,6 +56,18 @@ struct gev_ctx {
   int fft_lg[4] = {-1, -1, -1, -1};
   bool fft_tuned = false;
   long long launches = 0;
+  // optional device timing of named regions (gev_ctx_set_timing): a CUDA event
+  // pair on the stream around each region, summed per name when the report is read
+  struct TimedRegion {
+    const char *name;
+    cudaEvent_t start, stop;
+  };
+  bool timing = false;
+  std::vector<TimedRegion> timed;
+  std::vector<cudaEvent_t> event_pool;
+  std::vector<std::string> timed_names;
+  std::vector<long> timed_count;
+  std::vector<double> timed_ms;
   size_t bytes_in_use = 0;
   std::string err;
   // lifetime: the handle returned by gev_ctx_create holds one reference and
@@ -67,6 +79,20 @@ struct gev_ctx {
 
 void ctx_retain(gev_ctx *ctx);
 void ctx_release(gev_ctx *ctx);
+
+// Times the work a scope enqueues on the context's stream when the context's
+// timing is on (an event before and after); costs nothing otherwise.  Names are
+// string literals: a kernel's name, or "phase:..." for a phase of main.cpp's
+// BENCHMARK breakdown (main.cpp:907-922).
+struct GevTimed {
+  gev_ctx *ctx;
+  long idx = -1;
+  GevTimed(gev_ctx *c, const char *name);
+  ~GevTimed() { stop(); }
+  void stop();  // ends the region before the scope does
+  GevTimed(const GevTimed &) = delete;
+  GevTimed &operator=(const GevTimed &) = delete;
+};
 
 struct gev_field {
   gev_ctx *ctx = nullptr;
@@ -280,8 +306,9 @@ __device__ __forceinline__ double wrap01_bits(double x) {
 
 // v * 2^-k rounded once to the nearest FP32 (ties to even): the int64 -> FP32
 // conversion rounds v, and the power-of-two factor is exact because the product
-// stays normal -- |RN(v)| lies in [1, 2^63] for v != 0, so for the deposit scales
-// -60 <= k <= 100 the result lies in [2^-100, 2^123].  One conversion and one
+// stays normal -- |RN(v)| lies in [1, 2^63] for v != 0, so for -64 <= k <= 126 the
+// result lies in [2^-126, 2^127].  The deposit scales keep k = kq + kg in [-64, 121]
+// (fx_group in gev_deposit_fx.cu).  One conversion and one
 // multiply; the same bits as building the float from v's leading bits with
 // integer instructions (about twenty a value), and 0.36 ms less per 512^3 cycle,
 // whose T00 + Tij gather converts seven sums a node.

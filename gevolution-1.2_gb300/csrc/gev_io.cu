@@ -611,6 +611,18 @@ int gev_checkpoint_save(gev_ctx *ctx, const char *path, gev_pcls *p, const gev_f
   return checkpoint_save(ctx, path, p, phi, chi, Bi, BiFT, a, tau, dtau, cycle, st, nullptr);
 }
 
+// reads one section through the host buffer without touching the device: true when
+// all its bytes are there and match its checksum
+static bool section_intact(FILE *f, const CkptSection &sec, void *buf, size_t bufbytes) {
+  Sum64 s;
+  for (uint64_t o = 0; o < sec.bytes; o += bufbytes) {
+    const size_t len = (size_t)(sec.bytes - o < bufbytes ? sec.bytes - o : bufbytes);
+    if (!get(f, (long long)(sec.offset + o), buf, len)) return false;
+    s.add(buf, len);
+  }
+  return s.acc == sec.checksum;
+}
+
 static int checkpoint_load(gev_ctx *ctx, const char *path, gev_pcls *p, gev_field *phi, gev_field *chi, gev_field *Bi,
                            gev_field *BiFT, int flags, gev_checkpoint_info *info, double *diag) {
   if (!ctx || !path || (p && p->ctx != ctx) || (phi && !field_shape(ctx, phi, GEV_FIELD_REAL, 1)) ||
@@ -632,6 +644,22 @@ static int checkpoint_load(gev_ctx *ctx, const char *path, gev_pcls *p, gev_fiel
   HostBuf stage_h;
   GEV_CHECK_CUDA(ctx, cudaMallocAsync(&stage_d.p, STAGE_BYTES, ctx->stream));
   GEV_CHECK_CUDA(ctx, cudaMallocHost(&stage_h.p, STAGE_BYTES));
+  // every section this load reads is checked first, so that a damaged or truncated
+  // file is refused before anything on the device is overwritten
+  {
+    bool ok = true;
+    if (p) ok = h.sec[SEC_PCLS].bytes == h.numpcl * sizeof(gev_part) &&
+                section_intact(F.f, h.sec[SEC_PCLS], stage_h.p, STAGE_BYTES);
+    gev_field *fl0[3] = {phi, chi, Bi};
+    for (int k = 0; ok && k < 3; ++k)
+      if (fl0[k] && h.sec[SEC_PHI + k].bytes) ok = section_intact(F.f, h.sec[SEC_PHI + k], stage_h.p, STAGE_BYTES);
+    if (ok && BiFT) {
+      const bool from_b = h.sec[SEC_BIFT].bytes == 0 || (flags & GEV_CKPT_FROM_B);
+      const CkptSection &sec = h.sec[from_b ? SEC_B : SEC_BIFT];
+      if (sec.bytes) ok = section_intact(F.f, sec, stage_h.p, STAGE_BYTES);
+    }
+    if (!ok) return gev_fail(ctx, GEV_EINVAL, "checkpoint_load: file damaged or truncated (nothing was loaded)");
+  }
   int rc;
   if (p) {
     Sum64 s;

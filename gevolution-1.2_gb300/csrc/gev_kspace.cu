@@ -266,6 +266,7 @@ int launch_kspace(gev_ctx *ctx, int op, const void *in, void *out, double p1, do
   const int threads = 256, blocks = grid_for(ctx, n, threads, 16);
   const T *gk2 = (const T *)ctx->d_gridk2;
   const C *ks = (const C *)ctx->d_kshift;
+  GevTimed tm_(ctx, op == 0 ? "k_poisson" : "k_kspace");
   switch (op) {
     case 0:
       k_poisson<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, (T)p1, (T)p2, make_kdim(N), n);
@@ -328,6 +329,7 @@ int gev_project_scalar_evolve_vector(gev_ctx *ctx, const gev_field *SijFT, gev_f
   const int N = ctx->N, NH = N / 2 + 1;
   const size_t n = (size_t)N * N * NH;
   const int blocks = grid_for(ctx, n, 256, 16);
+  GevTimed tm_(ctx, "k_project_evolve");
   if (ctx->prec == GEV_PREC_FP64)
     k_project_evolve<double><<<blocks, 256, 0, ctx->stream>>>(
         (const CT<double>::C *)SijFT->d, (CT<double>::C *)chiFT->d, (CT<double>::C *)BiFT->d,

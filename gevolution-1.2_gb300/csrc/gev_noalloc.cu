@@ -14,7 +14,11 @@
 // that loads the library holds that megabyte until the process exits.  In host
 // code the array's name is only a host-side stand-in, not a device address, so
 // the host side looks the device address up with cudaGetSymbolAddress, once per
-// device, with that device current, and passes it to the kernels.
+// device, with that device current, and passes it to the kernels.  CUDA loads
+// modules and kernels lazily (the default since CUDA 12.2), and loading places
+// the array and the kernels on the GPU, which allocates; the same set-up
+// therefore loads all three kernels (cudaFuncGetAttributes), so that no later
+// call, whatever its n or precision, loads anything.
 #include <mutex>
 
 #include "gev_internal.cuh"
@@ -105,10 +109,15 @@ extern "C" int gev_sum_noalloc(int device, const void *data, int precision, size
     std::lock_guard<std::mutex> lk(g_addr_mu);
     if (!g_addr[device]) {
       void *p = nullptr;
-      const cudaError_t e = cudaGetSymbolAddress(&p, g_sum_partials);
+      cudaFuncAttributes fa;
+      cudaError_t e = cudaFuncGetAttributes(&fa, k_sum_chunks<double>);
+      if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_sum_chunks<float>);
+      if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, k_sum_partials);
+      if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_sum_partials);
       if (e != cudaSuccess || !p) {
         if (errbuf && errbuf_len)
-          snprintf(errbuf, errbuf_len, "sum_noalloc: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+          snprintf(errbuf, errbuf_len, "sum_noalloc: set-up (kernel load / cudaGetSymbolAddress): %s",
+                   cudaGetErrorString(e));
         rc = GEV_ECUDA;
       } else {
         g_addr[device] = p;

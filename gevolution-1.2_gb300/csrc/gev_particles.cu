@@ -912,6 +912,7 @@ void free_arrays(PclsArrays &A) {
 int scan_cells(gev_ctx *ctx, gev_pcls *p) {
   const long C = (long)ctx->N * ctx->N * ctx->N;
   const long nb = (C + SCAN_TILE - 1) / SCAN_TILE;
+  GevTimed tm_(ctx, "k_scan");
   k_scan_reduce<<<(unsigned)nb, SCAN_T, 0, ctx->stream>>>(p->count, C, p->scan_tmp);
   GEV_LAUNCH_CHECK(ctx);
   k_scan_blocks<<<1, 1024, 0, ctx->stream>>>(p->scan_tmp, nb);
@@ -976,22 +977,28 @@ int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, 
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(maxbits_dev, 0, sizeof(unsigned long long), ctx->stream));
   const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
   if (ctx->prec == GEV_PREC_FP64) {
+    GevTimed tm_(ctx, "k_kick_drift");
     k_kick_drift<double, double><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, (const double *)phi->d,
                                                                   (const double *)chi->d, (const double *)Bi->d, pk, pd,
                                                                   maxbits_dev, nullptr, nullptr);
     GEV_LAUNCH_CHECK(ctx);
+    tm_.stop();
+    GevTimed tr_(ctx, "relink");
     return pcls_relink(ctx, p);
   }
   // mixed form: histogram in the update, then scan and one move (no ID order)
   const long C = (long)N * N * N;
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->count, 0, C * sizeof(uint32_t), ctx->stream));
+  GevTimed tm_(ctx, "k_kick_drift");
   k_kick_drift<float, float><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, (const float *)phi->d,
                                                               (const float *)chi->d, (const float *)Bi->d, pk, pd,
                                                               maxbits_dev, p->count, p->rank);
   GEV_LAUNCH_CHECK(ctx);
+  tm_.stop();
   if (p->n == 0) return GEV_OK;
   int rc = scan_cells(ctx, p);
   if (rc) return rc;
+  GevTimed tv_(ctx, "k_move");
   k_move<<<grid_for(ctx, (size_t)(p->n + 3) / 4, 256, 16), 256, 0, ctx->stream>>>(p->cur, p->alt, p->start, p->rank,
                                                                                   p->n);
   GEV_LAUNCH_CHECK(ctx);

@@ -80,6 +80,7 @@ int sum_async(gev_sim *s, const gev_field *f, double *dst_dev) {
   gev_ctx *ctx = s->ctx;
   const int nb = ctx->sms * 8;
   RC(ctx_ensure_red(ctx, (size_t)nb + 4));
+  GevTimed tm_(ctx, "k_sum_to");
   if (ctx->prec == GEV_PREC_FP64)
     k_sum_to<double><<<nb, 256, 0, ctx->stream>>>((const double *)f->d, f->comp_elems, ctx->d_red);
   else
@@ -196,8 +197,13 @@ int gev_sim_step_fields(gev_sim *s) {
   // stress-energy (main.cpp:378-450)
   // (projection_init + projection_*: the target is replaced, not zeroed and re-read)
   // (T00 and Tij read the same particles and phi: one sweep deposits both)
-  RC(projection_replace_t00_tij(ctx, s->pcls, s->source, s->Sij, a, s->phi));
-  if (st.vector_elliptic) RC(projection_replace(ctx, s->pcls, s->Bi, 1, 1., s->phi));
+  {
+    GevTimed tm_(ctx, "phase:projections");
+    RC(projection_replace_t00_tij(ctx, s->pcls, s->source, s->Sij, a, s->phi));
+    if (st.vector_elliptic) RC(projection_replace(ctx, s->pcls, s->Bi, 1, 1., s->phi));
+  }
+  // the rest of this part is main.cpp's gravity solver time (main.cpp:454-602)
+  GevTimed tm_solver(ctx, "phase:gravity solver");
   RC(sum_async(s, s->source, s->dev_words + 0));  // T00hom, main.cpp:459-463
 
   // phi (main.cpp:470-491)
@@ -260,8 +266,11 @@ int gev_sim_step_particles(gev_sim *s) {
   const int nf_kick = 1. / a_kick < st.z_relax + 1. ? 3 : 2;
   rk4bg(a, fourpiG, cm, 0.5 * dtau);
   const int nf_drift = 1. / a < st.z_relax + 1. ? 3 : 0;
-  RC(pcls_kick_drift_async(ctx, s->pcls, (dtau + st.dtau_old) / 2., a_kick, nf_kick, dtau, a, nf_drift, s->phi, s->chi,
-                           s->Bi, (unsigned long long *)(s->dev_words + 1)));
+  {
+    GevTimed tm_(ctx, "phase:update particles");
+    RC(pcls_kick_drift_async(ctx, s->pcls, (dtau + st.dtau_old) / 2., a_kick, nf_kick, dtau, a, nf_drift, s->phi,
+                             s->chi, s->Bi, (unsigned long long *)(s->dev_words + 1)));
+  }
   rk4bg(a, fourpiG, cm, 0.5 * dtau);
   GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(s->host_words, s->dev_words, 4 * sizeof(double), cudaMemcpyDeviceToHost,
                                       ctx->stream));

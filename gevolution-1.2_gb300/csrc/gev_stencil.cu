@@ -217,6 +217,7 @@ int gev_prepare_source_tensor(gev_ctx *ctx, const gev_field *phi, const gev_fiel
     return gev_fail(ctx, GEV_EINVAL, "prepare_source_tensor: phi (1 comp), Tij and Sij (6 comps) real fields");
   const size_t V = (size_t)ctx->N * ctx->N * ctx->N;
   const int blocks = grid_for(ctx, V, 256, 16);
+  GevTimed tm_(ctx, "k_source_tensor");
   if (ctx->prec == GEV_PREC_FP64)
     k_source_tensor<double><<<blocks, 256, 0, ctx->stream>>>((const double *)phi->d, (const double *)Tij->d,
                                                              (double *)Sij->d, coeff, ctx->N, lg_pow2(ctx->N),
@@ -241,6 +242,7 @@ int gev_prepare_source_scalar(gev_ctx *ctx, const gev_field *phi, const gev_fiel
     return gev_fail(ctx, GEV_EINVAL, "prepare_source_scalar: four 1-component real fields");
   const size_t V = (size_t)ctx->N * ctx->N * ctx->N;
   const int blocks = grid_for(ctx, V, 256, 16);
+  GevTimed tm_(ctx, "k_source_scalar");
   if (ctx->prec == GEV_PREC_FP64)
     k_source_scalar<double><<<blocks, 256, 0, ctx->stream>>>((const double *)phi->d, (const double *)chi->d,
                                                              (const double *)source->d, bgmodel, (double *)result->d,

@@ -42,6 +42,8 @@ _SIGS = {
     "gev_ctx_stream": [_vp, ctypes.POINTER(_vp)],
     "gev_ctx_info": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_size_t)],
     "gev_ctx_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
+    "gev_ctx_set_timing": [_vp, _i],
+    "gev_ctx_timing_report": [_vp, ctypes.c_char_p, ctypes.c_size_t, _i],
     "gev_ctx_fft_tiles": [_vp, ctypes.POINTER(_i)],
     "gev_ctx_set_fft_tiles": [_vp, ctypes.POINTER(_i)],
     "gev_field_create": [_vp, _i, _i, ctypes.POINTER(_vp)],
@@ -148,6 +150,21 @@ class Context:
         n = ctypes.c_longlong()
         _check(lib().gev_ctx_launch_count(self.handle, ctypes.byref(n)), self, "gev_ctx_launch_count")
         return n.value
+
+    def set_timing(self, on=True):
+        """Brackets the library's kernels and cycle phases with CUDA events (see timing())."""
+        _check(lib().gev_ctx_set_timing(self.handle, 1 if on else 0), self, "gev_ctx_set_timing")
+
+    def timing(self, reset=True):
+        """Device time per kernel / phase since the last reset: {name: (count, total_ms)}."""
+        buf = ctypes.create_string_buffer(1 << 16)
+        _check(lib().gev_ctx_timing_report(self.handle, buf, len(buf), 1 if reset else 0), self,
+               "gev_ctx_timing_report")
+        out = {}
+        for ln in buf.value.decode().splitlines():
+            name, cnt, ms = ln.split("\t")
+            out[name] = (int(cnt), float(ms))
+        return out
 
     def fft_tiles(self):
         """log2 of the lines a tile of the r2c rows, y, z and c2r rows FFT passes."""

@@ -67,6 +67,18 @@ const char *gev_ctx_last_error(gev_ctx *ctx);
 const char *gev_strerror(int status);
 /* count of kernels this library launched on the context since creation */
 int gev_ctx_launch_count(gev_ctx *ctx, long long *count);
+/* device timing, no counterpart in the reference's API: the reference's
+ * -DBENCHMARK build prints wall-time sums per phase of the main loop
+ * (main.cpp:907-922).  While timing is on, the library brackets each of its
+ * kernels, and each phase of gev_sim_step, with CUDA events on the context's
+ * stream.  gev_ctx_timing_report waits for the stream and writes one line per
+ * name, "name\tcount\ttotal_ms\n": kernel names (k_...) and the phases
+ * "phase:projections", "phase:gravity solver", "phase:fft" (every 3-D
+ * transform, inside the gravity solver) and "phase:update particles" (update_q
+ * and update_pos with the relink).  reset != 0 clears the sums.  Returns
+ * GEV_EINVAL if the report does not fit into len bytes (it is truncated). */
+int gev_ctx_set_timing(gev_ctx *ctx, int on);
+int gev_ctx_timing_report(gev_ctx *ctx, char *buf, size_t len, int reset);
 /* the FFT tile widths in use, log2 of the lines a tile, for the r2c rows, y, z and
  * c2r rows passes: in the mixed form each is chosen by timing its candidates once,
  * on the context's first transform; every width gives the same bits */
@@ -196,9 +208,12 @@ int gev_cross_spectrum(gev_ctx *ctx, const gev_field *f1, const gev_field *f2, d
  * with GEV_EINVAL.  On error a message goes to errbuf (may be NULL).
  *
  * Scratch: 1 MiB of partial sums in a static device array, held on every GPU
- * that loads the library until the process exits.  The first call on a device
- * looks up that array's device address (cudaGetSymbolAddress), so make it before
- * any stream capture.  All calls on a GPU share the one array: calls whose work
+ * that loads the library until the process exits.  The first call on a device,
+ * with any n and either precision, does all of the set-up: it loads the
+ * function's kernels and the array onto the GPU (CUDA loads modules lazily, and
+ * loading allocates) and looks up the array's device address
+ * (cudaGetSymbolAddress); later calls load and allocate nothing.  Make that first
+ * call before any stream capture.  All calls on a GPU share the one array: calls whose work
  * overlaps on that GPU (other streams, other host threads) race and must be
  * serialised by the caller.  Nothing in it has to start at zero. */
 #define GEV_SUM_NOALLOC_MAX_N 1073741824LL /* 2^30 values, e.g. one component of a 1024^3 field */

@@ -8,11 +8,13 @@
  * operation, which makes it bit-identical to gevolution.hpp compiled against the
  * single-rank LATfield2 shim under oracle/ref_shim (checked in tests/).
  */
+#define _POSIX_C_SOURCE 199309L
 #include "gev_oracle.h"
 
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #ifndef M_PI
 #define M_PI 3.14159265358979323846
@@ -42,7 +44,15 @@ static struct {
   cx *tw;
 } g_tw[TWCACHE];
 
+static const cx *twiddles_locked(int L);
+/* the cache is shared by the threads of the parallel FFT loops below */
 static const cx *twiddles(int L) {
+  const cx *t;
+#pragma omp critical(gevo_twiddles)
+  t = twiddles_locked(L);
+  return t;
+}
+static const cx *twiddles_locked(int L) {
   for (int i = 0; i < TWCACHE; i++)
     if (g_tw[i].L == L) return g_tw[i].tw;
   int slot = -1;
@@ -94,40 +104,58 @@ static void fft_rec(int L, int L0, const cx *in, long is, cx *out, const cx *tw,
   }
 }
 
+/* one line with a given twiddle table and a caller-owned scratch of L values */
+static void fft1d_tw(int L, cx *data, int sign, const cx *tw, cx *scratch) {
+  memcpy(scratch, data, sizeof(cx) * (size_t)L);
+  fft_rec(L, L, scratch, 1, data, tw, sign);
+}
+
 void gevo_fft1d(int L, double *data, int sign) {
   const cx *tw = twiddles(L);
   cx *in = (cx *)malloc(sizeof(cx) * (size_t)L);
-  memcpy(in, data, sizeof(cx) * (size_t)L);
-  fft_rec(L, L, in, 1, (cx *)data, tw, sign);
+  fft1d_tw(L, (cx *)data, sign, tw, in);
   free(in);
 }
+
+/* The 3-D transforms run their independent lines on OpenMP threads (when built
+ * with -fopenmp).  Each line is transformed by the same code on the same values
+ * whichever thread takes it, so the result does not depend on the thread count. */
 
 /* r2c along x, then c2c along y and z (unnormalised, FFTW sign). */
 void gevo_fft_r2c(int N, const double *in, double *outd) {
   const int NH = N / 2 + 1;
   cx *out = (cx *)outd;
-  cx *line = (cx *)malloc(sizeof(cx) * (size_t)N);
-  for (long z = 0; z < N; z++)
-    for (long y = 0; y < N; y++) {
+  const cx *tw = twiddles(N);
+#pragma omp parallel
+  {
+    cx *line = (cx *)malloc(sizeof(cx) * (size_t)N);
+    cx *scr = (cx *)malloc(sizeof(cx) * (size_t)N);
+#pragma omp for schedule(static)
+    for (long zy = 0; zy < (long)N * N; zy++) {
+      const long z = zy / N, y = zy % N;
       const double *src = in + (size_t)N * (y + (size_t)N * z);
       for (int x = 0; x < N; x++) line[x] = C(src[x], 0.0);
-      gevo_fft1d(N, (double *)line, -1);
+      fft1d_tw(N, line, -1, tw, scr);
       cx *dst = out + (size_t)NH * (y + (size_t)N * z);
       for (int k = 0; k < NH; k++) dst[k] = line[k];
     }
-  for (long z = 0; z < N; z++)
-    for (long kx = 0; kx < NH; kx++) {
-      for (long y = 0; y < N; y++) line[y] = out[kx + NH * (y + (size_t)N * z)];
-      gevo_fft1d(N, (double *)line, -1);
-      for (long y = 0; y < N; y++) out[kx + NH * (y + (size_t)N * z)] = line[y];
-    }
-  for (long y = 0; y < N; y++)
-    for (long kx = 0; kx < NH; kx++) {
-      for (long z = 0; z < N; z++) line[z] = out[kx + NH * (y + (size_t)N * z)];
-      gevo_fft1d(N, (double *)line, -1);
-      for (long z = 0; z < N; z++) out[kx + NH * (y + (size_t)N * z)] = line[z];
-    }
-  free(line);
+#pragma omp for schedule(static)
+    for (long z = 0; z < N; z++)
+      for (long kx = 0; kx < NH; kx++) {
+        for (long y = 0; y < N; y++) line[y] = out[kx + NH * (y + (size_t)N * z)];
+        fft1d_tw(N, line, -1, tw, scr);
+        for (long y = 0; y < N; y++) out[kx + NH * (y + (size_t)N * z)] = line[y];
+      }
+#pragma omp for schedule(static)
+    for (long y = 0; y < N; y++)
+      for (long kx = 0; kx < NH; kx++) {
+        for (long z = 0; z < N; z++) line[z] = out[kx + NH * (y + (size_t)N * z)];
+        fft1d_tw(N, line, -1, tw, scr);
+        for (long z = 0; z < N; z++) out[kx + NH * (y + (size_t)N * z)] = line[z];
+      }
+    free(scr);
+    free(line);
+  }
 }
 
 /* c2c along z and y (inverse) into a copy, then c2r along x; input untouched.
@@ -138,31 +166,40 @@ void gevo_fft_c2r(int N, const double *ind, double *out) {
   const size_t n = (size_t)N * N * NH;
   cx *tmp = (cx *)malloc(sizeof(cx) * n);
   memcpy(tmp, ind, sizeof(cx) * n);
-  cx *line = (cx *)malloc(sizeof(cx) * (size_t)N);
-  for (long y = 0; y < N; y++)
-    for (long kx = 0; kx < NH; kx++) {
-      for (long z = 0; z < N; z++) line[z] = tmp[kx + NH * (y + (size_t)N * z)];
-      gevo_fft1d(N, (double *)line, +1);
-      for (long z = 0; z < N; z++) tmp[kx + NH * (y + (size_t)N * z)] = line[z];
-    }
-  for (long z = 0; z < N; z++)
-    for (long kx = 0; kx < NH; kx++) {
-      for (long y = 0; y < N; y++) line[y] = tmp[kx + NH * (y + (size_t)N * z)];
-      gevo_fft1d(N, (double *)line, +1);
-      for (long y = 0; y < N; y++) tmp[kx + NH * (y + (size_t)N * z)] = line[y];
-    }
-  for (long z = 0; z < N; z++)
-    for (long y = 0; y < N; y++) {
+  const cx *tw = twiddles(N);
+#pragma omp parallel
+  {
+    cx *line = (cx *)malloc(sizeof(cx) * (size_t)N);
+    cx *scr = (cx *)malloc(sizeof(cx) * (size_t)N);
+#pragma omp for schedule(static)
+    for (long y = 0; y < N; y++)
+      for (long kx = 0; kx < NH; kx++) {
+        for (long z = 0; z < N; z++) line[z] = tmp[kx + NH * (y + (size_t)N * z)];
+        fft1d_tw(N, line, +1, tw, scr);
+        for (long z = 0; z < N; z++) tmp[kx + NH * (y + (size_t)N * z)] = line[z];
+      }
+#pragma omp for schedule(static)
+    for (long z = 0; z < N; z++)
+      for (long kx = 0; kx < NH; kx++) {
+        for (long y = 0; y < N; y++) line[y] = tmp[kx + NH * (y + (size_t)N * z)];
+        fft1d_tw(N, line, +1, tw, scr);
+        for (long y = 0; y < N; y++) tmp[kx + NH * (y + (size_t)N * z)] = line[y];
+      }
+#pragma omp for schedule(static)
+    for (long zy = 0; zy < (long)N * N; zy++) {
+      const long z = zy / N, y = zy % N;
       const cx *src = tmp + (size_t)NH * (y + (size_t)N * z);
       for (int k = 0; k < NH; k++) line[k] = src[k];
       line[0].im = 0.0;
       line[N / 2].im = 0.0;
       for (int k = 1; k < N / 2; k++) line[N - k] = cconj(src[k]);
-      gevo_fft1d(N, (double *)line, +1);
+      fft1d_tw(N, line, +1, tw, scr);
       double *dst = out + (size_t)N * (y + (size_t)N * z);
       for (int x = 0; x < N; x++) dst[x] = line[x].re;
     }
-  free(line);
+    free(scr);
+    free(line);
+  }
   free(tmp);
 }
 
@@ -186,6 +223,7 @@ void gevo_kspace_tables(int N, double *gridk2, double *kshift) {
   double *gk2 = (double *)malloc(sizeof(double) * N);                 \
   cx *ks = (cx *)malloc(sizeof(cx) * N);                              \
   gevo_kspace_tables(N, gk2, (double *)ks);                           \
+  _Pragma("omp parallel for schedule(static)")                        \
   for (long kz = 0; kz < N; kz++)                                     \
     for (long ky = 0; ky < N; ky++)                                   \
       for (long kx = 0; kx < NH; kx++) {                              \
@@ -361,6 +399,7 @@ static inline size_t SI(int N, int x, int y, int z) {
  * Sij may be the same array as Tij. */
 void gevo_prepare_source_tensor(int N, const double *phi, const double *T, double *S, double coeff) {
   const size_t V = (size_t)N * N * N;
+#pragma omp parallel for schedule(static)
   for (int z = 0; z < N; z++)
     for (int y = 0; y < N; y++)
       for (int x = 0; x < N; x++) {
@@ -410,6 +449,7 @@ void gevo_prepare_source_tensor(int N, const double *phi, const double *T, doubl
 void gevo_prepare_source_scalar(int N, const double *phi, const double *chi, const double *source,
                                 double bgmodel, double *result, double coeff, double coeff2,
                                 double coeff3) {
+#pragma omp parallel for schedule(static)
   for (int z = 0; z < N; z++)
     for (int y = 0; y < N; y++)
       for (int x = 0; x < N; x++) {
@@ -449,28 +489,53 @@ void gevo_wrap(double *p) {
   }
 }
 
-static int g_sortN;
 static long cell_index(int N, const gevo_part *q) {
   return (long)gevo_cell_of(N, q->pos[0]) +
          (long)N * ((long)gevo_cell_of(N, q->pos[1]) + (long)N * (long)gevo_cell_of(N, q->pos[2]));
 }
-static int cmp_part(const void *a, const void *b) {
+static int cmp_id(const void *a, const void *b) {
   const gevo_part *p = (const gevo_part *)a, *q = (const gevo_part *)b;
-  long ca = cell_index(g_sortN, p), cb = cell_index(g_sortN, q);
-  if (ca != cb) return ca < cb ? -1 : 1;
-  if (p->ID != q->ID) return p->ID < q->ID ? -1 : 1;
-  return 0;
+  return p->ID < q->ID ? -1 : (p->ID > q->ID ? 1 : 0);
 }
 
+/* (cell, ID) order: a stable counting sort by cell, then each cell's run sorted
+ * by ID (insertion sort; qsort for long runs).  IDs are unique, so the order is
+ * a total order and does not depend on how it is reached. */
 void gevo_sort(int N, long np, gevo_part *p, long *cell_start) {
-  g_sortN = N;
-  qsort(p, (size_t)np, sizeof(gevo_part), cmp_part);
-  if (cell_start) {
-    const long V = (long)N * N * N;
-    for (long c = 0; c <= V; c++) cell_start[c] = 0;
-    for (long i = 0; i < np; i++) cell_start[cell_index(N, p + i) + 1]++;
-    for (long c = 0; c < V; c++) cell_start[c + 1] += cell_start[c];
+  const long V = (long)N * N * N;
+  long *cs = cell_start ? cell_start : (long *)malloc(sizeof(long) * (size_t)(V + 1));
+  long *key = (long *)malloc(sizeof(long) * (size_t)(np > 0 ? np : 1));
+  long *fill = (long *)malloc(sizeof(long) * (size_t)V);
+  gevo_part *tmp = (gevo_part *)malloc(sizeof(gevo_part) * (size_t)(np > 0 ? np : 1));
+#pragma omp parallel for schedule(static)
+  for (long i = 0; i < np; i++) key[i] = cell_index(N, p + i);
+  for (long c = 0; c <= V; c++) cs[c] = 0;
+  for (long i = 0; i < np; i++) cs[key[i] + 1]++;
+  for (long c = 0; c < V; c++) cs[c + 1] += cs[c];
+  memcpy(fill, cs, sizeof(long) * (size_t)V);
+  for (long i = 0; i < np; i++) tmp[fill[key[i]]++] = p[i];
+#pragma omp parallel for schedule(dynamic, 4096)
+  for (long c = 0; c < V; c++) {
+    const long b = cs[c], e = cs[c + 1];
+    if (e - b > 64) {
+      qsort(tmp + b, (size_t)(e - b), sizeof(gevo_part), cmp_id);
+      continue;
+    }
+    for (long i = b + 1; i < e; i++) {
+      const gevo_part t = tmp[i];
+      long j = i - 1;
+      while (j >= b && tmp[j].ID > t.ID) {
+        tmp[j + 1] = tmp[j];
+        j--;
+      }
+      tmp[j + 1] = t;
+    }
   }
+  memcpy(p, tmp, sizeof(gevo_part) * (size_t)np);
+  free(tmp);
+  free(fill);
+  free(key);
+  if (!cell_start) free(cs);
 }
 
 /* ===================================================================== */
@@ -487,6 +552,7 @@ static void ext_open(ext_t *E, int N, const double *f) {
   E->M = N + 1;
   const size_t M = (size_t)E->M;
   E->e = (double *)calloc(M * M * M, sizeof(double));
+#pragma omp parallel for schedule(static)
   for (int z = 0; z < N; z++)
     for (int y = 0; y < N; y++)
       for (int x = 0; x < N; x++) E->e[x + M * (y + M * z)] = f[SI(N, x, y, z)];
@@ -495,15 +561,20 @@ static inline double *EX(ext_t *E, int x, int y, int z) {
   const size_t M = (size_t)E->M;
   return E->e + x + M * (y + M * (size_t)z);
 }
-/* the *_comm halo fold (x, then y, then z) and write-back */
+/* the *_comm halo fold (x, then y, then z) and write-back; within one fold every
+ * statement adds one halo value into one interior value */
 static void ext_close(ext_t *E, double *f) {
   const int N = E->N;
+#pragma omp parallel for schedule(static)
   for (int z = 0; z <= N; z++)
     for (int y = 0; y <= N; y++) *EX(E, 0, y, z) += *EX(E, N, y, z);
+#pragma omp parallel for schedule(static)
   for (int z = 0; z <= N; z++)
     for (int x = 0; x < N; x++) *EX(E, x, 0, z) += *EX(E, x, N, z);
+#pragma omp parallel for schedule(static)
   for (int y = 0; y < N; y++)
     for (int x = 0; x < N; x++) *EX(E, x, y, 0) += *EX(E, x, y, N);
+#pragma omp parallel for schedule(static)
   for (int z = 0; z < N; z++)
     for (int y = 0; y < N; y++)
       for (int x = 0; x < N; x++) f[SI(N, x, y, z)] = *EX(E, x, y, z);
@@ -526,7 +597,117 @@ static void local_cube_phi(int N, const double *phi, int x, int y, int z, double
   l[7] = phi[SI(N, x + 1, y + 1, z + 1)];
 }
 
-/* projection_T00_project, gevolution.hpp:926-1022, + scalarProjectionCIC_comm */
+/* The deposits run over chunks of z planes on OpenMP threads, in two phases per
+ * chunk.  (1) Each nonempty cell's sums over its particles (the reference's
+ * local cube) are formed into a buffer, one cell per iteration.  (2) Each
+ * target plane t of the field with the upper halo is owned by one thread, which
+ * adds to it first the upper halves (corners at z + 1) of the cells of plane
+ * t - 1 and then the lower halves of the cells of plane t, each in site order.
+ * One loop over all cells in site order adds to every field value in exactly
+ * that order (a cell adds at most once to any one value), so the sums do not
+ * depend on the thread count. */
+typedef struct {
+  int N;
+  double dx, a, mass;
+  const gevo_part *p;
+  const long *cs;
+  const double *phi;
+  ext_t *E;
+} dep_t;
+typedef void (*dep_cell_fn)(const dep_t *D, long c, int x, int y, int z, double *out);
+typedef void (*dep_half_fn)(const dep_t *D, const double *v, int x, int y, int t);
+
+static void dep_run(const dep_t *D, int nv, dep_cell_fn cell, dep_half_fn lower, dep_half_fn upper) {
+  const int N = D->N;
+  const long P = (long)N * N;
+  long pl = (1L << 20) / P;
+  const int zc = pl < 1 ? 1 : (pl > N ? N : (int)pl);
+  /* slot s holds cell plane z0 - 1 + s */
+  double *buf = (double *)malloc(sizeof(double) * (size_t)nv * (size_t)P * (size_t)(zc + 1));
+  for (int z0 = 0; z0 < N; z0 += zc) {
+    const int z1 = z0 + zc < N ? z0 + zc : N;
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (long k = 0; k < P * (z1 - z0); k++) {
+      const long c = P * z0 + k;
+      if (D->cs[c + 1] == D->cs[c]) continue;
+      cell(D, c, (int)(c % N), (int)((c / N) % N), (int)(c / P), buf + (size_t)nv * (size_t)(P + k));
+    }
+    const int tend = z1 == N ? N + 1 : z1;
+#pragma omp parallel for schedule(static, 1)
+    for (int t = z0; t < tend; t++) {
+      if (t >= 1) {
+        const int zc_ = t - 1;
+        const double *slot = buf + (size_t)nv * (size_t)P * (size_t)(zc_ - (z0 - 1));
+        for (long k = 0; k < P; k++) {
+          const long c = P * zc_ + k;
+          if (D->cs[c + 1] == D->cs[c]) continue;
+          upper(D, slot + (size_t)nv * k, (int)(k % N), (int)(k / N), t);
+        }
+      }
+      if (t < N) {
+        const double *slot = buf + (size_t)nv * (size_t)P * (size_t)(t - (z0 - 1));
+        for (long k = 0; k < P; k++) {
+          const long c = P * t + k;
+          if (D->cs[c + 1] == D->cs[c]) continue;
+          lower(D, slot + (size_t)nv * k, (int)(k % N), (int)(k / N), t);
+        }
+      }
+    }
+    /* the last plane of the chunk feeds the next chunk's first target plane */
+    memcpy(buf, buf + (size_t)nv * (size_t)P * (size_t)(z1 - z0), sizeof(double) * (size_t)nv * (size_t)P);
+  }
+  free(buf);
+}
+
+/* ---- projection_T00_project, gevolution.hpp:926-1022, + scalarProjectionCIC_comm ---- */
+static void t00_cell(const dep_t *D, long c, int x, int y, int z, double *lc) {
+  const int N = D->N;
+  const double dx = D->dx, a = D->a;
+  const gevo_part *p = D->p;
+  const double ref[3] = {x * dx, y * dx, z * dx};
+  double e = a, f = 0., l[8];
+  for (int i = 0; i < 8; i++) lc[i] = 0.;
+  local_cube_phi(N, D->phi, x, y, z, l);
+  for (long j = D->cs[c]; j < D->cs[c + 1]; j++) {
+    double up[3], dn[3];
+    for (int i = 0; i < 3; i++) {
+      up[i] = (p[j].pos[i] - ref[i]) / dx;
+      dn[i] = 1.0 - up[i];
+    }
+    if (D->phi) {
+      const double *q = p[j].vel;
+      f = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+      e = sqrt(f + a * a);
+      f = 3. * e + f / e;
+    }
+    lc[0] += dn[0] * dn[1] * dn[2] * (e + f * l[0]);
+    lc[1] += dn[0] * dn[1] * up[2] * (e + f * l[1]);
+    lc[2] += dn[0] * up[1] * dn[2] * (e + f * l[2]);
+    lc[3] += dn[0] * up[1] * up[2] * (e + f * l[3]);
+    lc[4] += up[0] * dn[1] * dn[2] * (e + f * l[4]);
+    lc[5] += up[0] * dn[1] * up[2] * (e + f * l[5]);
+    lc[6] += up[0] * up[1] * dn[2] * (e + f * l[6]);
+    lc[7] += up[0] * up[1] * up[2] * (e + f * l[7]);
+  }
+}
+/* the eight corner sums times the mass factor; lower: corners 0 2 4 6 at z = t */
+static void cic8_lower(const dep_t *D, const double *lc, int x, int y, int t) {
+  ext_t *E = D->E;
+  const double mass = D->mass;
+  *EX(E, x, y, t) += lc[0] * mass;
+  *EX(E, x, y + 1, t) += lc[2] * mass;
+  *EX(E, x + 1, y, t) += lc[4] * mass;
+  *EX(E, x + 1, y + 1, t) += lc[6] * mass;
+}
+static void cic8_upper(const dep_t *D, const double *lc, int x, int y, int t) {
+  ext_t *E = D->E;
+  const double mass = D->mass;
+  *EX(E, x, y, t) += lc[1] * mass;
+  *EX(E, x, y + 1, t) += lc[3] * mass;
+  *EX(E, x + 1, y, t) += lc[5] * mass;
+  *EX(E, x + 1, y + 1, t) += lc[7] * mass;
+}
+
 void gevo_deposit_T00(int N, long np, const gevo_part *p, const long *cs, double m, double a,
                       const double *phi, double coeff, double *T00) {
   (void)np;
@@ -536,91 +717,99 @@ void gevo_deposit_T00(int N, long np, const gevo_part *p, const long *cs, double
   mass /= a;
   ext_t E;
   ext_open(&E, N, T00);
-  double e = a, f = 0.;
-  for (int z = 0; z < N; z++)
-    for (int y = 0; y < N; y++)
-      for (int x = 0; x < N; x++) {
-        const long c = x + (long)N * (y + (long)N * z);
-        if (cs[c + 1] == cs[c]) continue;
-        const double ref[3] = {x * dx, y * dx, z * dx};
-        double lc[8] = {0, 0, 0, 0, 0, 0, 0, 0}, l[8];
-        local_cube_phi(N, phi, x, y, z, l);
-        for (long j = cs[c]; j < cs[c + 1]; j++) {
-          double up[3], dn[3];
-          for (int i = 0; i < 3; i++) {
-            up[i] = (p[j].pos[i] - ref[i]) / dx;
-            dn[i] = 1.0 - up[i];
-          }
-          if (phi) {
-            const double *q = p[j].vel;
-            f = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-            e = sqrt(f + a * a);
-            f = 3. * e + f / e;
-          }
-          lc[0] += dn[0] * dn[1] * dn[2] * (e + f * l[0]);
-          lc[1] += dn[0] * dn[1] * up[2] * (e + f * l[1]);
-          lc[2] += dn[0] * up[1] * dn[2] * (e + f * l[2]);
-          lc[3] += dn[0] * up[1] * up[2] * (e + f * l[3]);
-          lc[4] += up[0] * dn[1] * dn[2] * (e + f * l[4]);
-          lc[5] += up[0] * dn[1] * up[2] * (e + f * l[5]);
-          lc[6] += up[0] * up[1] * dn[2] * (e + f * l[6]);
-          lc[7] += up[0] * up[1] * up[2] * (e + f * l[7]);
-        }
-        *EX(&E, x, y, z) += lc[0] * mass;
-        *EX(&E, x, y, z + 1) += lc[1] * mass;
-        *EX(&E, x, y + 1, z) += lc[2] * mass;
-        *EX(&E, x, y + 1, z + 1) += lc[3] * mass;
-        *EX(&E, x + 1, y, z) += lc[4] * mass;
-        *EX(&E, x + 1, y, z + 1) += lc[5] * mass;
-        *EX(&E, x + 1, y + 1, z) += lc[6] * mass;
-        *EX(&E, x + 1, y + 1, z + 1) += lc[7] * mass;
-      }
+  const dep_t D = {N, dx, a, mass, p, cs, phi, &E};
+  dep_run(&D, 8, t00_cell, cic8_lower, cic8_upper);
   ext_close(&E, T00);
 }
 
-/* scalarProjectionCIC_project (LATfield2, used by main.cpp:402 and
- * ic_basic.hpp:2180): plain CIC mass deposit m/dx^3 * w, + comm fold */
+/* ---- scalarProjectionCIC_project (LATfield2, used by main.cpp:402 and
+ * ic_basic.hpp:2180): plain CIC mass deposit m/dx^3 * w, + comm fold ---- */
+static void mass_cell(const dep_t *D, long c, int x, int y, int z, double *lc) {
+  const double dx = D->dx;
+  const gevo_part *p = D->p;
+  const double ref[3] = {x * dx, y * dx, z * dx};
+  for (int i = 0; i < 8; i++) lc[i] = 0.;
+  for (long j = D->cs[c]; j < D->cs[c + 1]; j++) {
+    double up[3], dn[3];
+    for (int i = 0; i < 3; i++) {
+      up[i] = (p[j].pos[i] - ref[i]) / dx;
+      dn[i] = 1.0 - up[i];
+    }
+    lc[0] += dn[0] * dn[1] * dn[2];
+    lc[1] += dn[0] * dn[1] * up[2];
+    lc[2] += dn[0] * up[1] * dn[2];
+    lc[3] += dn[0] * up[1] * up[2];
+    lc[4] += up[0] * dn[1] * dn[2];
+    lc[5] += up[0] * dn[1] * up[2];
+    lc[6] += up[0] * up[1] * dn[2];
+    lc[7] += up[0] * up[1] * up[2];
+  }
+}
+
 void gevo_deposit_mass(int N, long np, const gevo_part *p, const long *cs, double m, double *rho) {
   (void)np;
   const double dx = 1.0 / (double)N;
   const double mass = m / (dx * dx * dx);
   ext_t E;
   ext_open(&E, N, rho);
-  for (int z = 0; z < N; z++)
-    for (int y = 0; y < N; y++)
-      for (int x = 0; x < N; x++) {
-        const long c = x + (long)N * (y + (long)N * z);
-        if (cs[c + 1] == cs[c]) continue;
-        const double ref[3] = {x * dx, y * dx, z * dx};
-        double lc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-        for (long j = cs[c]; j < cs[c + 1]; j++) {
-          double up[3], dn[3];
-          for (int i = 0; i < 3; i++) {
-            up[i] = (p[j].pos[i] - ref[i]) / dx;
-            dn[i] = 1.0 - up[i];
-          }
-          lc[0] += dn[0] * dn[1] * dn[2];
-          lc[1] += dn[0] * dn[1] * up[2];
-          lc[2] += dn[0] * up[1] * dn[2];
-          lc[3] += dn[0] * up[1] * up[2];
-          lc[4] += up[0] * dn[1] * dn[2];
-          lc[5] += up[0] * dn[1] * up[2];
-          lc[6] += up[0] * up[1] * dn[2];
-          lc[7] += up[0] * up[1] * up[2];
-        }
-        *EX(&E, x, y, z) += lc[0] * mass;
-        *EX(&E, x, y, z + 1) += lc[1] * mass;
-        *EX(&E, x, y + 1, z) += lc[2] * mass;
-        *EX(&E, x, y + 1, z + 1) += lc[3] * mass;
-        *EX(&E, x + 1, y, z) += lc[4] * mass;
-        *EX(&E, x + 1, y, z + 1) += lc[5] * mass;
-        *EX(&E, x + 1, y + 1, z) += lc[6] * mass;
-        *EX(&E, x + 1, y + 1, z + 1) += lc[7] * mass;
-      }
+  const dep_t D = {N, dx, 1., mass, p, cs, NULL, &E};
+  dep_run(&D, 8, mass_cell, cic8_lower, cic8_upper);
   ext_close(&E, rho);
 }
 
-/* projection_T0i_project, gevolution.hpp:1045-1147, + vectorProjectionCICNGP_comm */
+/* ---- projection_T0i_project, gevolution.hpp:1045-1147, + vectorProjectionCICNGP_comm ----
+ * per cell: the 12 link sums, then the 8 corner values of phi */
+static void t0i_cell(const dep_t *D, long c, int x, int y, int z, double *qi) {
+  const double dx = D->dx, mass = D->mass;
+  const gevo_part *p = D->p;
+  const double ref[3] = {x * dx, y * dx, z * dx};
+  for (int i = 0; i < 12; i++) qi[i] = 0.;
+  local_cube_phi(D->N, D->phi, x, y, z, qi + 12);
+  for (long j = D->cs[c]; j < D->cs[c + 1]; j++) {
+    double up[3], dn[3];
+    for (int i = 0; i < 3; i++) {
+      up[i] = (p[j].pos[i] - ref[i]) / dx;
+      dn[i] = 1.0 - up[i];
+    }
+    const double *q = p[j].vel;
+    double w = mass * q[0];
+    qi[0] += w * dn[1] * dn[2];
+    qi[1] += w * up[1] * dn[2];
+    qi[2] += w * dn[1] * up[2];
+    qi[3] += w * up[1] * up[2];
+    w = mass * q[1];
+    qi[4] += w * dn[0] * dn[2];
+    qi[5] += w * up[0] * dn[2];
+    qi[6] += w * dn[0] * up[2];
+    qi[7] += w * up[0] * up[2];
+    w = mass * q[2];
+    qi[8] += w * dn[0] * dn[1];
+    qi[9] += w * up[0] * dn[1];
+    qi[10] += w * dn[0] * up[1];
+    qi[11] += w * up[0] * up[1];
+  }
+}
+static void t0i_lower(const dep_t *D, const double *qi, int x, int y, int t) {
+  ext_t *E = D->E;
+  const double *l = qi + 12;
+  *EX(&E[0], x, y, t) += qi[0] * (1. + l[0] + l[4]);
+  *EX(&E[1], x, y, t) += qi[4] * (1. + l[0] + l[2]);
+  *EX(&E[2], x, y, t) += qi[8] * (1. + l[0] + l[1]);
+  *EX(&E[1], x + 1, y, t) += qi[5] * (1. + l[4] + l[6]);
+  *EX(&E[2], x + 1, y, t) += qi[9] * (1. + l[4] + l[5]);
+  *EX(&E[0], x, y + 1, t) += qi[1] * (1. + l[2] + l[6]);
+  *EX(&E[2], x, y + 1, t) += qi[10] * (1. + l[2] + l[3]);
+  *EX(&E[2], x + 1, y + 1, t) += qi[11] * (1. + l[6] + l[7]);
+}
+static void t0i_upper(const dep_t *D, const double *qi, int x, int y, int t) {
+  ext_t *E = D->E;
+  const double *l = qi + 12;
+  *EX(&E[0], x, y, t) += qi[2] * (1. + l[1] + l[5]);
+  *EX(&E[1], x, y, t) += qi[6] * (1. + l[1] + l[3]);
+  *EX(&E[0], x, y + 1, t) += qi[3] * (1. + l[3] + l[7]);
+  *EX(&E[1], x + 1, y, t) += qi[7] * (1. + l[5] + l[7]);
+}
+
 void gevo_deposit_T0i(int N, long np, const gevo_part *p, const long *cs, double m,
                       const double *phi, double coeff, double *T0i) {
   (void)np;
@@ -630,54 +819,77 @@ void gevo_deposit_T0i(int N, long np, const gevo_part *p, const long *cs, double
   mass *= m;
   ext_t E[3];
   for (int c = 0; c < 3; c++) ext_open(&E[c], N, T0i + c * V);
-  for (int z = 0; z < N; z++)
-    for (int y = 0; y < N; y++)
-      for (int x = 0; x < N; x++) {
-        const long c = x + (long)N * (y + (long)N * z);
-        if (cs[c + 1] == cs[c]) continue;
-        const double ref[3] = {x * dx, y * dx, z * dx};
-        double qi[12] = {0}, l[8];
-        local_cube_phi(N, phi, x, y, z, l);
-        for (long j = cs[c]; j < cs[c + 1]; j++) {
-          double up[3], dn[3];
-          for (int i = 0; i < 3; i++) {
-            up[i] = (p[j].pos[i] - ref[i]) / dx;
-            dn[i] = 1.0 - up[i];
-          }
-          const double *q = p[j].vel;
-          double w = mass * q[0];
-          qi[0] += w * dn[1] * dn[2];
-          qi[1] += w * up[1] * dn[2];
-          qi[2] += w * dn[1] * up[2];
-          qi[3] += w * up[1] * up[2];
-          w = mass * q[1];
-          qi[4] += w * dn[0] * dn[2];
-          qi[5] += w * up[0] * dn[2];
-          qi[6] += w * dn[0] * up[2];
-          qi[7] += w * up[0] * up[2];
-          w = mass * q[2];
-          qi[8] += w * dn[0] * dn[1];
-          qi[9] += w * up[0] * dn[1];
-          qi[10] += w * dn[0] * up[1];
-          qi[11] += w * up[0] * up[1];
-        }
-        *EX(&E[0], x, y, z) += qi[0] * (1. + l[0] + l[4]);
-        *EX(&E[1], x, y, z) += qi[4] * (1. + l[0] + l[2]);
-        *EX(&E[2], x, y, z) += qi[8] * (1. + l[0] + l[1]);
-        *EX(&E[1], x + 1, y, z) += qi[5] * (1. + l[4] + l[6]);
-        *EX(&E[2], x + 1, y, z) += qi[9] * (1. + l[4] + l[5]);
-        *EX(&E[0], x, y + 1, z) += qi[1] * (1. + l[2] + l[6]);
-        *EX(&E[2], x, y + 1, z) += qi[10] * (1. + l[2] + l[3]);
-        *EX(&E[0], x, y, z + 1) += qi[2] * (1. + l[1] + l[5]);
-        *EX(&E[1], x, y, z + 1) += qi[6] * (1. + l[1] + l[3]);
-        *EX(&E[0], x, y + 1, z + 1) += qi[3] * (1. + l[3] + l[7]);
-        *EX(&E[1], x + 1, y, z + 1) += qi[7] * (1. + l[5] + l[7]);
-        *EX(&E[2], x + 1, y + 1, z) += qi[11] * (1. + l[6] + l[7]);
-      }
+  const dep_t D = {N, dx, 1., mass, p, cs, phi, E};
+  dep_run(&D, 20, t0i_cell, t0i_lower, t0i_upper);
   for (int c = 0; c < 3; c++) ext_close(&E[c], T0i + c * V);
 }
 
-/* projection_Tij_project, gevolution.hpp:1172-1297, + symtensorProjectionCICNGP_comm */
+/* ---- projection_Tij_project, gevolution.hpp:1172-1297, + symtensorProjectionCICNGP_comm ----
+ * component slots: 0=00 1=01 2=02 3=11 4=12 5=22; per cell: the 6 plaquette
+ * sums, then the 24 diagonal corner sums */
+static const int tij_diag[3] = {0, 3, 5};
+static void tij_cell(const dep_t *D, long c, int x, int y, int z, double *tij) {
+  const double dx = D->dx, a = D->a, mass = D->mass;
+  const gevo_part *p = D->p;
+  const double ref[3] = {(double)x * dx, (double)y * dx, (double)z * dx};
+  double *tii = tij + 6, l[8];
+  for (int i = 0; i < 30; i++) tij[i] = 0.;
+  local_cube_phi(D->N, D->phi, x, y, z, l);
+  for (long j = D->cs[c]; j < D->cs[c + 1]; j++) {
+    double up[3], dn[3];
+    for (int i = 0; i < 3; i++) {
+      up[i] = (p[j].pos[i] - ref[i]) / dx;
+      dn[i] = 1.0 - up[i];
+    }
+    const double *q = p[j].vel;
+    double f = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
+    const double e = sqrt(f + a * a);
+    f = 4. + a * a / (f + a * a);
+    for (int i = 0; i < 3; i++) {
+      const double w = mass * q[i] * q[i] / e;
+      tii[0 + i * 8] += w * dn[0] * dn[1] * dn[2] * (1. + f * l[0]);
+      tii[1 + i * 8] += w * dn[0] * dn[1] * up[2] * (1. + f * l[1]);
+      tii[2 + i * 8] += w * dn[0] * up[1] * dn[2] * (1. + f * l[2]);
+      tii[3 + i * 8] += w * dn[0] * up[1] * up[2] * (1. + f * l[3]);
+      tii[4 + i * 8] += w * up[0] * dn[1] * dn[2] * (1. + f * l[4]);
+      tii[5 + i * 8] += w * up[0] * dn[1] * up[2] * (1. + f * l[5]);
+      tii[6 + i * 8] += w * up[0] * up[1] * dn[2] * (1. + f * l[6]);
+      tii[7 + i * 8] += w * up[0] * up[1] * up[2] * (1. + f * l[7]);
+    }
+    double w = mass * q[0] * q[1] / e;
+    tij[0] += w * dn[2] * (1. + f * 0.25 * (l[0] + l[2] + l[4] + l[6]));
+    tij[1] += w * up[2] * (1. + f * 0.25 * (l[1] + l[3] + l[5] + l[7]));
+    w = mass * q[0] * q[2] / e;
+    tij[2] += w * dn[1] * (1. + f * 0.25 * (l[0] + l[1] + l[4] + l[5]));
+    tij[3] += w * up[1] * (1. + f * 0.25 * (l[2] + l[3] + l[6] + l[7]));
+    w = mass * q[1] * q[2] / e;
+    tij[4] += w * dn[0] * (1. + f * 0.25 * (l[0] + l[1] + l[2] + l[3]));
+    tij[5] += w * up[0] * (1. + f * 0.25 * (l[4] + l[5] + l[6] + l[7]));
+  }
+}
+static void tij_lower(const dep_t *D, const double *tij, int x, int y, int t) {
+  ext_t *E = D->E;
+  const double *tii = tij + 6;
+  for (int i = 0; i < 3; i++) *EX(&E[tij_diag[i]], x, y, t) += tii[8 * i];
+  *EX(&E[1], x, y, t) += tij[0];
+  *EX(&E[2], x, y, t) += tij[2];
+  *EX(&E[4], x, y, t) += tij[4];
+  for (int i = 0; i < 3; i++) *EX(&E[tij_diag[i]], x + 1, y, t) += tii[4 + 8 * i];
+  *EX(&E[4], x + 1, y, t) += tij[5];
+  for (int i = 0; i < 3; i++) *EX(&E[tij_diag[i]], x, y + 1, t) += tii[2 + 8 * i];
+  *EX(&E[2], x, y + 1, t) += tij[3];
+  for (int i = 0; i < 3; i++) *EX(&E[tij_diag[i]], x + 1, y + 1, t) += tii[6 + 8 * i];
+}
+static void tij_upper(const dep_t *D, const double *tij, int x, int y, int t) {
+  ext_t *E = D->E;
+  const double *tii = tij + 6;
+  for (int i = 0; i < 3; i++) *EX(&E[tij_diag[i]], x, y, t) += tii[1 + 8 * i];
+  *EX(&E[1], x, y, t) += tij[1];
+  for (int i = 0; i < 3; i++) *EX(&E[tij_diag[i]], x + 1, y, t) += tii[5 + 8 * i];
+  for (int i = 0; i < 3; i++) *EX(&E[tij_diag[i]], x, y + 1, t) += tii[3 + 8 * i];
+  for (int i = 0; i < 3; i++) *EX(&E[tij_diag[i]], x + 1, y + 1, t) += tii[7 + 8 * i];
+}
+
 void gevo_deposit_Tij(int N, long np, const gevo_part *p, const long *cs, double m, double a,
                       const double *phi, double coeff, double *Tij) {
   (void)np;
@@ -686,64 +898,10 @@ void gevo_deposit_Tij(int N, long np, const gevo_part *p, const long *cs, double
   double mass = coeff / (dx * dx * dx);
   mass *= m;
   mass /= a;
-  /* component slots: 0=00 1=01 2=02 3=11 4=12 5=22 */
-  static const int diag[3] = {0, 3, 5};
   ext_t E[6];
   for (int c = 0; c < 6; c++) ext_open(&E[c], N, Tij + c * V);
-  for (int z = 0; z < N; z++)
-    for (int y = 0; y < N; y++)
-      for (int x = 0; x < N; x++) {
-        const long c = x + (long)N * (y + (long)N * z);
-        if (cs[c + 1] == cs[c]) continue;
-        const double ref[3] = {(double)x * dx, (double)y * dx, (double)z * dx};
-        double tij[6] = {0}, tii[24] = {0}, l[8];
-        local_cube_phi(N, phi, x, y, z, l);
-        for (long j = cs[c]; j < cs[c + 1]; j++) {
-          double up[3], dn[3];
-          for (int i = 0; i < 3; i++) {
-            up[i] = (p[j].pos[i] - ref[i]) / dx;
-            dn[i] = 1.0 - up[i];
-          }
-          const double *q = p[j].vel;
-          double f = q[0] * q[0] + q[1] * q[1] + q[2] * q[2];
-          const double e = sqrt(f + a * a);
-          f = 4. + a * a / (f + a * a);
-          for (int i = 0; i < 3; i++) {
-            const double w = mass * q[i] * q[i] / e;
-            tii[0 + i * 8] += w * dn[0] * dn[1] * dn[2] * (1. + f * l[0]);
-            tii[1 + i * 8] += w * dn[0] * dn[1] * up[2] * (1. + f * l[1]);
-            tii[2 + i * 8] += w * dn[0] * up[1] * dn[2] * (1. + f * l[2]);
-            tii[3 + i * 8] += w * dn[0] * up[1] * up[2] * (1. + f * l[3]);
-            tii[4 + i * 8] += w * up[0] * dn[1] * dn[2] * (1. + f * l[4]);
-            tii[5 + i * 8] += w * up[0] * dn[1] * up[2] * (1. + f * l[5]);
-            tii[6 + i * 8] += w * up[0] * up[1] * dn[2] * (1. + f * l[6]);
-            tii[7 + i * 8] += w * up[0] * up[1] * up[2] * (1. + f * l[7]);
-          }
-          double w = mass * q[0] * q[1] / e;
-          tij[0] += w * dn[2] * (1. + f * 0.25 * (l[0] + l[2] + l[4] + l[6]));
-          tij[1] += w * up[2] * (1. + f * 0.25 * (l[1] + l[3] + l[5] + l[7]));
-          w = mass * q[0] * q[2] / e;
-          tij[2] += w * dn[1] * (1. + f * 0.25 * (l[0] + l[1] + l[4] + l[5]));
-          tij[3] += w * up[1] * (1. + f * 0.25 * (l[2] + l[3] + l[6] + l[7]));
-          w = mass * q[1] * q[2] / e;
-          tij[4] += w * dn[0] * (1. + f * 0.25 * (l[0] + l[1] + l[2] + l[3]));
-          tij[5] += w * up[0] * (1. + f * 0.25 * (l[4] + l[5] + l[6] + l[7]));
-        }
-        for (int i = 0; i < 3; i++) *EX(&E[diag[i]], x, y, z) += tii[8 * i];
-        *EX(&E[1], x, y, z) += tij[0];
-        *EX(&E[2], x, y, z) += tij[2];
-        *EX(&E[4], x, y, z) += tij[4];
-        for (int i = 0; i < 3; i++) *EX(&E[diag[i]], x + 1, y, z) += tii[4 + 8 * i];
-        *EX(&E[4], x + 1, y, z) += tij[5];
-        for (int i = 0; i < 3; i++) *EX(&E[diag[i]], x, y + 1, z) += tii[2 + 8 * i];
-        *EX(&E[2], x, y + 1, z) += tij[3];
-        for (int i = 0; i < 3; i++) *EX(&E[diag[i]], x, y, z + 1) += tii[1 + 8 * i];
-        *EX(&E[1], x, y, z + 1) += tij[1];
-        for (int i = 0; i < 3; i++) *EX(&E[diag[i]], x + 1, y + 1, z) += tii[6 + 8 * i];
-        for (int i = 0; i < 3; i++) *EX(&E[diag[i]], x + 1, y, z + 1) += tii[5 + 8 * i];
-        for (int i = 0; i < 3; i++) *EX(&E[diag[i]], x, y + 1, z + 1) += tii[3 + 8 * i];
-        for (int i = 0; i < 3; i++) *EX(&E[diag[i]], x + 1, y + 1, z + 1) += tii[7 + 8 * i];
-      }
+  const dep_t D = {N, dx, a, mass, p, cs, phi, E};
+  dep_run(&D, 30, tij_cell, tij_lower, tij_upper);
   for (int c = 0; c < 6; c++) ext_close(&E[c], Tij + c * V);
 }
 
@@ -946,6 +1104,8 @@ double gevo_kick(int N, long np, gevo_part *p, int kind, double dtau, const doub
                  const double *chi, const double *Bi, int nfield, double a, double a2N) {
   const double params[2] = {a, a2N};
   double vmax = 0.;
+  /* particles are independent and the maximum does not depend on the order */
+#pragma omp parallel for schedule(static) reduction(max : vmax)
   for (long j = 0; j < np; j++) {
     int c[3];
     double r[3];
@@ -962,6 +1122,7 @@ void gevo_drift(int N, long np, gevo_part *p, int kind, double dtau, const doubl
                 const double *chi, const double *Bi, int nfield, double a, double a2N,
                 long *cell_start) {
   const double params[2] = {a, a2N};
+#pragma omp parallel for schedule(static)
   for (long j = 0; j < np; j++) {
     if (kind == 0) {
       int c[3];
@@ -973,6 +1134,7 @@ void gevo_drift(int N, long np, gevo_part *p, int kind, double dtau, const doubl
       for (int l = 0; l < 3; l++) p[j].pos[l] += dtau * p[j].vel[l] / params[0];
     }
   }
+#pragma omp parallel for schedule(static)
   for (long j = 0; j < np; j++)
     for (int l = 0; l < 3; l++) gevo_wrap(&p[j].pos[l]);
   gevo_sort(N, np, p, cell_start);
@@ -1048,15 +1210,25 @@ double gevo_next_dtau(const gevo_sim *s) {
   return s->steplimit / H;
 }
 
-/* main.cpp:372-879 for CDM only, GR, no outputs */
-int gevo_sim_step(gevo_sim *s) {
+static double wall_s(void) {
+  struct timespec t;
+  clock_gettime(CLOCK_MONOTONIC, &t);
+  return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+/* main.cpp:372-598 for CDM only, GR: the stress-energy deposits and the phi, chi
+ * and B solves.  Timed into t_phase as main.cpp's BENCHMARK build times them
+ * (projection_time 372-453, gravity_solver_time 454-602 with fft_time and
+ * fft_count for the transforms). */
+int gevo_sim_step_fields(gevo_sim *s) {
   const int N = s->N;
   const size_t V = (size_t)N * N * N;
   const size_t K = (size_t)N * N * (N / 2 + 1) * 2;
   const double dx = 1.0 / (double)N;
   const gevo_cosmo *cm = &s->cosmo;
   const double fourpiG = s->fourpiG;
-  double a = s->a;
+  const double a = s->a;
+  double t0 = wall_s(), t1;
 
   memset(s->source, 0, V * sizeof(double));
   gevo_deposit_T00(N, s->np, s->p, s->cell_start, s->mass, a, s->phi, 1., s->source);
@@ -1066,43 +1238,74 @@ int gevo_sim_step(gevo_sim *s) {
   }
   memset(s->Sij, 0, 6 * V * sizeof(double));
   gevo_deposit_Tij(N, s->np, s->p, s->cell_start, s->mass, a, s->phi, 1., s->Sij);
+  t1 = wall_s();
+  s->t_phase[0] += t1 - t0;
+  t0 = t1;
 
   double T00hom = 0.;
   for (size_t i = 0; i < V; i++) T00hom += s->source[i];
   T00hom /= (double)V;
   s->T00hom = T00hom;
 
+  double tf = 0.;
+#define GEVO_FFT(call)      \
+  do {                      \
+    const double f0 = wall_s(); \
+    call;                   \
+    tf += wall_s() - f0;    \
+  } while (0)
   if (s->dtau_old > 0.) {
     const double H = gevo_hconf(a, fourpiG, cm);
     gevo_prepare_source_scalar(N, s->phi, s->chi, s->source, cm->Omega_cdm + cm->Omega_b, s->source,
                                3. * H * dx * dx / s->dtau_old, fourpiG * dx * dx / a,
                                3. * H * H * dx * dx);
-    gevo_fft_r2c(N, s->source, s->scalarFT);
+    GEVO_FFT(gevo_fft_r2c(N, s->source, s->scalarFT));
     gevo_poisson(N, s->scalarFT, s->scalarFT, 1. / (dx * dx), 3. * H / s->dtau_old);
-    gevo_fft_c2r(N, s->scalarFT, s->phi);
+    GEVO_FFT(gevo_fft_c2r(N, s->scalarFT, s->phi));
+    s->fft_count += 2;
   }
   s->phik0 = s->scalarFT[0];
 
   gevo_prepare_source_tensor(N, s->phi, s->Sij, s->Sij, 2. * fourpiG * dx * dx / a);
-  for (int c = 0; c < 6; c++) gevo_fft_r2c(N, s->Sij + c * V, s->SijFT + c * K);
+  GEVO_FFT(for (int c = 0; c < 6; c++) gevo_fft_r2c(N, s->Sij + c * V, s->SijFT + c * K));
   gevo_project_scalar(N, s->SijFT, s->scalarFT, 0);
-  gevo_fft_c2r(N, s->scalarFT, s->chi);
+  GEVO_FFT(gevo_fft_c2r(N, s->scalarFT, s->chi));
+  s->fft_count += 7;
 
   if (s->vector_elliptic) {
-    for (int c = 0; c < 3; c++) gevo_fft_r2c(N, s->Bi + c * V, s->BiFT + c * K);
+    GEVO_FFT(for (int c = 0; c < 3; c++) gevo_fft_r2c(N, s->Bi + c * V, s->BiFT + c * K));
     gevo_project_vector(N, s->BiFT, s->BiFT, fourpiG * dx * dx, 0.);
+    s->fft_count += 1;
   } else {
     gevo_evolve_vector(N, s->SijFT, s->BiFT, a * a * s->dtau_old);
   }
-  for (int c = 0; c < 3; c++) gevo_fft_c2r(N, s->BiFT + c * K, s->Bi + c * V);
+  GEVO_FFT(for (int c = 0; c < 3; c++) gevo_fft_c2r(N, s->BiFT + c * K, s->Bi + c * V));
+  s->fft_count += 3;
+#undef GEVO_FFT
+  t1 = wall_s();
+  s->t_phase[1] += t1 - t0;
+  s->t_phase[2] += tf;
+  return 0;
+}
 
-  /* particle update, main.cpp:764-822 */
+/* main.cpp:743-872: the kick (update_q_time), the background half step, the
+ * drift with the relink (moveParts_time), the second half step and the next dtau */
+int gevo_sim_step_particles(gevo_sim *s) {
+  const int N = s->N;
+  const gevo_cosmo *cm = &s->cosmo;
+  const double fourpiG = s->fourpiG;
+  double a = s->a;
   const double dtau = s->dtau;
+  double t0 = wall_s(), t1;
   double maxvel = gevo_kick(N, s->np, s->p, 0, (dtau + s->dtau_old) / 2., s->phi, s->chi, s->Bi,
                             (1. / a < s->z_relax + 1. ? 3 : 2), a, a * a * N);
+  t1 = wall_s();
+  s->t_phase[3] += t1 - t0;
   gevo_rk4bg(&a, fourpiG, cm, 0.5 * dtau);
+  t0 = wall_s();
   gevo_drift(N, s->np, s->p, 0, dtau, s->phi, s->chi, s->Bi, (1. / a < s->z_relax + 1. ? 3 : 0), a,
              a * a * N, s->cell_start);
+  s->t_phase[4] += wall_s() - t0;
   gevo_rk4bg(&a, fourpiG, cm, 0.5 * dtau);
   maxvel /= sqrt(maxvel * maxvel + 1.0);
   s->maxvel = maxvel;
@@ -1112,4 +1315,10 @@ int gevo_sim_step(gevo_sim *s) {
   s->dtau = gevo_next_dtau(s);
   s->cycle++;
   return 0;
+}
+
+/* main.cpp:372-879 for CDM only, GR, no outputs */
+int gevo_sim_step(gevo_sim *s) {
+  gevo_sim_step_fields(s);
+  return gevo_sim_step_particles(s);
 }

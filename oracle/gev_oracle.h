@@ -110,6 +110,12 @@ typedef struct {
   gevo_cosmo cosmo;
   int vector_elliptic;
   int cycle;
+  /* wall time in seconds of the phases of main.cpp's BENCHMARK breakdown
+   * (main.cpp:907-922), summed over cycles: [0] projections, [1] gravity solver,
+   * [2] thereof FFTs, [3] update momenta, [4] move particles; fft_count counts the
+   * 3-D transforms as main.cpp does */
+  double t_phase[5];
+  long fft_count;
 } gevo_sim;
 
 int gevo_sim_alloc(gevo_sim *s, int N, long np);
@@ -117,6 +123,11 @@ void gevo_sim_free(gevo_sim *s);
 /* one cycle of the main loop body (GR): deposits, phi/chi/B solves, kick, drift,
  * background, next dtau.  Returns 0. */
 int gevo_sim_step(gevo_sim *s);
+/* the same cycle in two parts, for a loop that takes spectra where main.cpp
+ * writes them: main.cpp:372-598 (deposits, phi, chi, B) and main.cpp:743-872
+ * (kick, background, drift, next dtau) */
+int gevo_sim_step_fields(gevo_sim *s);
+int gevo_sim_step_particles(gevo_sim *s);
 double gevo_next_dtau(const gevo_sim *s);
 
 /* ---- initial conditions (restating the mPk path of ic_basic.hpp) ----

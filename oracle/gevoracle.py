@@ -41,7 +41,11 @@ class SimStruct(ctypes.Structure):
         (n, _dp) for n in ("phi", "chi", "source", "Sij", "Bi", "scalarFT", "SijFT", "BiFT")] + [
         (n, ctypes.c_double) for n in ("a", "tau", "dtau", "dtau_old", "fourpiG", "Cf", "steplimit", "z_relax",
                                        "maxvel", "T00hom", "phik0")] + [
-        ("cosmo", Cosmo), ("vector_elliptic", ctypes.c_int), ("cycle", ctypes.c_int)]
+        ("cosmo", Cosmo), ("vector_elliptic", ctypes.c_int), ("cycle", ctypes.c_int),
+        ("t_phase", ctypes.c_double * 5), ("fft_count", ctypes.c_long)]
+
+# the phases of main.cpp's BENCHMARK breakdown (main.cpp:907-922), in t_phase order
+PHASES = ("projections", "gravity solver", "thereof FFTs", "update momenta", "move particles")
 
 
 def build(force=False):
@@ -50,10 +54,12 @@ def build(force=False):
     return so
 
 
-def build_ref():
-    """Builds oracle/_ref/libgevref.so from the reference sources when they exist."""
-    src = os.environ.get("GEV_REFERENCE_SRC", "/root/reference")
-    if not os.path.exists(os.path.join(src, "gevolution.hpp")):
+def build_ref(src=None):
+    """Builds oracle/_ref/ from the gevolution-1.2 source tree: `src`, else the
+    GEV_REFERENCE_SRC environment variable.  Returns None when neither names a tree
+    holding gevolution.hpp (the libraries already built under _ref/ stay usable)."""
+    src = src or os.environ.get("GEV_REFERENCE_SRC")
+    if not src or not os.path.exists(os.path.join(src, "gevolution.hpp")):
         return None
     subprocess.run(["make", "-s", "-C", HERE, "ref", "REF_SRC=" + src], check=True)
     return os.path.join(HERE, "_ref", "libgevref.so")
@@ -353,6 +359,20 @@ class Sim:
             lib().gevo_sim_step(ctypes.byref(self.s))
         else:
             impl.gevref_sim_step(ctypes.byref(self.s))
+
+    def step_fields(self):
+        """main.cpp:372-598: deposits and the phi, chi, B solves."""
+        lib().gevo_sim_step_fields(ctypes.byref(self.s))
+
+    def step_particles(self):
+        """main.cpp:743-872: kick, background, drift, next dtau."""
+        lib().gevo_sim_step_particles(ctypes.byref(self.s))
+
+    def phase_seconds(self):
+        """Wall seconds per phase of main.cpp's BENCHMARK breakdown, summed over cycles."""
+        out = {k: float(self.s.t_phase[i]) for i, k in enumerate(PHASES)}
+        out["fft_count"] = int(self.s.fft_count)
+        return out
 
     # views onto the state
     def _arr(self, name, shape, dtype):

@@ -1,9 +1,9 @@
 """Generates the golden vectors in tests/golden/ from gevolution 1.2's own
 gevolution.hpp / background.hpp compiled against the single-rank LATfield2 shim
-(oracle/_ref/libgevref.so, built by `make -C oracle ref` where the reference
-sources are present).
+(oracle/_ref/libgevref.so, built by `make -C oracle ref REF_SRC=<tree>`, or here
+from the tree that GEV_REFERENCE_SRC names).
 
-    python tests/golden/make_golden.py
+    GEV_REFERENCE_SRC=<gevolution-1.2 source tree> python tests/golden/make_golden.py
 
     python tests/golden/make_golden.py gadget     # only the Gadget-2 files
     python tests/golden/make_golden.py spectra    # only the power spectra

@@ -246,6 +246,12 @@ def test_damaged_hibernation_files_are_refused(gpu, tmp_path):
         gpu.Sim(gpu.Context(16, gpu.PREC_FP64), 16 ** 3).restart(path)
     s2.restart(path)  # the intact file still loads
     assert os.path.getsize(path) == len(raw)
+    # a refused load leaves the store and the fields as they were
+    before = (s2.particles().download().tobytes(), s2.field("phi").download().tobytes())
+    open(bad, "wb").write(flipped)
+    with pytest.raises(gpu.GevError):
+        s2.restart(bad)
+    assert (s2.particles().download().tobytes(), s2.field("phi").download().tobytes()) == before
 
 
 def pinned(gpu, n):

@@ -47,10 +47,35 @@ def test_two_ranks_take_the_slowest_time():
     assert all(abs(r[4] - 64 ** 3 * 5 * 2 / 0.020) < 1e-6 * r[4] for r in res)
 
 
-def test_replicas_get_distinct_seeds():
+def seed_worker(rank, world, port, out):
+    import torch.distributed as dist
     sys.path.insert(0, ROOT)
     import bench
-    # run_ours seeds rank r's replica with seed + 1000 r: independent simulations, no collective on the data path
-    src = open(os.path.join(ROOT, "bench.py")).read()
-    assert "seed=args.seed + 1000 * rank" in src
+    dist.init_process_group("gloo", rank=rank, world_size=world, init_method="tcp://127.0.0.1:%d" % port)
+    import torch
+    seeds = [torch.zeros(1, dtype=torch.int64) for _ in range(world)]
+    dist.all_gather(seeds, torch.tensor([bench.replica_seed(1, rank)], dtype=torch.int64))
+    out.put((rank, [int(t.item()) for t in seeds]))
+    dist.destroy_process_group()
+
+
+def test_replicas_get_distinct_seeds():
+    """Each rank's replica is an independent simulation: the seeds the ranks derive
+    (gathered over two gloo ranks) differ, and the aggregate is linear in the ranks."""
+    torch = pytest.importorskip("torch")
+    sys.path.insert(0, ROOT)
+    import bench
+    mp = torch.multiprocessing.get_context("spawn")
+    q = mp.Queue()
+    port = free_port()
+    procs = [mp.Process(target=seed_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    seeds = res[0][1]
+    assert res[1][1] == seeds and len(set(seeds)) == 2
+    assert len({bench.replica_seed(1, r) for r in range(8)}) == 8
     assert bench.aggregate_value(512, 20, 8, 40.0) == 8 * bench.aggregate_value(512, 20, 1, 40.0)

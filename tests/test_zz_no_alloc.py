@@ -38,8 +38,9 @@ def test_sum_noalloc_matches_field_sum_two_calls(gpu, prec):
     err = ctypes.create_string_buffer(256)
     out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda:0")
     rng = np.random.default_rng(11 + prec)
-    # first call: one component of a 96^3 field (106 partial sums); second call: a 24^3 field (2 partial sums)
-    for N, ncomp, comp in ((96, 3, 2), (24, 1, 0)):
+    # first call: one component of a 96^3 field (108 whole chunks of 8192 values); second: a
+    # 100^3 field (123 chunks, the last one partial); third: a 24^3 field (2 chunks, one partial)
+    for N, ncomp, comp in ((96, 3, 2), (100, 1, 0), (24, 1, 0)):
         ctx = gpu.Context(N, prec)
         x = 0.25 + rng.standard_normal((ncomp, N, N, N))
         f = ctx.real(ncomp).upload(x)
