@@ -218,3 +218,20 @@ int gevo_write_power_spectrum(const double *kbin, const double *power, const dou
   free(power2);
   return 0;
 }
+
+/* hibernate's rescale of B before it is written (hibernation.hpp:529-538, the
+ * parabolic vector method): every component divided by a^2 N */
+void gevo_hibernate_b(int N, double *Bi, double a) {
+  const size_t n = 3 * (size_t)N * N * N;
+  for (size_t i = 0; i < n; i++) Bi[i] /= a * a * N;
+}
+
+/* readIC's restart of the vector potential from the stored B (ic_read.hpp:307-318):
+ * every component multiplied by a^2 / (numpts * numpts), an int product, then the
+ * forward transform (plan_Bi->execute(FFT_FORWARD)) into BiFT.  B is modified. */
+void gevo_restart_bift_from_b(int N, double *Bi, double a, double *BiFT) {
+  const size_t V = (size_t)N * N * N;
+  const size_t K = (size_t)N * N * (N / 2 + 1) * 2;
+  for (size_t i = 0; i < 3 * V; i++) Bi[i] *= a * a / (N * N);
+  for (int c = 0; c < 3; c++) gevo_fft_r2c(N, Bi + c * V, BiFT + c * K);
+}

@@ -193,6 +193,13 @@ int gevo_gadget2_save(const char *fname, int N, long np, const gevo_part *p, con
  * returns their number or -1 */
 long gevo_gadget2_load(const char *fname, int N, gevo_part *dst, long cap, void *hdr256, int id_bytes);
 
+/* hibernation of B and its restart (the parabolic vector method): hibernate
+ * divides B by a^2 N before writing it (hibernation.hpp:529-538); readIC multiplies
+ * the stored B by a^2 / (N N) and transforms it forward into BiFT
+ * (ic_read.hpp:307-318).  Both modify Bi (3 components). */
+void gevo_hibernate_b(int N, double *Bi, double a);
+void gevo_restart_bift_from_b(int N, double *Bi, double a, double *BiFT);
+
 /* writePowerSpectrum (tools.hpp:268-345); exact = the EXACT_OUTPUT_REDSHIFTS build */
 int gevo_write_power_spectrum(const double *kbin, const double *power, const double *kscatter, const double *pscatter,
                               const int *occupation, int numbins, double rescalek, double rescalep,

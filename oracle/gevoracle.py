@@ -412,6 +412,28 @@ class Sim:
         return {k: getattr(c, k) for k, _ in Cosmo._fields_}
 
 
+# ------------------------------------------------------ hibernation of B --
+def hibernate_b(Bi, a):
+    """B as hibernate writes it: B / (a^2 N) (hibernation.hpp:529-538)."""
+    B = np.ascontiguousarray(Bi, np.float64).copy()
+    N = B.shape[-1]
+    L = lib()
+    L.gevo_hibernate_b.argtypes = [ctypes.c_int, _vp, ctypes.c_double]
+    L.gevo_hibernate_b(N, _p(B), a)
+    return B
+
+
+def restart_bift_from_b(B_stored, a):
+    """readIC's restart of BiFT from the stored B (ic_read.hpp:307-318)."""
+    B = np.ascontiguousarray(B_stored, np.float64).copy()
+    N = B.shape[-1]
+    F = np.zeros((3, N, N, N // 2 + 1), np.complex128)
+    L = lib()
+    L.gevo_restart_bift_from_b.argtypes = [ctypes.c_int, _vp, ctypes.c_double, _vp]
+    L.gevo_restart_bift_from_b(N, _p(B), a, _p(F))
+    return F
+
+
 # ------------------------------------------------------ Gadget-2 snapshots --
 _GADGET_REF = None
 

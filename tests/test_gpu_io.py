@@ -218,6 +218,40 @@ def test_restart_from_B_follows_readIC(gpu, tmp_path):
     assert np.array_equal(BiFT.download(), BiFT0)
 
 
+def test_restart_from_B_matches_the_oracle(gpu, oracle, tmp_path):
+    """The B-only restart against the oracle's restatement of hibernate's B / (a^2 N)
+    (hibernation.hpp:529-538) and readIC's a^2 / N^2 rescale and forward transform
+    (ic_read.hpp:307-318), then three more cycles on both from the restarted state:
+    BiFT to the FFTs' rounding, positions within 1e-9 of a cell, fields within 1e-10."""
+    N = 16
+    path = str(tmp_path / "hib")
+    o = oracle.Sim(N).ic(**oracle.default_icparams(N, 5.0 * N, seed=6))
+    for _ in range(3):
+        o.step()
+    c = gpu.Context(N, gpu.PREC_FP64)
+    s = gpu.Sim(c, N ** 3)
+    from z0_common import load_sim
+    load_sim(s, o)
+    s.hibernate(path)
+    a = o.s.a
+    s2 = gpu.Sim(gpu.Context(N, gpu.PREC_FP64), N ** 3)
+    s2.restart(path, flags=gpu.CKPT_FROM_B)
+    # the oracle restarts from the same stored B
+    want = oracle.restart_bift_from_b(oracle.hibernate_b(o.field("Bi"), a), a)
+    got = s2.field("BiFT").download()
+    assert np.abs(got - want).max() <= 2e-14 * np.abs(want).max()
+    o.spectrum("BiFT")[:] = want
+    for _ in range(3):
+        o.step()
+        s2.step()
+    g = s2.particles().download()
+    assert (g["ID"] == o.particles["ID"]).all()
+    assert np.abs(g["pos"] - o.particles["pos"]).max() * N < 1e-9
+    for name in ("phi", "chi", "Bi"):
+        ref = o.field(name)
+        assert np.abs(s2.field(name).download() - ref).max() <= 1e-10 * np.abs(ref).max(), name
+
+
 def test_damaged_hibernation_files_are_refused(gpu, tmp_path):
     N = 8
     path = str(tmp_path / "hib")
