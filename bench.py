@@ -634,7 +634,9 @@ def run_serve(args, gpu):
     for r in burst:
         srv.submit(as_fp64(gpu, r))
     srv.drain(1800.0)
-    sres = [r for r in srv.poll(100000) if r["status"] == 0]
+    sall = srv.poll(100000)
+    sres = [r for r in sall if r["status"] == 0]
+    sfail = [{"N": r["N"], "status": r["status"]} for r in sall if r["status"] != 0]
     s_span = time.perf_counter() - t0
     srv.close()
     cap = len(bres) / b_span * 3600.0
@@ -664,7 +666,7 @@ def run_serve(args, gpu):
         "max_active_seen": st["max_active_seen"],
         "burst": {"requests": len(bres), "makespan_s": b_span, "sims_per_hour": cap,
                   "max_active_seen": bst["max_active_seen"]},
-        "sequential_fp64": {"requests": len(sres), "makespan_s": s_span, "sims_per_hour": seq_rate,
+        "sequential_fp64": {"requests": len(sres), "failed": sfail, "makespan_s": s_span, "sims_per_hour": seq_rate,
                             "note": "the burst's own requests in the plain FP64 form, run one at a time (a server "
                                     "with one slot) on the same GPU"},
         "capacity_vs_sequential_fp64": cap / seq_rate,

@@ -388,13 +388,162 @@ __global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArray
   }
 }
 
+// ------------------------------------------------------------ dense cells --
+// In a clustered state some cells hold hundreds of particles.  The gather walks a
+// cell once for each of its 8 corner nodes, and the 32 nodes of a warp walk cells
+// of very different sizes, so a dense cell costs 8 long walks at a small fraction
+// of the warp.  Cells with more than HEAVY_T particles are therefore summed once: a
+// warp per cell forms the same integer contributions the gather would form at the
+// cell's 8 corners (the same FP32 weight factors, rounded the same way) and adds
+// them; the gather adds these 38 sums instead of walking the cell.  Integer sums
+// do not depend on the order or grouping of the additions, so the result is the
+// same bits whichever cells take this path.
+//
+// Per dense cell, 38 int64 sums, corner k = dx + 2 dy + 4 dz of the cell:
+//   [k]          T00 at corner k
+//   [8 + 3k + c] the diagonal Tij_cc at corner k
+//   [32 + dz]    Tij_01 at corner (0, 0, dz)   (the plaquettes the gather's nodes own)
+//   [34 + dy]    Tij_02 at corner (0, dy, 0)
+//   [36 + dx]    Tij_12 at corner (dx, 0, 0)
+// A hash (open addressing, keys cell + 1) maps a dense cell to its slot.  When the
+// slots run out, the remaining dense cells are walked by the gather as before.
+constexpr uint32_t HEAVY_T = 8;
+constexpr int HEAVY_NS = 38;
+struct HeavyTab {
+  uint32_t *keys, *vals;  // hash: cell + 1 -> slot (0xffffffff: no slot)
+  uint32_t mask;          // hash size - 1 (a power of two)
+  uint32_t *list;         // slot -> cell
+  uint32_t *count;        // dense cells found (may exceed cap)
+  uint32_t cap;           // slots
+  long long *sums;        // slot * HEAVY_NS + index
+};
+__device__ __forceinline__ uint32_t heavy_hash(uint32_t c, uint32_t mask) { return (c * 2654435761u) & mask; }
+// the slot of dense cell c, or 0xffffffff (not inserted or no slot left)
+__device__ __forceinline__ uint32_t heavy_slot(const HeavyTab &H, uint32_t c) {
+  uint32_t h = heavy_hash(c, H.mask);
+  for (uint32_t probe = 0; probe <= H.mask; ++probe) {
+    const uint32_t k = H.keys[h];
+    if (k == c + 1u) return H.vals[h];
+    if (k == 0u) return 0xffffffffu;
+    h = (h + 1u) & H.mask;
+  }
+  return 0xffffffffu;
+}
+
+// every cell with more than HEAVY_T particles into the hash and, while slots last,
+// the list (the hash holds at least twice the most dense cells there can be)
+__global__ void __launch_bounds__(256) k_heavy_find(const uint32_t *__restrict__ start, unsigned C, HeavyTab H) {
+  for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
+    if (start[c + 1] - start[c] <= HEAVY_T) continue;
+    uint32_t h = heavy_hash(c, H.mask);
+    for (uint32_t probe = 0; probe <= H.mask; ++probe) {
+      if (atomicCAS(&H.keys[h], 0u, c + 1u) == 0u) {
+        const uint32_t slot = atomicAdd(H.count, 1u);
+        H.vals[h] = slot < H.cap ? slot : 0xffffffffu;
+        if (slot < H.cap) H.list[slot] = c;
+        break;
+      }
+      h = (h + 1u) & H.mask;
+    }
+  }
+}
+
+// One warp per dense cell: each lane takes every 32nd particle of the cell and forms
+// its contributions to the cell's 8 corners exactly as k_dep_gather's add() forms
+// them for a node, then the warp adds the lanes' int64 sums.
+template <int KIND>
+__global__ void __launch_bounds__(256) k_heavy_sums(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
+                                                    const float *__restrict__ phi, FxParams p, Div32 dN,
+                                                    const uint32_t *__restrict__ fxb, HeavyTab H) {
+  constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
+  const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
+  const int N = p.N;
+  const int lane = threadIdx.x & 31;
+  const uint32_t nheavy = min(*H.count, H.cap);
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nheavy; s += warps) {
+    const uint32_t c = H.list[s];
+    int x, y, z;
+    cell_xyz(c, N, p.lg, dN, x, y, z);
+    const Nb3 b = nb3(c, x, y, z, N);
+    // phi at the cell's 8 corners, f[dx + 2 dy + 4 dz]
+    float f[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const unsigned ik = c + ((k & 1) ? b.xp : 0u) + ((k & 2) ? b.yp : 0u) + ((k & 4) ? b.zp : 0u);
+      f[k] = phi != nullptr ? __ldg(&phi[ik]) : 0.f;
+    }
+    // the gather's plaquette sums at the corners that own them, in its order
+    float s01[2], s02[2], s12[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      s01[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[4 * d], f[2 + 4 * d]), f[1 + 4 * d]), f[3 + 4 * d]);
+      s02[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[2 * d], f[2 * d + 4]), f[1 + 2 * d]), f[1 + 2 * d + 4]);
+      s12[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[d], f[d + 4]), f[d + 2]), f[d + 6]);
+    }
+    long long acc[HEAVY_NS];
+#pragma unroll
+    for (int k = 0; k < HEAVY_NS; ++k) acc[k] = 0;
+    const uint32_t j0 = start[c], j1 = start[c + 1];
+    for (uint32_t j = j0 + lane; j < j1; j += 32) {
+      uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
+      if constexpr (KIND == FX_T00) {
+        const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
+        v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), q.x);
+        v1 = make_uint4(q.y, 0u, 0u, 0u);
+      } else {
+        const uint4 *rec = A.rec + 3 * (size_t)j;
+        v0 = __ldg(rec);
+        v1 = __ldg(rec + 1);
+        v2 = __ldg(rec + 2);
+      }
+      const float u0 = __uint_as_float(v0.x), u1 = __uint_as_float(v0.y), u2 = __uint_as_float(v0.z);
+      const float wl0[2] = {__fsub_rn(1.f, u0), u0}, wl1[2] = {__fsub_rn(1.f, u1), u1},
+                  wl2[2] = {__fsub_rn(1.f, u2), u2};
+      const float fT = __uint_as_float(v1.y), qf = __fmul_rn(0.25f, fT);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+        const float w = __fmul_rn(__fmul_rn(wl0[dx], wl1[dy]), wl2[dz]);
+        if (DO00)
+          acc[k] += (long long)(int)v0.w *
+                    (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), f[k]))), sg00);
+        if (DOIJ) {
+          const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(fT, f[k]))), sgij);
+          acc[8 + 3 * k] += (long long)(int)v1.z * G;
+          acc[9 + 3 * k] += (long long)(int)v1.w * G;
+          acc[10 + 3 * k] += (long long)(int)v2.x * G;
+        }
+      }
+      if (DOIJ) {
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+          acc[32 + d] += (long long)(int)v2.y * (long long)gq(__fmul_rn(wl2[d], __fadd_rn(1.f, __fmul_rn(qf, s01[d]))), sgij);
+          acc[34 + d] += (long long)(int)v2.z * (long long)gq(__fmul_rn(wl1[d], __fadd_rn(1.f, __fmul_rn(qf, s02[d]))), sgij);
+          acc[36 + d] += (long long)(int)v2.w * (long long)gq(__fmul_rn(wl0[d], __fadd_rn(1.f, __fmul_rn(qf, s12[d]))), sgij);
+        }
+      }
+    }
+    long long *out = H.sums + (size_t)s * HEAVY_NS;
+#pragma unroll
+    for (int k = 0; k < HEAVY_NS; ++k) {
+      if (!DO00 && k < 8) continue;
+      if (!DOIJ && k >= 8) continue;
+      long long v = acc[k];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) out[k] = v;
+    }
+  }
+}
+
 // one thread per node (x, y, z); out: T00 (1 comp) and / or Tij (6 comps, 00 01 02 11 12 22).
 // Six resident blocks per SM (40 registers; 48 and five blocks for T00 alone): the
 // loop is latency-bound, and the warps hide more than the few spilled words cost.
 template <int KIND>
 __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
                                                     const float *__restrict__ phi, float *t00, float *tij, FxParams p,
-                                                    Div32 dN, const uint32_t *__restrict__ fxb) {
+                                                    Div32 dN, const uint32_t *__restrict__ fxb, HeavyTab H) {
   constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
   const int ks00 = (int)fxb[2], ksij = KIND == FX_T00TIJ ? (int)fxb[3] : (int)fxb[2];
   const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
@@ -465,15 +614,37 @@ __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(Pcls
       s1[q] = start[cb[q]];
       s2[q] = start[cb[q] + 1];
     }
+    // a dense cell's sums at this node's corner of it, instead of its particles
+    auto heavy = [&](uint32_t cell, int dx, int dy, int dz) -> bool {
+      const uint32_t slot = heavy_slot(H, cell);
+      if (slot == 0xffffffffu) return false;
+      const long long *hs = H.sums + (size_t)slot * HEAVY_NS;
+      const int k = dx + 2 * dy + 4 * dz;
+      if (DO00) a00 += hs[k];
+      if (DOIJ) {
+        ad0 += hs[8 + 3 * k];
+        ad1 += hs[9 + 3 * k];
+        ad2 += hs[10 + 3 * k];
+        if (dx == 0 && dy == 0) ao01 += hs[32 + dz];
+        if (dx == 0 && dz == 0) ao02 += hs[34 + dy];
+        if (dy == 0 && dz == 0) ao12 += hs[36 + dx];
+      }
+      return true;
+    };
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int dy = q >> 1, dz = q & 1;
-      if (x > 0) {
+      // cell A = (x - 1, ...), whose corner (1, dy, dz) this node is; cell B = (x, ...), corner (0, dy, dz)
+      const uint32_t eA = x > 0 ? s1[q] : start[cb[q] + b.xm + 1];
+      const bool skipA = eA - s0[q] > HEAVY_T && heavy(cb[q] + b.xm, 1, dy, dz);
+      const bool skipB = s2[q] - s1[q] > HEAVY_T && heavy(cb[q], 0, dy, dz);
+      if (x > 0 && !skipA && !skipB) {
         for (uint32_t j = s0[q]; j < s2[q]; ++j) add(j, j < s1[q] ? 1 : 0, dy, dz);
       } else {
-        for (uint32_t j = s1[q]; j < s2[q]; ++j) add(j, 0, dy, dz);
-        const uint32_t t1 = start[cb[q] + b.xm + 1];
-        for (uint32_t j = s0[q]; j < t1; ++j) add(j, 1, dy, dz);
+        if (!skipB)
+          for (uint32_t j = s1[q]; j < s2[q]; ++j) add(j, 0, dy, dz);
+        if (!skipA)
+          for (uint32_t j = s0[q]; j < eA; ++j) add(j, 1, dy, dz);
       }
     }
     if (DO00) {
@@ -541,6 +712,43 @@ __global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, floa
 
 }  // namespace
 
+// The dense-cell table of a particle store, allocated on its first gather deposit:
+// slots for one dense cell per HEAVY_SLOT_PER particles (more dense cells fall back
+// to the walk), and a hash of at least twice the most dense cells there can be
+// (n / (HEAVY_T + 1)).  Cleared (keys and count) on every call.
+constexpr long HEAVY_SLOT_PER = 16;
+static int heavy_table(gev_ctx *ctx, gev_pcls *p, HeavyTab &H) {
+  const long n = p->cap > 0 ? p->cap : 1;
+  const uint32_t cap = (uint32_t)(n / HEAVY_SLOT_PER > 1024 ? n / HEAVY_SLOT_PER : 1024);
+  uint64_t hs = 1024;
+  while (hs < 2 * (uint64_t)(n / (HEAVY_T + 1) + 1)) hs <<= 1;
+  const size_t b_keys = hs * 4, b_vals = hs * 4, b_list = (size_t)cap * 4, b_sums = (size_t)cap * HEAVY_NS * 8;
+  const size_t o_vals = (b_keys + 255) & ~(size_t)255, o_list = o_vals + ((b_vals + 255) & ~(size_t)255);
+  const size_t o_cnt = o_list + ((b_list + 255) & ~(size_t)255), o_sums = o_cnt + 256;
+  const size_t total = o_sums + b_sums;
+  if (!p->heavy) {
+    if (cudaMalloc(&p->heavy, total) != cudaSuccess) {
+      cudaGetLastError();
+      p->heavy = nullptr;
+      return gev_fail(ctx, GEV_ENOMEM, "deposit: dense-cell table allocation failed");
+    }
+    p->heavy_bytes = total;
+    ctx->bytes_in_use += total;
+    p->bytes += total;
+  }
+  char *b = (char *)p->heavy;
+  H.keys = (uint32_t *)b;
+  H.vals = (uint32_t *)(b + o_vals);
+  H.list = (uint32_t *)(b + o_list);
+  H.count = (uint32_t *)(b + o_cnt);
+  H.sums = (long long *)(b + o_sums);
+  H.mask = (uint32_t)(hs - 1);
+  H.cap = ctx->dense_cells ? cap : 0u;  // no slots: every dense cell is walked
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(H.keys, 0, b_keys, ctx->stream));
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(H.count, 0, 4, ctx->stream));
+  return GEV_OK;
+}
+
 // the fixed-point deposit of the mixed form; kind: 0 T00, 1 T0i, 2 Tij, 3 mass,
 // 4 T00 and Tij in one gather (out: T00, out2: Tij).  overwrite: every cell of the
 // target is written (the sum of this deposit alone), which spares the caller
@@ -605,25 +813,51 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     // of a few large blocks cannot (512^3 cycle: 29.7 ms at 96, 30.7 at 16, 31.8 at 12)
     const int gb = grid_for(ctx, (size_t)C, 256, 96);
     const Div32 dN = make_div32((unsigned)N);
+    HeavyTab H;
+    {
+      int rc = heavy_table(ctx, p, H);
+      if (rc) return rc;
+    }
     GevTimed tm_p(ctx, "k_fx_prep");
     if (kind == FX_T00) {
       k_fx_prep<FX_T00><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
+      {
+        GevTimed tm_h(ctx, "k_heavy_find+k_heavy_sums");
+        k_heavy_find<<<grid_for(ctx, (size_t)C, 256, 8), 256, 0, ctx->stream>>>(p->start, (unsigned)C, H);
+        GEV_LAUNCH_CHECK(ctx);
+        k_heavy_sums<FX_T00><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, fp, dN, p->bounds, H);
+        GEV_LAUNCH_CHECK(ctx);
+      }
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_T00><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
+      k_dep_gather<FX_T00><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, H);
     } else if (kind == FX_TIJ) {
       k_fx_prep<FX_TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
+      {
+        GevTimed tm_h(ctx, "k_heavy_find+k_heavy_sums");
+        k_heavy_find<<<grid_for(ctx, (size_t)C, 256, 8), 256, 0, ctx->stream>>>(p->start, (unsigned)C, H);
+        GEV_LAUNCH_CHECK(ctx);
+        k_heavy_sums<FX_TIJ><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, fp, dN, p->bounds, H);
+        GEV_LAUNCH_CHECK(ctx);
+      }
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
+      k_dep_gather<FX_TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, H);
     } else {
       k_fx_prep<FX_T00TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
+      {
+        GevTimed tm_h(ctx, "k_heavy_find+k_heavy_sums");
+        k_heavy_find<<<grid_for(ctx, (size_t)C, 256, 8), 256, 0, ctx->stream>>>(p->start, (unsigned)C, H);
+        GEV_LAUNCH_CHECK(ctx);
+        k_heavy_sums<FX_T00TIJ><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, fp, dN, p->bounds, H);
+        GEV_LAUNCH_CHECK(ctx);
+      }
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_T00TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
+      k_dep_gather<FX_T00TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, H);
     }
     GEV_LAUNCH_CHECK(ctx);
     return GEV_OK;

@@ -212,3 +212,39 @@ def test_particle_store_returns_its_bytes(gpu, oracle, prec):
     held = one_store()
     assert held >= base + N ** 3 * 56
     assert c.bytes_in_use() == base
+
+
+@pytest.mark.parametrize("N", [16, 32])
+def test_dense_cells_give_the_same_bits(gpu, N):
+    """Mixed-form T00, Tij and T00+Tij gathers with dense cells summed once per cell
+    (the default) against every cell walked by its corner nodes: the same integers are
+    added, so the fields are identical.  The particles are clustered: clumps from a
+    few hundred particles in one cell down to cells just over the threshold, at the
+    periodic edges too."""
+    rng = np.random.default_rng(N)
+    n = 4 * N ** 3
+    p = np.zeros(n, gpu.PART)
+    p["pos"] = rng.random((n, 3))
+    k = 0
+    for centre, count, spread in (((0.5, 0.5, 0.5), 600, 0.4), ((0.0, 0.0, 0.0), 300, 0.9), ((0.99, 0.2, 0.7), 40, 2.0),
+                                  ((0.3, 0.999, 0.001), 12, 1.0), ((0.7, 0.6, 0.1), 9, 0.5)):
+        pts = (np.array(centre) + (rng.random((count, 3)) - 0.5) * spread / N) % 1.0
+        p["pos"][k:k + count] = pts
+        k += count
+    p["vel"] = rng.standard_normal((n, 3)) * 1e-3
+    p["ID"] = rng.permutation(n)
+    phi_h = rng.standard_normal((1, N, N, N)) * 1e-5
+    out = {}
+    for dense in (True, False):
+        ctx = gpu.Context(N, gpu.PREC_MIXED)
+        ctx.set_dense_cells(dense)
+        pc = ctx.particles(n, 2e-4).upload(p)
+        phi = ctx.real(1).upload(phi_h)
+        f1, f6, g1, g6 = ctx.real(1), ctx.real(6), ctx.real(1), ctx.real(6)
+        gpu.projection_T00(pc, f1, 0.03, phi)
+        gpu.projection_Tij(pc, f6, 0.03, phi)
+        gpu.projection_T00_Tij(pc, g1, g6, 0.03, phi)
+        out[dense] = [f.download() for f in (f1, f6, g1, g6)]
+    for a, b in zip(out[True], out[False]):
+        assert a.tobytes() == b.tobytes()
+    assert out[True][0].tobytes() == out[True][2].tobytes() and out[True][1].tobytes() == out[True][3].tobytes()
