@@ -289,9 +289,9 @@ int gev_ctx_launch_count(gev_ctx *ctx, long long *count) {
   return GEV_OK;
 }
 
-int gev_ctx_set_dense_cells(gev_ctx *ctx, int on) {
+int gev_ctx_set_dense_split(gev_ctx *ctx, int on) {
   if (!ctx) return GEV_EINVAL;
-  ctx->dense_cells = on != 0;
+  ctx->dense_split = on != 0;
   return GEV_OK;
 }
 

@@ -388,154 +388,99 @@ __global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArray
   }
 }
 
-// ------------------------------------------------------------ dense cells --
-// In a clustered state some cells hold hundreds of particles.  The gather walks a
-// cell once for each of its 8 corner nodes, and the 32 nodes of a warp walk cells
-// of very different sizes, so a dense cell costs 8 long walks at a small fraction
-// of the warp.  Cells with more than HEAVY_T particles are therefore summed once: a
-// warp per cell forms the same integer contributions the gather would form at the
-// cell's 8 corners (the same FP32 weight factors, rounded the same way) and adds
-// them; the gather adds these 38 sums instead of walking the cell.  Integer sums
-// do not depend on the order or grouping of the additions, so the result is the
-// same bits whichever cells take this path.
-//
-// Per dense cell, 38 int64 sums, corner k = dx + 2 dy + 4 dz of the cell:
-//   [k]          T00 at corner k
-//   [8 + 3k + c] the diagonal Tij_cc at corner k
-//   [32 + dz]    Tij_01 at corner (0, 0, dz)   (the plaquettes the gather's nodes own)
-//   [34 + dy]    Tij_02 at corner (0, dy, 0)
-//   [36 + dx]    Tij_12 at corner (dx, 0, 0)
-// A hash (open addressing, keys cell + 1) maps a dense cell to its slot.  When the
-// slots run out, the remaining dense cells are walked by the gather as before.
-constexpr uint32_t HEAVY_T = 8;
-constexpr int HEAVY_NS = 38;
-struct HeavyTab {
-  uint32_t *keys, *vals;  // hash: cell + 1 -> slot (0xffffffff: no slot)
-  uint32_t mask;          // hash size - 1 (a power of two)
-  uint32_t *list;         // slot -> cell
-  uint32_t *count;        // dense cells found (may exceed cap)
-  uint32_t cap;           // slots
-  long long *sums;        // slot * HEAVY_NS + index
+// The int64 sums of one node and the contributions of particle j to them, the node
+// being corner (dx, dy, dz) of the particle's cell.  pn is phi at the node, s01 / s02
+// / s12 the plaquette sums of phi the node owns.  Every floating-point step is an
+// explicitly rounded intrinsic, so each kernel that forms a contribution forms the
+// same integer.
+struct NodeSums {
+  long long a00 = 0, ad0 = 0, ad1 = 0, ad2 = 0, ao01 = 0, ao02 = 0, ao12 = 0;
 };
-__device__ __forceinline__ uint32_t heavy_hash(uint32_t c, uint32_t mask) { return (c * 2654435761u) & mask; }
-// the slot of dense cell c, or 0xffffffff (not inserted or no slot left)
-__device__ __forceinline__ uint32_t heavy_slot(const HeavyTab &H, uint32_t c) {
-  uint32_t h = heavy_hash(c, H.mask);
-  for (uint32_t probe = 0; probe <= H.mask; ++probe) {
-    const uint32_t k = H.keys[h];
-    if (k == c + 1u) return H.vals[h];
-    if (k == 0u) return 0xffffffffu;
-    h = (h + 1u) & H.mask;
-  }
-  return 0xffffffffu;
-}
-
-// every cell with more than HEAVY_T particles into the hash and, while slots last,
-// the list (the hash holds at least twice the most dense cells there can be)
-__global__ void __launch_bounds__(256) k_heavy_find(const uint32_t *__restrict__ start, unsigned C, HeavyTab H) {
-  for (unsigned c = blockIdx.x * blockDim.x + threadIdx.x; c < C; c += gridDim.x * blockDim.x) {
-    if (start[c + 1] - start[c] <= HEAVY_T) continue;
-    uint32_t h = heavy_hash(c, H.mask);
-    for (uint32_t probe = 0; probe <= H.mask; ++probe) {
-      if (atomicCAS(&H.keys[h], 0u, c + 1u) == 0u) {
-        const uint32_t slot = atomicAdd(H.count, 1u);
-        H.vals[h] = slot < H.cap ? slot : 0xffffffffu;
-        if (slot < H.cap) H.list[slot] = c;
-        break;
-      }
-      h = (h + 1u) & H.mask;
-    }
-  }
-}
-
-// One warp per dense cell: each lane takes every 32nd particle of the cell and forms
-// its contributions to the cell's 8 corners exactly as k_dep_gather's add() forms
-// them for a node, then the warp adds the lanes' int64 sums.
+struct NodePhi {
+  float pn = 0.f, s01 = 0.f, s02 = 0.f, s12 = 0.f;
+};
 template <int KIND>
-__global__ void __launch_bounds__(256) k_heavy_sums(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
-                                                    const float *__restrict__ phi, FxParams p, Div32 dN,
-                                                    const uint32_t *__restrict__ fxb, HeavyTab H) {
+__device__ __forceinline__ void node_add(NodeSums &S, const PclsArrays &P, const PrepArrays &A, uint32_t j, int dx,
+                                         int dy, int dz, const NodePhi &f, float sg00, float sgij) {
   constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
-  const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
-  const int N = p.N;
-  const int lane = threadIdx.x & 31;
-  const uint32_t nheavy = min(*H.count, H.cap);
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nheavy; s += warps) {
-    const uint32_t c = H.list[s];
-    int x, y, z;
-    cell_xyz(c, N, p.lg, dN, x, y, z);
-    const Nb3 b = nb3(c, x, y, z, N);
-    // phi at the cell's 8 corners, f[dx + 2 dy + 4 dz]
-    float f[8];
+  uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
+  if constexpr (KIND == FX_T00) {
+    const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
+    v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), q.x);
+    v1 = make_uint4(q.y, 0u, 0u, 0u);
+  } else {
+    const uint4 *rec = A.rec + 3 * (size_t)j;
+    v0 = __ldg(rec);
+    v1 = __ldg(rec + 1);
+    v2 = __ldg(rec + 2);
+  }
+  const float u0 = __uint_as_float(v0.x), u1 = __uint_as_float(v0.y), u2 = __uint_as_float(v0.z);
+  const float w0 = dx ? u0 : __fsub_rn(1.f, u0), w1 = dy ? u1 : __fsub_rn(1.f, u1), w2 = dz ? u2 : __fsub_rn(1.f, u2);
+  const float w = __fmul_rn(__fmul_rn(w0, w1), w2);
+  if (DO00)
+    S.a00 += (long long)(int)v0.w * (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), f.pn))), sg00);
+  if (DOIJ) {
+    const float fT = __uint_as_float(v1.y);
+    const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(fT, f.pn))), sgij);
+    S.ad0 += (long long)(int)v1.z * G;
+    S.ad1 += (long long)(int)v1.w * G;
+    S.ad2 += (long long)(int)v2.x * G;
+    const float qf = __fmul_rn(0.25f, fT);
+    if (dx == 0 && dy == 0)
+      S.ao01 += (long long)(int)v2.y * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, f.s01))), sgij);
+    if (dx == 0 && dz == 0)
+      S.ao02 += (long long)(int)v2.z * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, f.s02))), sgij);
+    if (dy == 0 && dz == 0)
+      S.ao12 += (long long)(int)v2.w * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, f.s12))), sgij);
+  }
+}
+// phi at the node and its +x, +y, +z neighbours: the factors of the node's corner
+// (T00, diagonal Tij) and the three plaquette sums of the off-diagonal components
+__device__ __forceinline__ NodePhi node_phi(const float *__restrict__ phi, unsigned i, const Nb3 &b) {
+  NodePhi f;
+  if (phi != nullptr) {  // indices summed in 32 bits: the offsets wrap modulo 2^32
+    const unsigned i100 = i + b.xp, i010 = i + b.yp, i001 = i + b.zp;
+    const unsigned i110 = i100 + b.yp, i101 = i100 + b.zp, i011 = i010 + b.zp;
+    const float f000 = __ldg(&phi[i]), f100 = __ldg(&phi[i100]), f010 = __ldg(&phi[i010]);
+    const float f110 = __ldg(&phi[i110]), f001 = __ldg(&phi[i001]);
+    const float f101 = __ldg(&phi[i101]), f011 = __ldg(&phi[i011]);
+    f.pn = f000;
+    f.s01 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f010), f100), f110);  // l0 + l2 + l4 + l6 of the particles' cells
+    f.s02 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f100), f101);  // l0 + l1 + l4 + l5
+    f.s12 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f010), f011);  // l0 + l1 + l2 + l3
+  }
+  return f;
+}
+template <int KIND>
+__device__ __forceinline__ void node_store(const NodeSums &S, unsigned i, unsigned C, float *t00, float *tij,
+                                           int ks00, int ksij, int overwrite) {
+  constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
+  if (DO00) {
+    const float v = float_of_fixed(S.a00, ks00);
+    t00[i] = overwrite ? v : t00[i] + v;
+  }
+  if (DOIJ) {
+    const long long acc[6] = {S.ad0, S.ao01, S.ao02, S.ad1, S.ao12, S.ad2};
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const unsigned ik = c + ((k & 1) ? b.xp : 0u) + ((k & 2) ? b.yp : 0u) + ((k & 4) ? b.zp : 0u);
-      f[k] = phi != nullptr ? __ldg(&phi[ik]) : 0.f;
-    }
-    // the gather's plaquette sums at the corners that own them, in its order
-    float s01[2], s02[2], s12[2];
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      s01[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[4 * d], f[2 + 4 * d]), f[1 + 4 * d]), f[3 + 4 * d]);
-      s02[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[2 * d], f[2 * d + 4]), f[1 + 2 * d]), f[1 + 2 * d + 4]);
-      s12[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[d], f[d + 4]), f[d + 2]), f[d + 6]);
-    }
-    long long acc[HEAVY_NS];
-#pragma unroll
-    for (int k = 0; k < HEAVY_NS; ++k) acc[k] = 0;
-    const uint32_t j0 = start[c], j1 = start[c + 1];
-    for (uint32_t j = j0 + lane; j < j1; j += 32) {
-      uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
-      if constexpr (KIND == FX_T00) {
-        const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
-        v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), q.x);
-        v1 = make_uint4(q.y, 0u, 0u, 0u);
-      } else {
-        const uint4 *rec = A.rec + 3 * (size_t)j;
-        v0 = __ldg(rec);
-        v1 = __ldg(rec + 1);
-        v2 = __ldg(rec + 2);
-      }
-      const float u0 = __uint_as_float(v0.x), u1 = __uint_as_float(v0.y), u2 = __uint_as_float(v0.z);
-      const float wl0[2] = {__fsub_rn(1.f, u0), u0}, wl1[2] = {__fsub_rn(1.f, u1), u1},
-                  wl2[2] = {__fsub_rn(1.f, u2), u2};
-      const float fT = __uint_as_float(v1.y), qf = __fmul_rn(0.25f, fT);
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
-        const float w = __fmul_rn(__fmul_rn(wl0[dx], wl1[dy]), wl2[dz]);
-        if (DO00)
-          acc[k] += (long long)(int)v0.w *
-                    (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), f[k]))), sg00);
-        if (DOIJ) {
-          const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(fT, f[k]))), sgij);
-          acc[8 + 3 * k] += (long long)(int)v1.z * G;
-          acc[9 + 3 * k] += (long long)(int)v1.w * G;
-          acc[10 + 3 * k] += (long long)(int)v2.x * G;
-        }
-      }
-      if (DOIJ) {
-#pragma unroll
-        for (int d = 0; d < 2; ++d) {
-          acc[32 + d] += (long long)(int)v2.y * (long long)gq(__fmul_rn(wl2[d], __fadd_rn(1.f, __fmul_rn(qf, s01[d]))), sgij);
-          acc[34 + d] += (long long)(int)v2.z * (long long)gq(__fmul_rn(wl1[d], __fadd_rn(1.f, __fmul_rn(qf, s02[d]))), sgij);
-          acc[36 + d] += (long long)(int)v2.w * (long long)gq(__fmul_rn(wl0[d], __fadd_rn(1.f, __fmul_rn(qf, s12[d]))), sgij);
-        }
-      }
-    }
-    long long *out = H.sums + (size_t)s * HEAVY_NS;
-#pragma unroll
-    for (int k = 0; k < HEAVY_NS; ++k) {
-      if (!DO00 && k < 8) continue;
-      if (!DOIJ && k >= 8) continue;
-      long long v = acc[k];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) out[k] = v;
+    for (int c = 0; c < 6; ++c) {
+      const float v = float_of_fixed(acc[c], ksij);
+      float *o = tij + (size_t)c * C + i;
+      *o = overwrite ? v : *o + v;
     }
   }
 }
+
+// Nodes whose 8 neighbouring cells hold more than LONG_WALK particles (clustered
+// states) are left by k_dep_gather to k_dep_long, a warp per node: the 32 lanes of a
+// warp walk at full width where one thread per node would run 32 walks of very
+// different lengths.  The list holds 8 n / LONG_WALK + 1024 nodes, more than there
+// can be (the C walks add up to 8 n).
+constexpr uint32_t LONG_WALK = 16;
+struct LongList {
+  uint32_t *node;   // nodes handed over
+  uint32_t *count;  // how many (may exceed cap: the rest are walked by the gather)
+  uint32_t cap;     // 0: every node is walked by the gather
+};
 
 // one thread per node (x, y, z); out: T00 (1 comp) and / or Tij (6 comps, 00 01 02 11 12 22).
 // Six resident blocks per SM (40 registers; 48 and five blocks for T00 alone): the
@@ -543,8 +488,7 @@ __global__ void __launch_bounds__(256) k_heavy_sums(PclsArrays P, const uint32_t
 template <int KIND>
 __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
                                                     const float *__restrict__ phi, float *t00, float *tij, FxParams p,
-                                                    Div32 dN, const uint32_t *__restrict__ fxb, HeavyTab H) {
-  constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
+                                                    Div32 dN, const uint32_t *__restrict__ fxb, LongList L) {
   const int ks00 = (int)fxb[2], ksij = KIND == FX_T00TIJ ? (int)fxb[3] : (int)fxb[2];
   const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
   const int N = p.N;
@@ -553,57 +497,6 @@ __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(Pcls
     int x, y, z;
     cell_xyz(i, N, p.lg, dN, x, y, z);
     const Nb3 b = nb3(i, x, y, z, N);
-    // phi at the node and its +x, +y, +z neighbours: the factors of the node's corner
-    // (T00, diagonal Tij) and the three plaquette sums of the off-diagonal components
-    float pn = 0.f, s01 = 0.f, s02 = 0.f, s12 = 0.f;
-    if (phi != nullptr) {  // indices summed in 32 bits: the offsets wrap modulo 2^32
-      const unsigned i100 = i + b.xp, i010 = i + b.yp, i001 = i + b.zp;
-      const unsigned i110 = i100 + b.yp, i101 = i100 + b.zp, i011 = i010 + b.zp;
-      const float f000 = __ldg(&phi[i]), f100 = __ldg(&phi[i100]), f010 = __ldg(&phi[i010]);
-      const float f110 = __ldg(&phi[i110]), f001 = __ldg(&phi[i001]);
-      const float f101 = __ldg(&phi[i101]), f011 = __ldg(&phi[i011]);
-      pn = f000;
-      s01 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f010), f100), f110);  // l0 + l2 + l4 + l6 of the particles' cells
-      s02 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f100), f101);  // l0 + l1 + l4 + l5
-      s12 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f010), f011);  // l0 + l1 + l2 + l3
-    }
-    long long a00 = 0, ad0 = 0, ad1 = 0, ad2 = 0, ao01 = 0, ao02 = 0, ao12 = 0;
-    // the contributions of particle j to this node, the node being corner (dx, dy, dz)
-    // of the particle's cell
-    auto add = [&](uint32_t j, int dx, int dy, int dz) {
-      uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
-      if constexpr (KIND == FX_T00) {
-        const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
-        v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), q.x);
-        v1 = make_uint4(q.y, 0u, 0u, 0u);
-      } else {
-        const uint4 *rec = A.rec + 3 * (size_t)j;
-        v0 = __ldg(rec);
-        v1 = __ldg(rec + 1);
-        v2 = __ldg(rec + 2);
-      }
-      const float u0 = __uint_as_float(v0.x), u1 = __uint_as_float(v0.y), u2 = __uint_as_float(v0.z);
-      const float w0 = dx ? u0 : __fsub_rn(1.f, u0), w1 = dy ? u1 : __fsub_rn(1.f, u1),
-                  w2 = dz ? u2 : __fsub_rn(1.f, u2);
-      const float w = __fmul_rn(__fmul_rn(w0, w1), w2);
-      if (DO00)
-        a00 += (long long)(int)v0.w *
-               (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), pn))), sg00);
-      if (DOIJ) {
-        const float f = __uint_as_float(v1.y);
-        const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(f, pn))), sgij);
-        ad0 += (long long)(int)v1.z * G;
-        ad1 += (long long)(int)v1.w * G;
-        ad2 += (long long)(int)v2.x * G;
-        const float qf = __fmul_rn(0.25f, f);
-        if (dx == 0 && dy == 0)
-          ao01 += (long long)(int)v2.y * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, s01))), sgij);
-        if (dx == 0 && dz == 0)
-          ao02 += (long long)(int)v2.z * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, s02))), sgij);
-        if (dy == 0 && dz == 0)
-          ao12 += (long long)(int)v2.w * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, s12))), sgij);
-      }
-    };
     // the 4 cell pairs (x - 1, x) of rows (y - dy, z - dz): all their bounds first;
     // for x > 0 the two cells' particles are one contiguous run of the store
     const unsigned cb[4] = {i, i + b.zm, i + b.ym, i + b.ym + b.zm};
@@ -614,51 +507,94 @@ __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(Pcls
       s1[q] = start[cb[q]];
       s2[q] = start[cb[q] + 1];
     }
-    // a dense cell's sums at this node's corner of it, instead of its particles
-    auto heavy = [&](uint32_t cell, int dx, int dy, int dz) -> bool {
-      const uint32_t slot = heavy_slot(H, cell);
-      if (slot == 0xffffffffu) return false;
-      const long long *hs = H.sums + (size_t)slot * HEAVY_NS;
-      const int k = dx + 2 * dy + 4 * dz;
-      if (DO00) a00 += hs[k];
-      if (DOIJ) {
-        ad0 += hs[8 + 3 * k];
-        ad1 += hs[9 + 3 * k];
-        ad2 += hs[10 + 3 * k];
-        if (dx == 0 && dy == 0) ao01 += hs[32 + dz];
-        if (dx == 0 && dz == 0) ao02 += hs[34 + dy];
-        if (dy == 0 && dz == 0) ao12 += hs[36 + dx];
+    uint32_t walk = 0;
+    if (x > 0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) walk += s2[q] - s0[q];
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) walk += (start[cb[q] + b.xm + 1] - s0[q]) + (s2[q] - s1[q]);
+    }
+    if (walk > LONG_WALK && L.cap) {
+      const uint32_t k = atomicAdd(L.count, 1u);
+      if (k < L.cap) {
+        L.node[k] = i;
+        continue;
       }
-      return true;
-    };
+    }
+    const NodePhi f = node_phi(phi, i, b);
+    NodeSums S;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int dy = q >> 1, dz = q & 1;
-      // cell A = (x - 1, ...), whose corner (1, dy, dz) this node is; cell B = (x, ...), corner (0, dy, dz)
-      const uint32_t eA = x > 0 ? s1[q] : start[cb[q] + b.xm + 1];
-      const bool skipA = eA - s0[q] > HEAVY_T && heavy(cb[q] + b.xm, 1, dy, dz);
-      const bool skipB = s2[q] - s1[q] > HEAVY_T && heavy(cb[q], 0, dy, dz);
-      if (x > 0 && !skipA && !skipB) {
-        for (uint32_t j = s0[q]; j < s2[q]; ++j) add(j, j < s1[q] ? 1 : 0, dy, dz);
+      if (x > 0) {
+        for (uint32_t j = s0[q]; j < s2[q]; ++j) node_add<KIND>(S, P, A, j, j < s1[q] ? 1 : 0, dy, dz, f, sg00, sgij);
       } else {
-        if (!skipB)
-          for (uint32_t j = s1[q]; j < s2[q]; ++j) add(j, 0, dy, dz);
-        if (!skipA)
-          for (uint32_t j = s0[q]; j < eA; ++j) add(j, 1, dy, dz);
+        for (uint32_t j = s1[q]; j < s2[q]; ++j) node_add<KIND>(S, P, A, j, 0, dy, dz, f, sg00, sgij);
+        const uint32_t t1 = start[cb[q] + b.xm + 1];
+        for (uint32_t j = s0[q]; j < t1; ++j) node_add<KIND>(S, P, A, j, 1, dy, dz, f, sg00, sgij);
       }
     }
-    if (DO00) {
-      const float v = float_of_fixed(a00, ks00);
-      t00[i] = p.overwrite ? v : t00[i] + v;
-    }
-    if (DOIJ) {
-      const long long acc[6] = {ad0, ao01, ao02, ad1, ao12, ad2};
+    node_store<KIND>(S, i, C, t00, tij, ks00, ksij, p.overwrite);
+  }
+}
+
+// The nodes k_dep_gather handed over, a warp each: the node's 8 (cell, corner) runs
+// laid end to end, lane l taking walk positions l, l + 32, ...; the lanes' int64 sums
+// are then added across the warp and lane 0 writes the node.
+template <int KIND>
+__global__ void __launch_bounds__(256) k_dep_long(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
+                                                  const float *__restrict__ phi, float *t00, float *tij, FxParams p,
+                                                  Div32 dN, const uint32_t *__restrict__ fxb, LongList L) {
+  const int ks00 = (int)fxb[2], ksij = KIND == FX_T00TIJ ? (int)fxb[3] : (int)fxb[2];
+  const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
+  const int N = p.N;
+  const unsigned C = (unsigned)N * N * N;
+  const int lane = threadIdx.x & 31;
+  const uint32_t nlong = min(*L.count, L.cap);
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nlong; w += warps) {
+    const unsigned i = L.node[w];
+    int x, y, z;
+    cell_xyz(i, N, p.lg, dN, x, y, z);
+    const Nb3 b = nb3(i, x, y, z, N);
+    const unsigned cb[4] = {i, i + b.zm, i + b.ym, i + b.ym + b.zm};
+    // runs r = 2 q (cell x - 1, corner dx = 1) and 2 q + 1 (cell x, dx = 0)
+    uint32_t lo[8], end[8];
 #pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        const float v = float_of_fixed(acc[c], ksij);
-        float *o = tij + (size_t)c * C + i;
-        *o = p.overwrite ? v : *o + v;
-      }
+    for (int q = 0; q < 4; ++q) {
+      lo[2 * q] = start[cb[q] + b.xm];
+      end[2 * q] = start[cb[q] + b.xm + 1];
+      lo[2 * q + 1] = start[cb[q]];
+      end[2 * q + 1] = start[cb[q] + 1];
+    }
+    const NodePhi f = node_phi(phi, i, b);
+    NodeSums S;
+    uint32_t base = 0;
+#pragma unroll
+    for (int r = 0; r < 8; ++r) {
+      const uint32_t len = end[r] - lo[r];
+      const int q = r >> 1, dx = (r & 1) ? 0 : 1, dy = q >> 1, dz = q & 1;
+      // walk positions [base, base + len) of this run; lane l takes those equal to l mod 32
+      const uint32_t first = (uint32_t)((lane - (int)(base & 31u)) & 31);
+      for (uint32_t o = first; o < len; o += 32) node_add<KIND>(S, P, A, lo[r] + o, dx, dy, dz, f, sg00, sgij);
+      base += len;
+    }
+    long long v[7] = {S.a00, S.ad0, S.ad1, S.ad2, S.ao01, S.ao02, S.ao12};
+#pragma unroll
+    for (int k = 0; k < 7; ++k)
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+    if (lane == 0) {
+      NodeSums T;
+      T.a00 = v[0];
+      T.ad0 = v[1];
+      T.ad1 = v[2];
+      T.ad2 = v[3];
+      T.ao01 = v[4];
+      T.ao02 = v[5];
+      T.ao12 = v[6];
+      node_store<KIND>(T, i, C, t00, tij, ks00, ksij, p.overwrite);
     }
   }
 }
@@ -712,40 +648,27 @@ __global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, floa
 
 }  // namespace
 
-// The dense-cell table of a particle store, allocated on its first gather deposit:
-// slots for one dense cell per HEAVY_SLOT_PER particles (more dense cells fall back
-// to the walk), and a hash of at least twice the most dense cells there can be
-// (n / (HEAVY_T + 1)).  Cleared (keys and count) on every call.
-constexpr long HEAVY_SLOT_PER = 16;
-static int heavy_table(gev_ctx *ctx, gev_pcls *p, HeavyTab &H) {
+// The long-walk node list of a particle store (see LongList), allocated on its first
+// gather deposit, its counter cleared on every call.  gev_ctx_set_dense_split(ctx, 0)
+// gives it no room, so every node is walked by the gather; the same bits either way.
+static int long_list(gev_ctx *ctx, gev_pcls *p, LongList &L) {
   const long n = p->cap > 0 ? p->cap : 1;
-  const uint32_t cap = (uint32_t)(n / HEAVY_SLOT_PER > 1024 ? n / HEAVY_SLOT_PER : 1024);
-  uint64_t hs = 1024;
-  while (hs < 2 * (uint64_t)(n / (HEAVY_T + 1) + 1)) hs <<= 1;
-  const size_t b_keys = hs * 4, b_vals = hs * 4, b_list = (size_t)cap * 4, b_sums = (size_t)cap * HEAVY_NS * 8;
-  const size_t o_vals = (b_keys + 255) & ~(size_t)255, o_list = o_vals + ((b_vals + 255) & ~(size_t)255);
-  const size_t o_cnt = o_list + ((b_list + 255) & ~(size_t)255), o_sums = o_cnt + 256;
-  const size_t total = o_sums + b_sums;
+  const uint32_t cap = (uint32_t)(8 * n / LONG_WALK + 1024);
+  const size_t total = 256 + (size_t)cap * 4;
   if (!p->heavy) {
     if (cudaMalloc(&p->heavy, total) != cudaSuccess) {
       cudaGetLastError();
       p->heavy = nullptr;
-      return gev_fail(ctx, GEV_ENOMEM, "deposit: dense-cell table allocation failed");
+      return gev_fail(ctx, GEV_ENOMEM, "deposit: long-walk node list allocation failed");
     }
     p->heavy_bytes = total;
     ctx->bytes_in_use += total;
     p->bytes += total;
   }
-  char *b = (char *)p->heavy;
-  H.keys = (uint32_t *)b;
-  H.vals = (uint32_t *)(b + o_vals);
-  H.list = (uint32_t *)(b + o_list);
-  H.count = (uint32_t *)(b + o_cnt);
-  H.sums = (long long *)(b + o_sums);
-  H.mask = (uint32_t)(hs - 1);
-  H.cap = ctx->dense_cells ? cap : 0u;  // no slots: every dense cell is walked
-  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(H.keys, 0, b_keys, ctx->stream));
-  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(H.count, 0, 4, ctx->stream));
+  L.count = (uint32_t *)p->heavy;
+  L.node = (uint32_t *)((char *)p->heavy + 256);
+  L.cap = ctx->dense_split ? cap : 0u;
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(L.count, 0, 4, ctx->stream));
   return GEV_OK;
 }
 
@@ -813,9 +736,9 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     // of a few large blocks cannot (512^3 cycle: 29.7 ms at 96, 30.7 at 16, 31.8 at 12)
     const int gb = grid_for(ctx, (size_t)C, 256, 96);
     const Div32 dN = make_div32((unsigned)N);
-    HeavyTab H;
+    LongList LL;
     {
-      int rc = heavy_table(ctx, p, H);
+      int rc = long_list(ctx, p, LL);
       if (rc) return rc;
     }
     GevTimed tm_p(ctx, "k_fx_prep");
@@ -823,41 +746,32 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
       k_fx_prep<FX_T00><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
-      {
-        GevTimed tm_h(ctx, "k_heavy_find+k_heavy_sums");
-        k_heavy_find<<<grid_for(ctx, (size_t)C, 256, 8), 256, 0, ctx->stream>>>(p->start, (unsigned)C, H);
-        GEV_LAUNCH_CHECK(ctx);
-        k_heavy_sums<FX_T00><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, fp, dN, p->bounds, H);
-        GEV_LAUNCH_CHECK(ctx);
-      }
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_T00><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, H);
+      k_dep_gather<FX_T00><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
+      GEV_LAUNCH_CHECK(ctx);
+      tm_g.stop();
+      GevTimed tm_l(ctx, "k_dep_long");
+      k_dep_long<FX_T00><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
     } else if (kind == FX_TIJ) {
       k_fx_prep<FX_TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
-      {
-        GevTimed tm_h(ctx, "k_heavy_find+k_heavy_sums");
-        k_heavy_find<<<grid_for(ctx, (size_t)C, 256, 8), 256, 0, ctx->stream>>>(p->start, (unsigned)C, H);
-        GEV_LAUNCH_CHECK(ctx);
-        k_heavy_sums<FX_TIJ><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, fp, dN, p->bounds, H);
-        GEV_LAUNCH_CHECK(ctx);
-      }
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, H);
+      k_dep_gather<FX_TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
+      GEV_LAUNCH_CHECK(ctx);
+      tm_g.stop();
+      GevTimed tm_l(ctx, "k_dep_long");
+      k_dep_long<FX_TIJ><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
     } else {
       k_fx_prep<FX_T00TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
-      {
-        GevTimed tm_h(ctx, "k_heavy_find+k_heavy_sums");
-        k_heavy_find<<<grid_for(ctx, (size_t)C, 256, 8), 256, 0, ctx->stream>>>(p->start, (unsigned)C, H);
-        GEV_LAUNCH_CHECK(ctx);
-        k_heavy_sums<FX_T00TIJ><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, fp, dN, p->bounds, H);
-        GEV_LAUNCH_CHECK(ctx);
-      }
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_T00TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, H);
+      k_dep_gather<FX_T00TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
+      GEV_LAUNCH_CHECK(ctx);
+      tm_g.stop();
+      GevTimed tm_l(ctx, "k_dep_long");
+      k_dep_long<FX_T00TIJ><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
     }
     GEV_LAUNCH_CHECK(ctx);
     return GEV_OK;

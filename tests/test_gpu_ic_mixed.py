@@ -215,11 +215,11 @@ def test_particle_store_returns_its_bytes(gpu, oracle, prec):
 
 
 @pytest.mark.parametrize("N", [16, 32])
-def test_dense_cells_give_the_same_bits(gpu, N):
-    """Mixed-form T00, Tij and T00+Tij gathers with dense cells summed once per cell
-    (the default) against every cell walked by its corner nodes: the same integers are
-    added, so the fields are identical.  The particles are clustered: clumps from a
-    few hundred particles in one cell down to cells just over the threshold, at the
+def test_dense_split_gives_the_same_bits(gpu, N):
+    """Mixed-form T00, Tij and T00+Tij gathers with the nodes of long walks summed by a
+    warp each (the default) against every node walked by one thread: the same integers
+    are added, so the fields are identical.  The particles are clustered: clumps from a
+    few hundred particles in one cell down to walks just over the threshold, at the
     periodic edges too."""
     rng = np.random.default_rng(N)
     n = 4 * N ** 3
@@ -237,7 +237,7 @@ def test_dense_cells_give_the_same_bits(gpu, N):
     out = {}
     for dense in (True, False):
         ctx = gpu.Context(N, gpu.PREC_MIXED)
-        ctx.set_dense_cells(dense)
+        ctx.set_dense_split(dense)
         pc = ctx.particles(n, 2e-4).upload(p)
         phi = ctx.real(1).upload(phi_h)
         f1, f6, g1, g6 = ctx.real(1), ctx.real(6), ctx.real(1), ctx.real(6)

@@ -39,8 +39,8 @@ def test_sum_noalloc_matches_field_sum_two_calls(gpu, prec):
     out = torch.full((1,), float("nan"), dtype=torch.float64, device="cuda:0")
     rng = np.random.default_rng(11 + prec)
     # first call: one component of a 96^3 field (108 whole chunks of 8192 values); second: a
-    # 100^3 field (123 chunks, the last one partial); third: a 24^3 field (2 chunks, one partial)
-    for N, ncomp, comp in ((96, 3, 2), (100, 1, 0), (24, 1, 0)):
+    # 48^3 field (14 chunks, the last one partial); third: a 24^3 field (2 chunks, one partial)
+    for N, ncomp, comp in ((96, 3, 2), (48, 1, 0), (24, 1, 0)):
         ctx = gpu.Context(N, prec)
         x = 0.25 + rng.standard_normal((ncomp, N, N, N))
         f = ctx.real(ncomp).upload(x)
@@ -86,3 +86,14 @@ def test_sum_noalloc_edges(gpu):
     assert entry(0, ptr, 1, 100, out.data_ptr(), ctx.stream(), err, len(err)) == 0
     ctx.sync()
     assert out.item() == 100.0
+    # many chunks and a ragged last one: the first 96^3 - 777 values of a 96^3 field
+    N = 96
+    ctx2 = gpu.Context(N, 0)
+    x = np.random.default_rng(5).standard_normal((1, N, N, N))
+    f2 = ctx2.real(1).upload(x)
+    ptr2, _ = f2.device_ptr()
+    n = N ** 3 - 777
+    assert entry(0, ptr2, 0, n, out.data_ptr(), ctx2.stream(), err, len(err)) == 0
+    ctx2.sync()
+    flat = x.reshape(-1)[:n]
+    assert abs(out.item() - float(np.sum(flat))) <= TOL_SUM * float(np.abs(flat).sum())
