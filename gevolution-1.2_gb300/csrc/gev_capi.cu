@@ -289,12 +289,6 @@ int gev_ctx_launch_count(gev_ctx *ctx, long long *count) {
   return GEV_OK;
 }
 
-int gev_ctx_set_dense_split(gev_ctx *ctx, int on) {
-  if (!ctx) return GEV_EINVAL;
-  ctx->dense_split = on != 0;
-  return GEV_OK;
-}
-
 int gev_ctx_set_timing(gev_ctx *ctx, int on) {
   if (!ctx) return GEV_EINVAL;
   if (!on && ctx->timing) {

@@ -388,107 +388,14 @@ __global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArray
   }
 }
 
-// The int64 sums of one node and the contributions of particle j to them, the node
-// being corner (dx, dy, dz) of the particle's cell.  pn is phi at the node, s01 / s02
-// / s12 the plaquette sums of phi the node owns.  Every floating-point step is an
-// explicitly rounded intrinsic, so each kernel that forms a contribution forms the
-// same integer.
-struct NodeSums {
-  long long a00 = 0, ad0 = 0, ad1 = 0, ad2 = 0, ao01 = 0, ao02 = 0, ao12 = 0;
-};
-struct NodePhi {
-  float pn = 0.f, s01 = 0.f, s02 = 0.f, s12 = 0.f;
-};
-template <int KIND>
-__device__ __forceinline__ void node_add(NodeSums &S, const PclsArrays &P, const PrepArrays &A, uint32_t j, int dx,
-                                         int dy, int dz, const NodePhi &f, float sg00, float sgij) {
-  constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
-  uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
-  if constexpr (KIND == FX_T00) {
-    const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
-    v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), q.x);
-    v1 = make_uint4(q.y, 0u, 0u, 0u);
-  } else {
-    const uint4 *rec = A.rec + 3 * (size_t)j;
-    v0 = __ldg(rec);
-    v1 = __ldg(rec + 1);
-    v2 = __ldg(rec + 2);
-  }
-  const float u0 = __uint_as_float(v0.x), u1 = __uint_as_float(v0.y), u2 = __uint_as_float(v0.z);
-  const float w0 = dx ? u0 : __fsub_rn(1.f, u0), w1 = dy ? u1 : __fsub_rn(1.f, u1), w2 = dz ? u2 : __fsub_rn(1.f, u2);
-  const float w = __fmul_rn(__fmul_rn(w0, w1), w2);
-  if (DO00)
-    S.a00 += (long long)(int)v0.w * (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), f.pn))), sg00);
-  if (DOIJ) {
-    const float fT = __uint_as_float(v1.y);
-    const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(fT, f.pn))), sgij);
-    S.ad0 += (long long)(int)v1.z * G;
-    S.ad1 += (long long)(int)v1.w * G;
-    S.ad2 += (long long)(int)v2.x * G;
-    const float qf = __fmul_rn(0.25f, fT);
-    if (dx == 0 && dy == 0)
-      S.ao01 += (long long)(int)v2.y * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, f.s01))), sgij);
-    if (dx == 0 && dz == 0)
-      S.ao02 += (long long)(int)v2.z * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, f.s02))), sgij);
-    if (dy == 0 && dz == 0)
-      S.ao12 += (long long)(int)v2.w * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, f.s12))), sgij);
-  }
-}
-// phi at the node and its +x, +y, +z neighbours: the factors of the node's corner
-// (T00, diagonal Tij) and the three plaquette sums of the off-diagonal components
-__device__ __forceinline__ NodePhi node_phi(const float *__restrict__ phi, unsigned i, const Nb3 &b) {
-  NodePhi f;
-  if (phi != nullptr) {  // indices summed in 32 bits: the offsets wrap modulo 2^32
-    const unsigned i100 = i + b.xp, i010 = i + b.yp, i001 = i + b.zp;
-    const unsigned i110 = i100 + b.yp, i101 = i100 + b.zp, i011 = i010 + b.zp;
-    const float f000 = __ldg(&phi[i]), f100 = __ldg(&phi[i100]), f010 = __ldg(&phi[i010]);
-    const float f110 = __ldg(&phi[i110]), f001 = __ldg(&phi[i001]);
-    const float f101 = __ldg(&phi[i101]), f011 = __ldg(&phi[i011]);
-    f.pn = f000;
-    f.s01 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f010), f100), f110);  // l0 + l2 + l4 + l6 of the particles' cells
-    f.s02 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f100), f101);  // l0 + l1 + l4 + l5
-    f.s12 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f010), f011);  // l0 + l1 + l2 + l3
-  }
-  return f;
-}
-template <int KIND>
-__device__ __forceinline__ void node_store(const NodeSums &S, unsigned i, unsigned C, float *t00, float *tij,
-                                           int ks00, int ksij, int overwrite) {
-  constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
-  if (DO00) {
-    const float v = float_of_fixed(S.a00, ks00);
-    t00[i] = overwrite ? v : t00[i] + v;
-  }
-  if (DOIJ) {
-    const long long acc[6] = {S.ad0, S.ao01, S.ao02, S.ad1, S.ao12, S.ad2};
-#pragma unroll
-    for (int c = 0; c < 6; ++c) {
-      const float v = float_of_fixed(acc[c], ksij);
-      float *o = tij + (size_t)c * C + i;
-      *o = overwrite ? v : *o + v;
-    }
-  }
-}
-
-// Nodes whose 8 neighbouring cells hold more than LONG_WALK particles (clustered
-// states) are left by k_dep_gather to k_dep_long, a warp per node: the 32 lanes of a
-// warp walk at full width where one thread per node would run 32 walks of very
-// different lengths.  The list holds 8 n / LONG_WALK + 1024 nodes, more than there
-// can be (the C walks add up to 8 n).
-constexpr uint32_t LONG_WALK = 16;
-struct LongList {
-  uint32_t *node;   // nodes handed over
-  uint32_t *count;  // how many (may exceed cap: the rest are walked by the gather)
-  uint32_t cap;     // 0: every node is walked by the gather
-};
-
 // one thread per node (x, y, z); out: T00 (1 comp) and / or Tij (6 comps, 00 01 02 11 12 22).
 // Six resident blocks per SM (40 registers; 48 and five blocks for T00 alone): the
 // loop is latency-bound, and the warps hide more than the few spilled words cost.
 template <int KIND>
 __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
                                                     const float *__restrict__ phi, float *t00, float *tij, FxParams p,
-                                                    Div32 dN, const uint32_t *__restrict__ fxb, LongList L) {
+                                                    Div32 dN, const uint32_t *__restrict__ fxb) {
+  constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
   const int ks00 = (int)fxb[2], ksij = KIND == FX_T00TIJ ? (int)fxb[3] : (int)fxb[2];
   const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
   const int N = p.N;
@@ -497,6 +404,57 @@ __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(Pcls
     int x, y, z;
     cell_xyz(i, N, p.lg, dN, x, y, z);
     const Nb3 b = nb3(i, x, y, z, N);
+    // phi at the node and its +x, +y, +z neighbours: the factors of the node's corner
+    // (T00, diagonal Tij) and the three plaquette sums of the off-diagonal components
+    float pn = 0.f, s01 = 0.f, s02 = 0.f, s12 = 0.f;
+    if (phi != nullptr) {  // indices summed in 32 bits: the offsets wrap modulo 2^32
+      const unsigned i100 = i + b.xp, i010 = i + b.yp, i001 = i + b.zp;
+      const unsigned i110 = i100 + b.yp, i101 = i100 + b.zp, i011 = i010 + b.zp;
+      const float f000 = __ldg(&phi[i]), f100 = __ldg(&phi[i100]), f010 = __ldg(&phi[i010]);
+      const float f110 = __ldg(&phi[i110]), f001 = __ldg(&phi[i001]);
+      const float f101 = __ldg(&phi[i101]), f011 = __ldg(&phi[i011]);
+      pn = f000;
+      s01 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f010), f100), f110);  // l0 + l2 + l4 + l6 of the particles' cells
+      s02 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f100), f101);  // l0 + l1 + l4 + l5
+      s12 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f010), f011);  // l0 + l1 + l2 + l3
+    }
+    long long a00 = 0, ad0 = 0, ad1 = 0, ad2 = 0, ao01 = 0, ao02 = 0, ao12 = 0;
+    // the contributions of particle j to this node, the node being corner (dx, dy, dz)
+    // of the particle's cell
+    auto add = [&](uint32_t j, int dx, int dy, int dz) {
+      uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
+      if constexpr (KIND == FX_T00) {
+        const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
+        v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), q.x);
+        v1 = make_uint4(q.y, 0u, 0u, 0u);
+      } else {
+        const uint4 *rec = A.rec + 3 * (size_t)j;
+        v0 = __ldg(rec);
+        v1 = __ldg(rec + 1);
+        v2 = __ldg(rec + 2);
+      }
+      const float u0 = __uint_as_float(v0.x), u1 = __uint_as_float(v0.y), u2 = __uint_as_float(v0.z);
+      const float w0 = dx ? u0 : __fsub_rn(1.f, u0), w1 = dy ? u1 : __fsub_rn(1.f, u1),
+                  w2 = dz ? u2 : __fsub_rn(1.f, u2);
+      const float w = __fmul_rn(__fmul_rn(w0, w1), w2);
+      if (DO00)
+        a00 += (long long)(int)v0.w *
+               (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), pn))), sg00);
+      if (DOIJ) {
+        const float f = __uint_as_float(v1.y);
+        const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(f, pn))), sgij);
+        ad0 += (long long)(int)v1.z * G;
+        ad1 += (long long)(int)v1.w * G;
+        ad2 += (long long)(int)v2.x * G;
+        const float qf = __fmul_rn(0.25f, f);
+        if (dx == 0 && dy == 0)
+          ao01 += (long long)(int)v2.y * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, s01))), sgij);
+        if (dx == 0 && dz == 0)
+          ao02 += (long long)(int)v2.z * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, s02))), sgij);
+        if (dy == 0 && dz == 0)
+          ao12 += (long long)(int)v2.w * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, s12))), sgij);
+      }
+    };
     // the 4 cell pairs (x - 1, x) of rows (y - dy, z - dz): all their bounds first;
     // for x > 0 the two cells' particles are one contiguous run of the store
     const unsigned cb[4] = {i, i + b.zm, i + b.ym, i + b.ym + b.zm};
@@ -507,94 +465,29 @@ __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(Pcls
       s1[q] = start[cb[q]];
       s2[q] = start[cb[q] + 1];
     }
-    uint32_t walk = 0;
-    if (x > 0) {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) walk += s2[q] - s0[q];
-    } else {
-#pragma unroll
-      for (int q = 0; q < 4; ++q) walk += (start[cb[q] + b.xm + 1] - s0[q]) + (s2[q] - s1[q]);
-    }
-    if (walk > LONG_WALK && L.cap) {
-      const uint32_t k = atomicAdd(L.count, 1u);
-      if (k < L.cap) {
-        L.node[k] = i;
-        continue;
-      }
-    }
-    const NodePhi f = node_phi(phi, i, b);
-    NodeSums S;
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       const int dy = q >> 1, dz = q & 1;
       if (x > 0) {
-        for (uint32_t j = s0[q]; j < s2[q]; ++j) node_add<KIND>(S, P, A, j, j < s1[q] ? 1 : 0, dy, dz, f, sg00, sgij);
+        for (uint32_t j = s0[q]; j < s2[q]; ++j) add(j, j < s1[q] ? 1 : 0, dy, dz);
       } else {
-        for (uint32_t j = s1[q]; j < s2[q]; ++j) node_add<KIND>(S, P, A, j, 0, dy, dz, f, sg00, sgij);
+        for (uint32_t j = s1[q]; j < s2[q]; ++j) add(j, 0, dy, dz);
         const uint32_t t1 = start[cb[q] + b.xm + 1];
-        for (uint32_t j = s0[q]; j < t1; ++j) node_add<KIND>(S, P, A, j, 1, dy, dz, f, sg00, sgij);
+        for (uint32_t j = s0[q]; j < t1; ++j) add(j, 1, dy, dz);
       }
     }
-    node_store<KIND>(S, i, C, t00, tij, ks00, ksij, p.overwrite);
-  }
-}
-
-// The nodes k_dep_gather handed over, a warp each: the node's 8 (cell, corner) runs
-// laid end to end, lane l taking walk positions l, l + 32, ...; the lanes' int64 sums
-// are then added across the warp and lane 0 writes the node.
-template <int KIND>
-__global__ void __launch_bounds__(256) k_dep_long(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
-                                                  const float *__restrict__ phi, float *t00, float *tij, FxParams p,
-                                                  Div32 dN, const uint32_t *__restrict__ fxb, LongList L) {
-  const int ks00 = (int)fxb[2], ksij = KIND == FX_T00TIJ ? (int)fxb[3] : (int)fxb[2];
-  const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
-  const int N = p.N;
-  const unsigned C = (unsigned)N * N * N;
-  const int lane = threadIdx.x & 31;
-  const uint32_t nlong = min(*L.count, L.cap);
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nlong; w += warps) {
-    const unsigned i = L.node[w];
-    int x, y, z;
-    cell_xyz(i, N, p.lg, dN, x, y, z);
-    const Nb3 b = nb3(i, x, y, z, N);
-    const unsigned cb[4] = {i, i + b.zm, i + b.ym, i + b.ym + b.zm};
-    // runs r = 2 q (cell x - 1, corner dx = 1) and 2 q + 1 (cell x, dx = 0)
-    uint32_t lo[8], end[8];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      lo[2 * q] = start[cb[q] + b.xm];
-      end[2 * q] = start[cb[q] + b.xm + 1];
-      lo[2 * q + 1] = start[cb[q]];
-      end[2 * q + 1] = start[cb[q] + 1];
+    if (DO00) {
+      const float v = float_of_fixed(a00, ks00);
+      t00[i] = p.overwrite ? v : t00[i] + v;
     }
-    const NodePhi f = node_phi(phi, i, b);
-    NodeSums S;
-    uint32_t base = 0;
+    if (DOIJ) {
+      const long long acc[6] = {ad0, ao01, ao02, ad1, ao12, ad2};
 #pragma unroll
-    for (int r = 0; r < 8; ++r) {
-      const uint32_t len = end[r] - lo[r];
-      const int q = r >> 1, dx = (r & 1) ? 0 : 1, dy = q >> 1, dz = q & 1;
-      // walk positions [base, base + len) of this run; lane l takes those equal to l mod 32
-      const uint32_t first = (uint32_t)((lane - (int)(base & 31u)) & 31);
-      for (uint32_t o = first; o < len; o += 32) node_add<KIND>(S, P, A, lo[r] + o, dx, dy, dz, f, sg00, sgij);
-      base += len;
-    }
-    long long v[7] = {S.a00, S.ad0, S.ad1, S.ad2, S.ao01, S.ao02, S.ao12};
-#pragma unroll
-    for (int k = 0; k < 7; ++k)
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
-    if (lane == 0) {
-      NodeSums T;
-      T.a00 = v[0];
-      T.ad0 = v[1];
-      T.ad1 = v[2];
-      T.ad2 = v[3];
-      T.ao01 = v[4];
-      T.ao02 = v[5];
-      T.ao12 = v[6];
-      node_store<KIND>(T, i, C, t00, tij, ks00, ksij, p.overwrite);
+      for (int c = 0; c < 6; ++c) {
+        const float v = float_of_fixed(acc[c], ksij);
+        float *o = tij + (size_t)c * C + i;
+        *o = p.overwrite ? v : *o + v;
+      }
     }
   }
 }
@@ -647,30 +540,6 @@ __global__ void __launch_bounds__(256) k_face_fix(unsigned long long *face, floa
 }
 
 }  // namespace
-
-// The long-walk node list of a particle store (see LongList), allocated on its first
-// gather deposit, its counter cleared on every call.  gev_ctx_set_dense_split(ctx, 0)
-// gives it no room, so every node is walked by the gather; the same bits either way.
-static int long_list(gev_ctx *ctx, gev_pcls *p, LongList &L) {
-  const long n = p->cap > 0 ? p->cap : 1;
-  const uint32_t cap = (uint32_t)(8 * n / LONG_WALK + 1024);
-  const size_t total = 256 + (size_t)cap * 4;
-  if (!p->heavy) {
-    if (cudaMalloc(&p->heavy, total) != cudaSuccess) {
-      cudaGetLastError();
-      p->heavy = nullptr;
-      return gev_fail(ctx, GEV_ENOMEM, "deposit: long-walk node list allocation failed");
-    }
-    p->heavy_bytes = total;
-    ctx->bytes_in_use += total;
-    p->bytes += total;
-  }
-  L.count = (uint32_t *)p->heavy;
-  L.node = (uint32_t *)((char *)p->heavy + 256);
-  L.cap = ctx->dense_split ? cap : 0u;
-  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(L.count, 0, 4, ctx->stream));
-  return GEV_OK;
-}
 
 // the fixed-point deposit of the mixed form; kind: 0 T00, 1 T0i, 2 Tij, 3 mass,
 // 4 T00 and Tij in one gather (out: T00, out2: Tij).  overwrite: every cell of the
@@ -736,42 +605,25 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     // of a few large blocks cannot (512^3 cycle: 29.7 ms at 96, 30.7 at 16, 31.8 at 12)
     const int gb = grid_for(ctx, (size_t)C, 256, 96);
     const Div32 dN = make_div32((unsigned)N);
-    LongList LL;
-    {
-      int rc = long_list(ctx, p, LL);
-      if (rc) return rc;
-    }
     GevTimed tm_p(ctx, "k_fx_prep");
     if (kind == FX_T00) {
       k_fx_prep<FX_T00><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_T00><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
-      GEV_LAUNCH_CHECK(ctx);
-      tm_g.stop();
-      GevTimed tm_l(ctx, "k_dep_long");
-      k_dep_long<FX_T00><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
+      k_dep_gather<FX_T00><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
     } else if (kind == FX_TIJ) {
       k_fx_prep<FX_TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
-      GEV_LAUNCH_CHECK(ctx);
-      tm_g.stop();
-      GevTimed tm_l(ctx, "k_dep_long");
-      k_dep_long<FX_TIJ><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
+      k_dep_gather<FX_TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
     } else {
       k_fx_prep<FX_T00TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_T00TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
-      GEV_LAUNCH_CHECK(ctx);
-      tm_g.stop();
-      GevTimed tm_l(ctx, "k_dep_long");
-      k_dep_long<FX_T00TIJ><<<ctx->sms * 8, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, LL);
+      k_dep_gather<FX_T00TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
     }
     GEV_LAUNCH_CHECK(ctx);
     return GEV_OK;

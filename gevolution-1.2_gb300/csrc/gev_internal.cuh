@@ -55,9 +55,6 @@ struct gev_ctx {
   // passes, chosen by timing on the first transform (-1: the default)
   int fft_lg[4] = {-1, -1, -1, -1};
   bool fft_tuned = false;
-  // mixed-form gather deposits hand nodes with long walks to a warp each
-  // (gev_ctx_set_dense_split); the same bits either way
-  bool dense_split = true;
   long long launches = 0;
   // optional device timing of named regions (gev_ctx_set_timing): a CUDA event
   // pair on the stream around each region, summed per name when the report is read
@@ -145,10 +142,6 @@ struct gev_pcls {
   // mixed-form T00 / Tij deposit: per-particle prefactor records (12 words a particle),
   // kept in the alt array set's block; an allocation of its own only if that is smaller
   void *prep = nullptr;
-  // mixed-form T00 / Tij gather: the list of nodes whose walks a warp takes over
-  // (gev_deposit_fx.cu), allocated on the first gather deposit
-  void *heavy = nullptr;
-  size_t heavy_bytes = 0;
   size_t bytes = 0;  // device bytes this store counts in its context's bytes_in_use
 };
 

@@ -863,19 +863,7 @@ __global__ void __launch_bounds__(256, 2) k_kick_drift(PclsArrays P, long n, con
     T v0, v1, v2;
     drift_vel<T>(st, pd, r0, r1, r2, q0, q1, q2, v0, v1, v2);
     const uint32_t key = move_store<T>(P, i, pd, v0, v1, v2, c.x, c.y, c.z);
-    if (count) {
-      // the histogram of the relink, fused: the lanes moving into one cell take
-      // consecutive ranks with one atomic, so that the move writes a warp's particles
-      // of a cell to consecutive slots (in dense cells the per-lane atomics' order
-      // scattered them across the cell's range)
-      const unsigned lane = threadIdx.x & 31u;
-      const unsigned peers = __match_any_sync(__activemask(), key);
-      const int leader = __ffs(peers) - 1;
-      uint32_t base = 0u;
-      if ((int)lane == leader) base = atomicAdd(&count[key], (uint32_t)__popc(peers));
-      base = __shfl_sync(peers, base, leader);
-      rank[i] = base + (uint32_t)__popc(peers & ((1u << lane) - 1u));
-    }
+    if (count) rank[i] = atomicAdd(&count[key], 1u);  // the histogram of the relink, fused
   }
   block_max_to<T>(vmax, maxbits);
 }
@@ -1215,7 +1203,6 @@ int gev_pcls_destroy(gev_pcls *p) {
   cudaFree(p->big);
   cudaFree(p->bounds);
   cudaFree(p->prep);
-  cudaFree(p->heavy);
   cudaFree(p->scan_tmp);
   gev_ctx *ctx = p->ctx;
   if (ctx) ctx->bytes_in_use -= p->bytes;

@@ -43,7 +43,6 @@ _SIGS = {
     "gev_ctx_info": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i), ctypes.POINTER(ctypes.c_size_t)],
     "gev_ctx_launch_count": [_vp, ctypes.POINTER(ctypes.c_longlong)],
     "gev_ctx_set_timing": [_vp, _i],
-    "gev_ctx_set_dense_split": [_vp, _i],
     "gev_ctx_timing_report": [_vp, ctypes.c_char_p, ctypes.c_size_t, _i],
     "gev_ctx_fft_tiles": [_vp, ctypes.POINTER(_i)],
     "gev_ctx_set_fft_tiles": [_vp, ctypes.POINTER(_i)],
@@ -151,10 +150,6 @@ class Context:
         n = ctypes.c_longlong()
         _check(lib().gev_ctx_launch_count(self.handle, ctypes.byref(n)), self, "gev_ctx_launch_count")
         return n.value
-
-    def set_dense_split(self, on=True):
-        """Mixed-form gather deposits: nodes with walks over 16 particles to a warp each (same bits)."""
-        _check(lib().gev_ctx_set_dense_split(self.handle, 1 if on else 0), self, "gev_ctx_set_dense_split")
 
     def set_timing(self, on=True):
         """Brackets the library's kernels and cycle phases with CUDA events (see timing())."""

@@ -67,12 +67,6 @@ const char *gev_ctx_last_error(gev_ctx *ctx);
 const char *gev_strerror(int status);
 /* count of kernels this library launched on the context since creation */
 int gev_ctx_launch_count(gev_ctx *ctx, long long *count);
-/* mixed form, T00 / Tij deposits (no counterpart in the reference's API): a node of
- * the gather whose 8 neighbouring cells hold more than 16 particles is summed by a
- * warp (its walk split across 32 lanes) instead of one thread (the default, on).
- * Both ways add the same integers, so the results are the same bits; off is for
- * checking that. */
-int gev_ctx_set_dense_split(gev_ctx *ctx, int on);
 /* device timing, no counterpart in the reference's API: the reference's
  * -DBENCHMARK build prints wall-time sums per phase of the main loop
  * (main.cpp:907-922).  While timing is on, the library brackets each of its

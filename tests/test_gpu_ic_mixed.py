@@ -214,13 +214,13 @@ def test_particle_store_returns_its_bytes(gpu, oracle, prec):
     assert c.bytes_in_use() == base
 
 
-@pytest.mark.parametrize("N", [16, 32])
-def test_dense_split_gives_the_same_bits(gpu, N):
-    """Mixed-form T00, Tij and T00+Tij gathers with the nodes of long walks summed by a
-    warp each (the default) against every node walked by one thread: the same integers
-    are added, so the fields are identical.  The particles are clustered: clumps from a
-    few hundred particles in one cell down to walks just over the threshold, at the
-    periodic edges too."""
+@pytest.mark.parametrize("N", [12, 16, 32])
+def test_clustered_deposits(gpu, oracle, N):
+    """Mixed-form T00, Tij and T00+Tij gathers on clustered particles (clumps from a few
+    hundred particles in one cell down to a few, at the periodic edges too, beside empty
+    cells): the fused deposit gives the same bits as the two separate ones, and both
+    follow the FP64 restatement within the form's rounding (the fixed-point scale is
+    set by the fullest cell)."""
     rng = np.random.default_rng(N)
     n = 4 * N ** 3
     p = np.zeros(n, gpu.PART)
@@ -234,17 +234,15 @@ def test_dense_split_gives_the_same_bits(gpu, N):
     p["vel"] = rng.standard_normal((n, 3)) * 1e-3
     p["ID"] = rng.permutation(n)
     phi_h = rng.standard_normal((1, N, N, N)) * 1e-5
-    out = {}
-    for dense in (True, False):
-        ctx = gpu.Context(N, gpu.PREC_MIXED)
-        ctx.set_dense_split(dense)
-        pc = ctx.particles(n, 2e-4).upload(p)
-        phi = ctx.real(1).upload(phi_h)
-        f1, f6, g1, g6 = ctx.real(1), ctx.real(6), ctx.real(1), ctx.real(6)
-        gpu.projection_T00(pc, f1, 0.03, phi)
-        gpu.projection_Tij(pc, f6, 0.03, phi)
-        gpu.projection_T00_Tij(pc, g1, g6, 0.03, phi)
-        out[dense] = [f.download() for f in (f1, f6, g1, g6)]
-    for a, b in zip(out[True], out[False]):
-        assert a.tobytes() == b.tobytes()
-    assert out[True][0].tobytes() == out[True][2].tobytes() and out[True][1].tobytes() == out[True][3].tobytes()
+    ctx = gpu.Context(N, gpu.PREC_MIXED)
+    pc = ctx.particles(n, 2e-4).upload(p)
+    phi = ctx.real(1).upload(phi_h)
+    f1, f6, g1, g6 = ctx.real(1), ctx.real(6), ctx.real(1), ctx.real(6)
+    gpu.projection_T00(pc, f1, 0.03, phi)
+    gpu.projection_Tij(pc, f6, 0.03, phi)
+    gpu.projection_T00_Tij(pc, g1, g6, 0.03, phi)
+    assert f1.download().tobytes() == g1.download().tobytes()
+    assert f6.download().tobytes() == g6.download().tobytes()
+    for which, got in (("T00", f1.download()), ("Tij", f6.download())):
+        ref = oracle.deposit(which, N, p, 2e-4, 0.03, phi_h, 1.0)
+        assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), which
