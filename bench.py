@@ -261,9 +261,19 @@ def kernel_alg_bytes(name, N, prec, n=None):
 
 
 # DRAM traffic per launch (dram__bytes_read.sum + dram__bytes_write.sum) from ncu
-# captures of the kernels at late time (the state near z = 0 restarted from a
-# hibernation file: bench.py --op cycle), keyed by (kernel, grid, precision).
+# --set full captures at late time, keyed by (kernel, grid, precision): the 256^3
+# mixed simulation (500 Mpc/h, the 512^3 workload's cell size) evolved to z = 0.28
+# and restarted from its hibernation file (bench.py --op prepare / --op cycle), the
+# second cycle's launch.  Particles and cells both grow as N^3, so the 512^3 entry is
+# the 256^3 capture times 8.
+_LATE_256 = {
+    "k_dep_gather": 1.182689e9 + 0.559843e9,
+    "k_fx_prep": 0.403958e9 + 0.747005e9,
+}
 KERNEL_TRAFFIC = {}
+for _k, _v in _LATE_256.items():
+    KERNEL_TRAFFIC[(_k, 256, "mixed")] = _v
+    KERNEL_TRAFFIC[(_k, 512, "mixed")] = 8 * _v
 
 
 # ------------------------------------------------------------ our arm --------

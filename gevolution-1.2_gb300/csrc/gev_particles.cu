@@ -325,14 +325,17 @@ __global__ void k_gather(PclsArrays src, PclsArrays dst, const uint32_t *__restr
 // inside a cell then follows atomic timing, which changes no result of the mixed
 // form (its deposits add integers, the updates are per particle); downloads
 // restore the (cell, ID) order first.
-// Mixed form (FP32 momenta and offsets).  A warp moves 128 consecutive particles
-// per round, lane l the particles l, l + 32, l + 64 and l + 96, all four payloads
-// loaded before any store: every load and every store instruction of the warp
-// covers 32 consecutive particles, and the destinations of consecutive particles
-// (one cell's, or neighbouring cells') are consecutive too, so the scattered
-// stores still fill whole lines.
+// Mixed form (FP32 momenta and offsets).  The source holds the drifted positions
+// and their cell keys but not their in-cell offsets (k_kick_drift leaves them out):
+// each particle's offsets are split from its position again, as the drift split
+// them (pos_split, the same bits), and written with it.  A warp moves 128
+// consecutive particles per round, lane l the particles l, l + 32, l + 64 and
+// l + 96, all four payloads loaded before any store: every load and every store
+// instruction of the warp covers 32 consecutive particles, and the destinations of
+// consecutive particles (one cell's, or neighbouring cells') are consecutive too,
+// so the scattered stores still fill whole lines.
 __global__ void __launch_bounds__(256) k_move(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ start,
-                                              const uint32_t *__restrict__ rank, long n) {
+                                              const uint32_t *__restrict__ rank, long n, int N, int lg) {
   const float *svx = (const float *)src.vx, *svy = (const float *)src.vy, *svz = (const float *)src.vz;
   float *dvx = (float *)dst.vx, *dvy = (float *)dst.vy, *dvz = (float *)dst.vz;
   const int lane = threadIdx.x & 31;
@@ -342,7 +345,7 @@ __global__ void __launch_bounds__(256) k_move(PclsArrays src, PclsArrays dst, co
     uint32_t c[4], t[4];
     double X[4], Y[4], Z[4];
     long long D[4];
-    float VX[4], VY[4], VZ[4], RX[4], RY[4], RZ[4];
+    float VX[4], VY[4], VZ[4];
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       const long i = i0 + 32 * k;
@@ -356,9 +359,6 @@ __global__ void __launch_bounds__(256) k_move(PclsArrays src, PclsArrays dst, co
         VX[k] = svx[i];
         VY[k] = svy[i];
         VZ[k] = svz[i];
-        RX[k] = src.rx[i];
-        RY[k] = src.ry[i];
-        RZ[k] = src.rz[i];
       }
     }
 #pragma unroll
@@ -367,6 +367,11 @@ __global__ void __launch_bounds__(256) k_move(PclsArrays src, PclsArrays dst, co
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       if (i0 + 32 * k >= n) continue;
+      int cx;
+      float r0, r1, r2;
+      pos_split(X[k], N, lg, cx, r0);
+      pos_split(Y[k], N, lg, cx, r1);
+      pos_split(Z[k], N, lg, cx, r2);
       const uint32_t j = t[k];
       dst.px[j] = X[k];
       dst.py[j] = Y[k];
@@ -376,9 +381,9 @@ __global__ void __launch_bounds__(256) k_move(PclsArrays src, PclsArrays dst, co
       dvz[j] = VZ[k];
       dst.id[j] = D[k];
       dst.cell[j] = c[k];
-      dst.rx[j] = RX[k];
-      dst.ry[j] = RY[k];
-      dst.rz[j] = RZ[k];
+      dst.rx[j] = r0;
+      dst.ry[j] = r1;
+      dst.rz[j] = r2;
     }
   }
 }
@@ -738,7 +743,10 @@ __device__ __forceinline__ auto stencil(const T *phi, const T *chi, const T *Bi,
 }
 
 // pos += dtau v, periodic wrap into [0, 1), new cell key (and offset) for the relink
-template <typename T>
+// OFFSETS_LATER (mixed form, followed by k_move): the in-cell offsets are not
+// stored here; k_move splits them from the stored position again (the same bits)
+// as it moves the particle, which saves writing and re-reading them.
+template <typename T, bool OFFSETS_LATER = false>
 __device__ __forceinline__ uint32_t move_store(PclsArrays &P, long i, const Params &pr, T v0, T v1, T v2, double x,
                                                double y, double z) {
   const int N = pr.N, lg = pr.lg;
@@ -757,9 +765,11 @@ __device__ __forceinline__ uint32_t move_store(PclsArrays &P, long i, const Para
     pos_split(x, N, lg, cx, r0);
     pos_split(y, N, lg, cy, r1);
     pos_split(z, N, lg, cz, r2);
-    P.rx[i] = r0;
-    P.ry[i] = r1;
-    P.rz[i] = r2;
+    if (!OFFSETS_LATER) {
+      P.rx[i] = r0;
+      P.ry[i] = r1;
+      P.rz[i] = r2;
+    }
     key = (uint32_t)cx + (uint32_t)N * ((uint32_t)cy + (uint32_t)N * (uint32_t)cz);
   } else {
     x = wrap01(x + dtau * (double)v0);
@@ -862,7 +872,8 @@ __global__ void __launch_bounds__(256, 2) k_kick_drift(PclsArrays P, long n, con
     vmax = vv > vmax ? vv : vmax;
     T v0, v1, v2;
     drift_vel<T>(st, pd, r0, r1, r2, q0, q1, q2, v0, v1, v2);
-    const uint32_t key = move_store<T>(P, i, pd, v0, v1, v2, c.x, c.y, c.z);
+    // the mixed form (count given) leaves the in-cell offsets to k_move
+    const uint32_t key = move_store<T, sizeof(T) == 4>(P, i, pd, v0, v1, v2, c.x, c.y, c.z);
     if (count) rank[i] = atomicAdd(&count[key], 1u);  // the histogram of the relink, fused
   }
   block_max_to<T>(vmax, maxbits);
@@ -1000,7 +1011,7 @@ int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, 
   if (rc) return rc;
   GevTimed tv_(ctx, "k_move");
   k_move<<<grid_for(ctx, (size_t)(p->n + 3) / 4, 256, 16), 256, 0, ctx->stream>>>(p->cur, p->alt, p->start, p->rank,
-                                                                                  p->n);
+                                                                                  p->n, N, lg_pow2(N));
   GEV_LAUNCH_CHECK(ctx);
   std::swap(p->cur, p->alt);
   p->id_order = false;

@@ -173,12 +173,17 @@ def test_fused_entry_points_match_separate_calls(gpu, oracle, prec):
             gpu.projection_Tij(pc, Tij, 0.03, phi)
             mv = gpu.update_q(pc, 0, 2e-3, phi, chi, Bi, 3, 0.03, 0.03 * 0.03 * N)
             gpu.update_pos(pc, 0, 2e-3, phi, chi, Bi, 3, 0.031, 0.031 * 0.031 * N)
-        out.append((T00.download(), Tij.download(), mv, pc.download()))
+        first = (T00.download(), Tij.download())
+        # a deposit from the moved store: its cell keys and in-cell offsets (the fused
+        # path splits the offsets from the positions again as it moves them)
+        gpu.projection_T00_Tij(pc, T00, Tij, 0.031, phi)
+        out.append(first + (mv, pc.download(), T00.download(), Tij.download()))
     a, b = out
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
     assert a[2] == b[2]
     assert np.array_equal(a[3]["ID"], b[3]["ID"])
     assert np.array_equal(a[3]["pos"], b[3]["pos"]) and np.array_equal(a[3]["vel"], b[3]["vel"])
+    assert np.array_equal(a[4], b[4]) and np.array_equal(a[5], b[5])
 
 
 @pytest.mark.parametrize("prec", [0, 1])
