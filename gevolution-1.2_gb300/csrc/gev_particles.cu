@@ -328,26 +328,34 @@ __global__ void k_gather(PclsArrays src, PclsArrays dst, const uint32_t *__restr
 // Mixed form (FP32 momenta and offsets).  The source holds the drifted positions
 // and their cell keys but not their in-cell offsets (k_kick_drift leaves them out):
 // each particle's offsets are split from its position again, as the drift split
-// them (pos_split, the same bits), and written with it.  A warp moves 128
-// consecutive particles per round, lane l the particles l, l + 32, l + 64 and
-// l + 96, all four payloads loaded before any store: every load and every store
+// them (pos_split, the same bits), and written with it.  A warp moves 32 PER
+// consecutive particles per round, lane l the particles l, l + 32, l + 64,
+// l + 96 (and so on), all payloads loaded before any store: every load and every store
 // instruction of the warp covers 32 consecutive particles, and the destinations of
 // consecutive particles (one cell's, or neighbouring cells') are consecutive too,
 // so the scattered stores still fill whole lines.
-__global__ void __launch_bounds__(256) k_move(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ start,
+// A lane holds PER particles' payloads (182 registers for 8, one block of 256
+// threads per SM): in a clustered state the stores scatter within each dense
+// cell's range and the loads wait longer, and more bytes in flight per warp beat
+// more warps (the late-time 512^3 move took 5.19 ms with 8 or 6 a lane against 5.66
+// with 4 at two blocks per SM on one GPU; 2 a lane at four blocks and 1 at six were
+// slower than 4 on another).
+constexpr int MOVE_PER = 8;
+template <int PER>
+__global__ void __launch_bounds__(256, 1) k_move(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ start,
                                               const uint32_t *__restrict__ rank, long n, int N, int lg) {
   const float *svx = (const float *)src.vx, *svy = (const float *)src.vy, *svz = (const float *)src.vz;
   float *dvx = (float *)dst.vx, *dvy = (float *)dst.vy, *dvz = (float *)dst.vz;
   const int lane = threadIdx.x & 31;
-  const long nw = (n + 127) >> 7, nwarps = ((long)gridDim.x * blockDim.x) >> 5;
+  const long nw = (n + 32 * PER - 1) / (32 * PER), nwarps = ((long)gridDim.x * blockDim.x) >> 5;
   for (long w = (blockIdx.x * (long)blockDim.x + threadIdx.x) >> 5; w < nw; w += nwarps) {
-    const long i0 = (w << 7) + lane;
-    uint32_t c[4], t[4];
-    double X[4], Y[4], Z[4];
-    long long D[4];
-    float VX[4], VY[4], VZ[4];
+    const long i0 = w * (32 * PER) + lane;
+    uint32_t c[PER], t[PER];
+    double X[PER], Y[PER], Z[PER];
+    long long D[PER];
+    float VX[PER], VY[PER], VZ[PER];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < PER; ++k) {
       const long i = i0 + 32 * k;
       if (i < n) {
         c[k] = src.cell[i];
@@ -362,10 +370,10 @@ __global__ void __launch_bounds__(256) k_move(PclsArrays src, PclsArrays dst, co
       }
     }
 #pragma unroll
-    for (int k = 0; k < 4; ++k)
+    for (int k = 0; k < PER; ++k)
       if (i0 + 32 * k < n) t[k] += start[c[k]];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < PER; ++k) {
       if (i0 + 32 * k >= n) continue;
       int cx;
       float r0, r1, r2;
@@ -1010,8 +1018,8 @@ int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, 
   int rc = scan_cells(ctx, p);
   if (rc) return rc;
   GevTimed tv_(ctx, "k_move");
-  k_move<<<grid_for(ctx, (size_t)(p->n + 3) / 4, 256, 16), 256, 0, ctx->stream>>>(p->cur, p->alt, p->start, p->rank,
-                                                                                  p->n, N, lg_pow2(N));
+  k_move<MOVE_PER><<<grid_for(ctx, (size_t)(p->n + MOVE_PER - 1) / MOVE_PER, 256, 16), 256, 0, ctx->stream>>>(
+      p->cur, p->alt, p->start, p->rank, p->n, N, lg_pow2(N));
   GEV_LAUNCH_CHECK(ctx);
   std::swap(p->cur, p->alt);
   p->id_order = false;
