@@ -658,15 +658,19 @@ def run_serve(args, gpu):
         ens.append(gpu.request(N, seed=300000 + k, z_target=0.0, Omega_cdm=float(rng.uniform(0.25, 0.35)),
                                sigma8=float(rng.uniform(0.75, 0.87)), n_s=float(rng.uniform(0.94, 0.98)),
                                prec=gpu.PREC_MIXED))
-    srv = gpu.Server()
-    for r in ens:
-        srv.submit(r)
-    srv.drain(900.0)
-    eres = [r for r in srv.poll(100000) if r["status"] == 0]
-    est = srv.stats()
-    srv.close()
-    e_span = max(r["t_done"] for r in eres) - min(r["t_submit"] for r in eres)
-    e_steps = sum(float(r["N"]) ** 3 * r["cycles"] for r in eres)
+    def ensemble(workers):
+        srv = gpu.Server(workers=workers)
+        for r in ens:
+            srv.submit(r)
+        srv.drain(900.0)
+        got = [r for r in srv.poll(100000) if r["status"] == 0]
+        stats = srv.stats()
+        srv.close()
+        span = max(r["t_done"] for r in got) - min(r["t_submit"] for r in got)
+        return got, stats, span, sum(float(r["N"]) ** 3 * r["cycles"] for r in got)
+
+    eres, est, e_span, e_steps = ensemble(0)
+    eres1, _, e_span1, e_steps1 = ensemble(1)
     pct = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]  # noqa: E731
     return {
         "precision": "mixed", "arrivals": "Poisson %.3g/s for %.3g s" % (args.serve_rate, args.serve_seconds),
@@ -682,7 +686,9 @@ def run_serve(args, gpu):
         "capacity_vs_sequential_fp64": cap / seq_rate,
         "ensemble": {"simulations": len(eres), "sizes": "16 x 64^3, 16 x 96^3, 16 x 128^3, z = 100 -> 0",
                      "makespan_s": e_span, "particle_steps_per_s": e_steps / e_span,
-                     "max_active_seen": est["max_active_seen"]},
+                     "max_active_seen": est["max_active_seen"], "scheduler_threads": est["workers"],
+                     "one_scheduler_thread": {"simulations": len(eres1), "makespan_s": e_span1,
+                                              "particle_steps_per_s": e_steps1 / e_span1}},
     }
 
 

@@ -13,14 +13,21 @@
 // radix 8 (span L / 8^s); when log2 L is not a multiple of 3 a last radix-4 or
 // radix-2 stage follows.  A radix-8 stage runs in the registers of one thread
 // (its 8 inputs lie span/8 apart).  Between stages the tile goes through shared
-// memory, element-major (X[slot * B + c]) with bit 0 of the slot flipped by its
-// bit 3, which keeps every exchange pattern free of bank conflicts.  In-place
+// memory, element-major (X[slot * B + c]) with low bits of the slot flipped by
+// its bits 3 and up (SWZ): the column kernels flip bit 0 by bit 3; the row
+// kernels, whose 2- and 4-line tiles put 4 or 8 slots of one line in a half-warp,
+// flip bits 0-2 by bits 3-5, which removes the 2-way conflict of their last
+// radix-4 read (18% extra shared wavefronts at L = 256 by an emulation of the
+// bank pattern).  The wider flip measured faster for the rows (r2c rows 0.302 ->
+// 0.262 ms at 512^3) and slower for the columns (y pass 0.245 -> 0.283 ms).  In-place
 // DIF leaves frequency freq(p) in slot p, where freq is a fixed bit permutation
 // (the stage digits in reverse order): evaluated at compile time for the
 // register index and once per thread for the rest, so no table is read.
 //
 // Blocks are persistent (resident blocks per SM x SMs, looping over the tiles)
 // and stage the twiddle table in shared memory once.
+#include <atomic>
+
 #include "gev_fft_bfly.cuh"
 #include "gev_internal.cuh"
 
@@ -52,7 +59,7 @@ constexpr int col_min_blocks(int esize, int threads) {
   return (esize == 4 ? 1024 : 512) / threads > 0 ? (esize == 4 ? 1024 : 512) / threads : 1;
 }
 
-template <typename T, int SIGN, int L>
+template <typename T, int SIGN, int L, int SWZ = 1>
 struct RegFft {
   typedef typename CT<T>::C C;
   static constexpr int LG = ilog2c(L);
@@ -60,7 +67,7 @@ struct RegFft {
   static constexpr int NST = N8 + (REM ? 1 : 0);
   static constexpr int TPL = L / 8;  // threads per line
 
-  static __device__ __forceinline__ int phys(int p) { return p ^ ((p >> 3) & 1); }
+  static __device__ __forceinline__ int phys(int p) { return p ^ ((p >> 3) & SWZ); }
 
   // slot of register r of thread m in stage S (inputs and outputs alike)
   template <int S>
@@ -191,7 +198,7 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
                                                            const typename CT<T>::C *__restrict__ twHg,
                                                            const typename CT<T>::C *__restrict__ twN, int NH,
                                                            long nrows, int ntiles) {
-  typedef RegFft<T, -1, L> R;
+  typedef RegFft<T, -1, L, 7> R;
   typedef typename CT<T>::C C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
@@ -235,7 +242,7 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
                                                            const typename CT<T>::C *__restrict__ twHg,
                                                            const typename CT<T>::C *__restrict__ twN, int NH,
                                                            long nrows, int ntiles) {
-  typedef RegFft<T, +1, L> R;
+  typedef RegFft<T, +1, L, 7> R;
   typedef typename CT<T>::C C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C *tw = reinterpret_cast<C *>(smem_raw);
@@ -282,17 +289,19 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
 }
 
 // ------------------------------------------------------------------ launch --
+// per_sm: the kernel's resident blocks per SM, queried on its first launch (a
+// process-wide value; several host threads may launch it first at once)
 template <typename K>
-int launch_cfg(gev_ctx *ctx, K kern, int threads, size_t smem, long ntiles, int &per_sm, int &grid) {
-  if (per_sm <= 0) {
+int launch_cfg(gev_ctx *ctx, K kern, int threads, size_t smem, long ntiles, std::atomic<int> &per_sm, int &grid) {
+  int per = per_sm.load(std::memory_order_relaxed);
+  if (per <= 0) {
     if (smem > 48 * 1024 && cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
       return gev_fail(ctx, GEV_ECUDA, "fft: shared memory attribute");
-    int per = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, threads, smem) != cudaSuccess || per < 1)
       return gev_fail(ctx, GEV_ECUDA, "fft: occupancy query");
-    per_sm = per;
+    per_sm.store(per, std::memory_order_relaxed);
   }
-  const long g = (long)ctx->sms * per_sm;
+  const long g = (long)ctx->sms * per;
   grid = (int)(g < ntiles ? g : ntiles);
   return GEV_OK;
 }
@@ -301,7 +310,7 @@ template <typename T, int SIGN, int L, int LGB, bool POIS = false>
 int cols_LB(gev_ctx *ctx, const void *in, void *out, long ES, long PS, PoisArgs pois = PoisArgs{nullptr, 0.f, 0.f}) {
   static_assert(fits<L, LGB>(), "column tile too wide");
   typedef typename CT<T>::C C;
-  static int per_sm = 0;
+  static std::atomic<int> per_sm{0};
   constexpr int B = 1 << LGB, threads = (L / 8) * B;
   const int NH = ctx->N / 2 + 1;
   const long ntiles = (long)ctx->N * ((NH + B - 1) / B);
@@ -362,7 +371,7 @@ template <typename T, int L, int LGB>
 int r2c_LB(gev_ctx *ctx, const void *real, void *spec, long nrows) {
   static_assert(fits<L, LGB>(), "row tile too wide");
   typedef typename CT<T>::C C;
-  static int per_sm = 0;
+  static std::atomic<int> per_sm{0};
   constexpr int B = 1 << LGB, threads = (L / 8) * B;
   const int NH = ctx->N / 2 + 1;
   const long ntiles = (nrows + B - 1) / B;
@@ -381,7 +390,7 @@ template <typename T, int L, int LGB>
 int c2r_LB(gev_ctx *ctx, const void *spec, void *real, long nrows) {
   static_assert(fits<L, LGB>(), "row tile too wide");
   typedef typename CT<T>::C C;
-  static int per_sm = 0;
+  static std::atomic<int> per_sm{0};
   constexpr int B = 1 << LGB, threads = (L / 8) * B;
   const int NH = ctx->N / 2 + 1;
   const long ntiles = (nrows + B - 1) / B;

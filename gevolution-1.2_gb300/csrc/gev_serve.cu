@@ -1,6 +1,11 @@
 // gev_serve.cu -- continuous batching of independent simulations on one GPU
-// (include/gev_serve.h).  Host code: a scheduler thread drives the hot-path
-// library, one context (one CUDA stream) per admitted simulation.
+// (include/gev_serve.h).  Host code: scheduler threads drive the hot-path
+// library, one context (one CUDA stream) per admitted simulation.  Worker 0 also
+// admits requests; each admitted simulation is handed to the worker with the
+// fewest grid points in hand, and only that worker enqueues its cycles, so the
+// launches of different simulations are issued from several host threads at once
+// (a 64^3 cycle is some fifty short kernels: one thread cannot issue them as fast
+// as the GPU runs them for dozens of small simulations).
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -38,6 +43,7 @@ struct Active {
   int cycles = 0;
   long head = 0, tail = 0;  // events [tail, head) of the ring are in flight
   bool finishing = false;
+  int worker = 0;           // the scheduler thread that enqueues its cycles
 };
 
 struct Pending {
@@ -56,9 +62,11 @@ struct gev_server {
   std::deque<Pending> pending;
   std::vector<gev_result> done;
   std::vector<Active *> active;
+  std::mutex pool_mu;  // idle (taken before mu where both are held)
   std::map<std::pair<int, int>, std::vector<Slot *>> idle;
   std::map<std::pair<int, int>, size_t> footprint;
-  std::thread th;
+  int workers = 1;
+  std::vector<std::thread> th;
   bool stop = false;
   long next_id = 1;
   gev_server_stats st{};
@@ -98,6 +106,7 @@ void slot_measure(gev_server *s, Slot *sl) {
 Slot *slot_acquire(gev_server *s, int N, int prec, int *rc) {
   *rc = GEV_OK;
   auto key = std::make_pair(N, prec);
+  std::unique_lock<std::mutex> pk(s->pool_mu);
   auto &pool = s->idle[key];
   if (!pool.empty()) {
     Slot *sl = pool.back();
@@ -106,24 +115,32 @@ Slot *slot_acquire(gev_server *s, int N, int prec, int *rc) {
   }
   // the bytes it needs: measured for its size, else scaled as N^3 from the largest
   // size of its form measured so far, else unknown (the first slot is the probe)
-  auto fp = s->footprint.find(key);
-  bool known = fp != s->footprint.end();
-  size_t need = known ? fp->second : 0;
-  if (!known) {
-    int nk = 0;
-    size_t bk = 0;
-    for (auto &kv : s->footprint)
-      if (kv.first.second == prec && kv.first.first > nk) {
-        nk = kv.first.first;
-        bk = kv.second;
+  bool known;
+  size_t need;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto fp = s->footprint.find(key);
+    known = fp != s->footprint.end();
+    need = known ? fp->second : 0;
+    if (!known) {
+      int nk = 0;
+      size_t bk = 0;
+      for (auto &kv : s->footprint)
+        if (kv.first.second == prec && kv.first.first > nk) {
+          nk = kv.first.first;
+          bk = kv.second;
+        }
+      if (nk > 0) {
+        const double r = (double)N / (double)nk;
+        need = (size_t)((double)bk * r * r * r);
+        known = true;
       }
-    if (nk > 0) {
-      const double r = (double)N / (double)nk;
-      need = (size_t)((double)bk * r * r * r);
-      known = true;
     }
   }
-  auto fits = [&]() { return s->in_use + need <= s->budget; };
+  auto fits = [&]() {
+    std::lock_guard<std::mutex> lk(s->mu);
+    return s->in_use + need <= s->budget;
+  };
   while (!fits()) {  // release idle slots of other sizes, largest first
     Slot *victim = nullptr;
     std::vector<Slot *> *from = nullptr;
@@ -137,6 +154,7 @@ Slot *slot_acquire(gev_server *s, int N, int prec, int *rc) {
     from->erase(std::find(from->begin(), from->end(), victim));
     slot_destroy(s, victim);
   }
+  pk.unlock();
   Slot *sl = new Slot();
   sl->N = N;
   sl->prec = prec;
@@ -222,16 +240,24 @@ void finish(gev_server *s, Active *A, int status) {
   if (r.status) {
     slot_destroy(s, sl);  // a slot that failed is not reused
   } else {
+    std::lock_guard<std::mutex> pk(s->pool_mu);
     s->idle[std::make_pair(sl->N, sl->prec)].push_back(sl);
   }
   s->cv.notify_all();
 }
 
-void scheduler(gev_server *s) {
+// the worker with the fewest grid points among the simulations it enqueues
+int least_loaded_worker(gev_server *s) {
+  std::vector<double> load((size_t)s->workers, 0.);
+  for (Active *A : s->active) load[(size_t)A->worker] += (double)A->req.N * A->req.N * A->req.N;
+  return (int)(std::min_element(load.begin(), load.end()) - load.begin());
+}
+
+void scheduler(gev_server *s, int worker) {
   cudaSetDevice(s->device);
   while (true) {
-    // admission: requests in arrival order while their bytes fit
-    for (;;) {
+    // admission (worker 0): requests in arrival order while their bytes fit
+    for (; worker == 0;) {
       Pending p;
       {
         std::lock_guard<std::mutex> lk(s->mu);
@@ -283,6 +309,8 @@ void scheduler(gev_server *s) {
         std::lock_guard<std::mutex> lk(s->mu);
         s->st.admitted++;
         if (s->active.empty() && s->busy_since < 0.) s->busy_since = s->now();
+        // a failed admission is finished below by this worker
+        A->worker = (sl && !rc) ? least_loaded_worker(s) : 0;
         s->active.push_back(A);
         s->st.max_active_seen = std::max(s->st.max_active_seen, (long)s->active.size());
       }
@@ -308,11 +336,12 @@ void scheduler(gev_server *s) {
     // one round: each admitted simulation gets its next cycle enqueued, as far
     // as its in-flight window allows; finished ones hand back their result
     bool progressed = false;
-    std::vector<Active *> act;
+    std::vector<Active *> act;  // this worker's own: only it removes them
     {
       std::lock_guard<std::mutex> lk(s->mu);
       if (s->stop) break;
-      act = s->active;
+      for (Active *A : s->active)
+        if (A->worker == worker) act.push_back(A);
     }
     for (Active *A : act) {
       Slot *sl = A->slot;
@@ -374,7 +403,12 @@ int gev_server_footprint(int device, int N, int prec, size_t *bytes) {
 }
 
 int gev_server_create(int device, size_t bytes_budget, int max_active, int inflight, gev_server **out) {
-  if (!out || max_active < 0 || inflight < 0) return GEV_EINVAL;
+  return gev_server_create_workers(device, bytes_budget, max_active, inflight, 0, out);
+}
+
+int gev_server_create_workers(int device, size_t bytes_budget, int max_active, int inflight, int workers,
+                              gev_server **out) {
+  if (!out || max_active < 0 || inflight < 0 || workers < 0 || workers > GEV_SERVE_MAX_WORKERS) return GEV_EINVAL;
   if (cudaSetDevice(device) != cudaSuccess) return GEV_ENODEV;
   gev_server *s = new gev_server();
   s->device = device;
@@ -388,7 +422,12 @@ int gev_server_create(int device, size_t bytes_budget, int max_active, int infli
   s->budget = bytes_budget;
   s->st.bytes_budget = bytes_budget;
   s->t0 = Clock::now();
-  s->th = std::thread(scheduler, s);
+  if (workers == 0) {
+    const unsigned hc = std::thread::hardware_concurrency();
+    workers = hc >= 16 ? 4 : hc >= 8 ? 2 : 1;
+  }
+  s->workers = workers;
+  for (int k = 0; k < workers; ++k) s->th.emplace_back(scheduler, s, k);
   *out = s;
   return GEV_OK;
 }
@@ -436,6 +475,7 @@ int gev_server_stats_get(gev_server *s, gev_server_stats *out) {
   out->pending = (long)s->pending.size();
   out->bytes_in_use = s->in_use;
   out->bytes_peak = s->peak;
+  out->workers = s->workers;
   if (s->busy_since >= 0.) out->busy_seconds += s->now() - s->busy_since;
   return GEV_OK;
 }
@@ -447,7 +487,8 @@ int gev_server_destroy(gev_server *s) {
     s->stop = true;
   }
   s->cv.notify_all();
-  if (s->th.joinable()) s->th.join();
+  for (std::thread &t : s->th)
+    if (t.joinable()) t.join();
   for (Active *A : s->active) {
     if (A->slot) {
       cudaStreamSynchronize(A->slot->ctx->stream);

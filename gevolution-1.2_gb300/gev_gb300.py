@@ -744,11 +744,12 @@ class Result(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(n, _l) for n in ("submitted", "admitted", "completed", "failed", "active", "pending",
                                   "max_active_seen")] + [("particle_steps", _d), ("busy_seconds", _d)] + [
-        (n, ctypes.c_size_t) for n in ("bytes_budget", "bytes_in_use", "bytes_peak")]
+        (n, ctypes.c_size_t) for n in ("bytes_budget", "bytes_in_use", "bytes_peak")] + [("workers", _l)]
 
 
 _SERVE_SIGS = {
     "gev_server_create": [_i, ctypes.c_size_t, _i, _i, ctypes.POINTER(_vp)],
+    "gev_server_create_workers": [_i, ctypes.c_size_t, _i, _i, _i, ctypes.POINTER(_vp)],
     "gev_server_submit": [_vp, ctypes.POINTER(Request), ctypes.POINTER(_l)],
     "gev_server_poll": [_vp, ctypes.POINTER(Result), _i, ctypes.POINTER(_i)],
     "gev_server_drain": [_vp, _d],
@@ -786,10 +787,13 @@ def result_dict(r):
 class Server:
     """Continuous batching of simulations on one GPU (include/gev_serve.h)."""
 
-    def __init__(self, device=0, bytes_budget=0, max_active=0, inflight=0):
+    def __init__(self, device=0, bytes_budget=0, max_active=0, inflight=0, workers=0):
+        """workers: host threads that enqueue the simulations' cycles (0: chosen from
+        the host's hardware threads)."""
         self.handle = None
         h = _vp()
-        rc = _serve_lib().gev_server_create(device, bytes_budget, max_active, inflight, ctypes.byref(h))
+        rc = _serve_lib().gev_server_create_workers(device, bytes_budget, max_active, inflight, workers,
+                                                    ctypes.byref(h))
         if rc != OK:
             raise GevError("gev_server_create failed (%d)" % rc)
         self.handle = h.value

@@ -6,10 +6,10 @@
  * reaches its target.
  *
  * Each admitted simulation owns a context (gev_gb300.h) and so a CUDA stream of
- * its own; a scheduler thread inside the library enqueues one cycle
- * (gev_sim_step) per simulation in turn, keeping a bounded number of cycles in
- * flight on each stream, so that the kernels of different simulations overlap
- * on the device.  A simulation's work touches only its own buffers and every
+ * its own; scheduler threads inside the library enqueue one cycle
+ * (gev_sim_step) per simulation in turn, each thread its own share of the
+ * simulations, keeping a bounded number of cycles in flight on each stream, so
+ * that the kernels of different simulations overlap on the device.  A simulation's work touches only its own buffers and every
  * kernel is deterministic, so its result is the same bits whether it runs alone
  * or among others.  Contexts of a grid size are pooled and reused; a new request
  * is admitted when the bytes its grid size needs fit under the budget.
@@ -30,6 +30,7 @@ extern "C" {
 #endif
 
 #define GEV_SERVE_MAX_BINS 64
+#define GEV_SERVE_MAX_WORKERS 16
 
 typedef struct {
   int N;            /* grid points = particles per side (N % 4 == 0) */
@@ -57,6 +58,7 @@ typedef struct {
   double particle_steps;     /* summed over completed cycles */
   double busy_seconds;       /* time with at least one simulation admitted */
   size_t bytes_budget, bytes_in_use, bytes_peak;
+  long workers;              /* host threads that enqueue the simulations' cycles */
 } gev_server_stats;
 
 typedef struct gev_server gev_server;
@@ -65,6 +67,13 @@ typedef struct gev_server gev_server;
  * max_active: simulations on the device at once (0: no limit but the budget);
  * inflight: cycles enqueued ahead per simulation (0: 2) */
 int gev_server_create(int device, size_t bytes_budget, int max_active, int inflight, gev_server **out);
+/* the same with the number of host threads that enqueue the simulations' cycles
+ * (1 .. GEV_SERVE_MAX_WORKERS; 0: 4 on hosts with 16 or more hardware threads, 2
+ * with 8 or more, else 1, as gev_server_create chooses).  Worker 0 also admits
+ * requests; each admitted simulation is enqueued by one worker only, so its
+ * result does not depend on the count */
+int gev_server_create_workers(int device, size_t bytes_budget, int max_active, int inflight, int workers,
+                              gev_server **out);
 int gev_server_submit(gev_server *s, const gev_request *req, long *id);
 /* up to max completed results not yet returned; *n their number */
 int gev_server_poll(gev_server *s, gev_result *out, int max, int *n);

@@ -29,11 +29,14 @@ def run_alone(gpu, req):
             "occupation": occ}
 
 
-def test_results_same_alone_and_in_the_mix(gpu):
+@pytest.mark.parametrize("workers", [1, 4])
+def test_results_same_alone_and_in_the_mix(gpu, workers):
+    """With one scheduler thread and with four (each simulation's cycles enqueued by
+    one of them), every result is the same bits as the request run alone."""
     reqs = [gpu.request(32, seed=11, z_target=60.0), gpu.request(48, seed=12, z_target=80.0, Omega_cdm=0.3),
             gpu.request(32, seed=13, z_target=70.0, sigma8=0.85, prec=gpu.PREC_FP64),
             gpu.request(64, seed=14, z_target=75.0, n_s=0.95), gpu.request(32, seed=15, z_target=60.0)]
-    srv = gpu.Server()
+    srv = gpu.Server(workers=workers)
     ids = [srv.submit(r) for r in reqs]
     srv.drain(120.0)
     got = {r["id"]: r for r in srv.poll()}
