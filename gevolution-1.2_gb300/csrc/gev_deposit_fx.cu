@@ -388,106 +388,144 @@ __global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArray
   }
 }
 
-// one thread per node (x, y, z); out: T00 (1 comp) and / or Tij (6 comps, 00 01 02 11 12 22).
+// node i = (x, y, z): its 8 neighbouring cells' contributions, summed in int64 and
+// converted once; out: T00 (1 comp) and / or Tij (6 comps, 00 01 02 11 12 22)
+template <int KIND>
+__device__ __forceinline__ void gather_node(unsigned i, int x, int y, int z, const PclsArrays &P,
+                                            const uint32_t *__restrict__ start, const PrepArrays &A,
+                                            const float *__restrict__ phi, float *t00, float *tij, const FxParams &p,
+                                            int ks00, int ksij, float sg00, float sgij) {
+  constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
+  const int N = p.N;
+  const unsigned C = (unsigned)N * N * N;
+  const Nb3 b = nb3(i, x, y, z, N);
+  // phi at the node and its +x, +y, +z neighbours: the factors of the node's corner
+  // (T00, diagonal Tij) and the three plaquette sums of the off-diagonal components
+  float pn = 0.f, s01 = 0.f, s02 = 0.f, s12 = 0.f;
+  if (phi != nullptr) {  // indices summed in 32 bits: the offsets wrap modulo 2^32
+    const unsigned i100 = i + b.xp, i010 = i + b.yp, i001 = i + b.zp;
+    const unsigned i110 = i100 + b.yp, i101 = i100 + b.zp, i011 = i010 + b.zp;
+    const float f000 = __ldg(&phi[i]), f100 = __ldg(&phi[i100]), f010 = __ldg(&phi[i010]);
+    const float f110 = __ldg(&phi[i110]), f001 = __ldg(&phi[i001]);
+    const float f101 = __ldg(&phi[i101]), f011 = __ldg(&phi[i011]);
+    pn = f000;
+    s01 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f010), f100), f110);  // l0 + l2 + l4 + l6 of the particles' cells
+    s02 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f100), f101);  // l0 + l1 + l4 + l5
+    s12 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f010), f011);  // l0 + l1 + l2 + l3
+  }
+  long long a00 = 0, ad0 = 0, ad1 = 0, ad2 = 0, ao01 = 0, ao02 = 0, ao12 = 0;
+  // the contributions of particle j to this node, the node being corner (dx, dy, dz)
+  // of the particle's cell
+  auto add = [&](uint32_t j, int dx, int dy, int dz) {
+    uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
+    if constexpr (KIND == FX_T00) {
+      const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
+      v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), q.x);
+      v1 = make_uint4(q.y, 0u, 0u, 0u);
+    } else {
+      const uint4 *rec = A.rec + 3 * (size_t)j;
+      v0 = __ldg(rec);
+      v1 = __ldg(rec + 1);
+      v2 = __ldg(rec + 2);
+    }
+    const float u0 = __uint_as_float(v0.x), u1 = __uint_as_float(v0.y), u2 = __uint_as_float(v0.z);
+    const float w0 = dx ? u0 : __fsub_rn(1.f, u0), w1 = dy ? u1 : __fsub_rn(1.f, u1),
+                w2 = dz ? u2 : __fsub_rn(1.f, u2);
+    const float w = __fmul_rn(__fmul_rn(w0, w1), w2);
+    if (DO00)
+      a00 += (long long)(int)v0.w *
+             (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), pn))), sg00);
+    if (DOIJ) {
+      const float f = __uint_as_float(v1.y);
+      const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(f, pn))), sgij);
+      ad0 += (long long)(int)v1.z * G;
+      ad1 += (long long)(int)v1.w * G;
+      ad2 += (long long)(int)v2.x * G;
+      const float qf = __fmul_rn(0.25f, f);
+      if (dx == 0 && dy == 0)
+        ao01 += (long long)(int)v2.y * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, s01))), sgij);
+      if (dx == 0 && dz == 0)
+        ao02 += (long long)(int)v2.z * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, s02))), sgij);
+      if (dy == 0 && dz == 0)
+        ao12 += (long long)(int)v2.w * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, s12))), sgij);
+    }
+  };
+  // the 4 cell pairs (x - 1, x) of rows (y - dy, z - dz): all their bounds first;
+  // for x > 0 the two cells' particles are one contiguous run of the store
+  const unsigned cb[4] = {i, i + b.zm, i + b.ym, i + b.ym + b.zm};
+  uint32_t s0[4], s1[4], s2[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    s0[q] = start[cb[q] + b.xm];
+    s1[q] = start[cb[q]];
+    s2[q] = start[cb[q] + 1];
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int dy = q >> 1, dz = q & 1;
+    if (x > 0) {
+      for (uint32_t j = s0[q]; j < s2[q]; ++j) add(j, j < s1[q] ? 1 : 0, dy, dz);
+    } else {
+      for (uint32_t j = s1[q]; j < s2[q]; ++j) add(j, 0, dy, dz);
+      const uint32_t t1 = start[cb[q] + b.xm + 1];
+      for (uint32_t j = s0[q]; j < t1; ++j) add(j, 1, dy, dz);
+    }
+  }
+  if (DO00) {
+    const float v = float_of_fixed(a00, ks00);
+    t00[i] = p.overwrite ? v : t00[i] + v;
+  }
+  if (DOIJ) {
+    const long long acc[6] = {ad0, ao01, ao02, ad1, ao12, ad2};
+#pragma unroll
+    for (int c = 0; c < 6; ++c) {
+      const float v = float_of_fixed(acc[c], ksij);
+      float *o = tij + (size_t)c * C + i;
+      *o = p.overwrite ? v : *o + v;
+    }
+  }
+}
+
+// One thread per node.  While no cell holds more than PATCH_MC particles (the
+// nearly uniform early state) a warp takes 32 consecutive nodes of the flat index;
+// in a clustered state it takes the 32 nodes of a PX x PY x PZ patch (PX = 0: always
+// the flat index, for grids that the patch does not divide).  There the particles a
+// node walks (its 8 neighbouring cells) differ by orders of magnitude between
+// nodes, and a warp waits for its longest walk: a compact patch holds nodes of more
+// similar density than a line of 32 cells (lanes busy, counted from a 128^3 run at
+// z = 0: 17.8% in lines, 26.1% in 8 x 2 x 2 patches).  Measured over the last 20
+// cycles before z = 0 at 512^3: 13.41 ms against 14.58 ms in lines (4 x 4 x 2: 15.03,
+// 8 x 4 x 1: 14.20, 16 x 2 x 1: 14.16); in the first cycles the lines are faster
+// (the patch's nodes are four 32-byte row pieces rather than one 128-byte line).
+// Each node is one thread's either way, so the bits do not depend on the choice.
 // Six resident blocks per SM (40 registers; 48 and five blocks for T00 alone): the
 // loop is latency-bound, and the warps hide more than the few spilled words cost.
-template <int KIND>
+constexpr uint32_t PATCH_MC = 8;
+template <int KIND, int PX, int PY, int PZ>
 __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
                                                     const float *__restrict__ phi, float *t00, float *tij, FxParams p,
                                                     Div32 dN, const uint32_t *__restrict__ fxb) {
-  constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
   const int ks00 = (int)fxb[2], ksij = KIND == FX_T00TIJ ? (int)fxb[3] : (int)fxb[2];
   const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
   const int N = p.N;
   const unsigned C = (unsigned)N * N * N;
-  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
-    int x, y, z;
-    cell_xyz(i, N, p.lg, dN, x, y, z);
-    const Nb3 b = nb3(i, x, y, z, N);
-    // phi at the node and its +x, +y, +z neighbours: the factors of the node's corner
-    // (T00, diagonal Tij) and the three plaquette sums of the off-diagonal components
-    float pn = 0.f, s01 = 0.f, s02 = 0.f, s12 = 0.f;
-    if (phi != nullptr) {  // indices summed in 32 bits: the offsets wrap modulo 2^32
-      const unsigned i100 = i + b.xp, i010 = i + b.yp, i001 = i + b.zp;
-      const unsigned i110 = i100 + b.yp, i101 = i100 + b.zp, i011 = i010 + b.zp;
-      const float f000 = __ldg(&phi[i]), f100 = __ldg(&phi[i100]), f010 = __ldg(&phi[i010]);
-      const float f110 = __ldg(&phi[i110]), f001 = __ldg(&phi[i001]);
-      const float f101 = __ldg(&phi[i101]), f011 = __ldg(&phi[i011]);
-      pn = f000;
-      s01 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f010), f100), f110);  // l0 + l2 + l4 + l6 of the particles' cells
-      s02 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f100), f101);  // l0 + l1 + l4 + l5
-      s12 = __fadd_rn(__fadd_rn(__fadd_rn(f000, f001), f010), f011);  // l0 + l1 + l2 + l3
+  if (PX == 0 || fxb[1] <= PATCH_MC) {
+    for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
+      int x, y, z;
+      cell_xyz(i, N, p.lg, dN, x, y, z);
+      gather_node<KIND>(i, x, y, z, P, start, A, phi, t00, tij, p, ks00, ksij, sg00, sgij);
     }
-    long long a00 = 0, ad0 = 0, ad1 = 0, ad2 = 0, ao01 = 0, ao02 = 0, ao12 = 0;
-    // the contributions of particle j to this node, the node being corner (dx, dy, dz)
-    // of the particle's cell
-    auto add = [&](uint32_t j, int dx, int dy, int dz) {
-      uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
-      if constexpr (KIND == FX_T00) {
-        const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
-        v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), q.x);
-        v1 = make_uint4(q.y, 0u, 0u, 0u);
-      } else {
-        const uint4 *rec = A.rec + 3 * (size_t)j;
-        v0 = __ldg(rec);
-        v1 = __ldg(rec + 1);
-        v2 = __ldg(rec + 2);
-      }
-      const float u0 = __uint_as_float(v0.x), u1 = __uint_as_float(v0.y), u2 = __uint_as_float(v0.z);
-      const float w0 = dx ? u0 : __fsub_rn(1.f, u0), w1 = dy ? u1 : __fsub_rn(1.f, u1),
-                  w2 = dz ? u2 : __fsub_rn(1.f, u2);
-      const float w = __fmul_rn(__fmul_rn(w0, w1), w2);
-      if (DO00)
-        a00 += (long long)(int)v0.w *
-               (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), pn))), sg00);
-      if (DOIJ) {
-        const float f = __uint_as_float(v1.y);
-        const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(f, pn))), sgij);
-        ad0 += (long long)(int)v1.z * G;
-        ad1 += (long long)(int)v1.w * G;
-        ad2 += (long long)(int)v2.x * G;
-        const float qf = __fmul_rn(0.25f, f);
-        if (dx == 0 && dy == 0)
-          ao01 += (long long)(int)v2.y * (long long)gq(__fmul_rn(w2, __fadd_rn(1.f, __fmul_rn(qf, s01))), sgij);
-        if (dx == 0 && dz == 0)
-          ao02 += (long long)(int)v2.z * (long long)gq(__fmul_rn(w1, __fadd_rn(1.f, __fmul_rn(qf, s02))), sgij);
-        if (dy == 0 && dz == 0)
-          ao12 += (long long)(int)v2.w * (long long)gq(__fmul_rn(w0, __fadd_rn(1.f, __fmul_rn(qf, s12))), sgij);
-      }
-    };
-    // the 4 cell pairs (x - 1, x) of rows (y - dy, z - dz): all their bounds first;
-    // for x > 0 the two cells' particles are one contiguous run of the store
-    const unsigned cb[4] = {i, i + b.zm, i + b.ym, i + b.ym + b.zm};
-    uint32_t s0[4], s1[4], s2[4];
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      s0[q] = start[cb[q] + b.xm];
-      s1[q] = start[cb[q]];
-      s2[q] = start[cb[q] + 1];
-    }
-#pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      const int dy = q >> 1, dz = q & 1;
-      if (x > 0) {
-        for (uint32_t j = s0[q]; j < s2[q]; ++j) add(j, j < s1[q] ? 1 : 0, dy, dz);
-      } else {
-        for (uint32_t j = s1[q]; j < s2[q]; ++j) add(j, 0, dy, dz);
-        const uint32_t t1 = start[cb[q] + b.xm + 1];
-        for (uint32_t j = s0[q]; j < t1; ++j) add(j, 1, dy, dz);
-      }
-    }
-    if (DO00) {
-      const float v = float_of_fixed(a00, ks00);
-      t00[i] = p.overwrite ? v : t00[i] + v;
-    }
-    if (DOIJ) {
-      const long long acc[6] = {ad0, ao01, ao02, ad1, ao12, ad2};
-#pragma unroll
-      for (int c = 0; c < 6; ++c) {
-        const float v = float_of_fixed(acc[c], ksij);
-        float *o = tij + (size_t)c * C + i;
-        *o = p.overwrite ? v : *o + v;
-      }
+  } else if constexpr (PX > 0) {
+    static_assert(PX * PY * PZ == 32, "a patch is one warp");
+    const int lane = threadIdx.x & 31;
+    const int lx = lane % PX, ly = (lane / PX) % PY, lz = lane / (PX * PY);
+    const unsigned ppx = (unsigned)N / PX, ppy = (unsigned)N / PY, npatch = ppx * ppy * ((unsigned)N / PZ);
+    const unsigned nw = (gridDim.x * blockDim.x) >> 5;
+    for (unsigned q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; q < npatch; q += nw) {
+      const unsigned r = q / ppx, qz = r / ppy;
+      const int x = (int)(q - r * ppx) * PX + lx, y = (int)(r - qz * ppy) * PY + ly, z = (int)qz * PZ + lz;
+      const unsigned i = (unsigned)x + (unsigned)N * ((unsigned)y + (unsigned)N * (unsigned)z);
+      gather_node<KIND>(i, x, y, z, P, start, A, phi, t00, tij, p, ks00, ksij, sg00, sgij);
     }
   }
 }
@@ -605,25 +643,34 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     // of a few large blocks cannot (512^3 cycle: 29.7 ms at 96, 30.7 at 16, 31.8 at 12)
     const int gb = grid_for(ctx, (size_t)C, 256, 96);
     const Div32 dN = make_div32((unsigned)N);
+    // the patch walk needs N divisible by its 8 x 2 x 2 shape
+    const bool patch = N % 8 == 0;
+#define GEV_GATHER(K)                                                                                               \
+  do {                                                                                                              \
+    if (patch)                                                                                                      \
+      k_dep_gather<K, 8, 2, 2><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds); \
+    else                                                                                                            \
+      k_dep_gather<K, 0, 0, 0><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds); \
+  } while (0)
     GevTimed tm_p(ctx, "k_fx_prep");
     if (kind == FX_T00) {
       k_fx_prep<FX_T00><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_T00><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
+      GEV_GATHER(FX_T00);
     } else if (kind == FX_TIJ) {
       k_fx_prep<FX_TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
+      GEV_GATHER(FX_TIJ);
     } else {
       k_fx_prep<FX_T00TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
       GevTimed tm_g(ctx, "k_dep_gather");
-      k_dep_gather<FX_T00TIJ><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds);
+      GEV_GATHER(FX_T00TIJ);
     }
     GEV_LAUNCH_CHECK(ctx);
     return GEV_OK;
