@@ -638,10 +638,12 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     float *t00 = kind == FX_TIJ ? nullptr : (float *)out->d;
     float *tij = kind == FX_TIJ ? (float *)out->d : (out2 ? (float *)out2->d : nullptr);
     const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
-    // many small blocks (up to 96 a SM, 16 waves of the six resident): the block scheduler
+    // many small blocks (up to 384 a SM, 64 waves of the six resident): the block scheduler
     // refills an SM as soon as a block's nodes are done, which the long latency-bound walks
-    // of a few large blocks cannot (512^3 cycle: 29.7 ms at 96, 30.7 at 16, 31.8 at 12)
-    const int gb = grid_for(ctx, (size_t)C, 256, 96);
+    // of a few large blocks cannot (first 512^3 cycles: 29.7 ms a cycle at 96, 30.7 at 16,
+    // 31.8 at 12; late cycles, patch walk: gather 12.87 ms at 384, 13.09 at 192, 13.40 at 96,
+    // 13.84 at 48, 13.25 with one block per 256 nodes)
+    const int gb = grid_for(ctx, (size_t)C, 256, 384);
     const Div32 dN = make_div32((unsigned)N);
     // the patch walk needs N divisible by its 8 x 2 x 2 shape
     const bool patch = N % 8 == 0;
