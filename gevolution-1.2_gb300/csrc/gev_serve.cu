@@ -60,6 +60,7 @@ struct gev_server {
   std::mutex mu;
   std::condition_variable cv;
   std::deque<Pending> pending;
+  int admitting = 0;  // taken off pending, not yet on active (drain waits for them too)
   std::vector<gev_result> done;
   std::vector<Active *> active;
   std::mutex pool_mu;  // idle (taken before mu where both are held)
@@ -279,6 +280,7 @@ void scheduler(gev_server *s, int worker) {
       {
         std::lock_guard<std::mutex> lk(s->mu);
         s->pending.pop_front();
+        s->admitting++;
       }
       Active *A = new Active();
       A->id = p.id;
@@ -312,6 +314,7 @@ void scheduler(gev_server *s, int worker) {
         // a failed admission is finished below by this worker
         A->worker = (sl && !rc) ? least_loaded_worker(s) : 0;
         s->active.push_back(A);
+        s->admitting--;
         s->st.max_active_seen = std::max(s->st.max_active_seen, (long)s->active.size());
       }
       if (!sl || rc) {
@@ -460,9 +463,9 @@ int gev_server_drain(gev_server *s, double timeout_s) {
   if (!s) return GEV_EINVAL;
   std::unique_lock<std::mutex> lk(s->mu);
   const auto until = Clock::now() + std::chrono::duration<double>(timeout_s > 0. ? timeout_s : 1e9);
-  while (!s->pending.empty() || !s->active.empty()) {
-    if (s->cv.wait_until(lk, until) == std::cv_status::timeout && (!s->pending.empty() || !s->active.empty()))
-      return GEV_ETIMEOUT;
+  auto busy = [&]() { return !s->pending.empty() || s->admitting > 0 || !s->active.empty(); };
+  while (busy()) {
+    if (s->cv.wait_until(lk, until) == std::cv_status::timeout && busy()) return GEV_ETIMEOUT;
   }
   return GEV_OK;
 }
@@ -472,7 +475,7 @@ int gev_server_stats_get(gev_server *s, gev_server_stats *out) {
   std::lock_guard<std::mutex> lk(s->mu);
   *out = s->st;
   out->active = (long)s->active.size();
-  out->pending = (long)s->pending.size();
+  out->pending = (long)s->pending.size() + s->admitting;
   out->bytes_in_use = s->in_use;
   out->bytes_peak = s->peak;
   out->workers = s->workers;

@@ -85,3 +85,18 @@ def test_requests_arriving_while_others_run(gpu):
     srv.close()
     assert all(res[i]["status"] == 0 for i in [first] + later)
     assert all(res[i]["t_submit"] > res[first]["t_submit"] for i in later)
+
+
+def test_drain_returns_every_result_one_slot_at_a_time(gpu):
+    """With one simulation on the device at a time each request is admitted as the
+    previous one finishes; drain must not return while the last one is between the
+    queue and the device."""
+    srv = gpu.Server(max_active=1)
+    ids = [srv.submit(gpu.request(32, seed=60 + k, z_target=90.0)) for k in range(6)]
+    srv.drain(120.0)
+    res = {r["id"]: r for r in srv.poll()}
+    st = srv.stats()
+    srv.close()
+    assert sorted(res) == sorted(ids)
+    assert all(r["status"] == 0 for r in res.values())
+    assert st["completed"] == 6 and st["active"] == 0 and st["pending"] == 0
