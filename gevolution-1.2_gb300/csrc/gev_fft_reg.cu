@@ -130,9 +130,17 @@ struct RegFft {
 };
 
 // row of natural-order element k in the tile the row kernels write after the last
-// stage: bits 0-1 flipped by bits 4-5, so that the thread groups of a warp, whose
-// outputs lie 16 elements apart, fall on all four quarters of the banks
-__device__ __forceinline__ int nat(int k) { return k ^ ((k >> 4) & 3); }
+// stage.  With 4 or 8 lines a tile, bits 0-1 are flipped by bits 4-5, so that the
+// thread groups of a warp, whose outputs lie 16 elements apart, fall on all four
+// quarters of the banks.  With 2 lines a half-warp holds 8 threads of a line, whose
+// outputs differ in bit 0 and bits 4-5: bits 1-2 are flipped by bits 4-5 instead, so
+// that all 8 land in different bank pairs (r2c 0.833 -> 0.820 ms and c2r 0.827 ->
+// 0.818 ms for a 512^3 transform with 2-line row tiles; the same bits).
+template <int LGB>
+__device__ __forceinline__ int nat(int k) {
+  if constexpr (LGB == 1) return k ^ ((k >> 3) & 6);
+  return k ^ ((k >> 4) & 3);
+}
 
 template <typename C>
 __device__ __forceinline__ void stage_tw(C *tw, const C *__restrict__ g, int L) {
@@ -217,7 +225,7 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
     R::template run_from<0>(v, X, B, c, m, tw);
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 8; ++q) X[nat(kb | R::freq(q)) * B + c] = v[q];  // Z[k], natural order
+    for (int q = 0; q < 8; ++q) X[nat<LGB>(kb | R::freq(q)) * B + c] = v[q];  // Z[k], natural order
     __syncthreads();
     if (on) {
       C *dst = out + row * NH;
@@ -225,8 +233,8 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
       for (int r = 0; r <= 8; ++r) {
         if (r == 8 && m != 0) break;
         const int k = r < 8 ? m + r * R::TPL : L;
-        const C zk = X[nat(k & (L - 1)) * B + c];
-        const C zc = cconj(X[nat((L - k) & (L - 1)) * B + c]);
+        const C zk = X[nat<LGB>(k & (L - 1)) * B + c];
+        const C zc = cconj(X[nat<LGB>((L - k) & (L - 1)) * B + c]);
         const C E = cscale((T)0.5, cadd(zk, zc));
         const C d = csub(zk, zc);
         const C O = cmk<C>((T)0.5 * d.y, (T)-0.5 * d.x);  // -i/2 (zk - zc)
@@ -275,14 +283,14 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
     R::template run_from<0>(v, X, B, c, m, tw);
     __syncthreads();
 #pragma unroll
-    for (int q = 0; q < 8; ++q) X[nat(kb | R::freq(q)) * B + c] = v[q];
+    for (int q = 0; q < 8; ++q) X[nat<LGB>(kb | R::freq(q)) * B + c] = v[q];
     __syncthreads();
     if (on) {
       C *dst = reinterpret_cast<C *>(out) + row * L;
 #pragma unroll
       for (int r = 0; r < 8; ++r) {
         const int k = m + r * R::TPL;
-        dst[k] = X[nat(k) * B + c];
+        dst[k] = X[nat<LGB>(k) * B + c];
       }
     }
   }
