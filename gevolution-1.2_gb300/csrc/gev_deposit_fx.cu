@@ -52,22 +52,60 @@ __device__ __forceinline__ long face_index(int x, int y, int z, const FxParams &
   return (p.nPX + p.nPY) * NN + (long)(z / TZ) * NN + (long)y * p.N + x;
 }
 
+// the dense-cell tables of the gather deposit (k_dense_sums below)
+// dense above 12 particles: measured over the last 20 cycles before z = 0 at 512^3,
+// the cycle took 38.73 ms with 8, 37.97 with 12, 38.03 with 16, 38.34 with 24 and
+// 38.64 with 32 (the gather's remaining walks against the dense cells' own pass)
+constexpr uint32_t DENSE_T = 12;
+constexpr int DENSE_NS = 38;
+constexpr uint32_t DENSE_NONE = 0xffffffffu;
+struct DenseTab {
+  uint32_t *slot_of;  // per cell, valid for the cells above thr of this call
+  uint32_t *list;     // slot -> cell
+  uint32_t *count;    // dense cells found (may exceed cap)
+  uint32_t cap;
+  uint32_t thr;      // cells with more particles are dense
+  long long *sums;    // slot * DENSE_NS + index
+};
+
+
 // The fixed-point scale comes from the data, on the device: max |q|^2 over the
 // particles and the most particles in one cell.  A cell's sum has at most 8 x that
 // many contributions (its 8 neighbouring cells), each below c_max of the kind, and
 // must stay below 2^62; max reductions do not depend on order, so neither does the
 // scale.
+// For the gather kinds (D.slot_of set) the same pass over the cell counts gives every
+// cell with more than D.thr particles the next dense slot (a warp-aggregated counter),
+// or DENSE_NONE once the D.cap slots are taken: every such cell's entry is written,
+// and the gather reads only such cells' entries (the counts and the cell starts it
+// walks come from the same relink).
 __global__ void __launch_bounds__(256) k_fx_bounds(const float *__restrict__ vx, const float *__restrict__ vy,
                                                    const float *__restrict__ vz, long n,
                                                    const uint32_t *__restrict__ count, const float *__restrict__ phi,
-                                                   long C, uint32_t *bounds) {
+                                                   long C, uint32_t *bounds, DenseTab D) {
   float q2 = 0.f, ph = 0.f;
   uint32_t mc = 0u;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     q2 = fmaxf(q2, vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
-  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < C; c += (long)gridDim.x * blockDim.x) {
-    mc = max(mc, count[c]);
-    if (phi) ph = fmaxf(ph, fabsf(phi[c]));
+  const unsigned lane = threadIdx.x & 31u;
+  const long Cw = (C + 31) & ~31L;  // every lane of a warp runs the same iterations
+  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < Cw; c += (long)gridDim.x * blockDim.x) {
+    const uint32_t k = c < C ? count[c] : 0u;
+    mc = max(mc, k);
+    if (phi && c < C) ph = fmaxf(ph, fabsf(phi[c]));
+    if (D.slot_of == nullptr) continue;  // not a gather kind (uniform: a kernel argument)
+    const bool dense = k > D.thr;
+    const unsigned m = __ballot_sync(0xffffffffu, dense);
+    if (m == 0u) continue;
+    const int leader = __ffs(m) - 1;
+    uint32_t base = 0u;
+    if ((int)lane == leader) base = atomicAdd(D.count, (uint32_t)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (dense) {
+      const uint32_t slot = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
+      D.slot_of[c] = slot < D.cap ? slot : DENSE_NONE;
+      if (slot < D.cap) D.list[slot] = (uint32_t)c;
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     q2 = fmaxf(q2, __shfl_xor_sync(0xffffffffu, q2, o));
@@ -388,13 +426,129 @@ __global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArray
   }
 }
 
+// ------------------------------------------------------------ dense cells --
+// In a clustered state single cells hold tens to hundreds of particles, and each of
+// the cell's 8 corner nodes walks all of them: the thread with such a cell in its
+// walk keeps its warp busy long after the other lanes are done.  Cells with more
+// than D.thr particles are therefore summed once: a warp per cell forms the
+// contributions the gather would form at each of the cell's 8 corners (the same FP32
+// weight factors with the corner node's phi, rounded the same way) and adds them in
+// int64; the gather adds a dense cell's sums at its corner instead of walking it.
+// Integer sums do not depend on the grouping of the additions, so the result is the
+// same bits whichever cells take this path.  A cell finds its sums through a direct
+// cell -> slot map, which k_fx_bounds writes for the dense cells of this call as it
+// reduces the cell counts, and which the gather reads only for cells holding more
+// than D.thr particles.  Slots run out at `cap`; dense cells beyond it are walked as
+// before.  (A warp per dense cell through a hash map, with the gather walking dense
+// cells in a separate loop, ran slower than the plain walk: the lanes of a warp took
+// both loop shapes one after the other.)
+//
+// The 38 sums of a slot, corner k = dx + 2 dy + 4 dz of the cell:
+//   [k]          T00 at corner k
+//   [8 + 3k + c] the diagonal Tij_cc at corner k
+//   [32 + dz]    Tij_01 at corner (0, 0, dz)   (the plaquettes the gather's nodes own)
+//   [34 + dy]    Tij_02 at corner (0, dy, 0)
+//   [36 + dx]    Tij_12 at corner (dx, 0, 0)
+// A warp per dense cell: lane l takes the cell's particles l, l + 32, ... and forms
+// their contributions at the cell's 8 corners as gather_node's add() forms them for
+// a node; the lanes' int64 sums are added through shared memory (each lane writes its
+// 38, then lane k adds the 32 values of sum k).
+constexpr int DENSE_WARPS = 4;
+template <int KIND>
+__global__ void __launch_bounds__(32 * DENSE_WARPS) k_dense_sums(PclsArrays P, const uint32_t *__restrict__ start,
+                                                                PrepArrays A, const float *__restrict__ phi, FxParams p,
+                                                                Div32 dN, const uint32_t *__restrict__ fxb, DenseTab D) {
+  constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
+  __shared__ long long red[DENSE_WARPS][DENSE_NS][33];
+  const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
+  const int N = p.N;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const uint32_t nd = min(*D.count, D.cap);
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nd; s += warps) {
+    const uint32_t c = D.list[s];
+    int x, y, z;
+    cell_xyz(c, N, p.lg, dN, x, y, z);
+    const Nb3 b = nb3(c, x, y, z, N);
+    // phi at the cell's 8 corners f[dx + 2 dy + 4 dz] (indices summed in 32 bits)
+    float f[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const unsigned ik = c + ((k & 1) ? b.xp : 0u) + ((k & 2) ? b.yp : 0u) + ((k & 4) ? b.zp : 0u);
+      f[k] = phi != nullptr ? __ldg(&phi[ik]) : 0.f;
+    }
+    // the plaquette sums of the corner nodes that own them, in gather_node's order
+    float s01[2], s02[2], s12[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      s01[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[4 * d], f[2 + 4 * d]), f[1 + 4 * d]), f[3 + 4 * d]);
+      s02[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[2 * d], f[2 * d + 4]), f[1 + 2 * d]), f[1 + 2 * d + 4]);
+      s12[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[d], f[d + 4]), f[d + 2]), f[d + 6]);
+    }
+    long long acc[DENSE_NS];
+#pragma unroll
+    for (int k = 0; k < DENSE_NS; ++k) acc[k] = 0;
+    const uint32_t j1 = start[c + 1];
+    for (uint32_t j = start[c] + lane; j < j1; j += 32) {
+      uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
+      if constexpr (KIND == FX_T00) {
+        const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
+        v0 = make_uint4(__float_as_uint(P.rx[j]), __float_as_uint(P.ry[j]), __float_as_uint(P.rz[j]), q.x);
+        v1 = make_uint4(q.y, 0u, 0u, 0u);
+      } else {
+        const uint4 *rec = A.rec + 3 * (size_t)j;
+        v0 = __ldg(rec);
+        v1 = __ldg(rec + 1);
+        v2 = __ldg(rec + 2);
+      }
+      const float u0 = __uint_as_float(v0.x), u1 = __uint_as_float(v0.y), u2 = __uint_as_float(v0.z);
+      const float wl0[2] = {__fsub_rn(1.f, u0), u0}, wl1[2] = {__fsub_rn(1.f, u1), u1},
+                  wl2[2] = {__fsub_rn(1.f, u2), u2};
+      const float fT = __uint_as_float(v1.y), qf = __fmul_rn(0.25f, fT);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        const int dx = k & 1, dy = (k >> 1) & 1, dz = k >> 2;
+        const float w = __fmul_rn(__fmul_rn(wl0[dx], wl1[dy]), wl2[dz]);
+        if (DO00)
+          acc[k] += (long long)(int)v0.w *
+                    (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), f[k]))), sg00);
+        if (DOIJ) {
+          const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(fT, f[k]))), sgij);
+          acc[8 + 3 * k] += (long long)(int)v1.z * G;
+          acc[9 + 3 * k] += (long long)(int)v1.w * G;
+          acc[10 + 3 * k] += (long long)(int)v2.x * G;
+        }
+      }
+      if (DOIJ) {
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+          acc[32 + d] += (long long)(int)v2.y * (long long)gq(__fmul_rn(wl2[d], __fadd_rn(1.f, __fmul_rn(qf, s01[d]))), sgij);
+          acc[34 + d] += (long long)(int)v2.z * (long long)gq(__fmul_rn(wl1[d], __fadd_rn(1.f, __fmul_rn(qf, s02[d]))), sgij);
+          acc[36 + d] += (long long)(int)v2.w * (long long)gq(__fmul_rn(wl0[d], __fadd_rn(1.f, __fmul_rn(qf, s12[d]))), sgij);
+        }
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < DENSE_NS; ++k) red[wib][k][lane] = acc[k];
+    __syncwarp();
+    long long *out = D.sums + (size_t)s * DENSE_NS;
+    for (int k = lane; k < DENSE_NS; k += 32) {
+      long long v = 0;
+#pragma unroll 8
+      for (int l = 0; l < 32; ++l) v += red[wib][k][l];
+      out[k] = v;
+    }
+    __syncwarp();  // red is rewritten for the warp's next cell
+  }
+}
+
 // node i = (x, y, z): its 8 neighbouring cells' contributions, summed in int64 and
 // converted once; out: T00 (1 comp) and / or Tij (6 comps, 00 01 02 11 12 22)
 template <int KIND>
 __device__ __forceinline__ void gather_node(unsigned i, int x, int y, int z, const PclsArrays &P,
                                             const uint32_t *__restrict__ start, const PrepArrays &A,
                                             const float *__restrict__ phi, float *t00, float *tij, const FxParams &p,
-                                            int ks00, int ksij, float sg00, float sgij) {
+                                            int ks00, int ksij, float sg00, float sgij, const DenseTab &D) {
   constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
   const int N = p.N;
   const unsigned C = (unsigned)N * N * N;
@@ -460,15 +614,41 @@ __device__ __forceinline__ void gather_node(unsigned i, int x, int y, int z, con
     s1[q] = start[cb[q]];
     s2[q] = start[cb[q] + 1];
   }
+  // a dense cell's sums at this node's corner (dx, dy, dz) of it, if it has a slot
+  auto dense = [&](uint32_t cell, int dx, int dy, int dz) -> bool {
+    const uint32_t slot = D.slot_of[cell];
+    if (slot >= D.cap) return false;  // DENSE_NONE: no slot was left for it
+    const long long *hs = D.sums + (size_t)slot * DENSE_NS;
+    const int k = dx + 2 * dy + 4 * dz;
+    if (DO00) a00 += hs[k];
+    if (DOIJ) {
+      ad0 += hs[8 + 3 * k];
+      ad1 += hs[9 + 3 * k];
+      ad2 += hs[10 + 3 * k];
+      if (dx == 0 && dy == 0) ao01 += hs[32 + dz];
+      if (dx == 0 && dz == 0) ao02 += hs[34 + dy];
+      if (dy == 0 && dz == 0) ao12 += hs[36 + dx];
+    }
+    return true;
+  };
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int dy = q >> 1, dz = q & 1;
+    // cell A = (x - 1, ...), whose corner (1, dy, dz) this node is, particles [s0, eA);
+    // cell B = (x, ...), corner (0, dy, dz), particles [s1, s2)
+    const uint32_t eA = x > 0 ? s1[q] : start[cb[q] + b.xm + 1];
+    const bool skipA = eA - s0[q] > D.thr && dense(cb[q] + b.xm, 1, dy, dz);
+    const bool skipB = s2[q] - s1[q] > D.thr && dense(cb[q], 0, dy, dz);
     if (x > 0) {
-      for (uint32_t j = s0[q]; j < s2[q]; ++j) add(j, j < s1[q] ? 1 : 0, dy, dz);
+      // one loop over the contiguous pair, a summed cell cut off its end: every lane of
+      // a warp runs the same loop, whichever of its cells are dense
+      const uint32_t jb = skipA ? s1[q] : s0[q], je = skipB ? s1[q] : s2[q];
+      for (uint32_t j = jb; j < je; ++j) add(j, j < s1[q] ? 1 : 0, dy, dz);
     } else {
-      for (uint32_t j = s1[q]; j < s2[q]; ++j) add(j, 0, dy, dz);
-      const uint32_t t1 = start[cb[q] + b.xm + 1];
-      for (uint32_t j = s0[q]; j < t1; ++j) add(j, 1, dy, dz);
+      if (!skipB)
+        for (uint32_t j = s1[q]; j < s2[q]; ++j) add(j, 0, dy, dz);
+      if (!skipA)
+        for (uint32_t j = s0[q]; j < eA; ++j) add(j, 1, dy, dz);
     }
   }
   if (DO00) {
@@ -504,7 +684,7 @@ constexpr uint32_t PATCH_MC = 8;
 template <int KIND, int PX, int PY, int PZ>
 __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
                                                     const float *__restrict__ phi, float *t00, float *tij, FxParams p,
-                                                    Div32 dN, const uint32_t *__restrict__ fxb) {
+                                                    Div32 dN, const uint32_t *__restrict__ fxb, DenseTab D) {
   const int ks00 = (int)fxb[2], ksij = KIND == FX_T00TIJ ? (int)fxb[3] : (int)fxb[2];
   const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
   const int N = p.N;
@@ -513,7 +693,7 @@ __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(Pcls
     for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < C; i += gridDim.x * blockDim.x) {
       int x, y, z;
       cell_xyz(i, N, p.lg, dN, x, y, z);
-      gather_node<KIND>(i, x, y, z, P, start, A, phi, t00, tij, p, ks00, ksij, sg00, sgij);
+      gather_node<KIND>(i, x, y, z, P, start, A, phi, t00, tij, p, ks00, ksij, sg00, sgij, D);
     }
   } else if constexpr (PX > 0) {
     static_assert(PX * PY * PZ == 32, "a patch is one warp");
@@ -525,7 +705,7 @@ __global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(Pcls
       const unsigned r = q / ppx, qz = r / ppy;
       const int x = (int)(q - r * ppx) * PX + lx, y = (int)(r - qz * ppy) * PY + ly, z = (int)qz * PZ + lz;
       const unsigned i = (unsigned)x + (unsigned)N * ((unsigned)y + (unsigned)N * (unsigned)z);
-      gather_node<KIND>(i, x, y, z, P, start, A, phi, t00, tij, p, ks00, ksij, sg00, sgij);
+      gather_node<KIND>(i, x, y, z, P, start, A, phi, t00, tij, p, ks00, ksij, sg00, sgij, D);
     }
   }
 }
@@ -610,20 +790,15 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   const float *fphi = phi ? (const float *)phi->d : nullptr;
   const unsigned blocks = (unsigned)(ntx * nty * ntz);
   const long C = (long)N * N * N;
-  GevTimed tm_b(ctx, "k_fx_bounds+k_fx_scale");
-  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->bounds, 0, 16 * sizeof(uint32_t), ctx->stream));
-  k_fx_bounds<<<grid_for(ctx, (size_t)(p->n > C ? p->n : C), 256, 8), 256, 0, ctx->stream>>>(
-      (const float *)p->cur.vx, (const float *)p->cur.vy, (const float *)p->cur.vz, p->n, p->count,
-      kind == FX_MASS ? nullptr : fphi, C, p->bounds);
-  GEV_LAUNCH_CHECK(ctx);
-  k_fx_scale<<<1, 1, 0, ctx->stream>>>(p->bounds, kind, mass, a);
-  GEV_LAUNCH_CHECK(ctx);
-  tm_b.stop();
+  // gather kinds: the prefactor records live in the alt array set, which only a relink
+  // writes (an allocation of their own only if that block were too small), and the
+  // dense-cell tables after them when the block has room, else in an allocation of
+  // their own (slots for one dense cell in 64 particles)
+  void *rec = nullptr;
+  const size_t rec_bytes = (size_t)(p->cap > 0 ? p->cap : 1) * PREP_WORDS * 4;
+  DenseTab dt{nullptr, nullptr, nullptr, 0u, 0u, nullptr};
   if (gather) {
-    // the records live in the alt array set, which only a relink writes (an allocation
-    // of their own only if that block were too small)
-    const size_t rec_bytes = (size_t)(p->cap > 0 ? p->cap : 1) * PREP_WORDS * 4;
-    void *rec = p->alt.block_bytes >= rec_bytes ? p->alt.block : p->prep;
+    rec = p->alt.block_bytes >= rec_bytes ? p->alt.block : p->prep;
     if (!rec) {
       const size_t bytes = rec_bytes;
       if (cudaMalloc(&p->prep, bytes) != cudaSuccess) {
@@ -634,6 +809,44 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
       p->bytes += bytes;
       rec = p->prep;
     }
+    auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const long np = p->cap > 0 ? p->cap : 1;
+    const uint32_t dcap = (uint32_t)(np / 64 > 1024 ? np / 64 : 1024);
+    const size_t o_list = al((size_t)C * 4), o_count = o_list + al((size_t)dcap * 4), o_sums = o_count + 256;
+    const size_t dense_bytes = o_sums + (size_t)dcap * DENSE_NS * 8;
+    char *base = nullptr;
+    if (rec == p->alt.block && p->alt.block_bytes >= al(rec_bytes) + dense_bytes) {
+      base = (char *)p->alt.block + al(rec_bytes);
+    } else {
+      if (!p->dense) {
+        if (cudaMalloc(&p->dense, dense_bytes) != cudaSuccess) {
+          cudaGetLastError();
+          p->dense = nullptr;
+          return gev_fail(ctx, GEV_ENOMEM, "deposit: dense-cell table allocation failed");
+        }
+        ctx->bytes_in_use += dense_bytes;
+        p->bytes += dense_bytes;
+      }
+      base = (char *)p->dense;
+    }
+    dt.slot_of = (uint32_t *)base;
+    dt.list = (uint32_t *)(base + o_list);
+    dt.count = (uint32_t *)(base + o_count);
+    dt.sums = (long long *)(base + o_sums);
+    dt.cap = dcap;
+    dt.thr = DENSE_T;
+    GEV_CHECK_CUDA(ctx, cudaMemsetAsync(dt.count, 0, 4, ctx->stream));
+  }
+  GevTimed tm_b(ctx, "k_fx_bounds+k_fx_scale");
+  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->bounds, 0, 16 * sizeof(uint32_t), ctx->stream));
+  k_fx_bounds<<<grid_for(ctx, (size_t)(p->n > C ? p->n : C), 256, 8), 256, 0, ctx->stream>>>(
+      (const float *)p->cur.vx, (const float *)p->cur.vy, (const float *)p->cur.vz, p->n, p->count,
+      kind == FX_MASS ? nullptr : fphi, C, p->bounds, dt);
+  GEV_LAUNCH_CHECK(ctx);
+  k_fx_scale<<<1, 1, 0, ctx->stream>>>(p->bounds, kind, mass, a);
+  GEV_LAUNCH_CHECK(ctx);
+  tm_b.stop();
+  if (gather) {
     const PrepArrays pa = prep_arrays(rec, p->cap > 0 ? p->cap : 1);
     float *t00 = kind == FX_TIJ ? nullptr : (float *)out->d;
     float *tij = kind == FX_TIJ ? (float *)out->d : (out2 ? (float *)out2->d : nullptr);
@@ -647,30 +860,40 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     const Div32 dN = make_div32((unsigned)N);
     // the patch walk needs N divisible by its 8 x 2 x 2 shape
     const bool patch = N % 8 == 0;
+#define GEV_DENSE(K)                                                                                         \
+  do {                                                                                                       \
+    GevTimed tm_d(ctx, "k_dense_sums");                                                                      \
+    k_dense_sums<K><<<ctx->sms * 8, 32 * DENSE_WARPS, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, fp, dN,  \
+                                                                        p->bounds, dt);                     \
+    GEV_LAUNCH_CHECK(ctx);                                                                                   \
+  } while (0)
 #define GEV_GATHER(K)                                                                                               \
   do {                                                                                                              \
     if (patch)                                                                                                      \
-      k_dep_gather<K, 8, 2, 2><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds); \
+      k_dep_gather<K, 8, 2, 2><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, dt); \
     else                                                                                                            \
-      k_dep_gather<K, 0, 0, 0><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds); \
+      k_dep_gather<K, 0, 0, 0><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, dt); \
   } while (0)
     GevTimed tm_p(ctx, "k_fx_prep");
     if (kind == FX_T00) {
       k_fx_prep<FX_T00><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
+      GEV_DENSE(FX_T00);
       GevTimed tm_g(ctx, "k_dep_gather");
       GEV_GATHER(FX_T00);
     } else if (kind == FX_TIJ) {
       k_fx_prep<FX_TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
+      GEV_DENSE(FX_TIJ);
       GevTimed tm_g(ctx, "k_dep_gather");
       GEV_GATHER(FX_TIJ);
     } else {
       k_fx_prep<FX_T00TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
+      GEV_DENSE(FX_T00TIJ);
       GevTimed tm_g(ctx, "k_dep_gather");
       GEV_GATHER(FX_T00TIJ);
     }

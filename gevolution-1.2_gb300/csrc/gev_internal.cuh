@@ -142,6 +142,10 @@ struct gev_pcls {
   // mixed-form T00 / Tij deposit: per-particle prefactor records (12 words a particle),
   // kept in the alt array set's block; an allocation of its own only if that is smaller
   void *prep = nullptr;
+  // mixed-form gather deposit: the dense-cell tables (cell -> slot, slot -> cell, the
+  // slots' corner sums), after the prefactor records in the alt block when it has room,
+  // else an allocation of their own
+  void *dense = nullptr;
   size_t bytes = 0;  // device bytes this store counts in its context's bytes_in_use
 };
 

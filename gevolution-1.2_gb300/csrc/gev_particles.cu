@@ -1222,6 +1222,7 @@ int gev_pcls_destroy(gev_pcls *p) {
   cudaFree(p->big);
   cudaFree(p->bounds);
   cudaFree(p->prep);
+  cudaFree(p->dense);
   cudaFree(p->scan_tmp);
   gev_ctx *ctx = p->ctx;
   if (ctx) ctx->bytes_in_use -= p->bytes;
