@@ -87,24 +87,38 @@ __global__ void __launch_bounds__(256) k_fx_bounds(const float *__restrict__ vx,
   uint32_t mc = 0u;
   for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
     q2 = fmaxf(q2, vx[i] * vx[i] + vy[i] * vy[i] + vz[i] * vz[i]);
+  // Dense slots: a thread counts its dense cells as it reduces, the warp takes the
+  // slots of all its threads with one counter update (an exclusive scan of the
+  // threads' counts gives each thread its first slot), and each thread then hands out
+  // its own slots in a second pass over its cells (no warp-wide operation in either
+  // loop, so both keep their loads in flight)
   const unsigned lane = threadIdx.x & 31u;
-  const long Cw = (C + 31) & ~31L;  // every lane of a warp runs the same iterations
-  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < Cw; c += (long)gridDim.x * blockDim.x) {
-    const uint32_t k = c < C ? count[c] : 0u;
+  const long c_first = (long)blockIdx.x * blockDim.x + threadIdx.x, c_step = (long)gridDim.x * blockDim.x;
+  uint32_t ndense = 0u;
+  for (long c = c_first; c < C; c += c_step) {
+    const uint32_t k = count[c];
     mc = max(mc, k);
-    if (phi && c < C) ph = fmaxf(ph, fabsf(phi[c]));
-    if (D.slot_of == nullptr) continue;  // not a gather kind (uniform: a kernel argument)
-    const bool dense = k > D.thr;
-    const unsigned m = __ballot_sync(0xffffffffu, dense);
-    if (m == 0u) continue;
-    const int leader = __ffs(m) - 1;
+    if (phi) ph = fmaxf(ph, fabsf(phi[c]));
+    ndense += k > D.thr ? 1u : 0u;
+  }
+  if (D.slot_of != nullptr) {  // a gather kind (uniform: a kernel argument)
+    uint32_t incl = ndense;
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+      if ((int)lane >= o) incl += t;
+    }
+    const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
     uint32_t base = 0u;
-    if ((int)lane == leader) base = atomicAdd(D.count, (uint32_t)__popc(m));
-    base = __shfl_sync(0xffffffffu, base, leader);
-    if (dense) {
-      const uint32_t slot = base + (uint32_t)__popc(m & ((1u << lane) - 1u));
-      D.slot_of[c] = slot < D.cap ? slot : DENSE_NONE;
-      if (slot < D.cap) D.list[slot] = (uint32_t)c;
+    if (lane == 0u && tot > 0u) base = atomicAdd(D.count, tot);
+    uint32_t slot = __shfl_sync(0xffffffffu, base, 0) + incl - ndense;
+    if (ndense > 0u) {
+      for (long c = c_first; c < C; c += c_step) {
+        if (count[c] > D.thr) {
+          D.slot_of[c] = slot < D.cap ? slot : DENSE_NONE;
+          if (slot < D.cap) D.list[slot] = (uint32_t)c;
+          ++slot;
+        }
+      }
     }
   }
   for (int o = 16; o > 0; o >>= 1) {
