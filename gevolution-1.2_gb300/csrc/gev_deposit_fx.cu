@@ -53,18 +53,25 @@ __device__ __forceinline__ long face_index(int x, int y, int z, const FxParams &
 }
 
 // the dense-cell tables of the gather deposit (k_dense_sums below)
-// dense above 12 particles: measured over the last 20 cycles before z = 0 at 512^3,
-// the cycle took 38.73 ms with 8, 37.97 with 12, 38.03 with 16, 38.34 with 24 and
-// 38.64 with 32 (the gather's remaining walks against the dense cells' own pass)
-constexpr uint32_t DENSE_T = 12;
+// dense above 8 particles: measured over the last 20 cycles before z = 0 at 512^3 (the
+// gather's remaining walks against the dense cells' own pass), the cycle took 37.32 ms
+// with 8, 37.39 with 10, 37.58 with 12 and 37.83 with 16; before the small cells had
+// eight lanes each (a warp a cell), 38.73 with 8 and 37.97 with 12
+constexpr uint32_t DENSE_T = 8;
+// dense cells of more particles than this take a whole warp (the smaller, eight lanes)
+constexpr uint32_t DENSE_BIG = 64;
 constexpr int DENSE_NS = 38;
 constexpr uint32_t DENSE_NONE = 0xffffffffu;
+constexpr int DENSE_MASK_WORDS = 16;
+// Slots [0, cap) are for dense cells of up to `big` particles, summed by 8 lanes a cell;
+// slots [cap, cap + cap_big) for larger ones, summed by a whole warp.
 struct DenseTab {
   uint32_t *slot_of;  // per cell, valid for the cells above thr of this call
   uint32_t *list;     // slot -> cell
-  uint32_t *count;    // dense cells found (may exceed cap)
-  uint32_t cap;
-  uint32_t thr;      // cells with more particles are dense
+  uint32_t *count;    // [0] small and [1] big dense cells found (may exceed the caps)
+  uint32_t cap, cap_big;
+  uint32_t thr;       // cells with more particles are dense
+  uint32_t big;       // dense cells with more particles take a whole warp
   long long *sums;    // slot * DENSE_NS + index
 };
 
@@ -94,30 +101,60 @@ __global__ void __launch_bounds__(256) k_fx_bounds(const float *__restrict__ vx,
   // loop, so both keep their loads in flight)
   const unsigned lane = threadIdx.x & 31u;
   const long c_first = (long)blockIdx.x * blockDim.x + threadIdx.x, c_step = (long)gridDim.x * blockDim.x;
-  uint32_t ndense = 0u;
-  for (long c = c_first; c < C; c += c_step) {
+  // the iterations that met a dense cell, one bit each (up to DENSE_MASK_WORDS * 32
+  // iterations a thread; a grid with more makes the second pass read every count again)
+  uint32_t ndense = 0u, nbig = 0u, dmask[DENSE_MASK_WORDS];
+#pragma unroll
+  for (int w = 0; w < DENSE_MASK_WORDS; ++w) dmask[w] = 0u;
+  int it = 0;
+  for (long c = c_first; c < C; c += c_step, ++it) {
     const uint32_t k = count[c];
     mc = max(mc, k);
     if (phi) ph = fmaxf(ph, fabsf(phi[c]));
-    ndense += k > D.thr ? 1u : 0u;
+    const bool dense = k > D.thr;
+    ndense += dense ? 1u : 0u;
+    nbig += k > D.big ? 1u : 0u;
+    if (dense && it < DENSE_MASK_WORDS * 32) dmask[it >> 5] |= 1u << (it & 31);
   }
+  const bool masked = it <= DENSE_MASK_WORDS * 32;
   if (D.slot_of != nullptr) {  // a gather kind (uniform: a kernel argument)
-    uint32_t incl = ndense;
+    // small and big dense cells apart (ndense counts both, nbig the big ones)
+    const uint32_t nsmall = ndense - nbig;
+    uint32_t is = nsmall, ib = nbig;
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-      if ((int)lane >= o) incl += t;
+      const uint32_t ts = __shfl_up_sync(0xffffffffu, is, o), tb = __shfl_up_sync(0xffffffffu, ib, o);
+      if ((int)lane >= o) {
+        is += ts;
+        ib += tb;
+      }
     }
-    const uint32_t tot = __shfl_sync(0xffffffffu, incl, 31);
-    uint32_t base = 0u;
-    if (lane == 0u && tot > 0u) base = atomicAdd(D.count, tot);
-    uint32_t slot = __shfl_sync(0xffffffffu, base, 0) + incl - ndense;
+    const uint32_t tots = __shfl_sync(0xffffffffu, is, 31), totb = __shfl_sync(0xffffffffu, ib, 31);
+    uint32_t bs = 0u, bb = 0u;
+    if (lane == 0u) {
+      if (tots > 0u) bs = atomicAdd(&D.count[0], tots);
+      if (totb > 0u) bb = atomicAdd(&D.count[1], totb);
+    }
+    uint32_t ss = __shfl_sync(0xffffffffu, bs, 0) + is - nsmall, sb = __shfl_sync(0xffffffffu, bb, 0) + ib - nbig;
     if (ndense > 0u) {
-      for (long c = c_first; c < C; c += c_step) {
-        if (count[c] > D.thr) {
-          D.slot_of[c] = slot < D.cap ? slot : DENSE_NONE;
-          if (slot < D.cap) D.list[slot] = (uint32_t)c;
-          ++slot;
+      auto give = [&](long c) {
+        const uint32_t k = count[c];
+        if (k > D.big) {
+          const bool ok = sb < D.cap_big;
+          D.slot_of[c] = ok ? D.cap + sb : DENSE_NONE;
+          if (ok) D.list[D.cap + sb] = (uint32_t)c;
+          ++sb;
+        } else if (k > D.thr) {
+          const bool ok = ss < D.cap;
+          D.slot_of[c] = ok ? ss : DENSE_NONE;
+          if (ok) D.list[ss] = (uint32_t)c;
+          ++ss;
         }
+      };
+      if (masked) {
+        for (int w = 0; w < DENSE_MASK_WORDS; ++w)
+          for (uint32_t m = dmask[w]; m != 0u; m &= m - 1u) give(c_first + (long)(32 * w + __ffs(m) - 1) * c_step);
+      } else {
+        for (long c = c_first; c < C; c += c_step) give(c);
       }
     }
   }
@@ -463,23 +500,24 @@ __global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArray
 //   [32 + dz]    Tij_01 at corner (0, 0, dz)   (the plaquettes the gather's nodes own)
 //   [34 + dy]    Tij_02 at corner (0, dy, 0)
 //   [36 + dx]    Tij_12 at corner (dx, 0, 0)
-// A warp per dense cell: lane l takes the cell's particles l, l + 32, ... and forms
-// their contributions at the cell's 8 corners as gather_node's add() forms them for
-// a node; the lanes' int64 sums are added through shared memory (each lane writes its
-// 38, then lane k adds the 32 values of sum k).
+// A group of G lanes per dense cell (G = 8 for the small ones, four cells a warp; 32 for
+// the big ones): lane l of the group takes the cell's particles l, l + G, ... and forms
+// their contributions at the cell's 8 corners as gather_node's add() forms them for a
+// node; the lanes' int64 sums are added through shared memory (each lane writes its 38,
+// then lane g of the group adds the G values of sums g, g + G, ...).
 constexpr int DENSE_WARPS = 4;
-template <int KIND>
-__global__ void __launch_bounds__(32 * DENSE_WARPS) k_dense_sums(PclsArrays P, const uint32_t *__restrict__ start,
-                                                                PrepArrays A, const float *__restrict__ phi, FxParams p,
-                                                                Div32 dN, const uint32_t *__restrict__ fxb, DenseTab D) {
+template <int KIND, int G>
+__device__ __forceinline__ void dense_cell(bool has, uint32_t s, const PclsArrays &P, const uint32_t *__restrict__ start,
+                                           const PrepArrays &A, const float *__restrict__ phi, const FxParams &p,
+                                           const Div32 &dN, const DenseTab &D, float sg00, float sgij,
+                                           long long (*red)[33]) {
   constexpr bool DO00 = KIND == FX_T00 || KIND == FX_T00TIJ, DOIJ = KIND == FX_TIJ || KIND == FX_T00TIJ;
-  __shared__ long long red[DENSE_WARPS][DENSE_NS][33];
-  const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
   const int N = p.N;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  const uint32_t nd = min(*D.count, D.cap);
-  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t s = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; s < nd; s += warps) {
+  const int lane = threadIdx.x & 31, gl = lane & (G - 1), g0 = lane - gl;
+  long long acc[DENSE_NS];
+#pragma unroll
+  for (int k = 0; k < DENSE_NS; ++k) acc[k] = 0;
+  if (has) {
     const uint32_t c = D.list[s];
     int x, y, z;
     cell_xyz(c, N, p.lg, dN, x, y, z);
@@ -499,11 +537,8 @@ __global__ void __launch_bounds__(32 * DENSE_WARPS) k_dense_sums(PclsArrays P, c
       s02[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[2 * d], f[2 * d + 4]), f[1 + 2 * d]), f[1 + 2 * d + 4]);
       s12[d] = __fadd_rn(__fadd_rn(__fadd_rn(f[d], f[d + 4]), f[d + 2]), f[d + 6]);
     }
-    long long acc[DENSE_NS];
-#pragma unroll
-    for (int k = 0; k < DENSE_NS; ++k) acc[k] = 0;
     const uint32_t j1 = start[c + 1];
-    for (uint32_t j = start[c] + lane; j < j1; j += 32) {
+    for (uint32_t j = start[c] + gl; j < j1; j += G) {
       uint4 v0, v1, v2 = make_uint4(0u, 0u, 0u, 0u);
       if constexpr (KIND == FX_T00) {
         const uint2 q = __ldg(reinterpret_cast<const uint2 *>(A.rec) + j);
@@ -527,10 +562,10 @@ __global__ void __launch_bounds__(32 * DENSE_WARPS) k_dense_sums(PclsArrays P, c
           acc[k] += (long long)(int)v0.w *
                     (long long)gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(__uint_as_float(v1.x), f[k]))), sg00);
         if (DOIJ) {
-          const long long G = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(fT, f[k]))), sgij);
-          acc[8 + 3 * k] += (long long)(int)v1.z * G;
-          acc[9 + 3 * k] += (long long)(int)v1.w * G;
-          acc[10 + 3 * k] += (long long)(int)v2.x * G;
+          const long long Gw = gq(__fmul_rn(w, __fadd_rn(1.f, __fmul_rn(fT, f[k]))), sgij);
+          acc[8 + 3 * k] += (long long)(int)v1.z * Gw;
+          acc[9 + 3 * k] += (long long)(int)v1.w * Gw;
+          acc[10 + 3 * k] += (long long)(int)v2.x * Gw;
         }
       }
       if (DOIJ) {
@@ -542,18 +577,37 @@ __global__ void __launch_bounds__(32 * DENSE_WARPS) k_dense_sums(PclsArrays P, c
         }
       }
     }
+  }
 #pragma unroll
-    for (int k = 0; k < DENSE_NS; ++k) red[wib][k][lane] = acc[k];
-    __syncwarp();
+  for (int k = 0; k < DENSE_NS; ++k) red[k][lane] = acc[k];
+  __syncwarp();
+  if (has) {
     long long *out = D.sums + (size_t)s * DENSE_NS;
-    for (int k = lane; k < DENSE_NS; k += 32) {
+    for (int k = gl; k < DENSE_NS; k += G) {
       long long v = 0;
-#pragma unroll 8
-      for (int l = 0; l < 32; ++l) v += red[wib][k][l];
+#pragma unroll
+      for (int l = 0; l < G; ++l) v += red[k][g0 + l];
       out[k] = v;
     }
-    __syncwarp();  // red is rewritten for the warp's next cell
   }
+  __syncwarp();  // red is rewritten for the warp's next cells
+}
+
+// the small dense cells four to a warp, then the big ones a warp each
+template <int KIND>
+__global__ void __launch_bounds__(32 * DENSE_WARPS) k_dense_sums(PclsArrays P, const uint32_t *__restrict__ start,
+                                                                PrepArrays A, const float *__restrict__ phi, FxParams p,
+                                                                Div32 dN, const uint32_t *__restrict__ fxb, DenseTab D) {
+  __shared__ long long red[DENSE_WARPS][DENSE_NS][33];
+  const float sg00 = pow2f((int)fxb[6]), sgij = pow2f(KIND == FX_T00TIJ ? (int)fxb[8] : (int)fxb[6]);
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5, w0 = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t ns = min(D.count[0], D.cap), nb = min(D.count[1], D.cap_big);
+  for (uint32_t base = w0 * 4u; base < ns; base += warps * 4u) {
+    const uint32_t s = base + (uint32_t)(lane >> 3);
+    dense_cell<KIND, 8>(s < ns, s, P, start, A, phi, p, dN, D, sg00, sgij, red[wib]);
+  }
+  for (uint32_t b = w0; b < nb; b += warps) dense_cell<KIND, 32>(true, D.cap + b, P, start, A, phi, p, dN, D, sg00, sgij, red[wib]);
 }
 
 // node i = (x, y, z): its 8 neighbouring cells' contributions, summed in int64 and
@@ -631,7 +685,7 @@ __device__ __forceinline__ void gather_node(unsigned i, int x, int y, int z, con
   // a dense cell's sums at this node's corner (dx, dy, dz) of it, if it has a slot
   auto dense = [&](uint32_t cell, int dx, int dy, int dz) -> bool {
     const uint32_t slot = D.slot_of[cell];
-    if (slot >= D.cap) return false;  // DENSE_NONE: no slot was left for it
+    if (slot >= D.cap + D.cap_big) return false;  // DENSE_NONE: no slot was left for it
     const long long *hs = D.sums + (size_t)slot * DENSE_NS;
     const int k = dx + 2 * dy + 4 * dz;
     if (DO00) a00 += hs[k];
@@ -810,7 +864,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   // their own (slots for one dense cell in 64 particles)
   void *rec = nullptr;
   const size_t rec_bytes = (size_t)(p->cap > 0 ? p->cap : 1) * PREP_WORDS * 4;
-  DenseTab dt{nullptr, nullptr, nullptr, 0u, 0u, nullptr};
+  DenseTab dt{nullptr, nullptr, nullptr, 0u, 0u, 0u, 0u, nullptr};
   if (gather) {
     rec = p->alt.block_bytes >= rec_bytes ? p->alt.block : p->prep;
     if (!rec) {
@@ -826,8 +880,10 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const long np = p->cap > 0 ? p->cap : 1;
     const uint32_t dcap = (uint32_t)(np / 64 > 1024 ? np / 64 : 1024);
-    const size_t o_list = al((size_t)C * 4), o_count = o_list + al((size_t)dcap * 4), o_sums = o_count + 256;
-    const size_t dense_bytes = o_sums + (size_t)dcap * DENSE_NS * 8;
+    const uint32_t dcap_big = (uint32_t)(np / 256 > 1024 ? np / 256 : 1024);
+    const size_t nslots = (size_t)dcap + dcap_big;
+    const size_t o_list = al((size_t)C * 4), o_count = o_list + al(nslots * 4), o_sums = o_count + 256;
+    const size_t dense_bytes = o_sums + nslots * DENSE_NS * 8;
     char *base = nullptr;
     if (rec == p->alt.block && p->alt.block_bytes >= al(rec_bytes) + dense_bytes) {
       base = (char *)p->alt.block + al(rec_bytes);
@@ -848,8 +904,10 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     dt.count = (uint32_t *)(base + o_count);
     dt.sums = (long long *)(base + o_sums);
     dt.cap = dcap;
+    dt.cap_big = dcap_big;
     dt.thr = DENSE_T;
-    GEV_CHECK_CUDA(ctx, cudaMemsetAsync(dt.count, 0, 4, ctx->stream));
+    dt.big = DENSE_BIG;
+    GEV_CHECK_CUDA(ctx, cudaMemsetAsync(dt.count, 0, 8, ctx->stream));
   }
   GevTimed tm_b(ctx, "k_fx_bounds+k_fx_scale");
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->bounds, 0, 16 * sizeof(uint32_t), ctx->stream));
