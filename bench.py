@@ -267,9 +267,9 @@ def kernel_alg_bytes(name, N, prec, n=None):
 # second cycle's launch.  Particles and cells both grow as N^3, so the 512^3 entry is
 # the 256^3 capture times 8.
 _LATE_256 = {
-    "k_dep_gather": 0.873601e9 + 0.530477e9,
+    "k_dep_gather": 0.884165e9 + 0.526542e9,
     "k_fx_prep": 0.404148e9 + 0.747557e9,
-    "k_dense_sums": 0.198506e9 + 0.025382e9,
+    "k_dense_sums": 0.281905e9 + 0.050591e9,
 }
 KERNEL_TRAFFIC = {}
 for _k, _v in _LATE_256.items():
