@@ -251,3 +251,42 @@ def test_clustered_deposits(gpu, oracle, N):
     for which, got in (("T00", f1.download()), ("Tij", f6.download())):
         ref = oracle.deposit(which, N, p, 2e-4, 0.03, phi_h, 1.0)
         assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), which
+
+
+def test_dense_cells_beyond_the_slots_are_walked(gpu, oracle):
+    """A store holds one dense-cell slot for 64 particles (at least 1024): with many
+    cells above the dense threshold most of them get no slot and are walked.  The same
+    particles in a store with room for every dense cell give the same bits (integer
+    sums do not depend on which cells are summed apart), and both follow the FP64
+    restatement within the form's rounding."""
+    N = 64
+    rng = np.random.default_rng(7)
+    # 16,000 cells of 12 particles (small dense cells) and 2,000 of 70 (big ones, a warp
+    # each) beside sparse particles: 192,000 + 140,000 + 60,000 particles
+    cells = rng.choice(N ** 3, 18000, replace=False)
+    corner = np.stack([cells % N, (cells // N) % N, cells // (N * N)], 1).astype(float)
+    small = (corner[:16000, None, :] + rng.random((16000, 12, 3))) / N
+    big = (corner[16000:, None, :] + rng.random((2000, 70, 3))) / N
+    sparse = rng.random((60000, 3))
+    pos = np.concatenate([small.reshape(-1, 3), big.reshape(-1, 3), sparse]) % 1.0
+    n = len(pos)
+    p = np.zeros(n, gpu.PART)
+    p["pos"] = pos
+    p["vel"] = rng.standard_normal((n, 3)) * 1e-3
+    p["ID"] = rng.permutation(n)
+    phi_h = rng.standard_normal((1, N, N, N)) * 1e-5
+    ctx = gpu.Context(N, gpu.PREC_MIXED)
+    phi = ctx.real(1).upload(phi_h)
+    out = []
+    # capacity n: 6,125 small and 1,531 big slots for 16,000 and 2,000 dense cells;
+    # capacity 64 n: room for all of them
+    for cap in (n, 64 * n):
+        pc = ctx.particles(cap, 2e-4).upload(p)
+        t00, tij = ctx.real(1), ctx.real(6)
+        gpu.projection_T00_Tij(pc, t00, tij, 0.03, phi)
+        out.append((t00.download(), tij.download()))
+        del pc
+    assert out[0][0].tobytes() == out[1][0].tobytes() and out[0][1].tobytes() == out[1][1].tobytes()
+    for which, got in (("T00", out[0][0]), ("Tij", out[0][1])):
+        ref = oracle.deposit(which, N, p, 2e-4, 0.03, phi_h, 1.0)
+        assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), which
