@@ -746,11 +746,13 @@ __device__ __forceinline__ void gather_node(unsigned i, int x, int y, int z, con
 // 8 x 4 x 1: 14.20, 16 x 2 x 1: 14.16); in the first cycles the lines are faster
 // (the patch's nodes are four 32-byte row pieces rather than one 128-byte line).
 // Each node is one thread's either way, so the bits do not depend on the choice.
-// Six resident blocks per SM (40 registers; 48 and five blocks for T00 alone): the
-// loop is latency-bound, and the warps hide more than the few spilled words cost.
+// Five resident blocks per SM (48 registers, 124 B of spill stores): the loop is
+// latency-bound, and warps hide more than the few spilled words cost, up to a point
+// (the late 512^3 cycle took 8.82 ms in the gather at five blocks, 9.16 at six with 40
+// registers and 424 B of spills, 9.16 at four with 64 and 10.73 at three with 80).
 constexpr uint32_t PATCH_MC = 8;
 template <int KIND, int PX, int PY, int PZ>
-__global__ void __launch_bounds__(256, KIND == FX_T00 ? 5 : 6) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
+__global__ void __launch_bounds__(256, 5) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
                                                     const float *__restrict__ phi, float *t00, float *tij, FxParams p,
                                                     Div32 dN, const uint32_t *__restrict__ fxb, DenseTab D) {
   const int ks00 = (int)fxb[2], ksij = KIND == FX_T00TIJ ? (int)fxb[3] : (int)fxb[2];
@@ -923,7 +925,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     float *t00 = kind == FX_TIJ ? nullptr : (float *)out->d;
     float *tij = kind == FX_TIJ ? (float *)out->d : (out2 ? (float *)out2->d : nullptr);
     const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
-    // many small blocks (up to 384 a SM, 64 waves of the six resident): the block scheduler
+    // many small blocks (up to 384 a SM, about 77 waves of the five resident): the block scheduler
     // refills an SM as soon as a block's nodes are done, which the long latency-bound walks
     // of a few large blocks cannot (first 512^3 cycles: 29.7 ms a cycle at 96, 30.7 at 16,
     // 31.8 at 12; late cycles, patch walk: gather 12.87 ms at 384, 13.09 at 192, 13.40 at 96,
