@@ -290,3 +290,35 @@ def test_dense_cells_beyond_the_slots_are_walked(gpu, oracle):
     for which, got in (("T00", out[0][0]), ("Tij", out[0][1])):
         ref = oracle.deposit(which, N, p, 2e-4, 0.03, phi_h, 1.0)
         assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), which
+
+
+def test_dense_tables_of_a_sparse_store(gpu, oracle):
+    """Fewer particles than cells: the dense-cell tables (4 B a cell) do not fit behind
+    the prefactor records in the store's second array set and get an allocation of
+    their own; the clustered deposit still follows the FP64 restatement and the fused
+    deposit gives the separate ones' bits."""
+    N = 64
+    rng = np.random.default_rng(11)
+    cells = rng.choice(N ** 3, 4000, replace=False)
+    corner = np.stack([cells % N, (cells // N) % N, cells // (N * N)], 1).astype(float)
+    pos = ((corner[:, None, :] + rng.random((4000, 12, 3))) / N).reshape(-1, 3) % 1.0
+    n = len(pos)
+    p = np.zeros(n, gpu.PART)
+    p["pos"] = pos
+    p["vel"] = rng.standard_normal((n, 3)) * 1e-3
+    p["ID"] = rng.permutation(n)
+    phi_h = rng.standard_normal((1, N, N, N)) * 1e-5
+    ctx = gpu.Context(N, gpu.PREC_MIXED)
+    phi = ctx.real(1).upload(phi_h)
+    pc = ctx.particles(n, 2e-4).upload(p)
+    f1, f6, g1, g6 = ctx.real(1), ctx.real(6), ctx.real(1), ctx.real(6)
+    before = ctx.bytes_in_use()
+    gpu.projection_T00_Tij(pc, g1, g6, 0.03, phi)
+    assert ctx.bytes_in_use() - before >= 4 * N ** 3  # the tables' own allocation
+    gpu.projection_T00(pc, f1, 0.03, phi)
+    gpu.projection_Tij(pc, f6, 0.03, phi)
+    assert f1.download().tobytes() == g1.download().tobytes()
+    assert f6.download().tobytes() == g6.download().tobytes()
+    for which, got in (("T00", g1.download()), ("Tij", g6.download())):
+        ref = oracle.deposit(which, N, p, 2e-4, 0.03, phi_h, 1.0)
+        assert np.abs(got - ref).max() <= 1e-5 * np.abs(ref).max(), which
