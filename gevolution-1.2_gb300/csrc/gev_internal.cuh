@@ -129,7 +129,6 @@ struct gev_pcls {
   uint32_t *start = nullptr;  // per cell, N^3 + 1
   uint32_t *rank = nullptr;   // per particle
   uint32_t *perm = nullptr;   // per particle
-  uint32_t *big = nullptr;    // list of cells needing the block-wide ID sort (+1 counter)
   uint32_t *scan_tmp = nullptr;
   size_t scan_tmp_elems = 0;
   // false after a mixed-form relink that left each cell's run in atomic order

@@ -4,9 +4,9 @@
 // moveParticles with callbacks; main.cpp:743-806) by a structure-of-arrays
 // store kept in (cell, ID) order:
 //   relink = periodic counting sort: atomic histogram of cell keys, exclusive
-//   scan into cell starts, scatter, then each cell's run is ordered by ID (so
-//   the order -- and every sum over it -- is independent of atomic timing),
-//   then one gather of the payload.
+//   scan into cell starts, scatter, then each particle is ranked by ID within its
+//   cell's run (so the order -- and every sum over it -- is independent of atomic
+//   timing), then one gather of the payload.
 // update_q / update_pos (gevolution.hpp:570-903) run one thread per particle
 // in that order, so neighbouring threads gather neighbouring field cells.
 #include <cmath>
@@ -15,8 +15,6 @@
 #include "gev_internal.cuh"
 
 namespace {
-
-constexpr int SMALL_CELL = 32;  // runs up to this length are ordered by one thread
 
 // ------------------------------------------------------------ keys ------
 __device__ __forceinline__ int cell1(double p, double Nd, int N) {
@@ -247,56 +245,28 @@ __global__ void k_scatter(const uint32_t *__restrict__ cell, const uint32_t *__r
     perm[start[cell[i]] + rank[i]] = (uint32_t)i;
 }
 
-// order each cell's run by ID; long runs are queued for k_canon_big
-__global__ void k_canon(const uint32_t *__restrict__ start, long ncell, const int64_t *__restrict__ id,
-                        uint32_t *perm, uint32_t *big) {
-  for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < ncell; c += (long)gridDim.x * blockDim.x) {
+// The (cell, ID) order: slot k of the run [s, e) of its cell holds particle via[k]
+// (the store's own slot k where via is null); the particle's rank in the run is
+// the number of the run's particles before it by (ID, slot) -- a permutation of the
+// run even where IDs repeat, IDs in order of their slots -- and out[s + rank] gets
+// the particle.  One thread a particle: the lanes of a warp mostly walk the same run,
+// read from L1, and no thread sorts a cell alone (a thread a cell left most lanes
+// idle beside the cells of a few particles).  The work is the sum over the cells of
+// their squared counts.
+__global__ void k_id_rank(const uint32_t *__restrict__ start, const uint32_t *__restrict__ cell,
+                          const int64_t *__restrict__ id, const uint32_t *__restrict__ via, long n,
+                          uint32_t *__restrict__ out) {
+  for (long k = blockIdx.x * (long)blockDim.x + threadIdx.x; k < n; k += (long)gridDim.x * blockDim.x) {
+    const uint32_t i = via ? via[k] : (uint32_t)k;
+    const uint32_t c = cell[i];
     const uint32_t s = start[c], e = start[c + 1];
-    const uint32_t n = e - s;
-    if (n <= 1) continue;
-    if (n > SMALL_CELL) {
-      const uint32_t slot = atomicAdd(&big[0], 1u);
-      big[1 + slot] = (uint32_t)c;
-      continue;
+    const int64_t my = id[i];
+    uint32_t r = 0;
+    for (uint32_t j = s; j < e; ++j) {
+      const int64_t o = id[via ? via[j] : j];
+      r += (o < my || (o == my && j < (uint32_t)k)) ? 1u : 0u;
     }
-    int64_t key[SMALL_CELL];
-    uint32_t val[SMALL_CELL];
-    for (uint32_t j = 0; j < n; ++j) {
-      val[j] = perm[s + j];
-      key[j] = id[val[j]];
-    }
-    for (uint32_t j = 1; j < n; ++j) {
-      const int64_t k = key[j];
-      const uint32_t v = val[j];
-      int m = (int)j - 1;
-      while (m >= 0 && key[m] > k) {
-        key[m + 1] = key[m];
-        val[m + 1] = val[m];
-        --m;
-      }
-      key[m + 1] = k;
-      val[m + 1] = v;
-    }
-    for (uint32_t j = 0; j < n; ++j) perm[s + j] = val[j];
-  }
-}
-
-// one block per long run: rank by ID (IDs are unique), then copy back
-__global__ void k_canon_big(const uint32_t *__restrict__ start, const int64_t *__restrict__ id, uint32_t *perm,
-                            uint32_t *tmp, const uint32_t *__restrict__ big) {
-  const uint32_t nbig = big[0];
-  for (uint32_t b = blockIdx.x; b < nbig; b += gridDim.x) {
-    const uint32_t c = big[1 + b];
-    const uint32_t s = start[c], e = start[c + 1];
-    for (uint32_t i = s + threadIdx.x; i < e; i += blockDim.x) {
-      const int64_t k = id[perm[i]];
-      uint32_t r = 0;
-      for (uint32_t j = s; j < e; ++j) r += id[perm[j]] < k ? 1u : 0u;
-      tmp[s + r] = perm[i];
-    }
-    __syncthreads();
-    for (uint32_t i = s + threadIdx.x; i < e; i += blockDim.x) perm[i] = tmp[i];
-    __syncthreads();
+    if (s + r < e) out[s + r] = i;  // always, when slot k lies in its cell's run
   }
 }
 
@@ -394,11 +364,6 @@ __global__ void __launch_bounds__(256, 1) k_move(PclsArrays src, PclsArrays dst,
       dst.rz[j] = r2;
     }
   }
-}
-
-__global__ void k_iota(uint32_t *perm, long n) {
-  for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
-    perm[i] = (uint32_t)i;
 }
 
 // ------------------------------------------------------- particle updates --
@@ -1051,8 +1016,11 @@ static int relink_uploaded(gev_ctx *ctx, gev_pcls *p) {
   const long C = (long)ctx->N * ctx->N * ctx->N;
   const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->bounds + 15, 0, sizeof(uint32_t), ctx->stream));
-  k_unordered<<<pb, 256, 0, ctx->stream>>>(p->cur.cell, p->cur.id, p->n, p->bounds + 15);
-  GEV_LAUNCH_CHECK(ctx);
+  {
+    GevTimed tm_(ctx, "k_unordered");
+    k_unordered<<<pb, 256, 0, ctx->stream>>>(p->cur.cell, p->cur.id, p->n, p->bounds + 15);
+    GEV_LAUNCH_CHECK(ctx);
+  }
   uint32_t unordered = 1u;
   GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(&unordered, p->bounds + 15, sizeof(uint32_t), cudaMemcpyDeviceToHost, ctx->stream));
   GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -1066,16 +1034,11 @@ static int relink_uploaded(gev_ctx *ctx, gev_pcls *p) {
   return GEV_OK;
 }
 
-// perm = the store's particles in (cell, ID) order (each cell's run sorted by ID)
+// perm = the store's particles in (cell, ID) order (each cell's run ranked by ID)
 static int id_permutation(gev_ctx *ctx, gev_pcls *p) {
-  const long C = (long)ctx->N * ctx->N * ctx->N;
-  const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
-  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->big, 0, sizeof(uint32_t), ctx->stream));
-  k_iota<<<pb, 256, 0, ctx->stream>>>(p->perm, p->n);
-  GEV_LAUNCH_CHECK(ctx);
-  k_canon<<<grid_for(ctx, (size_t)C, 256, 16), 256, 0, ctx->stream>>>(p->start, C, p->cur.id, p->perm, p->big);
-  GEV_LAUNCH_CHECK(ctx);
-  k_canon_big<<<ctx->sms * 2, 256, 0, ctx->stream>>>(p->start, p->cur.id, p->perm, p->rank, p->big);
+  GevTimed tm_(ctx, "k_id_rank");
+  k_id_rank<<<grid_for(ctx, (size_t)p->n, 256, 16), 256, 0, ctx->stream>>>(p->start, p->cur.cell, p->cur.id, nullptr,
+                                                                          p->n, p->perm);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
@@ -1102,7 +1065,6 @@ int pcls_relink(gev_ctx *ctx, gev_pcls *p) {
     return GEV_OK;
   }
   GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->count, 0, C * sizeof(uint32_t), ctx->stream));
-  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->big, 0, sizeof(uint32_t), ctx->stream));
   const int pb = grid_for(ctx, (size_t)p->n, 256, 16);
   k_count<<<pb, 256, 0, ctx->stream>>>(p->cur.cell, p->n, p->count, p->rank);
   GEV_LAUNCH_CHECK(ctx);
@@ -1110,14 +1072,15 @@ int pcls_relink(gev_ctx *ctx, gev_pcls *p) {
   if (rc) return rc;
   k_scatter<<<pb, 256, 0, ctx->stream>>>(p->cur.cell, p->rank, p->n, p->start, p->perm);
   GEV_LAUNCH_CHECK(ctx);
-  k_canon<<<grid_for(ctx, (size_t)C, 256, 16), 256, 0, ctx->stream>>>(p->start, C, p->cur.id, p->perm, p->big);
-  GEV_LAUNCH_CHECK(ctx);
-  k_canon_big<<<ctx->sms * 2, 256, 0, ctx->stream>>>(p->start, p->cur.id, p->perm, p->rank, p->big);
-  GEV_LAUNCH_CHECK(ctx);
+  {
+    GevTimed tm_(ctx, "k_id_rank");
+    k_id_rank<<<pb, 256, 0, ctx->stream>>>(p->start, p->cur.cell, p->cur.id, p->perm, p->n, p->rank);
+    GEV_LAUNCH_CHECK(ctx);
+  }
   if (ctx->prec == GEV_PREC_FP64)
-    k_gather<double><<<pb, 256, 0, ctx->stream>>>(p->cur, p->alt, p->perm, p->n);
+    k_gather<double><<<pb, 256, 0, ctx->stream>>>(p->cur, p->alt, p->rank, p->n);
   else
-    k_gather<float><<<pb, 256, 0, ctx->stream>>>(p->cur, p->alt, p->perm, p->n);
+    k_gather<float><<<pb, 256, 0, ctx->stream>>>(p->cur, p->alt, p->rank, p->n);
   GEV_LAUNCH_CHECK(ctx);
   std::swap(p->cur, p->alt);
   p->id_order = true;
@@ -1194,11 +1157,11 @@ int gev_pcls_create(gev_ctx *ctx, long capacity, double mass, gev_pcls **out) {
     p->scan_tmp_elems = (size_t)((C + SCAN_TILE - 1) / SCAN_TILE) + 1;
     if (cudaMalloc(&p->count, C * 4) != cudaSuccess || cudaMalloc(&p->start, (C + 1) * 4) != cudaSuccess ||
         cudaMalloc(&p->rank, cap * 4) != cudaSuccess || cudaMalloc(&p->perm, cap * 4) != cudaSuccess ||
-        cudaMalloc(&p->big, (C + 1) * 4) != cudaSuccess || cudaMalloc(&p->bounds, 16 * 4) != cudaSuccess ||
+        cudaMalloc(&p->bounds, 16 * 4) != cudaSuccess ||
         cudaMalloc(&p->scan_tmp, p->scan_tmp_elems * 4) != cudaSuccess)
       rc = gev_fail(ctx, GEV_ENOMEM, "pcls_create: device allocation failed");
     else
-      ctx->bytes_in_use += (size_t)C * 12 + (size_t)cap * 8 + p->scan_tmp_elems * 4;
+      ctx->bytes_in_use += (size_t)C * 8 + (size_t)cap * 8 + p->scan_tmp_elems * 4;
   }
   p->bytes = ctx->bytes_in_use - bytes0;
   if (rc) {
@@ -1219,7 +1182,6 @@ int gev_pcls_destroy(gev_pcls *p) {
   cudaFree(p->start);
   cudaFree(p->rank);
   cudaFree(p->perm);
-  cudaFree(p->big);
   cudaFree(p->bounds);
   cudaFree(p->prep);
   cudaFree(p->dense);
@@ -1238,11 +1200,13 @@ int gev_pcls_upload(gev_pcls *p, const gev_part *host, long n) {
   if (n > 0) {
     if (const gev_part *h = (const gev_part *)host_alias(host)) {
       const int hb = grid_for(ctx, (size_t)((n + HREC - 1) / HREC), 1, 2);
+      GevTimed tm_(ctx, "k_unpack_host");
       if (ctx->prec == GEV_PREC_FP64)
         k_unpack_host<double><<<hb, 256, 0, ctx->stream>>>(h, n, p->cur, ctx->N);
       else
         k_unpack_host<float><<<hb, 256, 0, ctx->stream>>>(h, n, p->cur, ctx->N);
       GEV_LAUNCH_CHECK(ctx);
+      tm_.stop();
       return relink_uploaded(ctx, p);
     }
     gev_part *d = nullptr;
@@ -1274,11 +1238,13 @@ int gev_pcls_download(gev_pcls *p, gev_part *host, long *n) {
       perm = p->perm;
     }
     const int hb = grid_for(ctx, (size_t)((p->n + HREC - 1) / HREC), 1, 2);
+    GevTimed tm_(ctx, "k_pack_host");
     if (ctx->prec == GEV_PREC_FP64)
       k_pack_host<double><<<hb, 256, 0, ctx->stream>>>(h, p->n, p->cur, perm);
     else
       k_pack_host<float><<<hb, 256, 0, ctx->stream>>>(h, p->n, p->cur, perm);
     GEV_LAUNCH_CHECK(ctx);
+    tm_.stop();
     GEV_CHECK_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     return GEV_OK;
   }
