@@ -82,7 +82,7 @@ def parse():
     ap.add_argument("--serve-burst", type=int, default=24, help="requests submitted at once for the capacity run")
     ap.add_argument("--op", default=None,
                     help="one operation instead of the benchmark: prepare, cycle, table, r2c_alone, c2r_alone, "
-                         "fft_axis_y, fft_axis_z")
+                         "fft_axis_y, fft_axis_z, ensemble")
     ap.add_argument("--reps", type=int, default=3, help="--op: timed calls")
     ap.add_argument("--z-op", type=float, default=0.0,
                     help="--op prepare / table: evolve from z = 100 until this redshift first")
@@ -338,6 +338,7 @@ def run_ours(args, rank, world, local):
     early["value"] = N ** 3 / (early["ms_per_step"] / 1e3)
     kernels, phases, roof = kernel_table(kt, K, ms / K, N, args.prec)
     tiles = ctx.fft_tiles()
+    tiles["stencils"] = ctx.stencil_shapes()
     timed = {"first": n_pre, "last": n_pre + K - 1, "of": n_full, "z_from": 1.0 / a_start - 1.0,
              "z_to": 1.0 / st["a"] - 1.0}
     cufft = fft_vs_cufft(gpu, ctx, stream, N, args.prec, torch) if world == 1 else None
@@ -652,26 +653,6 @@ def run_serve(args, gpu):
     srv.close()
     cap = len(bres) / b_span * 3600.0
     seq_rate = len(sres) / s_span * 3600.0
-    # the batched ensemble: 16 simulations each at 64^3, 96^3 and 128^3, box 2.5 N,
-    # cosmologies and seeds as above, all to z = 0, admitted at once
-    ens = []
-    for k, N in enumerate([64] * 16 + [96] * 16 + [128] * 16):
-        ens.append(gpu.request(N, seed=300000 + k, z_target=0.0, Omega_cdm=float(rng.uniform(0.25, 0.35)),
-                               sigma8=float(rng.uniform(0.75, 0.87)), n_s=float(rng.uniform(0.94, 0.98)),
-                               prec=gpu.PREC_MIXED))
-    def ensemble(workers):
-        srv = gpu.Server(workers=workers)
-        for r in ens:
-            srv.submit(r)
-        srv.drain(900.0)
-        got = [r for r in srv.poll(100000) if r["status"] == 0]
-        stats = srv.stats()
-        srv.close()
-        span = max(r["t_done"] for r in got) - min(r["t_submit"] for r in got)
-        return got, stats, span, sum(float(r["N"]) ** 3 * r["cycles"] for r in got)
-
-    eres, est, e_span, e_steps = ensemble(0)
-    eres1, _, e_span1, e_steps1 = ensemble(1)
     pct = lambda q: lat[min(len(lat) - 1, int(round(q * (len(lat) - 1))))]  # noqa: E731
     return {
         "precision": "mixed", "arrivals": "Poisson %.3g/s for %.3g s" % (args.serve_rate, args.serve_seconds),
@@ -685,12 +666,58 @@ def run_serve(args, gpu):
                             "note": "the burst's own requests in the plain FP64 form, run one at a time (a server "
                                     "with one slot) on the same GPU"},
         "capacity_vs_sequential_fp64": cap / seq_rate,
-        "ensemble": {"simulations": len(eres), "sizes": "16 x 64^3, 16 x 96^3, 16 x 128^3, z = 100 -> 0",
-                     "makespan_s": e_span, "particle_steps_per_s": e_steps / e_span,
-                     "max_active_seen": est["max_active_seen"], "scheduler_threads": est["workers"],
-                     "one_scheduler_thread": {"simulations": len(eres1), "makespan_s": e_span1,
-                                              "particle_steps_per_s": e_steps1 / e_span1}},
+        "ensemble": run_ensemble(gpu, args.seed),
     }
+
+
+def run_ensemble(gpu, seed):
+    """The batched ensemble: 16 simulations each at 64^3, 96^3 and 128^3, box 2.5 N,
+    Omega_cdm U[0.25, 0.35], sigma8 U[0.75, 0.87], n_s U[0.94, 0.98], distinct seeds,
+    all to z = 0, admitted at once.  Run three ways on the same requests: cycles
+    enqueued directly by the default scheduler threads, the same with each cycle
+    enqueued as one CUDA graph, and directly by one scheduler thread."""
+    import numpy as np
+    rng = np.random.default_rng(seed + 301)
+    ens = []
+    for k, N in enumerate([64] * 16 + [96] * 16 + [128] * 16):
+        ens.append(gpu.request(N, seed=300000 + k, z_target=0.0, Omega_cdm=float(rng.uniform(0.25, 0.35)),
+                               sigma8=float(rng.uniform(0.75, 0.87)), n_s=float(rng.uniform(0.94, 0.98)),
+                               prec=gpu.PREC_MIXED))
+
+    def ensemble(workers, graphs):
+        srv = gpu.Server(workers=workers, graphs=graphs)
+        ids = [srv.submit(r) for r in ens]
+        srv.drain(900.0)
+        got = {r["id"]: r for r in srv.poll(100000)}
+        stats = srv.stats()
+        srv.close()
+        res = [got[i] for i in ids if i in got and got[i]["status"] == 0]
+        span = max(r["t_done"] for r in res) - min(r["t_submit"] for r in res)
+        steps = sum(float(r["N"]) ** 3 * r["cycles"] for r in res)
+        return res, stats, {"simulations": len(res), "makespan_s": span, "particle_steps_per_s": steps / span,
+                            "max_active_seen": stats["max_active_seen"], "scheduler_threads": stats["workers"]}
+
+    shapes = {}
+    for N in (64, 96, 128):  # the launch shapes the stencil tuner picks for each size
+        ctx = gpu.Context(N, gpu.PREC_MIXED)
+        phi, Tij = ctx.real(1), ctx.real(6)
+        gpu.prepare_source_tensor(phi.zero(), Tij.zero(), Tij, 1e-3)
+        shapes[str(N)] = ctx.stencil_shapes()
+        del phi, Tij, ctx
+    res_d, _, direct = ensemble(0, False)
+    res_g, st_g, graph = ensemble(0, True)
+    _, _, one = ensemble(1, False)
+    graph["graph_cycles"] = st_g["graph_cycles"]
+    graph["same_bits_as_direct"] = len(res_g) == len(res_d) and all(
+        a["cycles"] == b["cycles"] and a["a"] == b["a"] and np.array_equal(a["power"], b["power"])
+        for a, b in zip(res_d, res_g))
+    out = {"sizes": "16 x 64^3, 16 x 96^3, 16 x 128^3, z = 100 -> 0",
+           "cuda_device_max_connections": os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
+           "stencil_shapes": shapes}
+    out.update(direct)
+    out["graph_cycles"] = graph
+    out["one_scheduler_thread"] = one
+    return out
 
 
 def run_hbm_fit(gpu, device, torch, N=1024, steps=2):
@@ -849,10 +876,14 @@ def run_op(args):
       prepare    IC at z = 100, evolve to --z-op, write the hibernation file --state
       cycle      restart from --state, --reps cycles (the late-time cycle for ncu)
       table      restart from --state (or a fresh IC), time each operation of a cycle
+      ensemble   the 48-simulation batched ensemble alone (direct, graph and one-thread runs)
       r2c_alone, c2r_alone, fft_axis_y, fft_axis_z   one component of random values"""
     import numpy as np
-    import torch
     import gev_gb300 as gpu
+    if args.op == "ensemble":
+        print(json.dumps(run_ensemble(gpu, args.seed)))
+        return
+    import torch
     N = args.grid
     prec = gpu.PREC_MIXED if args.prec == "mixed" else gpu.PREC_FP64
     ctx = gpu.Context(N, prec)

@@ -26,7 +26,11 @@
 //
 // Blocks are persistent (resident blocks per SM x SMs, looping over the tiles)
 // and stage the twiddle table in shared memory once.
+#include <array>
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <utility>
 
 #include "gev_fft_bfly.cuh"
 #include "gev_internal.cuh"
@@ -575,11 +579,35 @@ int fft_cols_z_poisson(gev_ctx *ctx, const void *spec, void *out, double coeff, 
   }
 }
 
+// widths already timed in this process, per (device, N): a later context of a size
+// seen before takes them instead of timing again (a server creates dozens of
+// contexts of a few sizes)
+static std::mutex g_tiles_mu;
+static std::map<std::pair<int, int>, std::array<int, 4>> g_tiles;
+static void fft_tune_all(gev_ctx *ctx);
+
 void fft_autotune(gev_ctx *ctx) {
   if (ctx->fft_tuned) return;
   ctx->fft_tuned = true;
   const int N = ctx->N;
   if (ctx->prec == GEV_PREC_FP64 || !ctx->d_fft_scratch || !fft_reg_ok(N)) return;
+  const auto key = std::make_pair(ctx->device, N);
+  {
+    std::lock_guard<std::mutex> lk(g_tiles_mu);
+    const auto it = g_tiles.find(key);
+    if (it != g_tiles.end()) {
+      for (int p = 0; p < 4; ++p) ctx->fft_lg[p] = it->second[p];
+      return;
+    }
+  }
+  fft_tune_all(ctx);
+  std::lock_guard<std::mutex> lk(g_tiles_mu);
+  g_tiles[key] = {ctx->fft_lg[0], ctx->fft_lg[1], ctx->fft_lg[2], ctx->fft_lg[3]};
+}
+
+// times the candidate widths of the four passes on the context's scratch spectrum
+static void fft_tune_all(gev_ctx *ctx) {
+  const int N = ctx->N;
   k_tune_fill<<<grid_for(ctx, ctx->fft_scratch_bytes / 4, 256, 8), 256, 0, ctx->stream>>>(
       (float *)ctx->d_fft_scratch, ctx->fft_scratch_bytes / 4);
   if (cudaGetLastError() != cudaSuccess) return;

@@ -55,6 +55,11 @@ struct gev_ctx {
   // passes, chosen by timing on the first transform (-1: the default)
   int fft_lg[4] = {-1, -1, -1, -1};
   bool fft_tuned = false;
+  // FP32 source stencils (scalar, tensor): threads a block and the cap on blocks a
+  // SM of their grid-stride launches, chosen by timing on the first call
+  int st_threads[2] = {256, 256};
+  int st_per_sm[2] = {16, 16};
+  bool st_tuned = false;
   long long launches = 0;
   // optional device timing of named regions (gev_ctx_set_timing): a CUDA event
   // pair on the stream around each region, summed per name when the report is read
@@ -157,6 +162,10 @@ struct gev_sim {
   gev_sim_state st{};
   double *host_words = nullptr;  // pinned: [0] T00 sum, [1] max bits, [2] phi(k=0).re
   double *dev_words = nullptr;
+  // gev_sim_step_graph: the executable graph of the last captured cycle, and counts
+  // of cycles launched as a graph, instantiations, and cycles enqueued directly
+  cudaGraphExec_t gexec = nullptr;
+  long graph_launches = 0, graph_builds = 0, graph_direct = 0;
 };
 
 // ----------------------------------------------------------------- errors --

@@ -7,6 +7,7 @@
 // (a 64^3 cycle is some fifty short kernels: one thread cannot issue them as fast
 // as the GPU runs them for dozens of small simulations).
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -44,6 +45,8 @@ struct Active {
   long head = 0, tail = 0;  // events [tail, head) of the ring are in flight
   bool finishing = false;
   int worker = 0;           // the scheduler thread that enqueues its cycles
+  bool need_ic = false;     // admitted; its worker generates the initial conditions first
+  gev_ic_params ic{};
 };
 
 struct Pending {
@@ -67,6 +70,7 @@ struct gev_server {
   std::map<std::pair<int, int>, std::vector<Slot *>> idle;
   std::map<std::pair<int, int>, size_t> footprint;
   int workers = 1;
+  std::atomic<int> graphs{0};  // 1: cycles enqueued as CUDA graphs (gev_sim_step_graph)
   std::vector<std::thread> th;
   bool stop = false;
   long next_id = 1;
@@ -288,8 +292,8 @@ void scheduler(gev_server *s, int worker) {
       A->t_submit = p.t_submit;
       A->t_admit = s->now();
       A->slot = sl;
-      if (sl) {
-        gev_ic_params ic;
+      if (sl) {  // the initial conditions are generated by the worker that steps it
+        gev_ic_params &ic = A->ic;
         memset(&ic, 0, sizeof(ic));
         ic.h = p.req.h;
         ic.Omega_cdm = p.req.Omega_cdm;
@@ -303,8 +307,7 @@ void scheduler(gev_server *s, int worker) {
         ic.seed = p.req.seed;
         ic.ksphere = 1;
         ic.correct_displacement = 1;
-        rc = gev_sim_ic_generate(sl->sim, &ic);
-        if (!rc) slot_measure(s, sl);
+        A->need_ic = true;
         A->a_target = 1. / (1. + p.req.z_target);
       }
       {
@@ -348,6 +351,19 @@ void scheduler(gev_server *s, int worker) {
     }
     for (Active *A : act) {
       Slot *sl = A->slot;
+      if (A->need_ic) {  // on this worker's thread, so that several simulations start at once
+        A->need_ic = false;
+        const int rc = gev_sim_ic_generate(sl->sim, &A->ic);
+        if (rc) {
+          cudaGetLastError();
+          finish(s, A, rc);
+          remove_active(s, A);
+        } else {
+          slot_measure(s, sl);
+        }
+        progressed = true;
+        continue;
+      }
       const long R = (long)sl->ev.size();
       while (A->tail < A->head && cudaEventQuery(sl->ev[(size_t)(A->tail % R)]) == cudaSuccess) A->tail++;
       if (A->finishing) {
@@ -365,7 +381,9 @@ void scheduler(gev_server *s, int worker) {
         progressed = true;
         continue;
       }
-      const int rc = gev_sim_step(sl->sim);
+      const bool as_graph = s->graphs.load(std::memory_order_relaxed) != 0;
+      const long g0 = sl->sim->graph_launches;
+      const int rc = as_graph ? gev_sim_step_graph(sl->sim) : gev_sim_step(sl->sim);
       if (rc || cudaEventRecord(sl->ev[(size_t)(A->head % R)], sl->ctx->stream) != cudaSuccess) {
         cudaStreamSynchronize(sl->ctx->stream);
         cudaGetLastError();
@@ -378,6 +396,7 @@ void scheduler(gev_server *s, int worker) {
       {
         std::lock_guard<std::mutex> lk(s->mu);
         s->st.particle_steps += (double)A->req.N * A->req.N * A->req.N;
+        s->st.graph_cycles += sl->sim->graph_launches - g0;
       }
       progressed = true;
     }
@@ -432,6 +451,12 @@ int gev_server_create_workers(int device, size_t bytes_budget, int max_active, i
   s->workers = workers;
   for (int k = 0; k < workers; ++k) s->th.emplace_back(scheduler, s, k);
   *out = s;
+  return GEV_OK;
+}
+
+int gev_server_set_graphs(gev_server *s, int on) {
+  if (!s) return GEV_EINVAL;
+  s->graphs.store(on ? 1 : 0, std::memory_order_relaxed);
   return GEV_OK;
 }
 

@@ -140,6 +140,7 @@ int gev_sim_destroy(gev_sim *s) {
   gev_field_destroy(s->BiFT);
   if (s->host_words) cudaFreeHost(s->host_words);
   cudaFree(s->dev_words);
+  if (s->gexec) cudaGraphExecDestroy(s->gexec);
   gev_ctx *ctx = s->ctx;
   delete s;
   if (ctx) ctx_release(ctx);
@@ -287,6 +288,73 @@ int gev_sim_step_particles(gev_sim *s) {
 int gev_sim_step(gev_sim *s) {
   const int rc = gev_sim_step_fields(s);
   return rc ? rc : gev_sim_step_particles(s);
+}
+
+// The cycle of gev_sim_step as one CUDA graph.  The host runs the same code as
+// gev_sim_step with the stream under capture (thread-local mode: other host threads
+// keep driving their own streams), so the graph holds exactly the launches, copies
+// and scalar arguments a direct cycle would enqueue.  From one cycle to the next
+// the launch sequence keeps its shape and only scalar arguments and the particle
+// arrays' halves change, so the simulation's executable graph is updated in place
+// (cudaGraphExecUpdate) and instantiated again only when the shape changes.
+// Direct cycles do what a cycle sets up on first use (the FFT tile tuner, the
+// reduction and deposit scratch): the first two cycles of a run (the first has no
+// phi solve) and every cycle with the per-kernel timers on.  A capture the runtime
+// refuses leaves nothing enqueued; the host's side of the cycle (the background
+// state, the particle arrays' halves) is put back and the cycle runs directly.
+int gev_sim_step_graph(gev_sim *s) {
+  if (!s) return GEV_EINVAL;
+  gev_ctx *ctx = s->ctx;
+  if (s->st.cycle < 2 || s->st.dtau_old <= 0. || ctx->timing) {
+    s->graph_direct++;
+    return gev_sim_step(s);
+  }
+  const gev_sim_state st0 = s->st;
+  const PclsArrays cur0 = s->pcls->cur, alt0 = s->pcls->alt;
+  auto direct = [&]() {
+    cudaGetLastError();
+    s->st = st0;
+    s->pcls->cur = cur0;
+    s->pcls->alt = alt0;
+    s->graph_direct++;
+    return gev_sim_step(s);
+  };
+  if (cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) return direct();
+  const int rc = gev_sim_step(s);
+  cudaGraph_t g = nullptr;
+  const cudaError_t ce = cudaStreamEndCapture(ctx->stream, &g);
+  if (rc != GEV_OK || ce != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    return direct();
+  }
+  if (s->gexec) {
+    cudaGraphExecUpdateResultInfo info;
+    if (cudaGraphExecUpdate(s->gexec, g, &info) != cudaSuccess) {
+      cudaGetLastError();
+      cudaGraphExecDestroy(s->gexec);
+      s->gexec = nullptr;
+    }
+  }
+  if (!s->gexec) {
+    if (cudaGraphInstantiate(&s->gexec, g, 0) != cudaSuccess) {
+      s->gexec = nullptr;
+      cudaGraphDestroy(g);
+      return direct();
+    }
+    s->graph_builds++;
+  }
+  cudaGraphDestroy(g);
+  if (cudaGraphLaunch(s->gexec, ctx->stream) != cudaSuccess) return direct();
+  s->graph_launches++;
+  return GEV_OK;
+}
+
+int gev_sim_graph_info(gev_sim *s, long *launches, long *builds, long *direct) {
+  if (!s) return GEV_EINVAL;
+  if (launches) *launches = s->graph_launches;
+  if (builds) *builds = s->graph_builds;
+  if (direct) *direct = s->graph_direct;
+  return GEV_OK;
 }
 
 }  // extern "C"

@@ -2,6 +2,11 @@
 // reductions.  One thread per cell, x fastest so that a warp reads contiguous
 // rows; the +-1 neighbours in y and z come from rows already in L1/L2.
 // Periodic wrap replaces LATfield2's halo (updateHalo, main.cpp:518, 568).
+#include <array>
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "gev_internal.cuh"
 
 namespace {
@@ -207,9 +212,159 @@ __global__ void k_sum_final(const double *partial, int nb, double *out) {
 
 bool same_ctx(gev_ctx *ctx, const gev_field *f, int kind) { return f && f->ctx == ctx && f->kind == kind; }
 
+// ---------------------------------------------------------------- tuning --
+// The FP32 stencils are grid-stride loops over 4-cell vectors, each vector
+// computed alone, so every launch shape gives the same bits; which shape runs
+// fastest depends on the grid (a 64^3 field is 65,536 vectors, fewer than the GPU
+// holds threads).  On the first call of the first context of a size in the process
+// the candidates -- 128, 256 or 512 threads a block, at most 4, 8, 16 or 32 blocks a
+// SM -- are timed on scratch fields of that size filled with bounded values (three
+// rounds, the best time of each), and a shape replaces the default (256 threads, 16
+// blocks a SM) only when it is more than 3% faster; later contexts of that size take
+// the same shapes.  Grids above 256^3 keep the default: there every candidate
+// fills the GPU many times over, and the scratch (13 fields) would be large.
+constexpr int ST_THREADS[3] = {128, 256, 512};
+constexpr int ST_PER_SM[4] = {4, 8, 16, 32};
+constexpr int ST_TUNE_MAX_N = 256;
+
+__global__ void k_st_fill(float *s, size_t n) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+    s[i] = (float)((unsigned)(i * 2654435761u) >> 8) * (1.f / 16777216.f) - 0.5f;
+}
+
+void launch_scalar4(gev_ctx *ctx, int threads, int per_sm, const float *phi, const float *chi, const float *source,
+                    float bgmodel, float *result, float coeff, float coeff2, float coeff3) {
+  const size_t V = (size_t)ctx->N * ctx->N * ctx->N;
+  k_source_scalar4<<<grid_for(ctx, V / 4, threads, per_sm), threads, 0, ctx->stream>>>(
+      phi, chi, source, bgmodel, result, coeff, coeff2, coeff3, ctx->N, lg_pow2(ctx->N), make_div32(ctx->N));
+}
+
+void launch_tensor4(gev_ctx *ctx, int threads, int per_sm, const float *phi, const float *Tij, float *Sij,
+                    float coeff) {
+  const size_t V = (size_t)ctx->N * ctx->N * ctx->N;
+  k_source_tensor4<<<grid_for(ctx, V / 4, threads, per_sm), threads, 0, ctx->stream>>>(
+      phi, Tij, Sij, coeff, ctx->N, lg_pow2(ctx->N), make_div32(ctx->N));
+}
+
+// mean ms of 5 launches after one untimed launch; +inf when a launch fails
+template <typename F>
+float st_time_ms(gev_ctx *ctx, F &&fn) {
+  cudaEvent_t a = nullptr, b = nullptr;
+  float ms = 3.4e38f;
+  if (cudaEventCreate(&a) == cudaSuccess && cudaEventCreate(&b) == cudaSuccess) {
+    fn();
+    cudaEventRecord(a, ctx->stream);
+    for (int k = 0; k < 5; ++k) fn();
+    cudaEventRecord(b, ctx->stream);
+    if (cudaGetLastError() == cudaSuccess && cudaEventSynchronize(b) == cudaSuccess &&
+        cudaEventElapsedTime(&ms, a, b) == cudaSuccess)
+      ms /= 5.f;
+    else
+      ms = 3.4e38f;
+  }
+  cudaGetLastError();
+  if (a) cudaEventDestroy(a);
+  if (b) cudaEventDestroy(b);
+  return ms;
+}
+
+// shapes already timed in this process, per (device, N): a later context of a size
+// seen before takes them instead of timing again
+std::mutex g_shapes_mu;
+std::map<std::pair<int, int>, std::array<int, 4>> g_shapes;
+
+void stencil_tune(gev_ctx *ctx);
+
+void stencil_autotune(gev_ctx *ctx) {
+  if (ctx->st_tuned) return;
+  ctx->st_tuned = true;
+  const int N = ctx->N;
+  if (ctx->prec == GEV_PREC_FP64 || N % 4 != 0 || N > ST_TUNE_MAX_N) return;
+  const auto key = std::make_pair(ctx->device, N);
+  {
+    std::lock_guard<std::mutex> lk(g_shapes_mu);
+    const auto it = g_shapes.find(key);
+    if (it != g_shapes.end()) {
+      for (int k = 0; k < 2; ++k) {
+        ctx->st_threads[k] = it->second[k];
+        ctx->st_per_sm[k] = it->second[2 + k];
+      }
+      return;
+    }
+  }
+  stencil_tune(ctx);
+  std::lock_guard<std::mutex> lk(g_shapes_mu);
+  g_shapes[key] = {ctx->st_threads[0], ctx->st_threads[1], ctx->st_per_sm[0], ctx->st_per_sm[1]};
+}
+
+// times the candidates on scratch fields of the context's size
+void stencil_tune(gev_ctx *ctx) {
+  const int N = ctx->N;
+  const size_t V = (size_t)N * N * N;
+  float *tmp = nullptr;
+  if (cudaMallocAsync((void **)&tmp, 13 * V * sizeof(float), ctx->stream) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  k_st_fill<<<grid_for(ctx, 13 * V, 256, 8), 256, 0, ctx->stream>>>(tmp, 13 * V);
+  float *phi = tmp, *chi = tmp + V, *src = tmp + 2 * V, *res = tmp + 3 * V, *Tij = tmp + V, *Sij = tmp + 7 * V;
+  for (int which = 0; which < 2; ++which) {
+    float t[3][4];
+    for (auto &row : t)
+      for (float &x : row) x = 3.4e38f;
+    for (int round = 0; round < 3; ++round)
+      for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 4; ++b) {
+          const int th = ST_THREADS[a], ps = ST_PER_SM[b];
+          // shapes that give the same grid as a smaller cap are the same launch
+          if (b > 0 && grid_for(ctx, V / 4, th, ps) == grid_for(ctx, V / 4, th, ST_PER_SM[b - 1])) continue;
+          const float ms = which == 0 ? st_time_ms(ctx, [&] {
+            launch_scalar4(ctx, th, ps, phi, chi, src, 0.3f, res, 1e-3f, 1e-3f, 1e-3f);
+          })
+                                      : st_time_ms(ctx, [&] { launch_tensor4(ctx, th, ps, phi, Tij, Sij, 1e-3f); });
+          t[a][b] = fminf(t[a][b], ms);
+        }
+    int ba = 1, bb = 2;  // the default, 256 threads and 16 blocks a SM
+    const float tdef = t[1][2];
+    for (int a = 0; a < 3; ++a)
+      for (int b = 0; b < 4; ++b)
+        if (t[a][b] < 0.97f * tdef && t[a][b] < t[ba][bb]) {
+          ba = a;
+          bb = b;
+        }
+    ctx->st_threads[which] = ST_THREADS[ba];
+    ctx->st_per_sm[which] = ST_PER_SM[bb];
+  }
+  cudaFreeAsync(tmp, ctx->stream);
+  cudaGetLastError();
+}
+
 }  // namespace
 
 extern "C" {
+
+int gev_ctx_stencil_shapes(gev_ctx *ctx, int threads[2], int per_sm[2]) {
+  if (!ctx || !threads || !per_sm) return gev_fail(ctx, GEV_EINVAL, "ctx_stencil_shapes: null argument");
+  for (int k = 0; k < 2; ++k) {
+    threads[k] = ctx->st_threads[k];
+    per_sm[k] = ctx->st_per_sm[k];
+  }
+  return GEV_OK;
+}
+
+int gev_ctx_set_stencil_shapes(gev_ctx *ctx, const int threads[2], const int per_sm[2]) {
+  if (!ctx || !threads || !per_sm) return gev_fail(ctx, GEV_EINVAL, "ctx_set_stencil_shapes: null argument");
+  for (int k = 0; k < 2; ++k)
+    if ((threads[k] != 64 && threads[k] != 128 && threads[k] != 256 && threads[k] != 512) || per_sm[k] < 1 ||
+        per_sm[k] > 64)
+      return gev_fail(ctx, GEV_EINVAL, "ctx_set_stencil_shapes: 64, 128, 256 or 512 threads, 1..64 blocks a SM");
+  for (int k = 0; k < 2; ++k) {
+    ctx->st_threads[k] = threads[k];
+    ctx->st_per_sm[k] = per_sm[k];
+  }
+  ctx->st_tuned = true;
+  return GEV_OK;
+}
 
 int gev_prepare_source_tensor(gev_ctx *ctx, const gev_field *phi, const gev_field *Tij, gev_field *Sij, double coeff) {
   if (!ctx || !same_ctx(ctx, phi, GEV_FIELD_REAL) || !same_ctx(ctx, Tij, GEV_FIELD_REAL) ||
@@ -217,15 +372,15 @@ int gev_prepare_source_tensor(gev_ctx *ctx, const gev_field *phi, const gev_fiel
     return gev_fail(ctx, GEV_EINVAL, "prepare_source_tensor: phi (1 comp), Tij and Sij (6 comps) real fields");
   const size_t V = (size_t)ctx->N * ctx->N * ctx->N;
   const int blocks = grid_for(ctx, V, 256, 16);
+  stencil_autotune(ctx);
   GevTimed tm_(ctx, "k_source_tensor");
   if (ctx->prec == GEV_PREC_FP64)
     k_source_tensor<double><<<blocks, 256, 0, ctx->stream>>>((const double *)phi->d, (const double *)Tij->d,
                                                              (double *)Sij->d, coeff, ctx->N, lg_pow2(ctx->N),
                                                              make_div32(ctx->N));
   else if (ctx->N % 4 == 0)
-    k_source_tensor4<<<grid_for(ctx, V / 4, 256, 16), 256, 0, ctx->stream>>>(
-        (const float *)phi->d, (const float *)Tij->d, (float *)Sij->d, (float)coeff, ctx->N, lg_pow2(ctx->N),
-        make_div32(ctx->N));
+    launch_tensor4(ctx, ctx->st_threads[1], ctx->st_per_sm[1], (const float *)phi->d, (const float *)Tij->d,
+                   (float *)Sij->d, (float)coeff);
   else
     k_source_tensor<float><<<blocks, 256, 0, ctx->stream>>>((const float *)phi->d, (const float *)Tij->d,
                                                             (float *)Sij->d, (float)coeff, ctx->N, lg_pow2(ctx->N),
@@ -242,6 +397,7 @@ int gev_prepare_source_scalar(gev_ctx *ctx, const gev_field *phi, const gev_fiel
     return gev_fail(ctx, GEV_EINVAL, "prepare_source_scalar: four 1-component real fields");
   const size_t V = (size_t)ctx->N * ctx->N * ctx->N;
   const int blocks = grid_for(ctx, V, 256, 16);
+  stencil_autotune(ctx);
   GevTimed tm_(ctx, "k_source_scalar");
   if (ctx->prec == GEV_PREC_FP64)
     k_source_scalar<double><<<blocks, 256, 0, ctx->stream>>>((const double *)phi->d, (const double *)chi->d,
@@ -249,9 +405,9 @@ int gev_prepare_source_scalar(gev_ctx *ctx, const gev_field *phi, const gev_fiel
                                                              coeff, coeff2, coeff3, ctx->N, lg_pow2(ctx->N),
                                                              make_div32(ctx->N));
   else if (ctx->N % 4 == 0)
-    k_source_scalar4<<<grid_for(ctx, V / 4, 256, 16), 256, 0, ctx->stream>>>(
-        (const float *)phi->d, (const float *)chi->d, (const float *)source->d, (float)bgmodel, (float *)result->d,
-        (float)coeff, (float)coeff2, (float)coeff3, ctx->N, lg_pow2(ctx->N), make_div32(ctx->N));
+    launch_scalar4(ctx, ctx->st_threads[0], ctx->st_per_sm[0], (const float *)phi->d, (const float *)chi->d,
+                   (const float *)source->d, (float)bgmodel, (float *)result->d, (float)coeff, (float)coeff2,
+                   (float)coeff3);
   else
     k_source_scalar<float><<<blocks, 256, 0, ctx->stream>>>(
         (const float *)phi->d, (const float *)chi->d, (const float *)source->d, (float)bgmodel, (float *)result->d,

@@ -46,6 +46,8 @@ _SIGS = {
     "gev_ctx_timing_report": [_vp, ctypes.c_char_p, ctypes.c_size_t, _i],
     "gev_ctx_fft_tiles": [_vp, ctypes.POINTER(_i)],
     "gev_ctx_set_fft_tiles": [_vp, ctypes.POINTER(_i)],
+    "gev_ctx_stencil_shapes": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)],
+    "gev_ctx_set_stencil_shapes": [_vp, ctypes.POINTER(_i), ctypes.POINTER(_i)],
     "gev_field_create": [_vp, _i, _i, ctypes.POINTER(_vp)],
     "gev_field_destroy": [_vp],
     "gev_field_upload": [_vp, _vp],
@@ -176,6 +178,17 @@ class Context:
         """Pins the mixed form's FFT tile widths instead of timing them."""
         lg = (_i * 4)(r2c_rows, y, z, c2r_rows)
         _check(lib().gev_ctx_set_fft_tiles(self.handle, lg), self, "gev_ctx_set_fft_tiles")
+
+    def stencil_shapes(self):
+        """(threads a block, cap on blocks a SM) of the scalar and tensor source stencils."""
+        th, ps = (_i * 2)(), (_i * 2)()
+        _check(lib().gev_ctx_stencil_shapes(self.handle, th, ps), self, "gev_ctx_stencil_shapes")
+        return {"scalar": (th[0], ps[0]), "tensor": (th[1], ps[1])}
+
+    def set_stencil_shapes(self, scalar, tensor):
+        """Pins the source stencils' (threads, blocks a SM) instead of timing them."""
+        th, ps = (_i * 2)(scalar[0], tensor[0]), (_i * 2)(scalar[1], tensor[1])
+        _check(lib().gev_ctx_set_stencil_shapes(self.handle, th, ps), self, "gev_ctx_set_stencil_shapes")
 
     def bytes_in_use(self):
         b = ctypes.c_size_t()
@@ -420,6 +433,8 @@ _SIM_SIGS = {
     "gev_sim_field": [_vp, _i, ctypes.POINTER(_vp)],
     "gev_sim_particles": [_vp, ctypes.POINTER(_vp)],
     "gev_sim_step": [_vp],
+    "gev_sim_step_graph": [_vp],
+    "gev_sim_graph_info": [_vp, ctypes.POINTER(_l), ctypes.POINTER(_l), ctypes.POINTER(_l)],
 }
 
 SIM_FIELDS = {"phi": (0, FIELD_REAL, 1), "chi": (1, FIELD_REAL, 1), "source": (2, FIELD_REAL, 1),
@@ -505,6 +520,17 @@ class Sim:
 
     def step(self):
         _check(_sim_lib().gev_sim_step(self.handle), self.ctx, "gev_sim_step")
+
+    def step_graph(self):
+        """The same cycle enqueued as one CUDA graph (gev_sim_step_graph)."""
+        _check(_sim_lib().gev_sim_step_graph(self.handle), self.ctx, "gev_sim_step_graph")
+
+    def graph_info(self):
+        """(cycles launched as a graph, instantiations, cycles enqueued directly)."""
+        v = [_l(), _l(), _l()]
+        _check(_sim_lib().gev_sim_graph_info(self.handle, *[ctypes.byref(x) for x in v]), self.ctx,
+               "gev_sim_graph_info")
+        return tuple(x.value for x in v)
 
 
 class _Borrowed(Field):
@@ -744,12 +770,14 @@ class Result(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [(n, _l) for n in ("submitted", "admitted", "completed", "failed", "active", "pending",
                                   "max_active_seen")] + [("particle_steps", _d), ("busy_seconds", _d)] + [
-        (n, ctypes.c_size_t) for n in ("bytes_budget", "bytes_in_use", "bytes_peak")] + [("workers", _l)]
+        (n, ctypes.c_size_t) for n in ("bytes_budget", "bytes_in_use", "bytes_peak")] + [("workers", _l),
+                                                                                         ("graph_cycles", _l)]
 
 
 _SERVE_SIGS = {
     "gev_server_create": [_i, ctypes.c_size_t, _i, _i, ctypes.POINTER(_vp)],
     "gev_server_create_workers": [_i, ctypes.c_size_t, _i, _i, _i, ctypes.POINTER(_vp)],
+    "gev_server_set_graphs": [_vp, _i],
     "gev_server_submit": [_vp, ctypes.POINTER(Request), ctypes.POINTER(_l)],
     "gev_server_poll": [_vp, ctypes.POINTER(Result), _i, ctypes.POINTER(_i)],
     "gev_server_drain": [_vp, _d],
@@ -787,9 +815,9 @@ def result_dict(r):
 class Server:
     """Continuous batching of simulations on one GPU (include/gev_serve.h)."""
 
-    def __init__(self, device=0, bytes_budget=0, max_active=0, inflight=0, workers=0):
+    def __init__(self, device=0, bytes_budget=0, max_active=0, inflight=0, workers=0, graphs=False):
         """workers: host threads that enqueue the simulations' cycles (0: chosen from
-        the host's hardware threads)."""
+        the host's hardware threads); graphs: each cycle enqueued as one CUDA graph."""
         self.handle = None
         h = _vp()
         rc = _serve_lib().gev_server_create_workers(device, bytes_budget, max_active, inflight, workers,
@@ -797,6 +825,10 @@ class Server:
         if rc != OK:
             raise GevError("gev_server_create failed (%d)" % rc)
         self.handle = h.value
+        if graphs:
+            rc = _serve_lib().gev_server_set_graphs(self.handle, 1)
+            if rc != OK:
+                raise GevError("gev_server_set_graphs failed (%d)" % rc)
 
     def __del__(self):
         try:

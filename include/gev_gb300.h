@@ -86,6 +86,16 @@ int gev_ctx_fft_tiles(gev_ctx *ctx, int lg[4]);
 /* pins the mixed form's FFT tile widths (rows 1..3, columns 2..4, at most 1024
  * threads a tile) instead of timing them; GEV_EINVAL for the FP64 form */
 int gev_ctx_set_fft_tiles(gev_ctx *ctx, const int lg[4]);
+/* the launch shapes of the mixed form's source stencils (prepareFTsource scalar
+ * [0] and tensor [1]): threads a block and the cap on blocks a SM of their
+ * grid-stride grids.  On a context's first stencil call each is chosen by timing
+ * its candidates (128, 256, 512 threads; 4, 8, 16, 32 blocks a SM) on scratch
+ * fields, for grids up to 256^3 (larger grids keep 256 threads and 16 blocks a
+ * SM); every shape gives the same bits */
+int gev_ctx_stencil_shapes(gev_ctx *ctx, int threads[2], int per_sm[2]);
+/* pins those shapes instead of timing them: 64, 128, 256 or 512 threads, 1..64
+ * blocks a SM */
+int gev_ctx_set_stencil_shapes(gev_ctx *ctx, const int threads[2], const int per_sm[2]);
 
 /* ---- fields (Field<Real> / Field<Cplx>::initialize, main.cpp:226-237) ---- */
 int gev_field_create(gev_ctx *ctx, int kind, int ncomp, gev_field **out);

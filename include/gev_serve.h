@@ -59,6 +59,7 @@ typedef struct {
   double busy_seconds;       /* time with at least one simulation admitted */
   size_t bytes_budget, bytes_in_use, bytes_peak;
   long workers;              /* host threads that enqueue the simulations' cycles */
+  long graph_cycles;         /* cycles launched as one CUDA graph each (gev_server_set_graphs) */
 } gev_server_stats;
 
 typedef struct gev_server gev_server;
@@ -74,6 +75,10 @@ int gev_server_create(int device, size_t bytes_budget, int max_active, int infli
  * result does not depend on the count */
 int gev_server_create_workers(int device, size_t bytes_budget, int max_active, int inflight, int workers,
                               gev_server **out);
+/* on != 0: the schedulers enqueue each simulation's cycles with gev_sim_step_graph
+ * (one CUDA graph a cycle, updated in place from cycle to cycle) instead of
+ * gev_sim_step; results are the same bits either way.  Default off. */
+int gev_server_set_graphs(gev_server *s, int on);
 int gev_server_submit(gev_server *s, const gev_request *req, long *id);
 /* up to max completed results not yet returned; *n their number */
 int gev_server_poll(gev_server *s, gev_result *out, int max, int *n);

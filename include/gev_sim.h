@@ -57,6 +57,19 @@ int gev_sim_step(gev_sim *s);
  * Between the two, source, Sij, scalarFT and SijFT are free scratch. */
 int gev_sim_step_fields(gev_sim *s);
 int gev_sim_step_particles(gev_sim *s);
+/* the cycle of gev_sim_step enqueued as one CUDA graph: the host code of the cycle
+ * runs with the stream under capture (thread-local mode), and the simulation's
+ * executable graph is updated in place with the new cycle's arguments
+ * (instantiated again only if the launch sequence changed shape), then launched.
+ * The results are the same bits as gev_sim_step's.  The first two cycles of a run,
+ * and cycles with the per-kernel timers on, are enqueued directly (they set up
+ * what the cycle tunes or allocates on first use); a capture the runtime refuses
+ * also falls back to a direct cycle.  No call may be made on the simulation's
+ * stream from another thread while this one runs. */
+int gev_sim_step_graph(gev_sim *s);
+/* cycles launched as a graph, graph instantiations, and cycles enqueued directly
+ * by gev_sim_step_graph since the simulation was created (any pointer may be NULL) */
+int gev_sim_graph_info(gev_sim *s, long *launches, long *builds, long *direct);
 
 /* Zel'dovich initial conditions at z_in generated on the device, following the
  * power-spectrum branch of generateIC_basic (ic_basic.hpp:1626-2259): sc1
