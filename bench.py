@@ -673,9 +673,11 @@ def run_serve(args, gpu):
 def run_ensemble(gpu, seed):
     """The batched ensemble: 16 simulations each at 64^3, 96^3 and 128^3, box 2.5 N,
     Omega_cdm U[0.25, 0.35], sigma8 U[0.75, 0.87], n_s U[0.94, 0.98], distinct seeds,
-    all to z = 0, admitted at once.  Run three ways on the same requests: cycles
-    enqueued directly by the default scheduler threads, the same with each cycle
-    enqueued as one CUDA graph, and directly by one scheduler thread."""
+    all to z = 0, admitted at once.  Run four ways on the same requests: through the
+    server with cycles enqueued directly by the default scheduler threads, the same
+    with each cycle enqueued as one CUDA graph, and with one scheduler thread; and in
+    batched steps (gev_batch_run: one launch per kernel of a cycle for each grid
+    size's cohort of 16)."""
     import numpy as np
     rng = np.random.default_rng(seed + 301)
     ens = []
@@ -704,9 +706,52 @@ def run_ensemble(gpu, seed):
         gpu.prepare_source_tensor(phi.zero(), Tij.zero(), Tij, 1e-3)
         shapes[str(N)] = ctx.stencil_shapes()
         del phi, Tij, ctx
+    def ensemble_batched():
+        # the same requests advanced by gev_batch_run: one launch per kernel of a cycle for
+        # each grid size's cohort; contexts and initial conditions made by four host
+        # threads; timed from the first context to the last result's spectrum, as the
+        # server runs are
+        from concurrent.futures import ThreadPoolExecutor
+
+        def make(r):
+            c = gpu.Context(r.N, gpu.PREC_MIXED)
+            sim = gpu.Sim(c, r.N ** 3)
+            sim.ic_generate(**gpu.ic_params(r.boxsize, seed=r.seed, z_in=r.z_in, Omega_cdm=r.Omega_cdm,
+                                            Omega_b=r.Omega_b, sigma8=r.sigma8, n_s=r.n_s, h=r.h))
+            return c, sim
+
+        t0 = time.perf_counter()
+        with ThreadPoolExecutor(4) as ex:
+            runs = list(ex.map(make, ens))
+        b = gpu.Batch()
+        cycles = b.run([sim for _, sim in runs], [1.0 / (1.0 + r.z_target) for r in ens])
+        powers = []
+        for (c, sim), r in zip(runs, ens):
+            F = c.spectrum(1)
+            gpu.fft_r2c(sim.field("phi"), F)
+            _, pw, _, _, _ = gpu.cross_spectrum(F, None, r.numbins, False)
+            n3 = float(r.N) ** 3
+            powers.append(pw / (n3 * n3 * 2. * np.pi * np.pi))
+        span = time.perf_counter() - t0
+        nb, nd, nl = b.info()
+        steps = sum(float(r.N) ** 3 * k for r, k in zip(ens, cycles))
+        b.close()
+        del runs
+        return cycles, powers, {"simulations": len(ens), "makespan_s": span, "particle_steps_per_s": steps / span,
+                                "cycles_batched": nb, "cycles_direct": nd, "batched_launches": nl,
+                                "launches_per_cohort_cycle_note": "3 cohorts (64^3, 96^3, 128^3) of 16"}
+
     res_d, _, direct = ensemble(0, False)
     res_g, st_g, graph = ensemble(0, True)
     _, _, one = ensemble(1, False)
+    cyc_b, pow_b, batched = ensemble_batched()
+    # against the server's (direct) cycles: the same cycle counts, P(k) of phi to FP32
+    # rounding (the batched kernels are compiled apart and may fuse multiply-adds
+    # differently)
+    batched["same_cycles_as_server"] = len(res_d) == len(ens) and all(
+        a["cycles"] == k for a, k in zip(res_d, cyc_b))
+    batched["max_rel_pk_dev_vs_server"] = max(
+        float(np.max(np.abs(pw - a["power"]) / np.abs(a["power"]))) for a, pw in zip(res_d, pow_b))
     graph["graph_cycles"] = st_g["graph_cycles"]
     graph["same_bits_as_direct"] = len(res_g) == len(res_d) and all(
         a["cycles"] == b["cycles"] and a["a"] == b["a"] and np.array_equal(a["power"], b["power"])
@@ -716,6 +761,7 @@ def run_ensemble(gpu, seed):
            "stencil_shapes": shapes}
     out.update(direct)
     out["graph_cycles"] = graph
+    out["batched_per_phase"] = batched
     out["one_scheduler_thread"] = one
     return out
 

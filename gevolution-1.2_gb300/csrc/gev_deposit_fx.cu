@@ -29,7 +29,7 @@
 //     then adds to the field and clears.
 #include <cmath>
 
-#include "gev_internal.cuh"
+#include "gev_batch.cuh"
 
 namespace {
 
@@ -86,7 +86,7 @@ struct DenseTab {
 // or DENSE_NONE once the D.cap slots are taken: every such cell's entry is written,
 // and the gather reads only such cells' entries (the counts and the cell starts it
 // walks come from the same relink).
-__global__ void __launch_bounds__(256) k_fx_bounds(const float *__restrict__ vx, const float *__restrict__ vy,
+__device__ __forceinline__ void k_fx_bounds_body(const float *__restrict__ vx, const float *__restrict__ vy,
                                                    const float *__restrict__ vz, long n,
                                                    const uint32_t *__restrict__ count, const float *__restrict__ phi,
                                                    long C, uint32_t *bounds, DenseTab D) {
@@ -169,6 +169,12 @@ __global__ void __launch_bounds__(256) k_fx_bounds(const float *__restrict__ vx,
     atomicMax(&bounds[4], __float_as_uint(ph));
   }
 }
+__global__ void __launch_bounds__(256) k_fx_bounds(const float *__restrict__ vx, const float *__restrict__ vy,
+                                                   const float *__restrict__ vz, long n,
+                                                   const uint32_t *__restrict__ count, const float *__restrict__ phi,
+                                                   long C, uint32_t *bounds, DenseTab D) {
+  k_fx_bounds_body(vx, vy, vz, n, count, phi, C, bounds, D);
+}
 
 // per-particle contribution bounds, |phi| <= 1 taken for the (1 + f phi) factors:
 // T00 m (e + (3e + q^2/e)|phi|) <= m (4e + q^2/a); T0i m |q_i| (1 + 2|phi|) <= 3 m |q|;
@@ -208,7 +214,7 @@ __device__ void fx_group(uint32_t *bounds, int group, double pmax, double gmax, 
 // prefactor and weight-factor bounds per kind (|phi| <= phimax):
 // mass p = m, g = w; T00 p = m e, g = w (1 + (3 + q^2/e^2) phi) <= 1 + 4 phimax;
 // T0i p = m q_i, g = w (1 + 2 phi); Tij p = m q_i q_j / e <= m q^2 / a, g <= 1 + 5 phimax.
-__global__ void k_fx_scale(uint32_t *bounds, int kind, double mass, double a) {
+__device__ __forceinline__ void k_fx_scale_body(uint32_t *bounds, int kind, double mass, double a) {
   const double q2 = (double)__uint_as_float(bounds[0]);
   const double mc = (double)(bounds[1] > 0u ? bounds[1] : 1u);
   const double ph = (double)__uint_as_float(bounds[4]);
@@ -224,6 +230,9 @@ __global__ void k_fx_scale(uint32_t *bounds, int kind, double mass, double a) {
   } else {
     fx_group(bounds, 0, m * q2 / a, 1. + 5. * ph, mc);
   }
+}
+__global__ void k_fx_scale(uint32_t *bounds, int kind, double mass, double a) {
+  k_fx_scale_body(bounds, kind, mass, a);
 }
 
 // round(y) for |y| < 2^31, integer instructions only
@@ -435,7 +444,7 @@ inline PrepArrays prep_arrays(void *base, long) {
 }
 
 template <int KIND>
-__global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArrays A, FxParams p, int have_phi,
+__device__ __forceinline__ void k_fx_prep_body(PclsArrays P, long n, PrepArrays A, FxParams p, int have_phi,
                                                  const uint32_t *__restrict__ fxb) {
   const float sq0 = pow2f((int)fxb[5]), sq1 = pow2f((int)fxb[7]);
   const float sqT = KIND == FX_T00TIJ ? sq1 : pow2f((int)fxb[5]);  // Tij's prefactor scale
@@ -475,6 +484,11 @@ __global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArray
       o[2] = v2;
     }
   }
+}
+template <int KIND>
+__global__ void __launch_bounds__(256) k_fx_prep(PclsArrays P, long n, PrepArrays A, FxParams p, int have_phi,
+                                                 const uint32_t *__restrict__ fxb) {
+  k_fx_prep_body<KIND>(P, n, A, p, have_phi, fxb);
 }
 
 // ------------------------------------------------------------ dense cells --
@@ -595,7 +609,7 @@ __device__ __forceinline__ void dense_cell(bool has, uint32_t s, const PclsArray
 
 // the small dense cells four to a warp, then the big ones a warp each
 template <int KIND>
-__global__ void __launch_bounds__(32 * DENSE_WARPS) k_dense_sums(PclsArrays P, const uint32_t *__restrict__ start,
+__device__ __forceinline__ void k_dense_sums_body(PclsArrays P, const uint32_t *__restrict__ start,
                                                                 PrepArrays A, const float *__restrict__ phi, FxParams p,
                                                                 Div32 dN, const uint32_t *__restrict__ fxb, DenseTab D) {
   __shared__ long long red[DENSE_WARPS][DENSE_NS][33];
@@ -608,6 +622,12 @@ __global__ void __launch_bounds__(32 * DENSE_WARPS) k_dense_sums(PclsArrays P, c
     dense_cell<KIND, 8>(s < ns, s, P, start, A, phi, p, dN, D, sg00, sgij, red[wib]);
   }
   for (uint32_t b = w0; b < nb; b += warps) dense_cell<KIND, 32>(true, D.cap + b, P, start, A, phi, p, dN, D, sg00, sgij, red[wib]);
+}
+template <int KIND>
+__global__ void __launch_bounds__(32 * DENSE_WARPS) k_dense_sums(PclsArrays P, const uint32_t *__restrict__ start,
+                                                                PrepArrays A, const float *__restrict__ phi, FxParams p,
+                                                                Div32 dN, const uint32_t *__restrict__ fxb, DenseTab D) {
+  k_dense_sums_body<KIND>(P, start, A, phi, p, dN, fxb, D);
 }
 
 // node i = (x, y, z): its 8 neighbouring cells' contributions, summed in int64 and
@@ -752,7 +772,7 @@ __device__ __forceinline__ void gather_node(unsigned i, int x, int y, int z, con
 // registers and 424 B of spills, 9.16 at four with 64 and 10.73 at three with 80).
 constexpr uint32_t PATCH_MC = 8;
 template <int KIND, int PX, int PY, int PZ>
-__global__ void __launch_bounds__(256, 5) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
+__device__ __forceinline__ void k_dep_gather_body(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
                                                     const float *__restrict__ phi, float *t00, float *tij, FxParams p,
                                                     Div32 dN, const uint32_t *__restrict__ fxb, DenseTab D) {
   const int ks00 = (int)fxb[2], ksij = KIND == FX_T00TIJ ? (int)fxb[3] : (int)fxb[2];
@@ -778,6 +798,12 @@ __global__ void __launch_bounds__(256, 5) k_dep_gather(PclsArrays P, const uint3
       gather_node<KIND>(i, x, y, z, P, start, A, phi, t00, tij, p, ks00, ksij, sg00, sgij, D);
     }
   }
+}
+template <int KIND, int PX, int PY, int PZ>
+__global__ void __launch_bounds__(256, 5) k_dep_gather(PclsArrays P, const uint32_t *__restrict__ start, PrepArrays A,
+                                                    const float *__restrict__ phi, float *t00, float *tij, FxParams p,
+                                                    Div32 dN, const uint32_t *__restrict__ fxb, DenseTab D) {
+  k_dep_gather_body<KIND, PX, PY, PZ>(P, start, A, phi, t00, tij, p, dN, fxb, D);
 }
 
 // add the face accumulators into the field (or, with p.overwrite, store them) and
@@ -909,15 +935,16 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
     dt.cap_big = dcap_big;
     dt.thr = DENSE_T;
     dt.big = DENSE_BIG;
-    GEV_CHECK_CUDA(ctx, cudaMemsetAsync(dt.count, 0, 8, ctx->stream));
+    GEV_CHECK_CUDA(ctx, gev_zero_async(ctx, dt.count, 8));
   }
   GevTimed tm_b(ctx, "k_fx_bounds+k_fx_scale");
-  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->bounds, 0, 16 * sizeof(uint32_t), ctx->stream));
-  k_fx_bounds<<<grid_for(ctx, (size_t)(p->n > C ? p->n : C), 256, 8), 256, 0, ctx->stream>>>(
-      (const float *)p->cur.vx, (const float *)p->cur.vy, (const float *)p->cur.vz, p->n, p->count,
-      kind == FX_MASS ? nullptr : fphi, C, p->bounds, dt);
+  GEV_CHECK_CUDA(ctx, gev_zero_async(ctx, p->bounds, 16 * sizeof(uint32_t)));
+  gev_launch<k_fx_bounds_body, 256, 1>(ctx, k_fx_bounds, dim3(grid_for(ctx, (size_t)(p->n > C ? p->n : C), 256, 8)),
+                                       dim3(256), 0, (const float *)p->cur.vx, (const float *)p->cur.vy,
+                                       (const float *)p->cur.vz, p->n, (const uint32_t *)p->count,
+                                       kind == FX_MASS ? nullptr : fphi, C, p->bounds, dt);
   GEV_LAUNCH_CHECK(ctx);
-  k_fx_scale<<<1, 1, 0, ctx->stream>>>(p->bounds, kind, mass, a);
+  gev_launch<k_fx_scale_body, 32, 1>(ctx, k_fx_scale, dim3(1), dim3(1), 0, p->bounds, kind, mass, a);
   GEV_LAUNCH_CHECK(ctx);
   tm_b.stop();
   if (gather) {
@@ -937,34 +964,43 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
 #define GEV_DENSE(K)                                                                                         \
   do {                                                                                                       \
     GevTimed tm_d(ctx, "k_dense_sums");                                                                      \
-    k_dense_sums<K><<<ctx->sms * 8, 32 * DENSE_WARPS, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, fp, dN,  \
-                                                                        p->bounds, dt);                     \
+    gev_launch<k_dense_sums_body<K>, 32 * DENSE_WARPS, 1>(ctx, k_dense_sums<K>, dim3(ctx->sms * 8),          \
+                                                          dim3(32 * DENSE_WARPS), 0, p->cur,                 \
+                                                          (const uint32_t *)p->start, pa, fphi, fp, dN,      \
+                                                          (const uint32_t *)p->bounds, dt);                  \
     GEV_LAUNCH_CHECK(ctx);                                                                                   \
   } while (0)
 #define GEV_GATHER(K)                                                                                               \
   do {                                                                                                              \
     if (patch)                                                                                                      \
-      k_dep_gather<K, 8, 2, 2><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, dt); \
+      gev_launch<k_dep_gather_body<K, 8, 2, 2>, 256, 5>(ctx, k_dep_gather<K, 8, 2, 2>, dim3(gb), dim3(256), 0,      \
+                                                        p->cur, (const uint32_t *)p->start, pa, fphi, t00, tij, fp, \
+                                                        dN, (const uint32_t *)p->bounds, dt);                       \
     else                                                                                                            \
-      k_dep_gather<K, 0, 0, 0><<<gb, 256, 0, ctx->stream>>>(p->cur, p->start, pa, fphi, t00, tij, fp, dN, p->bounds, dt); \
+      gev_launch<k_dep_gather_body<K, 0, 0, 0>, 256, 5>(ctx, k_dep_gather<K, 0, 0, 0>, dim3(gb), dim3(256), 0,      \
+                                                        p->cur, (const uint32_t *)p->start, pa, fphi, t00, tij, fp, \
+                                                        dN, (const uint32_t *)p->bounds, dt);                       \
   } while (0)
     GevTimed tm_p(ctx, "k_fx_prep");
     if (kind == FX_T00) {
-      k_fx_prep<FX_T00><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
+      gev_launch<k_fx_prep_body<FX_T00>, 256, 1>(ctx, k_fx_prep<FX_T00>, dim3(pb), dim3(256), 0, p->cur, p->n, pa, fp,
+                                              (int)(fphi != nullptr), (const uint32_t *)p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
       GEV_DENSE(FX_T00);
       GevTimed tm_g(ctx, "k_dep_gather");
       GEV_GATHER(FX_T00);
     } else if (kind == FX_TIJ) {
-      k_fx_prep<FX_TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
+      gev_launch<k_fx_prep_body<FX_TIJ>, 256, 1>(ctx, k_fx_prep<FX_TIJ>, dim3(pb), dim3(256), 0, p->cur, p->n, pa, fp,
+                                              (int)(fphi != nullptr), (const uint32_t *)p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
       GEV_DENSE(FX_TIJ);
       GevTimed tm_g(ctx, "k_dep_gather");
       GEV_GATHER(FX_TIJ);
     } else {
-      k_fx_prep<FX_T00TIJ><<<pb, 256, 0, ctx->stream>>>(p->cur, p->n, pa, fp, fphi != nullptr, p->bounds);
+      gev_launch<k_fx_prep_body<FX_T00TIJ>, 256, 1>(ctx, k_fx_prep<FX_T00TIJ>, dim3(pb), dim3(256), 0, p->cur, p->n, pa, fp,
+                                              (int)(fphi != nullptr), (const uint32_t *)p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
       GEV_DENSE(FX_T00TIJ);

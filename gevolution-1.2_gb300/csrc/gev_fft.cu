@@ -27,7 +27,7 @@
 #include <vector>
 
 #include "gev_fft_bfly.cuh"
-#include "gev_internal.cuh"
+#include "gev_batch.cuh"
 
 namespace {
 
@@ -109,7 +109,7 @@ __device__ __forceinline__ void stage_tables(typename CT<T>::C *sh, const typena
 
 // y / z pass: one block = one plane x B consecutive kx columns.  in may equal out.
 template <typename T, int SIGN>
-__global__ void __launch_bounds__(256) k_fft_cols(const typename CT<T>::C *in, typename CT<T>::C *out, FftPlan pl,
+__device__ __forceinline__ void k_fft_cols_body(const typename CT<T>::C *in, typename CT<T>::C *out, FftPlan pl,
                                                   const typename CT<T>::C *__restrict__ twg,
                                                   const unsigned short *__restrict__ permg, int NH, long line_stride,
                                                   long plane_stride, int lgB) {
@@ -137,10 +137,17 @@ __global__ void __launch_bounds__(256) k_fft_cols(const typename CT<T>::C *in, t
     if (c < nbv) dst[(long)k * line_stride + c] = buf[perm[k] * B + c];
   }
 }
+template <typename T, int SIGN>
+__global__ void __launch_bounds__(256) k_fft_cols(const typename CT<T>::C *in, typename CT<T>::C *out, FftPlan pl,
+                                                  const typename CT<T>::C *__restrict__ twg,
+                                                  const unsigned short *__restrict__ permg, int NH, long line_stride,
+                                                  long plane_stride, int lgB) {
+  k_fft_cols_body<T, SIGN>(in, out, pl, twg, permg, NH, line_stride, plane_stride, lgB);
+}
 
 // x pass, forward: B rows of N reals -> N/2+1 complex each (row stride NH out)
 template <typename T>
-__global__ void __launch_bounds__(256) k_fft_r2c_rows(const T *__restrict__ in, typename CT<T>::C *__restrict__ out,
+__device__ __forceinline__ void k_fft_r2c_rows_body(const T *__restrict__ in, typename CT<T>::C *__restrict__ out,
                                                       FftPlan pl, const typename CT<T>::C *__restrict__ twHg,
                                                       const unsigned short *__restrict__ permg,
                                                       const typename CT<T>::C *__restrict__ twN, int NH, long nrows,
@@ -174,10 +181,18 @@ __global__ void __launch_bounds__(256) k_fft_r2c_rows(const T *__restrict__ in, 
     dst[(long)c * NH + k] = cadd(E, cmul(w, O));
   }
 }
+template <typename T>
+__global__ void __launch_bounds__(256) k_fft_r2c_rows(const T *__restrict__ in, typename CT<T>::C *__restrict__ out,
+                                                      FftPlan pl, const typename CT<T>::C *__restrict__ twHg,
+                                                      const unsigned short *__restrict__ permg,
+                                                      const typename CT<T>::C *__restrict__ twN, int NH, long nrows,
+                                                      int lgB, FastDiv divM, FastDiv divW) {
+  k_fft_r2c_rows_body<T>(in, out, pl, twHg, permg, twN, NH, nrows, lgB, divM, divW);
+}
 
 // x pass, backward: N/2+1 complex -> N reals per row
 template <typename T>
-__global__ void __launch_bounds__(256) k_fft_c2r_rows(const typename CT<T>::C *__restrict__ in, T *__restrict__ out,
+__device__ __forceinline__ void k_fft_c2r_rows_body(const typename CT<T>::C *__restrict__ in, T *__restrict__ out,
                                                       FftPlan pl, const typename CT<T>::C *__restrict__ twHg,
                                                       const unsigned short *__restrict__ permg,
                                                       const typename CT<T>::C *__restrict__ twN, int NH, long nrows,
@@ -221,6 +236,14 @@ __global__ void __launch_bounds__(256) k_fft_c2r_rows(const typename CT<T>::C *_
     dst[t] = buf[perm[i] * LD + c];
   }
 }
+template <typename T>
+__global__ void __launch_bounds__(256) k_fft_c2r_rows(const typename CT<T>::C *__restrict__ in, T *__restrict__ out,
+                                                      FftPlan pl, const typename CT<T>::C *__restrict__ twHg,
+                                                      const unsigned short *__restrict__ permg,
+                                                      const typename CT<T>::C *__restrict__ twN, int NH, long nrows,
+                                                      int lgB, FastDiv divM, FastDiv divW) {
+  k_fft_c2r_rows_body<T>(in, out, pl, twHg, permg, twN, NH, nrows, lgB, divM, divW);
+}
 
 inline int ilog2(int v) {
   int l = 0;
@@ -257,9 +280,9 @@ int run_cols(gev_ctx *ctx, const void *in, void *out, long line_stride, long pla
   const long blocks = (long)N * nchunks;
   const size_t smem = ((size_t)N + (size_t)N * B) * sizeof(C) + (size_t)N * 2;
   GevTimed tm_(ctx, "k_fft_cols");
-  k_fft_cols<T, SIGN><<<(unsigned)blocks, 256, smem, ctx->stream>>>(
-      (const C *)in, (C *)out, ctx->planN, (const C *)ctx->d_twN, (const unsigned short *)ctx->d_permN, NH,
-      line_stride, plane_stride, lgB);
+  gev_launch_if<sizeof(T) == 4, k_fft_cols_body<T, SIGN>, 256, 1>(
+      ctx, k_fft_cols<T, SIGN>, dim3((unsigned)blocks), dim3(256), smem, (const C *)in, (C *)out, ctx->planN,
+      (const C *)ctx->d_twN, (const unsigned short *)ctx->d_permN, NH, line_stride, plane_stride, lgB);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
@@ -279,9 +302,10 @@ int r2c_comp(gev_ctx *ctx, const void *real, void *spec) {
   const int lgB = batch_lg(M, sizeof(C), 1, 64, 32768), B = 1 << lgB;
   const size_t smem = ((size_t)M + (size_t)M * (B + 1)) * sizeof(C) + (size_t)M * 2;
   GevTimed tm_(ctx, "k_fft_r2c_rows");
-  k_fft_r2c_rows<T><<<(unsigned)((nrows + B - 1) / B), 256, smem, ctx->stream>>>(
-      (const T *)real, (C *)spec, ctx->planH, (const C *)ctx->d_twH, (const unsigned short *)ctx->d_permH,
-      (const C *)ctx->d_twN, NH, nrows, lgB, make_div(M), make_div(M + 1));
+  gev_launch_if<sizeof(T) == 4, k_fft_r2c_rows_body<T>, 256, 1>(
+      ctx, k_fft_r2c_rows<T>, dim3((unsigned)((nrows + B - 1) / B)), dim3(256), smem, (const T *)real, (C *)spec,
+      ctx->planH, (const C *)ctx->d_twH, (const unsigned short *)ctx->d_permH, (const C *)ctx->d_twN, NH, nrows,
+      lgB, make_div(M), make_div(M + 1));
   GEV_LAUNCH_CHECK(ctx);
   int rc = run_cols<T, -1>(ctx, spec, spec, NH, (long)N * NH);  // y: lines along ky, planes kz
   if (rc) return rc;
@@ -304,9 +328,10 @@ int c2r_comp(gev_ctx *ctx, const void *spec, void *real, void *scratch, const do
   const int lgB = batch_lg(M, sizeof(C), 1, 64, 32768), B = 1 << lgB;
   const size_t smem = ((size_t)M + (size_t)M * (B + 1) + (size_t)B * (M + 1)) * sizeof(C) + (size_t)M * 2;
   GevTimed tm_(ctx, "k_fft_c2r_rows");
-  k_fft_c2r_rows<T><<<(unsigned)((nrows + B - 1) / B), 256, smem, ctx->stream>>>(
-      (const C *)scratch, (T *)real, ctx->planH, (const C *)ctx->d_twH, (const unsigned short *)ctx->d_permH,
-      (const C *)ctx->d_twN, NH, nrows, lgB, make_div(M), make_div(M + 1));
+  gev_launch_if<sizeof(T) == 4, k_fft_c2r_rows_body<T>, 256, 1>(
+      ctx, k_fft_c2r_rows<T>, dim3((unsigned)((nrows + B - 1) / B)), dim3(256), smem, (const C *)scratch,
+      (T *)real, ctx->planH, (const C *)ctx->d_twH, (const unsigned short *)ctx->d_permH, (const C *)ctx->d_twN, NH,
+      nrows, lgB, make_div(M), make_div(M + 1));
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }

@@ -33,7 +33,7 @@
 #include <utility>
 
 #include "gev_fft_bfly.cuh"
-#include "gev_internal.cuh"
+#include "gev_batch.cuh"
 
 namespace {
 
@@ -166,9 +166,8 @@ __device__ __forceinline__ float poisson_factor(const PoisArgs &p, int kx, int k
 // y / z pass over B columns (consecutive kx) of one plane per tile; in may equal out.
 // POIS (FP32 z pass, lines along kz, planes ky): each element is multiplied by its
 // Poisson factor as it is loaded, the pass that follows the solve folded into it.
-template <typename T, int SIGN, int L, int LGB, bool POIS = false>
-__global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L / 8) << LGB))
-    k_fft_cols_reg(const typename CT<T>::C *in, typename CT<T>::C *out, const typename CT<T>::C *__restrict__ twg,
+template <typename T, int SIGN, int L, int LGB, bool POIS>
+__device__ __forceinline__ void k_fft_cols_reg_body(const typename CT<T>::C *in, typename CT<T>::C *out, const typename CT<T>::C *__restrict__ twg,
                    int NH, long ES, long PS, int ntiles, PoisArgs pois) {
   typedef RegFft<T, SIGN, L> R;
   typedef typename CT<T>::C C;
@@ -202,11 +201,17 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
     }
   }
 }
+template <typename T, int SIGN, int L, int LGB, bool POIS = false>
+__global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L / 8) << LGB))
+    k_fft_cols_reg(const typename CT<T>::C *in, typename CT<T>::C *out, const typename CT<T>::C *__restrict__ twg,
+                   int NH, long ES, long PS, int ntiles, PoisArgs pois) {
+  k_fft_cols_reg_body<T, SIGN, L, LGB, POIS>(in, out, twg, NH, ES, PS, ntiles, pois);
+}
 
 // x pass, forward: rows of N = 2L reals, each an L-point complex FFT followed by
 // the real-to-complex split into N/2+1 outputs (row stride NH)
 template <typename T, int L, int LGB>
-__global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L / 8) << LGB)) k_fft_r2c_rows_reg(const T *__restrict__ in, typename CT<T>::C *__restrict__ out,
+__device__ __forceinline__ void k_fft_r2c_rows_reg_body(const T *__restrict__ in, typename CT<T>::C *__restrict__ out,
                                                            const typename CT<T>::C *__restrict__ twHg,
                                                            const typename CT<T>::C *__restrict__ twN, int NH,
                                                            long nrows, int ntiles) {
@@ -247,10 +252,17 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
     }
   }
 }
+template <typename T, int L, int LGB>
+__global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L / 8) << LGB)) k_fft_r2c_rows_reg(const T *__restrict__ in, typename CT<T>::C *__restrict__ out,
+                                                           const typename CT<T>::C *__restrict__ twHg,
+                                                           const typename CT<T>::C *__restrict__ twN, int NH,
+                                                           long nrows, int ntiles) {
+  k_fft_r2c_rows_reg_body<T, L, LGB>(in, out, twHg, twN, NH, nrows, ntiles);
+}
 
 // x pass, backward: rows of N/2+1 complex -> N = 2L reals
 template <typename T, int L, int LGB>
-__global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L / 8) << LGB)) k_fft_c2r_rows_reg(const typename CT<T>::C *__restrict__ in, T *__restrict__ out,
+__device__ __forceinline__ void k_fft_c2r_rows_reg_body(const typename CT<T>::C *__restrict__ in, T *__restrict__ out,
                                                            const typename CT<T>::C *__restrict__ twHg,
                                                            const typename CT<T>::C *__restrict__ twN, int NH,
                                                            long nrows, int ntiles) {
@@ -299,8 +311,19 @@ __global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L /
     }
   }
 }
+template <typename T, int L, int LGB>
+__global__ void __launch_bounds__((L / 8) << LGB, col_min_blocks(sizeof(T), (L / 8) << LGB)) k_fft_c2r_rows_reg(const typename CT<T>::C *__restrict__ in, T *__restrict__ out,
+                                                           const typename CT<T>::C *__restrict__ twHg,
+                                                           const typename CT<T>::C *__restrict__ twN, int NH,
+                                                           long nrows, int ntiles) {
+  k_fft_c2r_rows_reg_body<T, L, LGB>(in, out, twHg, twN, NH, nrows, ntiles);
+}
 
 // ------------------------------------------------------------------ launch --
+// grids up to this size have batched forms of the passes (gev_batch.cuh): a batch
+// steps many small simulations; larger grids fill the GPU alone
+constexpr int BATCH_MAX_L = 256;
+
 // per_sm: the kernel's resident blocks per SM, queried on its first launch (a
 // process-wide value; several host threads may launch it first at once)
 template <typename K>
@@ -331,8 +354,9 @@ int cols_LB(gev_ctx *ctx, const void *in, void *out, long ES, long PS, PoisArgs 
   int rc = launch_cfg(ctx, k_fft_cols_reg<T, SIGN, L, LGB, POIS>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
   GevTimed tm_(ctx, "k_fft_cols_reg");
-  k_fft_cols_reg<T, SIGN, L, LGB, POIS><<<grid, threads, smem, ctx->stream>>>((const C *)in, (C *)out,
-                                                                        (const C *)ctx->d_twN, NH, ES, PS, (int)ntiles, pois);
+  gev_launch_if<sizeof(T) == 4 && L <= BATCH_MAX_L, k_fft_cols_reg_body<T, SIGN, L, LGB, POIS>, threads, col_min_blocks(sizeof(T), threads)>(
+      ctx, k_fft_cols_reg<T, SIGN, L, LGB, POIS>, dim3(grid), dim3(threads), smem, (const C *)in, (C *)out,
+      (const C *)ctx->d_twN, NH, ES, PS, (int)ntiles, pois);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
@@ -392,8 +416,9 @@ int r2c_LB(gev_ctx *ctx, const void *real, void *spec, long nrows) {
   int rc = launch_cfg(ctx, k_fft_r2c_rows_reg<T, L, LGB>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
   GevTimed tm_(ctx, "k_fft_r2c_rows_reg");
-  k_fft_r2c_rows_reg<T, L, LGB><<<grid, threads, smem, ctx->stream>>>(
-      (const T *)real, (C *)spec, (const C *)ctx->d_twH, (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
+  gev_launch_if<sizeof(T) == 4 && 2 * L <= BATCH_MAX_L, k_fft_r2c_rows_reg_body<T, L, LGB>, threads, col_min_blocks(sizeof(T), threads)>(
+      ctx, k_fft_r2c_rows_reg<T, L, LGB>, dim3(grid), dim3(threads), smem, (const T *)real, (C *)spec,
+      (const C *)ctx->d_twH, (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
@@ -411,8 +436,9 @@ int c2r_LB(gev_ctx *ctx, const void *spec, void *real, long nrows) {
   int rc = launch_cfg(ctx, k_fft_c2r_rows_reg<T, L, LGB>, threads, smem, ntiles, per_sm, grid);
   if (rc) return rc;
   GevTimed tm_(ctx, "k_fft_c2r_rows_reg");
-  k_fft_c2r_rows_reg<T, L, LGB><<<grid, threads, smem, ctx->stream>>>(
-      (const C *)spec, (T *)real, (const C *)ctx->d_twH, (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
+  gev_launch_if<sizeof(T) == 4 && 2 * L <= BATCH_MAX_L, k_fft_c2r_rows_reg_body<T, L, LGB>, threads, col_min_blocks(sizeof(T), threads)>(
+      ctx, k_fft_c2r_rows_reg<T, L, LGB>, dim3(grid), dim3(threads), smem, (const C *)spec, (T *)real,
+      (const C *)ctx->d_twH, (const C *)ctx->d_twN, NH, nrows, (int)ntiles);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
@@ -588,6 +614,10 @@ static void fft_tune_all(gev_ctx *ctx);
 
 void fft_autotune(gev_ctx *ctx) {
   if (ctx->fft_tuned) return;
+  if (ctx->rec) {  // a recorded cycle cannot time anything: batch only tuned contexts
+    ctx->rec->bad = true;
+    return;
+  }
   ctx->fft_tuned = true;
   const int N = ctx->N;
   if (ctx->prec == GEV_PREC_FP64 || !ctx->d_fft_scratch || !fft_reg_ok(N)) return;

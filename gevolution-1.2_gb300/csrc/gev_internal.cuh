@@ -30,6 +30,8 @@ struct FftPlan {
   int R[GEV_MAX_RADICES];
 };
 
+struct GevRecorder;  // gev_batch.cuh
+
 struct gev_ctx {
   int device = 0;
   int N = 0;
@@ -80,6 +82,9 @@ struct gev_ctx {
   // stream and buffers outlive all of them whatever order they are destroyed in
   int refs = 1;
   bool closed = false;
+  // set while a cycle is recorded for a batched step (gev_batch.cuh): launches on the
+  // batched path are recorded instead of enqueued
+  GevRecorder *rec = nullptr;
 };
 
 void ctx_retain(gev_ctx *ctx);

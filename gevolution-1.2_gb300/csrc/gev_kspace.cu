@@ -7,7 +7,7 @@
 // by a per-k denominator are done once as a reciprocal.  The k = 0 point gets
 // the reference's special value.  Streaming: HBM-bound in the FP32 form,
 // FP64-pipe-bound in the FP64 form.
-#include "gev_internal.cuh"
+#include "gev_batch.cuh"
 
 namespace {
 
@@ -43,8 +43,8 @@ __device__ __forceinline__ bool kidx(size_t id, const KDim &kd, KIdx<T> &k) {
 
 // solveModifiedPoissonFT, gevolution.hpp:501-535; coeff already divided by -N^3
 template <typename T>
-__global__ void k_poisson(const typename CT<T>::C *src, typename CT<T>::C *pot, const T *__restrict__ gk2, T coeff,
-                          T modif, KDim kd, size_t n) {
+__device__ __forceinline__ void k_poisson_body(const typename CT<T>::C *src, typename CT<T>::C *pot,
+                                               const T *__restrict__ gk2, T coeff, T modif, KDim kd, size_t n) {
   const int N = kd.N, NH = kd.NH;
   typedef typename CT<T>::C C;
   for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < n; id += (size_t)gridDim.x * blockDim.x) {
@@ -60,6 +60,11 @@ __global__ void k_poisson(const typename CT<T>::C *src, typename CT<T>::C *pot, 
     }
     pot[id] = out;
   }
+}
+template <typename T>
+__global__ void k_poisson(const typename CT<T>::C *src, typename CT<T>::C *pot, const T *__restrict__ gk2, T coeff,
+                          T modif, KDim kd, size_t n) {
+  k_poisson_body<T>(src, pot, gk2, coeff, modif, kd, n);
 }
 
 // projectFTscalar, gevolution.hpp:211-265: chi at one k != 0
@@ -146,9 +151,10 @@ __global__ void k_evolve_vector(const typename CT<T>::C *__restrict__ S, typenam
 // projectFTscalar (add = 0) and evolveFTvector in one pass: the six SijFT components
 // read once for both, the same arithmetic as the two kernels
 template <typename T>
-__global__ void k_project_evolve(const typename CT<T>::C *__restrict__ S, typename CT<T>::C *chi,
-                                 typename CT<T>::C *B, const T *__restrict__ gk2,
-                                 const typename CT<T>::C *__restrict__ ks, T a2dtau, KDim kd, size_t n) {
+__device__ __forceinline__ void k_project_evolve_body(const typename CT<T>::C *__restrict__ S, typename CT<T>::C *chi,
+                                                      typename CT<T>::C *B, const T *__restrict__ gk2,
+                                                      const typename CT<T>::C *__restrict__ ks, T a2dtau, KDim kd,
+                                                      size_t n) {
   const int N = kd.N;
   typedef typename CT<T>::C C;
   for (size_t id = blockIdx.x * (size_t)blockDim.x + threadIdx.x; id < n; id += (size_t)gridDim.x * blockDim.x) {
@@ -170,6 +176,12 @@ __global__ void k_project_evolve(const typename CT<T>::C *__restrict__ S, typena
     B[n + id] = cadd(B[n + id], d1);
     B[2 * n + id] = cadd(B[2 * n + id], d2);
   }
+}
+template <typename T>
+__global__ void k_project_evolve(const typename CT<T>::C *__restrict__ S, typename CT<T>::C *chi,
+                                 typename CT<T>::C *B, const T *__restrict__ gk2,
+                                 const typename CT<T>::C *__restrict__ ks, T a2dtau, KDim kd, size_t n) {
+  k_project_evolve_body<T>(S, chi, B, gk2, ks, a2dtau, kd, n);
 }
 
 // projectFTvector, gevolution.hpp:350-392 (S may equal B)
@@ -269,7 +281,8 @@ int launch_kspace(gev_ctx *ctx, int op, const void *in, void *out, double p1, do
   GevTimed tm_(ctx, op == 0 ? "k_poisson" : "k_kspace");
   switch (op) {
     case 0:
-      k_poisson<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, (T)p1, (T)p2, make_kdim(N), n);
+      gev_launch_if<sizeof(T) == 4, k_poisson_body<T>, 256, 1>(ctx, k_poisson<T>, dim3(blocks), dim3(threads), 0, (const C *)in, (C *)out,
+                                            gk2, (T)p1, (T)p2, make_kdim(N), n);
       break;
     case 1:
       k_project_scalar<T><<<blocks, threads, 0, ctx->stream>>>((const C *)in, (C *)out, gk2, ks, add, make_kdim(N), n);
@@ -335,9 +348,10 @@ int gev_project_scalar_evolve_vector(gev_ctx *ctx, const gev_field *SijFT, gev_f
         (const CT<double>::C *)SijFT->d, (CT<double>::C *)chiFT->d, (CT<double>::C *)BiFT->d,
         (const double *)ctx->d_gridk2, (const CT<double>::C *)ctx->d_kshift, a2dtau, make_kdim(N), n);
   else
-    k_project_evolve<float><<<blocks, 256, 0, ctx->stream>>>(
-        (const CT<float>::C *)SijFT->d, (CT<float>::C *)chiFT->d, (CT<float>::C *)BiFT->d,
-        (const float *)ctx->d_gridk2, (const CT<float>::C *)ctx->d_kshift, (float)a2dtau, make_kdim(N), n);
+    gev_launch<k_project_evolve_body<float>, 256, 1>(
+        ctx, k_project_evolve<float>, dim3(blocks), dim3(256), 0, (const CT<float>::C *)SijFT->d,
+        (CT<float>::C *)chiFT->d, (CT<float>::C *)BiFT->d, (const float *)ctx->d_gridk2,
+        (const CT<float>::C *)ctx->d_kshift, (float)a2dtau, make_kdim(N), n);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }

@@ -12,7 +12,7 @@
 #include <cmath>
 #include <cstring>
 
-#include "gev_internal.cuh"
+#include "gev_batch.cuh"
 
 namespace {
 
@@ -175,7 +175,7 @@ __device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t *s
   return before + x - v;
 }
 
-__global__ void __launch_bounds__(SCAN_T) k_scan_reduce(const uint32_t *__restrict__ in, long n, uint32_t *bsum) {
+__device__ __forceinline__ void k_scan_reduce_body(const uint32_t *__restrict__ in, long n, uint32_t *bsum) {
   __shared__ uint32_t sh[64];
   const long base = (long)blockIdx.x * SCAN_TILE;
   uint32_t s = 0;
@@ -187,9 +187,12 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_reduce(const uint32_t *__restri
   block_exclusive_scan(s, sh, total);
   if (threadIdx.x == 0) bsum[blockIdx.x] = total;
 }
+__global__ void __launch_bounds__(SCAN_T) k_scan_reduce(const uint32_t *__restrict__ in, long n, uint32_t *bsum) {
+  k_scan_reduce_body(in, n, bsum);
+}
 
 // one block: exclusive scan of nb block sums in place
-__global__ void __launch_bounds__(1024) k_scan_blocks(uint32_t *bsum, long nb) {
+__device__ __forceinline__ void k_scan_blocks_body(uint32_t *bsum, long nb) {
   __shared__ uint32_t sh[64];
   const long per = (nb + blockDim.x - 1) / blockDim.x;
   const long b0 = threadIdx.x * per;
@@ -203,8 +206,11 @@ __global__ void __launch_bounds__(1024) k_scan_blocks(uint32_t *bsum, long nb) {
     off += v;
   }
 }
+__global__ void __launch_bounds__(1024) k_scan_blocks(uint32_t *bsum, long nb) {
+  k_scan_blocks_body(bsum, nb);
+}
 
-__global__ void __launch_bounds__(SCAN_T) k_scan_down(const uint32_t *__restrict__ in, long n,
+__device__ __forceinline__ void k_scan_down_body(const uint32_t *__restrict__ in, long n,
                                                       const uint32_t *__restrict__ bsum, uint32_t *out,
                                                       uint32_t total_n) {
   // one word of padding per 32: the thread-major accesses (tid * SCAN_PER + k) then
@@ -237,6 +243,11 @@ __global__ void __launch_bounds__(SCAN_T) k_scan_down(const uint32_t *__restrict
     if (i < n) out[i] = tile[pad(k * SCAN_T + threadIdx.x)];
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) out[n] = total_n;
+}
+__global__ void __launch_bounds__(SCAN_T) k_scan_down(const uint32_t *__restrict__ in, long n,
+                                                      const uint32_t *__restrict__ bsum, uint32_t *out,
+                                                      uint32_t total_n) {
+  k_scan_down_body(in, n, bsum, out, total_n);
 }
 
 __global__ void k_scatter(const uint32_t *__restrict__ cell, const uint32_t *__restrict__ rank, long n,
@@ -312,7 +323,7 @@ __global__ void k_gather(PclsArrays src, PclsArrays dst, const uint32_t *__restr
 // slower than 4 on another).
 constexpr int MOVE_PER = 8;
 template <int PER>
-__global__ void __launch_bounds__(256, 1) k_move(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ start,
+__device__ __forceinline__ void k_move_body(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ start,
                                               const uint32_t *__restrict__ rank, long n, int N, int lg) {
   const float *svx = (const float *)src.vx, *svy = (const float *)src.vy, *svz = (const float *)src.vz;
   float *dvx = (float *)dst.vx, *dvy = (float *)dst.vy, *dvz = (float *)dst.vz;
@@ -364,6 +375,11 @@ __global__ void __launch_bounds__(256, 1) k_move(PclsArrays src, PclsArrays dst,
       dst.rz[j] = r2;
     }
   }
+}
+template <int PER>
+__global__ void __launch_bounds__(256, 1) k_move(PclsArrays src, PclsArrays dst, const uint32_t *__restrict__ start,
+                                              const uint32_t *__restrict__ rank, long n, int N, int lg) {
+  k_move_body<PER>(src, dst, start, rank, n, N, lg);
 }
 
 // ------------------------------------------------------- particle updates --
@@ -824,7 +840,7 @@ __global__ void __launch_bounds__(256) k_update_pos(PclsArrays P, long n, const 
 // in one pass: both read the same cell and the same phi / chi / B values.  The
 // drift's scale factor (after the background half step) comes in pd.
 template <typename T, typename V>
-__global__ void __launch_bounds__(256, 2) k_kick_drift(PclsArrays P, long n, const T *__restrict__ phi,
+__device__ __forceinline__ void k_kick_drift_body(PclsArrays P, long n, const T *__restrict__ phi,
                                                     const T *__restrict__ chi, const T *__restrict__ Bi, Params pk,
                                                     Params pd, unsigned long long *maxbits, uint32_t *count,
                                                     uint32_t *rank) {
@@ -850,6 +866,13 @@ __global__ void __launch_bounds__(256, 2) k_kick_drift(PclsArrays P, long n, con
     if (count) rank[i] = atomicAdd(&count[key], 1u);  // the histogram of the relink, fused
   }
   block_max_to<T>(vmax, maxbits);
+}
+template <typename T, typename V>
+__global__ void __launch_bounds__(256, 2) k_kick_drift(PclsArrays P, long n, const T *__restrict__ phi,
+                                                    const T *__restrict__ chi, const T *__restrict__ Bi, Params pk,
+                                                    Params pd, unsigned long long *maxbits, uint32_t *count,
+                                                    uint32_t *rank) {
+  k_kick_drift_body<T, V>(P, n, phi, chi, Bi, pk, pd, maxbits, count, rank);
 }
 
 template <typename V>
@@ -897,11 +920,14 @@ int scan_cells(gev_ctx *ctx, gev_pcls *p) {
   const long C = (long)ctx->N * ctx->N * ctx->N;
   const long nb = (C + SCAN_TILE - 1) / SCAN_TILE;
   GevTimed tm_(ctx, "k_scan");
-  k_scan_reduce<<<(unsigned)nb, SCAN_T, 0, ctx->stream>>>(p->count, C, p->scan_tmp);
+  gev_launch<k_scan_reduce_body, SCAN_T, 1>(ctx, k_scan_reduce, dim3((unsigned)nb), dim3(SCAN_T), 0,
+                                            (const uint32_t *)p->count, C, p->scan_tmp);
   GEV_LAUNCH_CHECK(ctx);
-  k_scan_blocks<<<1, 1024, 0, ctx->stream>>>(p->scan_tmp, nb);
+  gev_launch<k_scan_blocks_body, 1024, 1>(ctx, k_scan_blocks, dim3(1), dim3(1024), 0, p->scan_tmp, nb);
   GEV_LAUNCH_CHECK(ctx);
-  k_scan_down<<<(unsigned)nb, SCAN_T, 0, ctx->stream>>>(p->count, C, p->scan_tmp, p->start, (uint32_t)p->n);
+  gev_launch<k_scan_down_body, SCAN_T, 1>(ctx, k_scan_down, dim3((unsigned)nb), dim3(SCAN_T), 0,
+                                          (const uint32_t *)p->count, C, (const uint32_t *)p->scan_tmp, p->start,
+                                          (uint32_t)p->n);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
@@ -958,7 +984,7 @@ int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, 
   const double a2N_k = a_k * a_k * N, a2N_d = a_d * a_d * N;
   const Params pk = make_params(dtau_k, a_k, a2N_k, nfield_k, N);
   const Params pd = make_params(dtau_d, a_d, a2N_d, nfield_d, N);
-  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(maxbits_dev, 0, sizeof(unsigned long long), ctx->stream));
+  GEV_CHECK_CUDA(ctx, gev_zero_async(ctx, maxbits_dev, sizeof(unsigned long long)));
   const int blocks = grid_for(ctx, (size_t)p->n, 256, 16);
   if (ctx->prec == GEV_PREC_FP64) {
     GevTimed tm_(ctx, "k_kick_drift");
@@ -972,19 +998,21 @@ int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, 
   }
   // mixed form: histogram in the update, then scan and one move (no ID order)
   const long C = (long)N * N * N;
-  GEV_CHECK_CUDA(ctx, cudaMemsetAsync(p->count, 0, C * sizeof(uint32_t), ctx->stream));
+  GEV_CHECK_CUDA(ctx, gev_zero_async(ctx, p->count, C * sizeof(uint32_t)));
   GevTimed tm_(ctx, "k_kick_drift");
-  k_kick_drift<float, float><<<blocks, 256, 0, ctx->stream>>>(p->cur, p->n, (const float *)phi->d,
-                                                              (const float *)chi->d, (const float *)Bi->d, pk, pd,
-                                                              maxbits_dev, p->count, p->rank);
+  gev_launch<k_kick_drift_body<float, float>, 256, 2>(ctx, k_kick_drift<float, float>, dim3(blocks), dim3(256), 0,
+                                                      p->cur, p->n, (const float *)phi->d, (const float *)chi->d,
+                                                      (const float *)Bi->d, pk, pd, maxbits_dev, p->count, p->rank);
   GEV_LAUNCH_CHECK(ctx);
   tm_.stop();
   if (p->n == 0) return GEV_OK;
   int rc = scan_cells(ctx, p);
   if (rc) return rc;
   GevTimed tv_(ctx, "k_move");
-  k_move<MOVE_PER><<<grid_for(ctx, (size_t)(p->n + MOVE_PER - 1) / MOVE_PER, 256, 16), 256, 0, ctx->stream>>>(
-      p->cur, p->alt, p->start, p->rank, p->n, N, lg_pow2(N));
+  gev_launch<k_move_body<MOVE_PER>, 256, 1>(ctx, k_move<MOVE_PER>,
+                                            dim3(grid_for(ctx, (size_t)(p->n + MOVE_PER - 1) / MOVE_PER, 256, 16)),
+                                            dim3(256), 0, p->cur, p->alt, (const uint32_t *)p->start,
+                                            (const uint32_t *)p->rank, p->n, N, lg_pow2(N));
   GEV_LAUNCH_CHECK(ctx);
   std::swap(p->cur, p->alt);
   p->id_order = false;

@@ -10,7 +10,7 @@
 #include <cmath>
 #include <cstring>
 
-#include "gev_internal.cuh"
+#include "gev_batch.cuh"
 
 namespace {
 
@@ -33,7 +33,7 @@ void rk4bg(double &a, double fourpiG, const gev_cosmology &c, double dtau) {
 // FP64 add per 8 values (converting and adding every value in FP64 would issue two
 // FP64-pipe instructions per cell on GB300).
 template <typename T>
-__global__ void k_sum_to(const T *__restrict__ f, size_t n, double *partial) {
+__device__ __forceinline__ void k_sum_to_body(const T *__restrict__ f, size_t n, double *partial) {
   __shared__ double sh[256];
   double s = 0.;
   if constexpr (sizeof(T) == 4) {
@@ -57,7 +57,11 @@ __global__ void k_sum_to(const T *__restrict__ f, size_t n, double *partial) {
   }
   if (threadIdx.x == 0) partial[blockIdx.x] = sh[0];
 }
-__global__ void k_sum_fin(const double *partial, int nb, double *out) {
+template <typename T>
+__global__ void k_sum_to(const T *__restrict__ f, size_t n, double *partial) {
+  k_sum_to_body<T>(f, n, partial);
+}
+__device__ __forceinline__ void k_sum_fin_body(const double *partial, int nb, double *out) {
   __shared__ double sh[256];
   double s = 0.;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) s += partial[i];
@@ -69,6 +73,7 @@ __global__ void k_sum_fin(const double *partial, int nb, double *out) {
   }
   if (threadIdx.x == 0) out[0] = sh[0];
 }
+__global__ void k_sum_fin(const double *partial, int nb, double *out) { k_sum_fin_body(partial, nb, out); }
 
 #define RC(x)                 \
   do {                        \
@@ -84,14 +89,17 @@ int sum_async(gev_sim *s, const gev_field *f, double *dst_dev) {
   if (ctx->prec == GEV_PREC_FP64)
     k_sum_to<double><<<nb, 256, 0, ctx->stream>>>((const double *)f->d, f->comp_elems, ctx->d_red);
   else
-    k_sum_to<float><<<nb, 256, 0, ctx->stream>>>((const float *)f->d, f->comp_elems, ctx->d_red);
+    gev_launch<k_sum_to_body<float>, 256, 1>(ctx, k_sum_to<float>, dim3(nb), dim3(256), 0, (const float *)f->d,
+                                             f->comp_elems, ctx->d_red);
   GEV_LAUNCH_CHECK(ctx);
-  k_sum_fin<<<1, 256, 0, ctx->stream>>>(ctx->d_red, nb, dst_dev);
+  gev_launch<k_sum_fin_body, 256, 1>(ctx, k_sum_fin, dim3(1), dim3(256), 0, (const double *)ctx->d_red, nb, dst_dev);
   GEV_LAUNCH_CHECK(ctx);
   return GEV_OK;
 }
 
 }  // namespace
+
+__global__ void __launch_bounds__(256) k_zero4(uint32_t *p, size_t n4) { k_zero4_body(p, n4); }
 
 int pcls_kick_drift_async(gev_ctx *ctx, gev_pcls *p, double dtau_k, double a_k, int nfield_k, double dtau_d,
                           double a_d, int nfield_d, const gev_field *phi, const gev_field *chi, const gev_field *Bi,
@@ -273,8 +281,7 @@ int gev_sim_step_particles(gev_sim *s) {
                              s->chi, s->Bi, (unsigned long long *)(s->dev_words + 1)));
   }
   rk4bg(a, fourpiG, cm, 0.5 * dtau);
-  GEV_CHECK_CUDA(ctx, cudaMemcpyAsync(s->host_words, s->dev_words, 4 * sizeof(double), cudaMemcpyDeviceToHost,
-                                      ctx->stream));
+  GEV_CHECK_CUDA(ctx, gev_d2h_async(ctx, s->host_words, s->dev_words, 4 * sizeof(double)));
 
   st.a = a;
   st.tau += dtau;

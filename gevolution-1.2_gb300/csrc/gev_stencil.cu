@@ -7,7 +7,7 @@
 #include <mutex>
 #include <utility>
 
-#include "gev_internal.cuh"
+#include "gev_batch.cuh"
 
 namespace {
 
@@ -67,8 +67,8 @@ __device__ __forceinline__ unsigned next4(unsigned i, int x, int N) {
   return x + 4 == N ? i + 4u - (unsigned)N : i + 4u;
 }
 
-__global__ void k_source_tensor4(const float *__restrict__ phi, const float *Tij, float *Sij, float coeff, int N,
-                                 int lg, Div32 dN) {
+__device__ __forceinline__ void k_source_tensor4_body(const float *__restrict__ phi, const float *Tij, float *Sij,
+                                                      float coeff, int N, int lg, Div32 dN) {
   const unsigned V = (unsigned)N * N * N, V4 = V / 4;
   const float h = 0.5f;
   for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < V4; q += gridDim.x * blockDim.x) {
@@ -125,9 +125,14 @@ __global__ void k_source_tensor4(const float *__restrict__ phi, const float *Tij
   }
 }
 
-__global__ void k_source_scalar4(const float *__restrict__ phi, const float *__restrict__ chi, const float *source,
-                                 float bgmodel, float *result, float coeff, float coeff2, float coeff3, int N,
+__global__ void k_source_tensor4(const float *__restrict__ phi, const float *Tij, float *Sij, float coeff, int N,
                                  int lg, Div32 dN) {
+  k_source_tensor4_body(phi, Tij, Sij, coeff, N, lg, dN);
+}
+
+__device__ __forceinline__ void k_source_scalar4_body(const float *__restrict__ phi, const float *__restrict__ chi,
+                                                      const float *source, float bgmodel, float *result, float coeff,
+                                                      float coeff2, float coeff3, int N, int lg, Div32 dN) {
   const unsigned V4 = (unsigned)N * N * N / 4;
   for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < V4; q += gridDim.x * blockDim.x) {
     const unsigned i = q * 4u;
@@ -158,6 +163,11 @@ __global__ void k_source_scalar4(const float *__restrict__ phi, const float *__r
     }
     st4(result + i, make_float4(R[0], R[1], R[2], R[3]));
   }
+}
+__global__ void k_source_scalar4(const float *__restrict__ phi, const float *__restrict__ chi, const float *source,
+                                 float bgmodel, float *result, float coeff, float coeff2, float coeff3, int N,
+                                 int lg, Div32 dN) {
+  k_source_scalar4_body(phi, chi, source, bgmodel, result, coeff, coeff2, coeff3, N, lg, dN);
 }
 
 // prepareFTsource (scalar), gevolution.hpp:169-192; result may equal source
@@ -235,15 +245,17 @@ __global__ void k_st_fill(float *s, size_t n) {
 void launch_scalar4(gev_ctx *ctx, int threads, int per_sm, const float *phi, const float *chi, const float *source,
                     float bgmodel, float *result, float coeff, float coeff2, float coeff3) {
   const size_t V = (size_t)ctx->N * ctx->N * ctx->N;
-  k_source_scalar4<<<grid_for(ctx, V / 4, threads, per_sm), threads, 0, ctx->stream>>>(
-      phi, chi, source, bgmodel, result, coeff, coeff2, coeff3, ctx->N, lg_pow2(ctx->N), make_div32(ctx->N));
+  gev_launch<k_source_scalar4_body, 512, 1>(ctx, k_source_scalar4, dim3(grid_for(ctx, V / 4, threads, per_sm)),
+                                            dim3(threads), 0, phi, chi, source, bgmodel, result, coeff, coeff2,
+                                            coeff3, ctx->N, lg_pow2(ctx->N), make_div32(ctx->N));
 }
 
 void launch_tensor4(gev_ctx *ctx, int threads, int per_sm, const float *phi, const float *Tij, float *Sij,
                     float coeff) {
   const size_t V = (size_t)ctx->N * ctx->N * ctx->N;
-  k_source_tensor4<<<grid_for(ctx, V / 4, threads, per_sm), threads, 0, ctx->stream>>>(
-      phi, Tij, Sij, coeff, ctx->N, lg_pow2(ctx->N), make_div32(ctx->N));
+  gev_launch<k_source_tensor4_body, 512, 1>(ctx, k_source_tensor4, dim3(grid_for(ctx, V / 4, threads, per_sm)),
+                                            dim3(threads), 0, phi, Tij, Sij, coeff, ctx->N, lg_pow2(ctx->N),
+                                            make_div32(ctx->N));
 }
 
 // mean ms of 5 launches after one untimed launch; +inf when a launch fails
@@ -277,6 +289,10 @@ void stencil_tune(gev_ctx *ctx);
 
 void stencil_autotune(gev_ctx *ctx) {
   if (ctx->st_tuned) return;
+  if (ctx->rec) {  // a recorded cycle cannot time anything: batch only tuned contexts
+    ctx->rec->bad = true;
+    return;
+  }
   ctx->st_tuned = true;
   const int N = ctx->N;
   if (ctx->prec == GEV_PREC_FP64 || N % 4 != 0 || N > ST_TUNE_MAX_N) return;

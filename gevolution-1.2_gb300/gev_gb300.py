@@ -533,6 +533,74 @@ class Sim:
         return tuple(x.value for x in v)
 
 
+_BATCH_SIGS = {
+    "gev_batch_create": [_i, ctypes.POINTER(_vp)],
+    "gev_batch_destroy": [_vp],
+    "gev_batch_step": [_vp, ctypes.POINTER(_vp), _i],
+    "gev_batch_info": [_vp, ctypes.POINTER(_l), ctypes.POINTER(_l), ctypes.POINTER(_l)],
+    "gev_batch_run": [_vp, ctypes.POINTER(_vp), _i, ctypes.POINTER(_d), ctypes.POINTER(_i)],
+}
+
+
+def _batch_lib():
+    L = lib()
+    if not getattr(L, "_batch_ready", False):
+        for name, args in _BATCH_SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        L._batch_ready = True
+    return L
+
+
+class Batch:
+    """One cycle of many simulations with one launch per kernel for each cohort of
+    simulations of one grid size (gev_batch_step, include/gev_sim.h)."""
+
+    def __init__(self, device=0):
+        self.handle = None
+        h = _vp()
+        rc = _batch_lib().gev_batch_create(device, ctypes.byref(h))
+        if rc != OK:
+            raise GevError("gev_batch_create failed (%d)" % rc)
+        self.handle = h.value
+
+    def __del__(self):
+        try:
+            if self.handle:
+                _batch_lib().gev_batch_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
+
+    def close(self):
+        self.__del__()
+
+    def step(self, sims):
+        arr = (_vp * max(1, len(sims)))(*[s.handle for s in sims])
+        rc = _batch_lib().gev_batch_step(self.handle, arr, len(sims))
+        if rc != OK:
+            _check(rc, sims[0].ctx if sims else None, "gev_batch_step")
+
+    def run(self, sims, a_targets):
+        """main.cpp's loop for each simulation in batched steps, each until the cycle that
+        passes its target scale factor; returns the cycles each ran (waits at the end)."""
+        n = len(sims)
+        arr = (_vp * max(1, n))(*[s.handle for s in sims])
+        at = (_d * max(1, n))(*a_targets)
+        cyc = (_i * max(1, n))()
+        rc = _batch_lib().gev_batch_run(self.handle, arr, n, at, cyc)
+        if rc != OK:
+            _check(rc, sims[0].ctx if sims else None, "gev_batch_run")
+        return [cyc[k] for k in range(n)]
+
+    def info(self):
+        """(cycles run batched, cycles run directly, batched kernel launches)."""
+        v = [_l(), _l(), _l()]
+        _check(_batch_lib().gev_batch_info(self.handle, *[ctypes.byref(x) for x in v]), None, "gev_batch_info")
+        return tuple(x.value for x in v)
+
+
 class _Borrowed(Field):
     def __init__(self, f):
         self.ctx, self.kind, self.ncomp = f.ctx, f.kind, f.ncomp

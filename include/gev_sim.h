@@ -71,6 +71,32 @@ int gev_sim_step_graph(gev_sim *s);
  * by gev_sim_step_graph since the simulation was created (any pointer may be NULL) */
 int gev_sim_graph_info(gev_sim *s, long *launches, long *builds, long *direct);
 
+/* Batched cycles: one cycle of each of many simulations, with one launch per kernel
+ * of the cycle for each cohort of simulations of one grid size.  Each simulation's
+ * cycle is recorded (the host runs gev_sim_step's code, the launches are kept rather
+ * than enqueued); simulations with the same launch sequence form a cohort, and each
+ * kernel runs once for the whole cohort on the batch's stream, every block on its own
+ * simulation's arguments -- the same bits as gev_sim_step.  The batch's stream waits
+ * for the work already queued on each simulation's stream, and each simulation's
+ * stream then waits for the batch, so the calls of gev_sim.h and gev_gb300.h on a
+ * simulation keep their order.  Batched: mixed-form simulations from their third
+ * cycle on (the first two tune and allocate on first use), with the per-kernel timers
+ * off, on grids up to 256^3; every other simulation takes a direct cycle
+ * (gev_sim_step) on its own stream, as does one whose cycle uses an operation that
+ * has no batched form.  Nothing is waited for but the batch's staging buffers (a ring
+ * of three). */
+typedef struct gev_batch gev_batch;
+int gev_batch_create(int device, gev_batch **out);
+int gev_batch_destroy(gev_batch *b);
+/* one cycle of each of sims[0 .. n-1] (distinct simulations on the batch's device) */
+int gev_batch_step(gev_batch *b, gev_sim *const *sims, int n);
+/* cycles run batched, cycles run directly, batched kernel launches (NULL to skip) */
+int gev_batch_info(gev_batch *b, long *batched, long *direct, long *launches);
+/* main.cpp's loop for each simulation, in batched steps: each of sims[0 .. n-1] runs
+ * cycles until the first whose scale factor passes a_target[i]; cycles[i] = the cycles
+ * it ran.  Returns once the device has finished them. */
+int gev_batch_run(gev_batch *b, gev_sim *const *sims, int n, const double *a_target, int *cycles);
+
 /* Zel'dovich initial conditions at z_in generated on the device, following the
  * power-spectrum branch of generateIC_basic (ic_basic.hpp:1626-2259): sc1
  * template tiled N/4 times, a tabulated BBKS spectrum normalised to sigma8 and
