@@ -670,7 +670,7 @@ def run_serve(args, gpu):
     }
 
 
-def run_ensemble(gpu, seed):
+def run_ensemble(gpu, seed, lanes=(1, 4)):
     """The batched ensemble: 16 simulations each at 64^3, 96^3 and 128^3, box 2.5 N,
     Omega_cdm U[0.25, 0.35], sigma8 U[0.75, 0.87], n_s U[0.94, 0.98], distinct seeds,
     all to z = 0, admitted at once.  Run four ways on the same requests: through the
@@ -706,11 +706,13 @@ def run_ensemble(gpu, seed):
         gpu.prepare_source_tensor(phi.zero(), Tij.zero(), Tij, 1e-3)
         shapes[str(N)] = ctx.stencil_shapes()
         del phi, Tij, ctx
-    def ensemble_batched():
+    def ensemble_batched(lanes=1):
         # the same requests advanced by gev_batch_run: one launch per kernel of a cycle for
         # each grid size's cohort; contexts and initial conditions made by four host
         # threads; timed from the first context to the last result's spectrum, as the
-        # server runs are
+        # server runs are.  lanes > 1: the requests dealt round-robin to that many batches,
+        # each run by its own host thread, so that the lanes' cohorts drift out of step and
+        # different phases of the cycle share the GPU
         from concurrent.futures import ThreadPoolExecutor
 
         def make(r):
@@ -723,8 +725,19 @@ def run_ensemble(gpu, seed):
         t0 = time.perf_counter()
         with ThreadPoolExecutor(4) as ex:
             runs = list(ex.map(make, ens))
-        b = gpu.Batch()
-        cycles = b.run([sim for _, sim in runs], [1.0 / (1.0 + r.z_target) for r in ens])
+        batches = [gpu.Batch() for _ in range(lanes)]
+        lane_of = [k % lanes for k in range(len(ens))]
+
+        def run_lane(li):
+            ks = [k for k in range(len(ens)) if lane_of[k] == li]
+            cyc = batches[li].run([runs[k][1] for k in ks], [1.0 / (1.0 + ens[k].z_target) for k in ks])
+            return dict(zip(ks, cyc))
+
+        cycles = [0] * len(ens)
+        with ThreadPoolExecutor(lanes) as ex:
+            for part in ex.map(run_lane, range(lanes)):
+                for k, c in part.items():
+                    cycles[k] = c
         powers = []
         for (c, sim), r in zip(runs, ens):
             F = c.spectrum(1)
@@ -733,18 +746,25 @@ def run_ensemble(gpu, seed):
             n3 = float(r.N) ** 3
             powers.append(pw / (n3 * n3 * 2. * np.pi * np.pi))
         span = time.perf_counter() - t0
-        nb, nd, nl = b.info()
+        info = [b.info() for b in batches]
         steps = sum(float(r.N) ** 3 * k for r, k in zip(ens, cycles))
-        b.close()
+        for b in batches:
+            b.close()
         del runs
-        return cycles, powers, {"simulations": len(ens), "makespan_s": span, "particle_steps_per_s": steps / span,
-                                "cycles_batched": nb, "cycles_direct": nd, "batched_launches": nl,
-                                "launches_per_cohort_cycle_note": "3 cohorts (64^3, 96^3, 128^3) of 16"}
+        return cycles, powers, {"simulations": len(ens), "lanes": lanes, "makespan_s": span,
+                                "particle_steps_per_s": steps / span, "cycles_batched": sum(i[0] for i in info),
+                                "cycles_direct": sum(i[1] for i in info), "batched_launches": sum(i[2] for i in info),
+                                "cohorts": "per lane: 64^3, 96^3 and 128^3, %d simulations each" % (16 // lanes)}
 
     res_d, _, direct = ensemble(0, False)
     res_g, st_g, graph = ensemble(0, True)
     _, _, one = ensemble(1, False)
     cyc_b, pow_b, batched = ensemble_batched()
+    more_lanes = []
+    for nl_ in lanes[1:]:
+        cyc_l, pow_l, bl = ensemble_batched(nl_)
+        bl["same_bits_as_one_lane"] = cyc_l == cyc_b and all(np.array_equal(a, b) for a, b in zip(pow_l, pow_b))
+        more_lanes.append(bl)
     # against the server's (direct) cycles: the same cycle counts, P(k) of phi to FP32
     # rounding (the batched kernels are compiled apart and may fuse multiply-adds
     # differently)
@@ -762,6 +782,7 @@ def run_ensemble(gpu, seed):
     out.update(direct)
     out["graph_cycles"] = graph
     out["batched_per_phase"] = batched
+    out["batched_per_phase_lanes"] = more_lanes
     out["one_scheduler_thread"] = one
     return out
 
@@ -927,7 +948,7 @@ def run_op(args):
     import numpy as np
     import gev_gb300 as gpu
     if args.op == "ensemble":
-        print(json.dumps(run_ensemble(gpu, args.seed)))
+        print(json.dumps(run_ensemble(gpu, args.seed, lanes=(1, 2, 4, 8))))
         return
     import torch
     N = args.grid
