@@ -88,7 +88,11 @@ int gev_sim_graph_info(gev_sim *s, long *launches, long *builds, long *direct);
 typedef struct gev_batch gev_batch;
 int gev_batch_create(int device, gev_batch **out);
 int gev_batch_destroy(gev_batch *b);
-/* one cycle of each of sims[0 .. n-1] (distinct simulations on the batch's device) */
+/* one cycle of each of sims[0 .. n-1] (distinct simulations on the batch's device).
+ * A batch and its simulations are driven from one host thread at a time; separate
+ * batches over separate simulations may run in separate threads.  GEV_EINVAL (null,
+ * repeated or foreign simulations) leaves every simulation as it was; after any other
+ * error the simulations of the call are in an undefined state. */
 int gev_batch_step(gev_batch *b, gev_sim *const *sims, int n);
 /* cycles run batched, cycles run directly, batched kernel launches (NULL to skip) */
 int gev_batch_info(gev_batch *b, long *batched, long *direct, long *launches);
