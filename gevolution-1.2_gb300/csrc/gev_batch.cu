@@ -190,6 +190,8 @@ int gev_batch_step(gev_batch *b, gev_sim *const *sims, int n) {
   // cohorts: equal launch sequences
   std::map<std::vector<unsigned long long>, std::vector<int>> cohorts;  // -> positions in idx
   for (size_t k = 0; k < idx.size(); ++k) cohorts[signature(b->rec[k])].push_back((int)k);
+  for (auto &c : cohorts)
+    if (c.second.size() > 65535) return GEV_EINVAL;  // gridDim.y holds a cohort
   // the batch's stream starts after each simulation's queued work
   while (b->ev.size() < idx.size()) {
     cudaEvent_t e = nullptr;

@@ -5,7 +5,7 @@
 // its code in a __device__ body function of the same parameters; gev_launch either
 // launches the kernel on the context's stream or, while the context records a cycle
 // (ctx->rec set), records the body's launch: its grid, block and shared memory and
-// its arguments packed into a trivially copyable struct.  The executor (gev_sim.cu)
+// its arguments packed into a trivially copyable struct.  The executor (gev_batch.cu)
 // lays the packed arguments of a cohort's simulations side by side in a device table
 // and launches the body's batched form once, gridDim.y = the cohort's size, each block
 // reading its simulation's arguments from the table row blockIdx.y.  A body never
