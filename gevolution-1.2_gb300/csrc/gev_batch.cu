@@ -161,7 +161,8 @@ int gev_batch_info(gev_batch *b, long *batched, long *direct, long *launches) {
 }
 
 int gev_batch_step(gev_batch *b, gev_sim *const *sims, int n) {
-  if (!b || n < 0 || (n > 0 && !sims)) return GEV_EINVAL;
+  // (a cohort's size is gridDim.y of its launches: at most 65535)
+  if (!b || n < 0 || n > 65535 || (n > 0 && !sims)) return GEV_EINVAL;
   {
     std::set<const gev_sim *> seen;
     for (int i = 0; i < n; ++i)
@@ -190,8 +191,6 @@ int gev_batch_step(gev_batch *b, gev_sim *const *sims, int n) {
   // cohorts: equal launch sequences
   std::map<std::vector<unsigned long long>, std::vector<int>> cohorts;  // -> positions in idx
   for (size_t k = 0; k < idx.size(); ++k) cohorts[signature(b->rec[k])].push_back((int)k);
-  for (auto &c : cohorts)
-    if (c.second.size() > 65535) return GEV_EINVAL;  // gridDim.y holds a cohort
   // the batch's stream starts after each simulation's queued work
   while (b->ev.size() < idx.size()) {
     cudaEvent_t e = nullptr;
