@@ -168,3 +168,21 @@ def test_batch_run_to_targets_matches_direct_loops(gpu):
             k += 1
         assert ncyc == k
         assert_close(s, ref, N)
+
+
+def test_small_and_radix3_grids_and_an_empty_call(gpu):
+    """12^3 (the deposit walks nodes in lines: 12 is no multiple of its 8 x 2 x 2 patch;
+    radix-3 transforms) and 24^3 (patch walk, radix-3 transforms) in one call; an empty
+    call does nothing."""
+    specs = [(12, 61), (12, 62), (24, 63), (24, 64)]
+    batched = [make(gpu, N, gpu.PREC_MIXED, seed) for N, seed in specs]
+    direct = [make(gpu, N, gpu.PREC_MIXED, seed) for N, seed in specs]
+    b = gpu.Batch()
+    b.step([])
+    for _ in range(8):
+        b.step([s for _, s in batched])
+        for _, s in direct:
+            s.step()
+    for (N, _), (_, sb), (_, sd) in zip(specs, batched, direct):
+        assert_close(sb, sd, N)
+    assert b.info()[0] == len(specs) * 6

@@ -97,3 +97,16 @@ def test_server_with_graph_cycles_same_bits(gpu):
         assert mix["cycles"] == alone["cycles"] and mix["a"] == alone["a"]
         for k in ("kbin", "power", "occupation"):
             assert np.array_equal(mix[k], alone[k]), (i, k)
+
+
+def test_graph_cycles_radix3_and_line_walk_grids(gpu):
+    """24^3 (radix-3 transforms) and 12^3 (the deposit's line walk): graph cycles give the
+    same bits as direct ones."""
+    for N in (24, 12):
+        _, direct = new_sim(gpu, N, gpu.PREC_MIXED, seed=N)
+        _, graph = new_sim(gpu, N, gpu.PREC_MIXED, seed=N)
+        for _ in range(8):
+            direct.step()
+            graph.step_graph()
+        assert_same_bits(direct, graph)
+        assert graph.graph_info()[0] == 6
