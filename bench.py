@@ -82,7 +82,7 @@ def parse():
     ap.add_argument("--serve-burst", type=int, default=24, help="requests submitted at once for the capacity run")
     ap.add_argument("--op", default=None,
                     help="one operation instead of the benchmark: prepare, cycle, table, r2c_alone, c2r_alone, "
-                         "fft_axis_y, fft_axis_z, ensemble")
+                         "fft_axis_y, fft_axis_z, ensemble, batch_cycle")
     ap.add_argument("--reps", type=int, default=3, help="--op: timed calls")
     ap.add_argument("--z-op", type=float, default=0.0,
                     help="--op prepare / table: evolve from z = 100 until this redshift first")
@@ -943,12 +943,47 @@ def run_op(args):
       prepare    IC at z = 100, evolve to --z-op, write the hibernation file --state
       cycle      restart from --state, --reps cycles (the late-time cycle for ncu)
       table      restart from --state (or a fresh IC), time each operation of a cycle
-      ensemble   the 48-simulation batched ensemble alone (direct, graph and one-thread runs)
+      ensemble   the 48-simulation ensemble alone (server direct, graph and one-thread runs;
+                 batched in 1, 2, 4 and 8 lanes)
+      batch_cycle  16 simulations of --grid^3: --reps batched steps, then --reps direct
+                 cycles of each (one cohort, for launch lists)
       r2c_alone, c2r_alone, fft_axis_y, fft_axis_z   one component of random values"""
     import numpy as np
     import gev_gb300 as gpu
     if args.op == "ensemble":
         print(json.dumps(run_ensemble(gpu, args.seed, lanes=(1, 2, 4, 8))))
+        return
+    if args.op == "batch_cycle":
+        # 16 simulations of --grid^3 (mixed form): two direct cycles each, then --reps
+        # batched steps (one launch per kernel for the cohort), then --reps direct cycles of
+        # each simulation; host wall time of each phase with the device synchronised
+        N = args.grid
+        sims = []
+        for k in range(16):
+            c = gpu.Context(N, gpu.PREC_MIXED)
+            sim = gpu.Sim(c, N ** 3)
+            sim.ic_generate(**gpu.ic_params(2.5 * N, seed=args.seed + k))
+            sims.append((c, sim))
+        b = gpu.Batch()
+        for _ in range(2):
+            b.step([sim for _, sim in sims])
+        for c, _ in sims:
+            c.sync()
+        t0 = time.perf_counter()
+        for _ in range(args.reps):
+            b.step([sim for _, sim in sims])
+        for c, _ in sims:
+            c.sync()
+        t1 = time.perf_counter()
+        for _ in range(args.reps):
+            for _, sim in sims:
+                sim.step()
+        for c, _ in sims:
+            c.sync()
+        t2 = time.perf_counter()
+        print(json.dumps({"grid": N, "simulations": 16, "steps": args.reps, "batch_info": b.info(),
+                          "batched_ms_per_step": (t1 - t0) / args.reps * 1e3,
+                          "direct_ms_per_step": (t2 - t1) / args.reps * 1e3}))
         return
     import torch
     N = args.grid
