@@ -964,7 +964,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
 #define GEV_DENSE(K)                                                                                         \
   do {                                                                                                       \
     GevTimed tm_d(ctx, "k_dense_sums");                                                                      \
-    gev_launch<k_dense_sums_body<K>, 32 * DENSE_WARPS, 1>(ctx, k_dense_sums<K>, dim3(ctx->sms * 8),          \
+    gev_launch<k_dense_sums_body<K>, 32 * DENSE_WARPS, 4>(ctx, k_dense_sums<K>, dim3(ctx->sms * 8),          \
                                                           dim3(32 * DENSE_WARPS), 0, p->cur,                 \
                                                           (const uint32_t *)p->start, pa, fphi, fp, dN,      \
                                                           (const uint32_t *)p->bounds, dt);                  \
@@ -983,7 +983,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
   } while (0)
     GevTimed tm_p(ctx, "k_fx_prep");
     if (kind == FX_T00) {
-      gev_launch<k_fx_prep_body<FX_T00>, 256, 1>(ctx, k_fx_prep<FX_T00>, dim3(pb), dim3(256), 0, p->cur, p->n, pa, fp,
+      gev_launch<k_fx_prep_body<FX_T00>, 256, 8>(ctx, k_fx_prep<FX_T00>, dim3(pb), dim3(256), 0, p->cur, p->n, pa, fp,
                                               (int)(fphi != nullptr), (const uint32_t *)p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
@@ -991,7 +991,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
       GevTimed tm_g(ctx, "k_dep_gather");
       GEV_GATHER(FX_T00);
     } else if (kind == FX_TIJ) {
-      gev_launch<k_fx_prep_body<FX_TIJ>, 256, 1>(ctx, k_fx_prep<FX_TIJ>, dim3(pb), dim3(256), 0, p->cur, p->n, pa, fp,
+      gev_launch<k_fx_prep_body<FX_TIJ>, 256, 8>(ctx, k_fx_prep<FX_TIJ>, dim3(pb), dim3(256), 0, p->cur, p->n, pa, fp,
                                               (int)(fphi != nullptr), (const uint32_t *)p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();
@@ -999,7 +999,7 @@ int deposit_fx(gev_ctx *ctx, gev_pcls *p, gev_field *out, int kind, double mass,
       GevTimed tm_g(ctx, "k_dep_gather");
       GEV_GATHER(FX_TIJ);
     } else {
-      gev_launch<k_fx_prep_body<FX_T00TIJ>, 256, 1>(ctx, k_fx_prep<FX_T00TIJ>, dim3(pb), dim3(256), 0, p->cur, p->n, pa, fp,
+      gev_launch<k_fx_prep_body<FX_T00TIJ>, 256, 8>(ctx, k_fx_prep<FX_T00TIJ>, dim3(pb), dim3(256), 0, p->cur, p->n, pa, fp,
                                               (int)(fphi != nullptr), (const uint32_t *)p->bounds);
       GEV_LAUNCH_CHECK(ctx);
       tm_p.stop();

@@ -280,7 +280,7 @@ int run_cols(gev_ctx *ctx, const void *in, void *out, long line_stride, long pla
   const long blocks = (long)N * nchunks;
   const size_t smem = ((size_t)N + (size_t)N * B) * sizeof(C) + (size_t)N * 2;
   GevTimed tm_(ctx, "k_fft_cols");
-  gev_launch_if<sizeof(T) == 4, k_fft_cols_body<T, SIGN>, 256, 1>(
+  gev_launch_if<sizeof(T) == 4, k_fft_cols_body<T, SIGN>, 256, 5>(
       ctx, k_fft_cols<T, SIGN>, dim3((unsigned)blocks), dim3(256), smem, (const C *)in, (C *)out, ctx->planN,
       (const C *)ctx->d_twN, (const unsigned short *)ctx->d_permN, NH, line_stride, plane_stride, lgB);
   GEV_LAUNCH_CHECK(ctx);
@@ -302,7 +302,7 @@ int r2c_comp(gev_ctx *ctx, const void *real, void *spec) {
   const int lgB = batch_lg(M, sizeof(C), 1, 64, 32768), B = 1 << lgB;
   const size_t smem = ((size_t)M + (size_t)M * (B + 1)) * sizeof(C) + (size_t)M * 2;
   GevTimed tm_(ctx, "k_fft_r2c_rows");
-  gev_launch_if<sizeof(T) == 4, k_fft_r2c_rows_body<T>, 256, 1>(
+  gev_launch_if<sizeof(T) == 4, k_fft_r2c_rows_body<T>, 256, 5>(
       ctx, k_fft_r2c_rows<T>, dim3((unsigned)((nrows + B - 1) / B)), dim3(256), smem, (const T *)real, (C *)spec,
       ctx->planH, (const C *)ctx->d_twH, (const unsigned short *)ctx->d_permH, (const C *)ctx->d_twN, NH, nrows,
       lgB, make_div(M), make_div(M + 1));
@@ -328,7 +328,7 @@ int c2r_comp(gev_ctx *ctx, const void *spec, void *real, void *scratch, const do
   const int lgB = batch_lg(M, sizeof(C), 1, 64, 32768), B = 1 << lgB;
   const size_t smem = ((size_t)M + (size_t)M * (B + 1) + (size_t)B * (M + 1)) * sizeof(C) + (size_t)M * 2;
   GevTimed tm_(ctx, "k_fft_c2r_rows");
-  gev_launch_if<sizeof(T) == 4, k_fft_c2r_rows_body<T>, 256, 1>(
+  gev_launch_if<sizeof(T) == 4, k_fft_c2r_rows_body<T>, 256, 5>(
       ctx, k_fft_c2r_rows<T>, dim3((unsigned)((nrows + B - 1) / B)), dim3(256), smem, (const C *)scratch,
       (T *)real, ctx->planH, (const C *)ctx->d_twH, (const unsigned short *)ctx->d_permH, (const C *)ctx->d_twN, NH,
       nrows, lgB, make_div(M), make_div(M + 1));

@@ -348,7 +348,7 @@ int gev_project_scalar_evolve_vector(gev_ctx *ctx, const gev_field *SijFT, gev_f
         (const CT<double>::C *)SijFT->d, (CT<double>::C *)chiFT->d, (CT<double>::C *)BiFT->d,
         (const double *)ctx->d_gridk2, (const CT<double>::C *)ctx->d_kshift, a2dtau, make_kdim(N), n);
   else
-    gev_launch<k_project_evolve_body<float>, 256, 1>(
+    gev_launch<k_project_evolve_body<float>, 256, 5>(
         ctx, k_project_evolve<float>, dim3(blocks), dim3(256), 0, (const CT<float>::C *)SijFT->d,
         (CT<float>::C *)chiFT->d, (CT<float>::C *)BiFT->d, (const float *)ctx->d_gridk2,
         (const CT<float>::C *)ctx->d_kshift, (float)a2dtau, make_kdim(N), n);
