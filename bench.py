@@ -670,7 +670,7 @@ def run_serve(args, gpu):
     }
 
 
-def run_ensemble(gpu, seed, lanes=(1, 4)):
+def run_ensemble(gpu, seed, lanes=(1, "size")):
     """The batched ensemble: 16 simulations each at 64^3, 96^3 and 128^3, box 2.5 N,
     Omega_cdm U[0.25, 0.35], sigma8 U[0.75, 0.87], n_s U[0.94, 0.98], distinct seeds,
     all to z = 0, admitted at once.  Run four ways on the same requests: through the
@@ -725,8 +725,14 @@ def run_ensemble(gpu, seed, lanes=(1, 4)):
         t0 = time.perf_counter()
         with ThreadPoolExecutor(4) as ex:
             runs = list(ex.map(make, ens))
+        # lanes == "size": one batch per grid size, so that no cohort waits for another's steps
+        sizes = sorted({r.N for r in ens})
+        if lanes == "size":
+            lane_of = [sizes.index(r.N) for r in ens]
+            lanes = len(sizes)
+        else:
+            lane_of = [k % lanes for k in range(len(ens))]
         batches = [gpu.Batch() for _ in range(lanes)]
-        lane_of = [k % lanes for k in range(len(ens))]
 
         def run_lane(li):
             ks = [k for k in range(len(ens)) if lane_of[k] == li]
@@ -754,7 +760,9 @@ def run_ensemble(gpu, seed, lanes=(1, 4)):
         return cycles, powers, {"simulations": len(ens), "lanes": lanes, "makespan_s": span,
                                 "particle_steps_per_s": steps / span, "cycles_batched": sum(i[0] for i in info),
                                 "cycles_direct": sum(i[1] for i in info), "batched_launches": sum(i[2] for i in info),
-                                "cohorts": "per lane: 64^3, 96^3 and 128^3, %d simulations each" % (16 // lanes)}
+                                "cohorts": ("one lane per grid size" if len(set(lane_of)) == len(sizes) and all(
+                                    lane_of[k] == sizes.index(ens[k].N) for k in range(len(ens)))
+                                            else "per lane: 64^3, 96^3 and 128^3, %d simulations each" % (16 // lanes))}
 
     res_d, _, direct = ensemble(0, False)
     res_g, st_g, graph = ensemble(0, True)
@@ -951,7 +959,7 @@ def run_op(args):
     import numpy as np
     import gev_gb300 as gpu
     if args.op == "ensemble":
-        print(json.dumps(run_ensemble(gpu, args.seed, lanes=(1, 2, 4, 8))))
+        print(json.dumps(run_ensemble(gpu, args.seed, lanes=(1, "size", 2, 4, 8))))
         return
     if args.op == "batch_cycle":
         # 16 simulations of --grid^3 (mixed form): two direct cycles each, then --reps
