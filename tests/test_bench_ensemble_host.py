@@ -38,6 +38,10 @@ class FakeGpu:
         return SimpleNamespace(N=N, seed=seed, z_target=z_target, prec=prec, Omega_cdm=Omega_cdm, Omega_b=0.05,
                                sigma8=sigma8, n_s=n_s, h=0.67, z_in=100.0, boxsize=2.5 * N, numbins=numbins)
 
+    def Request(self, N, prec, boxsize, Omega_cdm, Omega_b, sigma8, n_s, h, z_in, z_target, seed, numbins):
+        return SimpleNamespace(N=N, seed=seed, z_target=z_target, prec=prec, Omega_cdm=Omega_cdm, Omega_b=Omega_b,
+                               sigma8=sigma8, n_s=n_s, h=h, z_in=z_in, boxsize=boxsize, numbins=numbins)
+
     def ic_params(self, boxsize, **kw):
         return dict(boxsize=boxsize, **kw)
 
@@ -81,7 +85,7 @@ class FakeGpu:
 
         return S()
 
-    def Server(self, workers=0, graphs=False):
+    def Server(self, workers=0, graphs=False, max_active=0):
         gpu = self
 
         class Srv:
@@ -106,8 +110,8 @@ class FakeGpu:
                         for i, r in enumerate(self.reqs)]
 
             def stats(self):
-                return {"max_active_seen": len(self.reqs), "workers": workers or 4,
-                        "graph_cycles": 5000 if graphs else 0}
+                return {"max_active_seen": max_active or len(self.reqs), "workers": workers or 4,
+                        "graph_cycles": 5000 if graphs else 0, "failed": 0}
 
             def close(self):
                 pass
@@ -158,3 +162,17 @@ def test_run_ensemble_orchestration():
     assert sum(b.n for b in gpu.batches) == 48 * 3
     assert out["graph_cycles"]["graph_cycles"] == 5000 and out["graph_cycles"]["same_bits_as_direct"]
     assert set(out["stencil_shapes"]) == {"64", "96", "128"}
+
+
+def test_run_serve_assembles_the_serving_object():
+    """run_serve with a short window of Poisson arrivals, a burst of four and the same
+    burst in the plain FP64 form one at a time; the serving object carries the
+    percentiles, the capacity ratio and the ensemble."""
+    gpu = FakeGpu()
+    args = SimpleNamespace(seed=1, serve_rate=40.0, serve_seconds=0.25, serve_burst=4)
+    out = bench.run_serve(args, gpu)
+    assert out["completed"] >= 1 and out["failed"] == 0
+    assert 0.0 < out["p50_s"] <= out["p99_s"] <= out["max_s"]
+    assert out["burst"]["requests"] == 4 and out["sequential_fp64"]["requests"] == 4
+    assert out["capacity_vs_sequential_fp64"] > 0.0
+    assert out["ensemble"]["simulations"] == 48 and out["ensemble"]["batched_per_phase"]["same_cycles_as_server"]
